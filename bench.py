@@ -1,0 +1,370 @@
+"""Benchmark of the compound-eye render path on one GB300 (or N replicas).
+
+Workload (default): the large-terrain plain render -- a 512 x 512-cell
+value-noise heightfield over 200 m plus 2000 cone plants (588,288 triangles,
+height-ramped vertex colours, simple_sky), a 6000-ommatidium sinewave-droplet
+eye (acceptance 1.5-4 deg), 256 samples per ommatidium, and a 1024-pose
+random walk (0.1 m steps, yaw noise 10 deg).  One step renders the whole
+trajectory: 1024 eye-frames = 1,572,864,000 rays.  Inputs are seeded
+synthetic data of these shapes (no dataset is used).
+
+Output: one JSON line (rank 0) with rays/s as the metric, eye-frames/s,
+the end-to-end number through the C ABI with host buffers, a roofline
+object for the render kernel and the CPU baseline (the OpenMP oracle on the
+host cores, on a bounded sample of the same workload).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "compound-ray_gb300"))
+
+POSES_PER_LAUNCH = 256
+NODE_BYTES = 64
+TRI_BYTES = 48
+SHADE_BYTES = 48
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--poses", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target wall time of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(poses):
+    import scenes
+
+    d = os.path.join(tempfile.gettempdir(), "cr_bench_terrain_%d_%d" % (scenes.SEED, poses))
+    info = scenes.terrain_scene(d, poses=poses)
+    return info
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(info, target_s, rank_threads=0):
+    """The CPU oracle (OpenMP C++ over its own BVH) on a bounded sample of the
+    same workload: the first poses of the trajectory, all ommatidia, all
+    samples, draws from a seeded normal/uniform generator."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gltf_ref
+    import oracle
+
+    ref = gltf_ref.load(info["gltf"])
+    v, c, f = ref.arrays()
+    sc = oracle.OracleScene(v, c, f, ref.miss)
+    omm = [cm for cm in ref.cameras if cm["kind"] == "compound"][0]["omm"]
+    N, spp = len(omm), info["spp"]
+    rng = np.random.default_rng(7)
+
+    def draws(P):
+        d = np.empty((P * N * spp, 2), np.float32)
+        d[:, 0] = rng.standard_normal(P * N * spp)
+        d[:, 1] = 1.0 - rng.random(P * N * spp)
+        return d
+
+    threads = rank_threads or oracle.max_threads()
+    d1 = draws(1)
+    t0 = time.perf_counter()
+    sc.render_draws(omm, spp, info["poses"][:1], d1, threads=threads)
+    one = time.perf_counter() - t0
+    P = max(1, min(len(info["poses"]), int(target_s / max(one, 1e-3))))
+    dP = draws(P)
+    t0 = time.perf_counter()
+    sc.render_draws(omm, spp, info["poses"][:P], dP, threads=threads)
+    dt = time.perf_counter() - t0
+    rays = P * N * spp
+    return {"value": rays / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d poses x %d ommatidia x %d samples (%d rays), %.1f s wall on %d threads" %
+                      (P, len(info["poses"]), N, spp, rays, dt, threads),
+            "eye_frames_per_s": P / dt}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    info = workload(args.poses)
+    N, spp = info["n_omm"], info["spp"]
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    per_step_target = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(info, per_step_target)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    value = statistics.mean(vals)
+    rays_step = args.poses * N * spp
+    line = {"impl": "reference", "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * rays_step / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "terrain %d tris, droplet eye 6000 omm x 256 spp, %d-pose trajectory" % (info["triangles"], args.poses),
+                       "rays_per_step": rays_step, "note": "each step times a bounded sample of the trajectory"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "eye_frames_per_s": value / (N * spp)}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    import eyeRendererHelperFunctions as eh
+
+    lib = eh.loadRenderer()
+    lib.setVerbosity(False)
+    info = workload(args.poses)
+    lib.loadGlTFscene(info["gltf"].encode())
+    err = eh.lastError(lib)
+    if err:
+        raise RuntimeError(err)
+    eh.gotoFirstCompoundEye(lib)
+    spp = info["spp"]
+    lib.setCurrentEyeSamplesPerOmmatidium(spp)
+    N = lib.getCurrentEyeOmmatidialCount()
+    P = args.poses
+    poses12 = info["poses"].astype(np.float32)
+    p16 = np.zeros((P, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = poses12[:, 3 * k:3 * k + 3]
+    d_poses = torch.from_numpy(p16).to(dev)
+    d_out = torch.empty((P, N, 3), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    lib.crSetStream(stream.cuda_stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+    chunks = [(s, min(POSES_PER_LAUNCH, P - s)) for s in range(0, P, POSES_PER_LAUNCH)]
+
+    def step(events=None):
+        for i, (s, n) in enumerate(chunks):
+            if events is not None:
+                events[i][0].record(stream)
+            rc = lib.crRenderPosesDevice(d_poses[s].data_ptr(), n, d_out[s].data_ptr())
+            if rc != 0:
+                raise RuntimeError(eh.lastError(lib))
+            if events is not None:
+                events[i][1].record(stream)
+
+    # Warm-up (includes generator initialisation on the first call).
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    if lib.crSynchronize() != 0:
+        raise RuntimeError(eh.lastError(lib))
+
+    # Traversal statistics for the roofline's per-ray bytes (not timed).
+    nodes = ctypes_double()
+    tris = ctypes_double()
+    if lib.crMeasureTraversal(d_poses.data_ptr(), min(16, P), nodes, tris) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    hit_frac = hit_fraction(lib, eh)
+
+    launch_ms = []
+    step_ms = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chunks]
+            step(ev)
+            torch.cuda.synchronize()
+            ms = [a.elapsed_time(b) for a, b in ev]
+            launch_ms.extend(zip([n for _, n in chunks], ms))
+            step_ms.append(sum(ms))
+        torch.cuda.synchronize()
+    if lib.crSynchronize() != 0:
+        raise RuntimeError(eh.lastError(lib))
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+        torch.distributed.barrier()
+    rays_step = P * N * spp
+    value = world * rays_step * args.steps / total_s
+
+    # End to end through the C ABI with host (pinned) buffers.
+    h_poses = torch.from_numpy(poses12.copy()).pin_memory()
+    h_out = torch.empty((P, N, 3), dtype=torch.float32).pin_memory()
+    lib.crSetStream(None)
+    pose_np = h_poses.numpy()
+    out_np = h_out.numpy()
+    lib.crRenderPoses(pose_np, P, out_np)  # warm the host path
+    e2e_s = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        if lib.crRenderPoses(pose_np, P, out_np) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_total = sum(e2e_s)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * rays_step * args.steps / e2e_total
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # Roofline of the render kernel: per-ray algorithmic bytes x rays per
+    # launch / mean launch time of the full 256-pose launches.
+    C = max(1, math.ceil(spp / 32)) if spp >= 32 else 1
+    full = [ms for n, ms in launch_ms if n == POSES_PER_LAUNCH] or [ms for _, ms in launch_ms]
+    launch_n = POSES_PER_LAUNCH if len(full) and P >= POSES_PER_LAUNCH else P
+    per_ray = (nodes.value * NODE_BYTES + tris.value * TRI_BYTES + hit_frac * SHADE_BYTES
+               + (2 * 32.0 + 32.0) / launch_n + (2 * 12.0 * C) / spp)
+    launch_s = statistics.mean(full) / 1000.0
+    achieved = per_ray * launch_n * N * spp / launch_s / 1e9
+    peak, src = peaks()
+    clk = clocks.summary()
+    line = {
+        "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "terrain %d tris, droplet eye 6000 omm x 256 spp, %d-pose trajectory" % (info["triangles"], P),
+                   "rays_per_step": rays_step, "eye_frames_per_step": P, "l2": "flushed (512 MB write) between steps",
+                   "poses_per_launch": POSES_PER_LAUNCH},
+        "eye_frames_per_s": value / (N * spp),
+        "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
+                "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},
+        "gpu_launches": args.steps * len(chunks) * (2 if spp > 32 else 1),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": src,
+                     "bytes_per_ray": per_ray, "node_visits_per_ray": nodes.value, "tri_tests_per_ray": tris.value,
+                     "hit_fraction": hit_frac, "launch_ms": statistics.mean(full),
+                     "kernel": "renderKernel<0> (+ combineChunksKernel)"},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(info, args.cpu_seconds)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_double():
+    import ctypes
+
+    return ctypes.c_double(0.0)
+
+
+def hit_fraction(lib, eh):
+    """Fraction of rays that hit geometry, from one recorded frame at the
+    camera's current pose (the 256-sample eye of the workload)."""
+    rec = eh.renderFrameRecorded(lib)
+    return float((rec["hitId"] >= 0).mean())
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

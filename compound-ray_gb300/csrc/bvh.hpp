@@ -1,0 +1,45 @@
+// Two-wide bounding volume hierarchy built on the host with binned SAH.
+//
+// Device layout (all little-endian, 16-byte aligned):
+//   node i = 4 x float4 (64 B):
+//     [0] = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//     [1] = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//     [2] = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//     [3] = (int child0, int child1, 0, 0)
+//   child >= 0 is an inner node index; child < 0 is a leaf whose bitwise
+//   complement packs (first triangle << 3) | (count - 1), count in 1..8.
+//   triangle j (BVH order) = 3 x float4: (v0, id) (v1, 0) (v2, 0) where id is
+//   the original global triangle id stored as integer bits.
+//   shade j = 3 x float4 colours at v0, v1, v2; c0.w holds 1.0 when the
+//   triangle uses vertex colours and 0.0 for a material base colour.
+// Node 0 is the root and is always an inner node.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace cr {
+
+struct BvhBuildStats {
+  uint32_t innerNodes = 0;
+  uint32_t leaves = 0;
+  uint32_t maxDepth = 0;
+  double sahCost = 0.0;
+};
+
+struct HostBvh {
+  std::vector<float> nodes;   // 16 floats per node
+  std::vector<float> tris;    // 12 floats per triangle, BVH order
+  std::vector<float> shade;   // 12 floats per triangle, BVH order
+  std::vector<uint32_t> order;  // BVH position -> original triangle id
+  BvhBuildStats stats;
+};
+
+// verts: 9 floats per triangle (world space); colours: 12 floats per triangle;
+// usesVertexColour: 1 byte per triangle.
+void buildBvh(const float* verts, const float* colours, const uint8_t* usesVertexColour, uint32_t triCount,
+              HostBvh& out);
+
+constexpr int kMaxLeafSize = 8;
+
+}  // namespace cr

@@ -1,0 +1,88 @@
+// Interface between the host runtime (eye_renderer.cpp) and the sm_103a
+// kernels (render.cu).  Plain pointers and sizes only.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace cr {
+
+// Device view of a scene: BVH nodes / triangles / shading records in the
+// layout described in bvh.hpp.
+struct DevScene {
+  const float4* nodes = nullptr;
+  const float4* tris = nullptr;
+  const float4* shade = nullptr;
+  uint32_t triCount = 0;
+  int miss = 0;  // 0 = default_background, 1 = simple_sky
+};
+
+// Device view of one compound eye.
+//  omm: N ommatidium records of 32 bytes (2 x float4).
+//  rng: XORWOW generator states, structure of arrays: 8 planes of N*spp
+//       32-bit words (d, v0..v4, boxmuller_flag, boxmuller_extra); the state
+//       of (ommatidium o, sample s) sits at index o*spp + s and holds the
+//       stream curand_init(42, s*N + o, 0) (shaders.cu:669-695).
+struct DevEye {
+  const float4* omm = nullptr;
+  uint32_t N = 0;
+  uint32_t spp = 1;
+  uint32_t* rng = nullptr;
+};
+
+// One pose = 4 x float4: position, local x axis, local y axis, local z axis
+// (w components unused).
+constexpr int kPoseFloats = 16;
+
+// Per-ray record written by the recording render variant (test and parity
+// use only): draws, ray, closest hit and the unscaled shaded colour.
+struct RayRecord {
+  float normalDraw, uniformDraw;
+  float ox, oy, oz;
+  float dx, dy, dz;
+  float t, b1, b2;
+  int32_t hitId;  // original global triangle id, -1 on a miss
+  float r, g, b;
+  float pad;
+};
+static_assert(sizeof(RayRecord) == 64, "ray record is 64 bytes");
+
+// Error bits raised by the kernels into a device word.
+enum : uint32_t {
+  kErrStackOverflow = 1u,
+  kErrRngDoubleFlag = 2u,
+};
+
+constexpr uint32_t kRngPlanes = 8;
+
+// Samples traced by one warp segment and number of segments per ommatidium.
+struct WarpPlan {
+  uint32_t segWidth;     // lanes per ommatidium segment (power of two <= 32)
+  uint32_t ommPerWarp;   // 32 / segWidth
+  uint32_t chunks;       // warp segments per ommatidium (spp > 32)
+  uint64_t tasks;        // warp tasks per pose batch
+};
+WarpPlan planWarps(uint32_t N, uint32_t spp);
+
+// Floats of scratch needed by launchRender for P poses (0 when spp <= 32).
+size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P);
+
+cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t stream);
+
+// Renders P poses of one eye.  out: P*N*3 floats, the per-ommatidium sums of
+// sample colour / spp.  scratch: renderScratchFloats() floats or null when
+// not needed.  rec: P*N*spp records or null.  stats: null, or two counters
+// that receive the node visits and triangle tests of every ray.  The
+// generator states advance by one frame per pose and are written back.
+cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* out,
+                         float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
+                         unsigned long long* stats = nullptr);
+
+// Projection of per-ommatidium sums into a w x h uchar4 frame.
+//  mode 0: single_dimension_fast (row 0, x < N), mode 1: single_dimension.
+cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, int h, int mode,
+                          cudaStream_t stream);
+
+}  // namespace cr

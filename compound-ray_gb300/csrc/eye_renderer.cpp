@@ -1,0 +1,855 @@
+// The C ABI of the headless compound-eye renderer (include/libEyeRenderer.h).
+//
+// Host state mirrors the reference's globals (libEyeRenderer3/libEyeRenderer.cpp:81-92):
+// one scene, a list of cameras with a current index, a render size
+// (default 400 x 400) and a verbosity flag.  Each compound camera owns its
+// ommatidium records, generator states and a "configured" flag, which the
+// first render of the eye sets (libEyeRenderer.cpp:178-179) and every sample
+// count or ommatidium count change clears (cameras/CompoundEye.cpp:30-48,
+// 98-115, 171-179).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/libEyeRenderer.h"
+#include "bvh.hpp"
+#include "device_api.hpp"
+#include "scene.hpp"
+
+namespace cr {
+namespace {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t count = 0;
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+  void ensure(size_t n) {
+    if (n <= count && ptr) return;
+    release();
+    if (n == 0) return;
+    check(cudaMalloc(reinterpret_cast<void**>(&ptr), n * sizeof(T)), "cudaMalloc");
+    count = n;
+  }
+};
+
+struct EyeDev {
+  DevBuf<float4> omm;
+  DevBuf<uint32_t> rng;
+  DevBuf<float> sums;  // N x 3 of the last frame
+  uint32_t N = 0, spp = 0;
+  bool configured = false;
+  bool haveSums = false;
+  void release() {
+    omm.release();
+    rng.release();
+    sums.release();
+    N = spp = 0;
+    configured = false;
+    haveSums = false;
+  }
+};
+
+constexpr uint32_t kMaxPosesPerLaunch = 256;
+
+struct Renderer {
+  SceneData scene;
+  bool loaded = false;
+  // The BVH is built on the host by loadGlTFscene and uploaded by the first
+  // call that needs the GPU, so every host-side entry point works without one.
+  std::unique_ptr<HostBvh> pendingBvh;
+  BvhBuildStats bvhStats;
+  DevBuf<float4> nodes, tris, shade;
+  DevScene dev;
+  std::vector<EyeDev> eyes;  // parallel to scene.cameras
+  size_t current = 0;
+  int width = 400, height = 400;
+  DevBuf<uchar4> frame;
+  std::vector<uchar4> hostFrame;
+  DevBuf<float4> poses;
+  DevBuf<float> scratch;
+  DevBuf<float> batchOut;
+  DevBuf<uint32_t> err;
+  cudaStream_t ownStream = nullptr;
+  cudaStream_t userStream = nullptr;
+  bool verbose = true;
+
+  cudaStream_t stream() {
+    if (userStream) return userStream;
+    if (!ownStream) check(cudaStreamCreateWithFlags(&ownStream, cudaStreamNonBlocking), "cudaStreamCreate");
+    return ownStream;
+  }
+
+  void releaseAll() {
+    for (EyeDev& e : eyes) e.release();
+    eyes.clear();
+    nodes.release();
+    tris.release();
+    shade.release();
+    frame.release();
+    poses.release();
+    scratch.release();
+    batchOut.release();
+    err.release();
+    hostFrame.clear();
+    dev = DevScene{};
+    pendingBvh.reset();
+    if (ownStream) cudaStreamDestroy(ownStream);
+    ownStream = nullptr;
+    loaded = false;
+    scene = SceneData{};
+    current = 0;
+  }
+
+  void ensureUploaded() {
+    if (!pendingBvh) return;
+    const HostBvh& b = *pendingBvh;
+    const size_t nn = b.nodes.size() / 4, nt = b.tris.size() / 4;
+    nodes.ensure(std::max<size_t>(1, nn));
+    tris.ensure(std::max<size_t>(1, nt));
+    shade.ensure(std::max<size_t>(1, nt));
+    cudaStream_t st = stream();
+    if (nn) check(cudaMemcpyAsync(nodes.ptr, b.nodes.data(), nn * sizeof(float4), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    if (nt) {
+      check(cudaMemcpyAsync(tris.ptr, b.tris.data(), nt * sizeof(float4), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+      check(cudaMemcpyAsync(shade.ptr, b.shade.data(), nt * sizeof(float4), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    }
+    check(cudaStreamSynchronize(st), "scene upload");
+    dev.nodes = nodes.ptr;
+    dev.tris = tris.ptr;
+    dev.shade = shade.ptr;
+    dev.triCount = static_cast<uint32_t>(scene.triangleCount());
+    dev.miss = static_cast<int>(scene.miss);
+    pendingBvh.reset();
+  }
+
+  Camera& cam() {
+    if (!loaded || scene.cameras.empty()) throw std::runtime_error("no scene loaded");
+    return scene.cameras[current];
+  }
+  bool compoundActive() const {
+    return loaded && !scene.cameras.empty() && scene.cameras[current].kind == CameraKind::Compound;
+  }
+
+  void ensureFrame() {
+    const size_t n = static_cast<size_t>(width) * static_cast<size_t>(height);
+    if (frame.count != n) {
+      frame.release();
+      frame.ensure(n);
+      if (n) check(cudaMemsetAsync(frame.ptr, 0, n * sizeof(uchar4), stream()), "cudaMemset");
+    }
+  }
+
+  uint32_t* errWord() {
+    if (!err.ptr) {
+      err.ensure(1);
+      check(cudaMemsetAsync(err.ptr, 0, sizeof(uint32_t), stream()), "cudaMemset");
+    }
+    return err.ptr;
+  }
+
+  void checkErrWord() {
+    uint32_t h = 0;
+    check(cudaMemcpyAsync(&h, errWord(), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream()), "cudaMemcpy");
+    check(cudaStreamSynchronize(stream()), "render");
+    if (h != 0) {
+      check(cudaMemsetAsync(errWord(), 0, sizeof(uint32_t), stream()), "cudaMemset");
+      throw std::runtime_error("render kernel raised error flags " + std::to_string(h) +
+                               ((h & kErrStackOverflow) ? " (BVH traversal stack overflow)" : ""));
+    }
+  }
+
+  // Makes the device side of compound camera `i` match its host record.
+  EyeDev& syncEye(size_t i) {
+    ensureUploaded();
+    Camera& c = scene.cameras[i];
+    EyeDev& e = eyes[i];
+    const uint32_t N = static_cast<uint32_t>(c.omm.size());
+    const uint32_t spp = static_cast<uint32_t>(std::max(1, c.spp));
+    if (e.N != N || e.spp != spp || !e.omm.ptr) {
+      const bool countChanged = e.N != N || !e.omm.ptr;
+      if (countChanged) {
+        e.omm.release();
+        e.omm.ensure(std::max<size_t>(1, 2 * static_cast<size_t>(N)));
+        e.sums.release();
+        e.sums.ensure(std::max<size_t>(1, 3 * static_cast<size_t>(N)));
+      }
+      e.rng.release();
+      e.rng.ensure(std::max<size_t>(1, static_cast<size_t>(kRngPlanes) * N * spp));
+      e.N = N;
+      e.spp = spp;
+      e.configured = false;
+      e.haveSums = false;
+      if (N) check(cudaMemcpyAsync(e.omm.ptr, c.omm.data(), sizeof(Ommatidium) * N, cudaMemcpyHostToDevice, stream()),
+                   "cudaMemcpy");
+    }
+    return e;
+  }
+
+  DevEye devEye(EyeDev& e) {
+    DevEye d;
+    d.omm = e.omm.ptr;
+    d.N = e.N;
+    d.spp = e.spp;
+    d.rng = e.rng.ptr;
+    return d;
+  }
+
+  void ensureRng(EyeDev& e) {
+    if (e.configured) return;
+    check(launchRngInit(devEye(e), errWord(), stream()), "rng init launch");
+    e.configured = true;
+  }
+
+  static void packPose(const Camera& c, float* p16) {
+    const f3 v[4] = {c.position, c.ls.x, c.ls.y, c.ls.z};
+    for (int k = 0; k < 4; ++k) {
+      p16[4 * k + 0] = v[k].x;
+      p16[4 * k + 1] = v[k].y;
+      p16[4 * k + 2] = v[k].z;
+      p16[4 * k + 3] = 0.f;
+    }
+  }
+
+  // Renders `count` poses already on the device into d_out (count x N x 3).
+  void renderDevicePoses(EyeDev& e, const float4* d_poses, size_t count, float* d_out, RayRecord* rec,
+                         unsigned long long* stats = nullptr) {
+    ensureRng(e);
+    for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
+      const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+      const size_t need = renderScratchFloats(e.N, e.spp, P);
+      if (need) scratch.ensure(need);
+      check(launchRender(dev, devEye(e), d_poses + 4 * first, P, d_out + 3 * first * e.N, need ? scratch.ptr : nullptr,
+                         errWord(), rec, stream(), stats),
+            "render launch");
+    }
+  }
+
+  void project(EyeDev& e, const std::string& shader) {
+    ensureFrame();
+    int mode = -1;
+    if (shader == "single_dimension_fast") mode = 0;
+    else if (shader == "single_dimension") mode = 1;
+    if (mode < 0) {
+      throw std::runtime_error("compound projection '" + shader +
+                               "' is not implemented; use single_dimension_fast or single_dimension "
+                               "(per-ommatidium colours are still available from getOmmatidialColoursF32)");
+    }
+    check(launchProject(e.sums.ptr, e.N, frame.ptr, width, height, mode, stream()), "projection launch");
+  }
+};
+
+Renderer& R() {
+  static Renderer r;
+  return r;
+}
+
+thread_local std::string g_lastError;
+
+void setError(const std::string& msg) {
+  g_lastError = msg;
+  std::cerr << "[libEyeRenderer3] ERROR: " << msg << std::endl;
+}
+
+template <typename F>
+auto guarded(const char* fn, F&& f, decltype(f()) fallback) -> decltype(f()) {
+  try {
+    return f();
+  } catch (const std::exception& ex) {
+    setError(std::string(fn) + ": " + ex.what());
+  } catch (...) {
+    setError(std::string(fn) + ": unknown error");
+  }
+  return fallback;
+}
+
+template <typename F>
+void guardedVoid(const char* fn, F&& f) {
+  try {
+    f();
+  } catch (const std::exception& ex) {
+    setError(std::string(fn) + ": " + ex.what());
+  } catch (...) {
+    setError(std::string(fn) + ": unknown error");
+  }
+}
+
+}  // namespace
+}  // namespace cr
+
+using namespace cr;
+
+extern "C" {
+
+void setVerbosity(bool v) { R().verbose = v; }
+
+void loadGlTFscene(const char* filepath) {
+  guardedVoid("loadGlTFscene", [&] {
+    if (!filepath) throw std::runtime_error("null path");
+    Renderer& r = R();
+    SceneData s;
+    loadGltfScene(filepath, s, r.verbose);
+    std::unique_ptr<HostBvh> bvh(new HostBvh);
+    buildBvh(s.triVerts.data(), s.triColours.data(), s.triUsesVertexColour.data(),
+             static_cast<uint32_t>(s.triangleCount()), *bvh);
+    if (bvh->stats.maxDepth + 2 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
+    const bool keepVerbose = r.verbose;
+    cudaStream_t user = r.userStream;
+    r.releaseAll();
+    r.verbose = keepVerbose;
+    r.userStream = user;
+    r.scene = std::move(s);
+    r.bvhStats = bvh->stats;
+    r.pendingBvh = std::move(bvh);
+    r.eyes.resize(r.scene.cameras.size());
+    r.current = 0;
+    r.loaded = true;
+    if (r.verbose)
+      std::cout << "[PyEye] Loaded scene '" << filepath << "': " << r.scene.triangleCount() << " triangles, "
+                << r.scene.cameras.size() << " cameras, BVH " << r.bvhStats.innerNodes << " inner nodes / "
+                << r.bvhStats.leaves << " leaves, depth " << r.bvhStats.maxDepth << "." << std::endl;
+  });
+}
+
+void stop(void) {
+  guardedVoid("stop", [&] {
+    Renderer& r = R();
+    if (r.verbose) std::cout << "[PyEye] Cleaning eye renderer resources." << std::endl;
+    const bool v = r.verbose;
+    r.releaseAll();
+    r.userStream = nullptr;
+    r.verbose = v;
+  });
+}
+
+void setRenderSize(int w, int h) {
+  guardedVoid("setRenderSize", [&] {
+    Renderer& r = R();
+    r.width = std::max(0, w);
+    r.height = std::max(0, h);
+    if (r.verbose) std::cout << "[PyEye] Resizing rendering buffer to (" << w << ", " << h << ")." << std::endl;
+    r.hostFrame.clear();
+  });
+}
+
+double renderFrame(void) {
+  return guarded(
+      "renderFrame",
+      [&]() -> double {
+        Renderer& r = R();
+        Camera& c = r.cam();
+        const auto t0 = std::chrono::steady_clock::now();
+        r.ensureFrame();
+        if (c.kind == CameraKind::Compound) {
+          EyeDev& e = r.syncEye(r.current);
+          float p16[16];
+          Renderer::packPose(c, p16);
+          r.poses.ensure(4);
+          check(cudaMemcpyAsync(r.poses.ptr, p16, sizeof(p16), cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
+          r.renderDevicePoses(e, r.poses.ptr, 1, e.sums.ptr, nullptr);
+          e.haveSums = true;
+          r.project(e, c.projection);
+        } else {
+          throw std::runtime_error("camera '" + c.name +
+                                   "' is not a compound eye; only compound eyes are rendered by this library");
+        }
+        r.checkErrWord();
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        r.hostFrame.clear();
+        if (r.verbose) std::cout << "[PyEye] Rendered frame in " << ms << "ms." << std::endl;
+        return ms;
+      },
+      -1.0);
+}
+
+void displayFrame(void) {}
+
+unsigned char* getFramePointer(void) {
+  return guarded(
+      "getFramePointer",
+      [&]() -> unsigned char* {
+        Renderer& r = R();
+        if (r.verbose) std::cout << "[PyEye] Retrieving frame pointer..." << std::endl;
+        const size_t n = static_cast<size_t>(r.width) * static_cast<size_t>(r.height);
+        r.hostFrame.assign(std::max<size_t>(n, 1), make_uchar4(0, 0, 0, 0));
+        if (n && r.loaded) {
+          r.ensureFrame();
+          check(cudaMemcpyAsync(r.hostFrame.data(), r.frame.ptr, n * sizeof(uchar4), cudaMemcpyDeviceToHost, r.stream()),
+                "cudaMemcpy");
+          check(cudaStreamSynchronize(r.stream()), "frame download");
+        }
+        return reinterpret_cast<unsigned char*>(r.hostFrame.data());
+      },
+      nullptr);
+}
+
+void saveFrameAs(char* ppmFilename) {
+  guardedVoid("saveFrameAs", [&] {
+    if (!ppmFilename) throw std::runtime_error("null file name");
+    Renderer& r = R();
+    const bool v = r.verbose;
+    r.verbose = false;
+    unsigned char* px = getFramePointer();
+    r.verbose = v;
+    if (!px) throw std::runtime_error("no frame");
+    const int w = r.width, h = r.height;
+    if (w < 1 || h < 1) throw std::invalid_argument("Image is ill-formed. Not saving");
+    std::ofstream f(ppmFilename, std::ios::out | std::ios::binary);
+    if (!f.is_open()) throw std::runtime_error("Could not open file for SavePPM");
+    f << "P6\n" << w << " " << h << "\n255\n";
+    std::vector<unsigned char> row(static_cast<size_t>(w) * 3);
+    // The buffer is stored bottom row first (sutil/sutil.cpp:404-418).
+    for (int j = h - 1; j >= 0; --j) {
+      const unsigned char* src = px + static_cast<size_t>(4) * w * j;
+      for (int i = 0; i < w; ++i) {
+        row[3 * i + 0] = src[4 * i + 0];
+        row[3 * i + 1] = src[4 * i + 1];
+        row[3 * i + 2] = src[4 * i + 2];
+      }
+      f.write(reinterpret_cast<const char*>(row.data()), static_cast<std::streamsize>(row.size()));
+    }
+    if (r.verbose) std::cout << "[PyEye] Saved render as '" << ppmFilename << "'" << std::endl;
+  });
+}
+
+size_t getCameraCount(void) {
+  return guarded("getCameraCount", [&]() -> size_t { return R().loaded ? R().scene.cameras.size() : 0; }, size_t{0});
+}
+
+static void setCurrentCameraIndex(long idx) {
+  Renderer& r = R();
+  const long n = static_cast<long>(r.scene.cameras.size());
+  if (n == 0) throw std::runtime_error("no scene loaded");
+  r.current = static_cast<size_t>(((idx % n) + n) % n);
+}
+
+void nextCamera(void) {
+  guardedVoid("nextCamera", [&] { setCurrentCameraIndex(static_cast<long>(R().current) + 1); });
+}
+void previousCamera(void) {
+  guardedVoid("previousCamera", [&] { setCurrentCameraIndex(static_cast<long>(R().current) - 1); });
+}
+size_t getCurrentCameraIndex(void) { return R().current; }
+const char* getCurrentCameraName(void) {
+  return guarded("getCurrentCameraName", [&]() -> const char* { return R().cam().name.c_str(); }, "");
+}
+void gotoCamera(int index) {
+  guardedVoid("gotoCamera", [&] { setCurrentCameraIndex(index); });
+}
+bool gotoCameraByName(char* name) {
+  return guarded(
+      "gotoCameraByName",
+      [&]() -> bool {
+        if (!name) return false;
+        setCurrentCameraIndex(0);
+        Renderer& r = R();
+        for (size_t i = 0; i < r.scene.cameras.size(); ++i) {
+          if (r.scene.cameras[r.current].name == name) return true;
+          setCurrentCameraIndex(static_cast<long>(r.current) + 1);
+        }
+        return false;
+      },
+      false);
+}
+
+void setCameraPosition(float x, float y, float z) {
+  guardedVoid("setCameraPosition", [&] { R().cam().position = f3{x, y, z}; });
+}
+void getCameraPosition(float& x, float& y, float& z) {
+  guardedVoid("getCameraPosition", [&] {
+    const f3 p = R().cam().position;
+    x = p.x;
+    y = p.y;
+    z = p.z;
+  });
+}
+void setCameraLocalSpace(float lxx, float lxy, float lxz, float lyx, float lyy, float lyz, float lzx, float lzy,
+                         float lzz) {
+  guardedVoid("setCameraLocalSpace", [&] {
+    LocalSpace& ls = R().cam().ls;
+    ls.x = f3{lxx, lxy, lxz};
+    ls.y = f3{lyx, lyy, lyz};
+    ls.z = f3{lzx, lzy, lzz};
+  });
+}
+
+// DataRecordCamera.h:57-81.
+static f3 toLocal(const LocalSpace& ls, f3 v) {
+  return f3{v.x * ls.x.x + v.y * ls.y.x + v.z * ls.z.x, v.x * ls.x.y + v.y * ls.y.y + v.z * ls.z.y,
+            v.x * ls.x.z + v.y * ls.y.z + v.z * ls.z.z};
+}
+static void rotateCam(Camera& c, float angle, f3 axis) {
+  c.ls.x = rotateAboutAxis(c.ls.x, angle, axis);
+  c.ls.y = rotateAboutAxis(c.ls.y, angle, axis);
+  c.ls.z = rotateAboutAxis(c.ls.z, angle, axis);
+}
+static void moveCam(Camera& c, f3 s) { c.position = f3{c.position.x + s.x, c.position.y + s.y, c.position.z + s.z}; }
+
+void rotateCameraAround(float angle, float x, float y, float z) {
+  guardedVoid("rotateCameraAround", [&] { rotateCam(R().cam(), angle, f3{x, y, z}); });
+}
+void rotateCameraLocallyAround(float angle, float x, float y, float z) {
+  guardedVoid("rotateCameraLocallyAround", [&] {
+    Camera& c = R().cam();
+    rotateCam(c, angle, toLocal(c.ls, f3{x, y, z}));
+  });
+}
+void translateCamera(float x, float y, float z) {
+  guardedVoid("translateCamera", [&] { moveCam(R().cam(), f3{x, y, z}); });
+}
+void translateCameraLocally(float x, float y, float z) {
+  guardedVoid("translateCameraLocally", [&] {
+    Camera& c = R().cam();
+    moveCam(c, toLocal(c.ls, f3{x, y, z}));
+  });
+}
+void resetCameraPose(void) {
+  guardedVoid("resetCameraPose", [&] {
+    Camera& c = R().cam();
+    c.ls = LocalSpace{};
+    c.position = f3{};
+  });
+}
+void setCameraPose(float posX, float posY, float posZ, float rotX, float rotY, float rotZ) {
+  // libEyeRenderer.cpp:380-388: reset, rotate about world X, Y, Z, translate.
+  guardedVoid("setCameraPose", [&] {
+    Camera& c = R().cam();
+    c.ls = LocalSpace{};
+    c.position = f3{};
+    rotateCam(c, rotX, f3{1, 0, 0});
+    rotateCam(c, rotY, f3{0, 1, 0});
+    rotateCam(c, rotZ, f3{0, 0, 1});
+    moveCam(c, f3{posX, posY, posZ});
+  });
+}
+
+bool isCompoundEyeActive(void) { return R().compoundActive(); }
+
+void setCurrentEyeSamplesPerOmmatidium(int s) {
+  guardedVoid("setCurrentEyeSamplesPerOmmatidium", [&] {
+    Renderer& r = R();
+    if (!r.compoundActive()) return;
+    r.scene.cameras[r.current].spp = std::max(1, s);
+    // Reallocating the generator states resets them (CompoundEye.cpp:171-179).
+    EyeDev& e = r.eyes[r.current];
+    e.rng.release();
+    e.spp = 0;
+    e.configured = false;
+  });
+}
+int getCurrentEyeSamplesPerOmmatidium(void) {
+  Renderer& r = R();
+  if (!r.compoundActive()) return -1;
+  return r.scene.cameras[r.current].spp;
+}
+void changeCurrentEyeSamplesPerOmmatidiumBy(int s) {
+  Renderer& r = R();
+  if (!r.compoundActive()) return;
+  setCurrentEyeSamplesPerOmmatidium(r.scene.cameras[r.current].spp + s);
+}
+size_t getCurrentEyeOmmatidialCount(void) {
+  Renderer& r = R();
+  if (!r.compoundActive()) return 0;
+  return r.scene.cameras[r.current].omm.size();
+}
+void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
+  guardedVoid("setOmmatidia", [&] {
+    Renderer& r = R();
+    if (!r.compoundActive()) return;
+    if (count && !omms) throw std::runtime_error("null ommatidium array");
+    Camera& c = r.scene.cameras[r.current];
+    std::vector<Ommatidium> v(count);
+    for (size_t i = 0; i < count; ++i) {
+      const OmmatidiumPacket& p = omms[i];
+      v[i] = Ommatidium{f3{p.posX, p.posY, p.posZ}, f3{p.dirX, p.dirY, p.dirZ}, p.acceptanceAngle, p.focalpointOffset};
+    }
+    EyeDev& e = r.eyes[r.current];
+    if (count != c.omm.size()) {
+      // A count change reallocates every eye buffer and resets the streams
+      // (CompoundEye.cpp:35-48); the same count only copies the records in.
+      e.release();
+    } else if (e.omm.ptr && count) {
+      check(cudaMemcpyAsync(e.omm.ptr, v.data(), sizeof(Ommatidium) * count, cudaMemcpyHostToDevice, r.stream()),
+            "cudaMemcpy");
+      check(cudaStreamSynchronize(r.stream()), "ommatidia upload");
+    }
+    c.omm = std::move(v);
+  });
+}
+const char* getCurrentEyeDataPath(void) {
+  Renderer& r = R();
+  if (!r.compoundActive()) return "";
+  return r.scene.cameras[r.current].eyeDataPath.c_str();
+}
+void setCurrentEyeShaderName(char* name) {
+  guardedVoid("setCurrentEyeShaderName", [&] {
+    Renderer& r = R();
+    if (!r.compoundActive() || !name) return;
+    r.scene.cameras[r.current].projection = name;
+  });
+}
+
+bool isInsideHitGeometry(float x, float y, float z, char* name) {
+  return guarded(
+      "isInsideHitGeometry",
+      [&]() -> bool {
+        if (!name) return false;
+        for (const HitboxMesh& h : R().scene.hitboxes)
+          if (h.name == name) return pointInsideHitbox(h, f3{x, y, z});
+        std::cerr << "WARNING: No hitbox with the given name \"" << name << "\" is present in the scene." << std::endl;
+        return false;
+      },
+      false);
+}
+
+static float3 boundsByName(const char* name, bool wantMax) {
+  if (!name) return make_float3(0.f, 0.f, 0.f);
+  const SceneData& s = R().scene;
+  for (const HitboxMesh& h : s.hitboxes)
+    if (h.name == name) {
+      const f3 v = wantMax ? h.worldMax : h.worldMin;
+      return make_float3(v.x, v.y, v.z);
+    }
+  for (const MeshPrim& m : s.meshes)
+    if (m.name == name) {
+      const f3 v = wantMax ? m.worldMax : m.worldMin;
+      return make_float3(v.x, v.y, v.z);
+    }
+  return make_float3(0.f, 0.f, 0.f);
+}
+float3 getGeometryMaxBounds(char* name) { return boundsByName(name, true); }
+float3 getGeometryMinBounds(char* name) { return boundsByName(name, false); }
+
+int crGetLastError(char* buf, size_t len) {
+  const int n = static_cast<int>(g_lastError.size());
+  if (buf && len) {
+    const size_t k = std::min(len - 1, g_lastError.size());
+    std::memcpy(buf, g_lastError.data(), k);
+    buf[k] = '\0';
+  }
+  g_lastError.clear();
+  return n;
+}
+
+int getOmmatidialColoursF32(float* out) {
+  return guarded(
+      "getOmmatidialColoursF32",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        EyeDev& e = r.eyes[r.current];
+        if (!e.haveSums) throw std::runtime_error("the current eye has not been rendered yet");
+        if (!out) throw std::runtime_error("null output");
+        if (e.N) {
+          check(cudaMemcpyAsync(out, e.sums.ptr, sizeof(float) * 3 * e.N, cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+          check(cudaStreamSynchronize(r.stream()), "colour download");
+        }
+        return 0;
+      },
+      -1);
+}
+
+int crRenderPoses(const float* poses, size_t count, float* out) {
+  return guarded(
+      "crRenderPoses",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (count == 0) return 0;
+        if (!poses || !out) throw std::runtime_error("null pose or output array");
+        EyeDev& e = r.syncEye(r.current);
+        std::vector<float> p16(16 * count);
+        for (size_t i = 0; i < count; ++i)
+          for (int k = 0; k < 4; ++k) {
+            p16[16 * i + 4 * k + 0] = poses[12 * i + 3 * k + 0];
+            p16[16 * i + 4 * k + 1] = poses[12 * i + 3 * k + 1];
+            p16[16 * i + 4 * k + 2] = poses[12 * i + 3 * k + 2];
+            p16[16 * i + 4 * k + 3] = 0.f;
+          }
+        r.poses.ensure(4 * count);
+        const size_t outFloats = 3 * count * e.N;
+        r.batchOut.ensure(std::max<size_t>(1, outFloats));
+        check(cudaMemcpyAsync(r.poses.ptr, p16.data(), p16.size() * sizeof(float), cudaMemcpyHostToDevice, r.stream()),
+              "cudaMemcpy");
+        r.renderDevicePoses(e, r.poses.ptr, count, r.batchOut.ptr, nullptr);
+        if (outFloats)
+          check(cudaMemcpyAsync(out, r.batchOut.ptr, outFloats * sizeof(float), cudaMemcpyDeviceToHost, r.stream()),
+                "cudaMemcpy");
+        // The last pose's colours become the eye's current frame.
+        if (e.N)
+          check(cudaMemcpyAsync(e.sums.ptr, r.batchOut.ptr + 3 * (count - 1) * e.N, 3 * e.N * sizeof(float),
+                                cudaMemcpyDeviceToDevice, r.stream()),
+                "cudaMemcpy");
+        e.haveSums = true;
+        r.checkErrWord();
+        return 0;
+      },
+      -1);
+}
+
+int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out) {
+  return guarded(
+      "crRenderPosesDevice",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (count == 0) return 0;
+        if (!d_poses || !d_out) throw std::runtime_error("null pose or output pointer");
+        EyeDev& e = r.syncEye(r.current);
+        r.renderDevicePoses(e, reinterpret_cast<const float4*>(d_poses), count, d_out, nullptr);
+        return 0;
+      },
+      -1);
+}
+
+int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, double* trisPerRay) {
+  return guarded(
+      "crMeasureTraversal",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (count == 0 || !d_poses) throw std::runtime_error("no poses");
+        EyeDev& e = r.syncEye(r.current);
+        DevBuf<unsigned long long> st;
+        st.ensure(2);
+        DevBuf<float> out;
+        out.ensure(std::max<size_t>(1, 3 * count * e.N));
+        check(cudaMemsetAsync(st.ptr, 0, 2 * sizeof(unsigned long long), r.stream()), "cudaMemset");
+        r.renderDevicePoses(e, reinterpret_cast<const float4*>(d_poses), count, out.ptr, nullptr, st.ptr);
+        unsigned long long h[2] = {0, 0};
+        check(cudaMemcpyAsync(h, st.ptr, sizeof(h), cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        r.checkErrWord();
+        const double rays = static_cast<double>(count) * e.N * e.spp;
+        if (nodesPerRay) *nodesPerRay = rays > 0 ? static_cast<double>(h[0]) / rays : 0.0;
+        if (trisPerRay) *trisPerRay = rays > 0 ? static_cast<double>(h[1]) / rays : 0.0;
+        st.release();
+        out.release();
+        return 0;
+      },
+      -1);
+}
+
+int crSetStream(void* stream) {
+  R().userStream = static_cast<cudaStream_t>(stream);
+  return 0;
+}
+
+int crSynchronize(void) {
+  return guarded(
+      "crSynchronize",
+      [&]() -> int {
+        Renderer& r = R();
+        check(cudaStreamSynchronize(r.stream()), "synchronize");
+        r.checkErrWord();
+        return 0;
+      },
+      -1);
+}
+
+int crRenderFrameRecorded(void* records) {
+  return guarded(
+      "crRenderFrameRecorded",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (!records) throw std::runtime_error("null record buffer");
+        Camera& c = r.cam();
+        EyeDev& e = r.syncEye(r.current);
+        const size_t n = static_cast<size_t>(e.N) * e.spp;
+        DevBuf<RayRecord> rec;
+        rec.ensure(std::max<size_t>(1, n));
+        float p16[16];
+        Renderer::packPose(c, p16);
+        r.poses.ensure(4);
+        check(cudaMemcpyAsync(r.poses.ptr, p16, sizeof(p16), cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
+        r.renderDevicePoses(e, r.poses.ptr, 1, e.sums.ptr, rec.ptr);
+        e.haveSums = true;
+        if (n) check(cudaMemcpyAsync(records, rec.ptr, n * sizeof(RayRecord), cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        r.checkErrWord();
+        rec.release();
+        return 0;
+      },
+      -1);
+}
+
+size_t crGetTriangleCount(void) { return R().loaded ? R().scene.triangleCount() : 0; }
+
+int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexColour) {
+  Renderer& r = R();
+  if (!r.loaded) {
+    setError("crGetSceneTriangles: no scene loaded");
+    return -1;
+  }
+  const SceneData& s = r.scene;
+  if (verts) std::memcpy(verts, s.triVerts.data(), s.triVerts.size() * sizeof(float));
+  if (colours) std::memcpy(colours, s.triColours.data(), s.triColours.size() * sizeof(float));
+  if (usesVertexColour) std::memcpy(usesVertexColour, s.triUsesVertexColour.data(), s.triUsesVertexColour.size());
+  return 0;
+}
+
+int crGetCameraLocalSpace(float* a) {
+  return guarded(
+      "crGetCameraLocalSpace",
+      [&]() -> int {
+        const LocalSpace& ls = R().cam().ls;
+        const f3 v[3] = {ls.x, ls.y, ls.z};
+        for (int k = 0; k < 3; ++k) {
+          a[3 * k] = v[k].x;
+          a[3 * k + 1] = v[k].y;
+          a[3 * k + 2] = v[k].z;
+        }
+        return 0;
+      },
+      -1);
+}
+
+int crGetRandomStates(uint32_t* out) {
+  return guarded(
+      "crGetRandomStates",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        EyeDev& e = r.eyes[r.current];
+        if (!e.configured || !e.rng.ptr) return -1;
+        const size_t n = static_cast<size_t>(kRngPlanes) * e.N * e.spp;
+        check(cudaMemcpyAsync(out, e.rng.ptr, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        check(cudaStreamSynchronize(r.stream()), "state download");
+        return 0;
+      },
+      -1);
+}
+
+int crGetBvhStats(uint32_t* innerNodes, uint32_t* leaves, uint32_t* maxDepth) {
+  Renderer& r = R();
+  if (!r.loaded) return -1;
+  if (innerNodes) *innerNodes = r.bvhStats.innerNodes;
+  if (leaves) *leaves = r.bvhStats.leaves;
+  if (maxDepth) *maxDepth = r.bvhStats.maxDepth;
+  return 0;
+}
+
+}  // extern "C"
+
+void* getWindowPointer() { return nullptr; }

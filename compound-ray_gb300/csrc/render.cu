@@ -1,0 +1,581 @@
+// Compound-eye render kernels for sm_103a.
+//
+// One fused kernel per batch of poses: every warp owns up to 32 samples of
+// one ommatidium (or several whole ommatidia when spp < 32), keeps their
+// XORWOW states in registers across all poses of the batch, and per pose
+//   1. draws one normal and one uniform number per sample (cuRAND, as
+//      libEyeRenderer3/shaders.cu:680-695),
+//   2. builds the splayed ray (shaders.cu:648-709),
+//   3. finds the closest triangle in the BVH2 (replaces optixTrace,
+//      shaders.cu:110-137),
+//   4. shades it with the lighting-off whitted closest-hit program or the
+//      miss program (shaders.cu:740-811, cuda/LocalGeometry.h:55-156),
+//   5. scales by 1/spp (shaders.cu:730) and reduces the warp's samples with
+//      shuffles, replacing the per-sample compound buffer and the second
+//      summing launch (shaders.cu:341-347, 396-406).
+//
+// This translation unit is compiled with --use_fast_math, as the reference's
+// shaders are (CMakeLists.txt:154-159, 193), so the random draws, ray
+// directions and shading follow the same approximate maths.  The triangle
+// test alone runs on explicitly rounded PTX (add/mul/fma/div .rn without
+// .ftz) so that a CPU implementation can repeat it bit for bit.
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+
+#include <cstdint>
+
+#include "device_api.hpp"
+
+namespace cr {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Small float3 algebra with the operator forms of the reference shaders.
+// ---------------------------------------------------------------------------
+struct v3 {
+  float x, y, z;
+};
+__device__ __forceinline__ v3 mk(float x, float y, float z) { return v3{x, y, z}; }
+__device__ __forceinline__ v3 operator+(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ v3 operator-(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ v3 operator*(float s, v3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ v3 operator*(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3 cross(v3 a, v3 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ v3 normalize(v3 v) {
+  const float invLen = 1.0f / sqrtf(dot(v, v));
+  return v * invLen;
+}
+
+// cos/sin of a float argument; with --use_fast_math these are the fast
+// hardware approximations, as in the reference build.
+__device__ __forceinline__ v3 rotatePoint(v3 point, float angle, v3 axis) {
+  return cosf(angle) * point + sinf(angle) * cross(axis, point) + (1 - cosf(angle)) * dot(axis, point) * axis;
+}
+
+// ---------------------------------------------------------------------------
+// Explicitly rounded single-precision operations (no FTZ, no contraction).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float xadd(float a, float b) {
+  float r;
+  asm("add.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float xsub(float a, float b) {
+  float r;
+  asm("sub.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float xmul(float a, float b) {
+  float r;
+  asm("mul.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float xfma(float a, float b, float c) {
+  float r;
+  asm("fma.rn.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float xdiv(float a, float b) {
+  float r;
+  asm("div.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float xneg(float a) { return __int_as_float(__float_as_int(a) ^ 0x80000000); }
+
+__device__ __forceinline__ float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+// Ray set up for the watertight triangle test (Woop, Benthin, Wald,
+// "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013) and the slab test.
+struct Ray {
+  float ox, oy, oz;
+  float idx, idy, idz;  // reciprocal direction for the slab test
+  int kx, ky, kz;
+  float nSx, nSy, Sz;  // -Sx, -Sy, Sz of the shear
+  float okx, oky, okz;
+};
+
+__device__ __forceinline__ float safeRcp(float d) {
+  const float tiny = 1e-20f;
+  const float dd = fabsf(d) < tiny ? copysignf(tiny, d) : d;
+  return xdiv(1.0f, dd);
+}
+
+__device__ __forceinline__ Ray setupRay(v3 o, v3 d) {
+  Ray r;
+  r.ox = o.x;
+  r.oy = o.y;
+  r.oz = o.z;
+  r.idx = safeRcp(d.x);
+  r.idy = safeRcp(d.y);
+  r.idz = safeRcp(d.z);
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = 0;
+  float m = ax;
+  if (ay > m) {
+    kz = 1;
+    m = ay;
+  }
+  if (az > m) kz = 2;
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  const float dkz = sel3(d.x, d.y, d.z, kz);
+  if (dkz < 0.0f) {
+    const int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  r.kx = kx;
+  r.ky = ky;
+  r.kz = kz;
+  r.nSx = xneg(xdiv(sel3(d.x, d.y, d.z, kx), dkz));
+  r.nSy = xneg(xdiv(sel3(d.x, d.y, d.z, ky), dkz));
+  r.Sz = xdiv(1.0f, dkz);
+  r.okx = sel3(o.x, o.y, o.z, kx);
+  r.oky = sel3(o.x, o.y, o.z, ky);
+  r.okz = sel3(o.x, o.y, o.z, kz);
+  return r;
+}
+
+struct Hit {
+  float t;
+  uint32_t id;   // original triangle id, 0xffffffff = none
+  uint32_t pos;  // BVH position of the triangle
+  float U, V, W, det;
+};
+
+// Watertight test of one triangle; updates `h` when the hit is closer in the
+// (t, id) order and lies in [tmin, h.t].
+__device__ __forceinline__ void testTriangle(const Ray& r, float4 v0, float4 v1, float4 v2, uint32_t pos, float tmin,
+                                             Hit& h) {
+  const float Akx = xsub(sel3(v0.x, v0.y, v0.z, r.kx), r.okx);
+  const float Aky = xsub(sel3(v0.x, v0.y, v0.z, r.ky), r.oky);
+  const float Akz = xsub(sel3(v0.x, v0.y, v0.z, r.kz), r.okz);
+  const float Bkx = xsub(sel3(v1.x, v1.y, v1.z, r.kx), r.okx);
+  const float Bky = xsub(sel3(v1.x, v1.y, v1.z, r.ky), r.oky);
+  const float Bkz = xsub(sel3(v1.x, v1.y, v1.z, r.kz), r.okz);
+  const float Ckx = xsub(sel3(v2.x, v2.y, v2.z, r.kx), r.okx);
+  const float Cky = xsub(sel3(v2.x, v2.y, v2.z, r.ky), r.oky);
+  const float Ckz = xsub(sel3(v2.x, v2.y, v2.z, r.kz), r.okz);
+  const float Ax = xfma(r.nSx, Akz, Akx);
+  const float Ay = xfma(r.nSy, Akz, Aky);
+  const float Bx = xfma(r.nSx, Bkz, Bkx);
+  const float By = xfma(r.nSy, Bkz, Bky);
+  const float Cx = xfma(r.nSx, Ckz, Ckx);
+  const float Cy = xfma(r.nSy, Ckz, Cky);
+  float U = xfma(Cx, By, xneg(xmul(Cy, Bx)));
+  float V = xfma(Ax, Cy, xneg(xmul(Ay, Cx)));
+  float W = xfma(Bx, Ay, xneg(xmul(By, Ax)));
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    const double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+    const double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+    const double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+    U = __double2float_rn(__dsub_rn(CxBy, CyBx));
+    V = __double2float_rn(__dsub_rn(AxCy, AyCx));
+    W = __double2float_rn(__dsub_rn(BxAy, ByAx));
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return;
+  const float det = xadd(xadd(U, V), W);
+  if (det == 0.0f) return;
+  const float Az = xmul(r.Sz, Akz);
+  const float Bz = xmul(r.Sz, Bkz);
+  const float Cz = xmul(r.Sz, Ckz);
+  const float T = xfma(U, Az, xfma(V, Bz, xmul(W, Cz)));
+  const float t = xdiv(T, det);
+  if (!(t >= tmin && t <= h.t)) return;
+  const uint32_t id = __float_as_uint(v0.w);
+  if (t == h.t && id >= h.id) return;
+  h.t = t;
+  h.id = id;
+  h.pos = pos;
+  h.U = U;
+  h.V = V;
+  h.W = W;
+  h.det = det;
+}
+
+constexpr int kStackSize = 64;
+// Relative widening of slab intervals so that rounding never culls a box
+// holding a hit the triangle test would accept.
+constexpr float kSlabPad = 4.76837158e-07f;  // 2^-21
+
+__device__ __forceinline__ void slab(float lo, float hi, float o, float id, float& tn, float& tf) {
+  const float a = (lo - o) * id;
+  const float b = (hi - o) * id;
+  tn = fminf(a, b);
+  tf = fmaxf(a, b);
+}
+
+// Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
+template <bool kCount>
+__device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
+                                             uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests) {
+  h.t = tmax;
+  h.id = 0xffffffffu;
+  h.pos = 0;
+  if (sc.triCount == 0) return;
+  int stack[kStackSize];
+  int sp = 0;
+  int node = 0;
+  for (;;) {
+    if (node >= 0) {
+      if (kCount) ++nodeVisits;
+      const float4* n = sc.nodes + 4 * node;
+      const float4 n0 = __ldg(n + 0);
+      const float4 n1 = __ldg(n + 1);
+      const float4 n2 = __ldg(n + 2);
+      const int4 n3 = __ldg(reinterpret_cast<const int4*>(n + 3));
+      float a0, b0, a1, b1, a2, b2;
+      slab(n0.x, n0.y, r.ox, r.idx, a0, b0);
+      slab(n0.z, n0.w, r.oy, r.idy, a1, b1);
+      slab(n2.x, n2.y, r.oz, r.idz, a2, b2);
+      float tn0 = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
+      float tf0 = fminf(fminf(b0, b1), fminf(b2, h.t));
+      slab(n1.x, n1.y, r.ox, r.idx, a0, b0);
+      slab(n1.z, n1.w, r.oy, r.idy, a1, b1);
+      slab(n2.z, n2.w, r.oz, r.idz, a2, b2);
+      float tn1 = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
+      float tf1 = fminf(fminf(b0, b1), fminf(b2, h.t));
+      tn0 = fmaf(-fabsf(tn0), kSlabPad, tn0);
+      tf0 = fmaf(fabsf(tf0), kSlabPad, tf0);
+      tn1 = fmaf(-fabsf(tn1), kSlabPad, tn1);
+      tf1 = fmaf(fabsf(tf1), kSlabPad, tf1);
+      const bool hit0 = tn0 <= tf0;
+      const bool hit1 = tn1 <= tf1;
+      if (hit0 && hit1) {
+        int first = n3.x, second = n3.y;
+        if (tn1 < tn0) {
+          first = n3.y;
+          second = n3.x;
+        }
+        if (sp >= kStackSize) {
+          atomicOr(errFlag, kErrStackOverflow);
+          return;
+        }
+        stack[sp++] = second;
+        node = first;
+        continue;
+      }
+      if (hit0) {
+        node = n3.x;
+        continue;
+      }
+      if (hit1) {
+        node = n3.y;
+        continue;
+      }
+    } else {
+      const uint32_t code = ~static_cast<uint32_t>(node);
+      const uint32_t first = code >> 3;
+      const uint32_t count = (code & 7u) + 1u;
+      if (kCount) triTests += count;
+      for (uint32_t k = 0; k < count; ++k) {
+        const float4* t = sc.tris + 3 * (first + k);
+        testTriangle(r, __ldg(t), __ldg(t + 1), __ldg(t + 2), first + k, tmin, h);
+      }
+    }
+    if (sp == 0) return;
+    node = stack[--sp];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Shading (lighting off): closest hit and miss programs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ v3 linearize(v3 c) { return mk(powf(c.x, 2.2f), powf(c.y, 2.2f), powf(c.z, 2.2f)); }
+
+__device__ __forceinline__ v3 shadeHit(const DevScene& sc, uint32_t pos, float b1, float b2) {
+  const float4* s = sc.shade + 3 * pos;
+  const float4 c0 = __ldg(s);
+  if (c0.w == 0.0f) return mk(c0.x, c0.y, c0.z);  // material base colour
+  const float4 c1 = __ldg(s + 1);
+  const float4 c2 = __ldg(s + 2);
+  const float w0 = 1.0f - b1 - b2;
+  const v3 C = mk(w0 * c0.x + b1 * c1.x + b2 * c2.x, w0 * c0.y + b1 * c1.y + b2 * c2.y, w0 * c0.z + b1 * c1.z + b2 * c2.z);
+  return linearize(C);
+}
+
+#define CR_PI_F 3.14159265358979323846f
+
+__device__ __forceinline__ v3 shadeMiss(int miss, v3 dirIn) {
+  const v3 dir = normalize(dirIn);
+  if (miss == 1) {
+    const float mix = fminf(fmaxf(0.0f, (asinf(dir.y) * 2.0f) / CR_PI_F), 1.0f);
+    const v3 upper = mk(1.0f / 255.0f, 31.0f / 255.0f, 117.0f / 255.0f);
+    const v3 lower = mk(143.0f / 255.0f * 0.8f, 179.0f / 255.0f * 0.8f, 203.0f / 255.0f * 0.8f);
+    return lower * (1.0f - mix) + upper * mix;
+  }
+  v3 c = mk((atan2f(dir.z, dir.x) + CR_PI_F) / (CR_PI_F * 2.0f), (asinf(dir.y) + CR_PI_F / 2.0f) / CR_PI_F, 0.0f);
+  const float border = 0.01f;
+  if (fabsf(dir.x) < border || fabsf(dir.y) < border || fabsf(dir.z) < border) c = mk(0.f, 0.f, 0.f);
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Generator state transfer (structure of arrays, see DevEye).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void loadState(const uint32_t* rng, size_t plane, size_t idx, curandState& st) {
+  st.d = rng[idx];
+  st.v[0] = rng[plane + idx];
+  st.v[1] = rng[2 * plane + idx];
+  st.v[2] = rng[3 * plane + idx];
+  st.v[3] = rng[4 * plane + idx];
+  st.v[4] = rng[5 * plane + idx];
+  st.boxmuller_flag = static_cast<int>(rng[6 * plane + idx]);
+  st.boxmuller_flag_double = 0;
+  st.boxmuller_extra = __uint_as_float(rng[7 * plane + idx]);
+  st.boxmuller_extra_double = 0.0;
+}
+__device__ __forceinline__ void storeState(uint32_t* rng, size_t plane, size_t idx, const curandState& st) {
+  rng[idx] = st.d;
+  rng[plane + idx] = st.v[0];
+  rng[2 * plane + idx] = st.v[1];
+  rng[3 * plane + idx] = st.v[2];
+  rng[4 * plane + idx] = st.v[3];
+  rng[5 * plane + idx] = st.v[4];
+  rng[6 * plane + idx] = static_cast<uint32_t>(st.boxmuller_flag);
+  rng[7 * plane + idx] = __float_as_uint(st.boxmuller_extra);
+}
+
+__global__ void rngInitKernel(DevEye eye, uint32_t* errFlag) {
+  const size_t total = static_cast<size_t>(eye.N) * eye.spp;
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const uint32_t o = static_cast<uint32_t>(idx / eye.spp);
+  const uint32_t s = static_cast<uint32_t>(idx % eye.spp);
+  // Same stream as the reference's id = launch_dims.x * launch_idx.y + launch_idx.x.
+  const int id = static_cast<int>(eye.N * s + o);
+  curandState st;
+  curand_init(42, id, 0, &st);
+  if (st.boxmuller_flag_double != 0) atomicOr(errFlag, kErrRngDoubleFlag);
+  storeState(eye.rng, total, idx, st);
+}
+
+__constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
+
+// kMode: 0 = render, 1 = render and record every ray, 2 = render and count
+// node visits / triangle tests into stats[0..1].
+template <int kMode>
+__global__ void __launch_bounds__(128) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
+                                                    uint32_t P, WarpPlan plan, float* __restrict__ out,
+                                                    float* __restrict__ scratch, uint32_t* errFlag,
+                                                    RayRecord* __restrict__ rec, unsigned long long* stats) {
+  constexpr bool kRecord = kMode == 1;
+  constexpr bool kCount = kMode == 2;
+  uint32_t nodeVisits = 0, triTests = 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t task = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (task >= plan.tasks) return;  // whole warps exit together
+  const uint32_t group = static_cast<uint32_t>(task / plan.chunks);
+  const uint32_t chunk = static_cast<uint32_t>(task % plan.chunks);
+  const uint32_t o = group * plan.ommPerWarp + lane / plan.segWidth;
+  const uint32_t s = chunk * 32u + lane % plan.segWidth;
+  const bool valid = o < eye.N && s < eye.spp;
+  const size_t plane = static_cast<size_t>(eye.N) * eye.spp;
+  const size_t sidx = static_cast<size_t>(o) * eye.spp + s;
+
+  curandState st;
+  v3 axis = mk(0.f, 1.f, 0.f), relPos = mk(0.f, 0.f, 0.f), perp = mk(0.f, 0.f, 1.f);
+  float sd = 0.f, fpo = 0.f;
+  if (valid) {
+    loadState(eye.rng, plane, sidx, st);
+    const float4 a = __ldg(eye.omm + 2 * o);
+    const float4 b = __ldg(eye.omm + 2 * o + 1);
+    axis = mk(a.w, b.x, b.y);
+    const v3 pos = mk(a.x, a.y, a.z);
+    fpo = b.w;
+    sd = b.z / FWHM_SD_RATIO;
+    // generateOffsetRay's perpendicular axis (shaders.cu:655-657), including
+    // its test on the component sum.
+    perp = cross(mk(0.0f, 1.0f, 0.0f), axis);
+    perp = (perp.x + perp.y + perp.z == 0.0f) ? mk(0.0f, 0.0f, 1.0f) : normalize(perp);
+    relPos = pos - normalize(axis) * fpo;
+  }
+  const float invSpp = 1.0f / static_cast<float>(eye.spp);
+
+  for (uint32_t p = 0; p < P; ++p) {
+    v3 col = mk(0.f, 0.f, 0.f);
+    if (valid) {
+      const float4* pp = poses + 4 * p;
+      const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
+      const float nd = curand_normal(&st);
+      const float ud = curand_uniform(&st);
+      const float splayAngle = nd * sd;
+      const float axisAngle = ud * CR_PI_F;
+      const v3 splayed = rotatePoint(axis, splayAngle, perp);
+      const v3 rel = rotatePoint(splayed, axisAngle, axis);
+      const v3 org = mk(P0.x, P0.y, P0.z) + mk(X.x, X.y, X.z) * relPos.x + mk(Y.x, Y.y, Y.z) * relPos.y +
+                     mk(Z.x, Z.y, Z.z) * relPos.z;
+      const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
+      const Ray ray = setupRay(org, dir);
+      Hit h;
+      traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+      v3 c;
+      float b1 = 0.f, b2 = 0.f;
+      if (h.id != 0xffffffffu) {
+        b1 = xdiv(h.V, h.det);
+        b2 = xdiv(h.W, h.det);
+        c = shadeHit(sc, h.pos, b1, b2);
+      } else {
+        c = shadeMiss(sc.miss, dir);
+      }
+      if (kRecord) {
+        RayRecord& R = rec[(static_cast<size_t>(p) * eye.N + o) * eye.spp + s];
+        R.normalDraw = nd;
+        R.uniformDraw = ud;
+        R.ox = org.x;
+        R.oy = org.y;
+        R.oz = org.z;
+        R.dx = dir.x;
+        R.dy = dir.y;
+        R.dz = dir.z;
+        R.t = h.id != 0xffffffffu ? h.t : -1.0f;
+        R.b1 = b1;
+        R.b2 = b2;
+        R.hitId = h.id != 0xffffffffu ? static_cast<int32_t>(h.id) : -1;
+        R.r = c.x;
+        R.g = c.y;
+        R.b = c.z;
+        R.pad = 0.f;
+      }
+      col = c * invSpp;
+    }
+    // Segmented butterfly reduction over the samples of each ommatidium.
+    for (uint32_t m = plan.segWidth >> 1; m >= 1u; m >>= 1) {
+      col.x += __shfl_xor_sync(0xffffffffu, col.x, static_cast<int>(m));
+      col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
+      col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
+    }
+    if ((lane % plan.segWidth) == 0u && o < eye.N) {
+      float* dst = plan.chunks == 1 ? out + (static_cast<size_t>(p) * eye.N + o) * 3
+                                    : scratch + ((static_cast<size_t>(p) * eye.N + o) * plan.chunks + chunk) * 3;
+      dst[0] = col.x;
+      dst[1] = col.y;
+      dst[2] = col.z;
+    }
+  }
+  if (valid) storeState(eye.rng, plane, sidx, st);
+  if (kCount) {
+    unsigned long long nv = nodeVisits, tt = triTests;
+    for (int m = 16; m >= 1; m >>= 1) {
+      nv += __shfl_xor_sync(0xffffffffu, nv, m);
+      tt += __shfl_xor_sync(0xffffffffu, tt, m);
+    }
+    if (lane == 0) {
+      atomicAdd(stats, nv);
+      atomicAdd(stats + 1, tt);
+    }
+  }
+}
+
+// Sums the per-chunk partials of each (pose, ommatidium) in chunk order.
+__global__ void combineChunksKernel(const float* __restrict__ scratch, uint32_t chunks, size_t count,
+                                    float* __restrict__ out) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float* src = scratch + i * chunks * 3;
+  float x = 0.f, y = 0.f, z = 0.f;
+  for (uint32_t c = 0; c < chunks; ++c) {
+    x += src[3 * c];
+    y += src[3 * c + 1];
+    z += src[3 * c + 2];
+  }
+  out[3 * i] = x;
+  out[3 * i + 1] = y;
+  out[3 * i + 2] = z;
+}
+
+__device__ __forceinline__ uchar4 makeColour(float r, float g, float b) {
+  // make_color (shaders.cu:180-189): clamp, gamma 1/2.2 (a double constant
+  // narrowed to float), scale to 255 and truncate.
+  const float invGamma = static_cast<float>(1.0 / static_cast<double>(2.2f));
+  return make_uchar4(static_cast<uint8_t>(powf(fminf(fmaxf(r, 0.0f), 1.0f), invGamma) * 255.0f),
+                     static_cast<uint8_t>(powf(fminf(fmaxf(g, 0.0f), 1.0f), invGamma) * 255.0f),
+                     static_cast<uint8_t>(powf(fminf(fmaxf(b, 0.0f), 1.0f), invGamma) * 255.0f), 255u);
+}
+
+__global__ void projectKernel(const float* __restrict__ sums, uint32_t N, uchar4* frame, int w, int h, int mode) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= w || y >= h) return;
+  if (mode == 0) {
+    // single_dimension_fast (shaders.cu:396-406): only row 0, x < N.
+    if (y > 0 || static_cast<uint32_t>(x) >= N) return;
+    frame[x] = makeColour(sums[3 * x], sums[3 * x + 1], sums[3 * x + 2]);
+    return;
+  }
+  // single_dimension (shaders.cu:375-390): every pixel, ommatidium x*N/w.
+  if (N == 0) return;
+  const uint32_t o = static_cast<uint32_t>((static_cast<uint64_t>(x) * N) / static_cast<uint64_t>(w));
+  frame[static_cast<size_t>(y) * w + x] = makeColour(sums[3 * o], sums[3 * o + 1], sums[3 * o + 2]);
+}
+
+}  // namespace
+
+WarpPlan planWarps(uint32_t N, uint32_t spp) {
+  WarpPlan p;
+  if (spp >= 32) {
+    p.segWidth = 32;
+    p.ommPerWarp = 1;
+    p.chunks = (spp + 31) / 32;
+  } else {
+    uint32_t w = 1;
+    while (w < spp) w <<= 1;
+    p.segWidth = w;
+    p.ommPerWarp = 32 / w;
+    p.chunks = 1;
+  }
+  const uint64_t groups = (static_cast<uint64_t>(N) + p.ommPerWarp - 1) / p.ommPerWarp;
+  p.tasks = groups * p.chunks;
+  return p;
+}
+
+size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P) {
+  const WarpPlan p = planWarps(N, spp);
+  if (p.chunks == 1) return 0;
+  return static_cast<size_t>(P) * N * p.chunks * 3;
+}
+
+cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t stream) {
+  const size_t total = static_cast<size_t>(eye.N) * eye.spp;
+  if (total == 0) return cudaSuccess;
+  const unsigned blocks = static_cast<unsigned>((total + 255) / 256);
+  rngInitKernel<<<blocks, 256, 0, stream>>>(eye, errFlag);
+  return cudaGetLastError();
+}
+
+cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* out,
+                         float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
+                         unsigned long long* stats) {
+  if (P == 0 || eye.N == 0) return cudaSuccess;
+  const WarpPlan plan = planWarps(eye.N, eye.spp);
+  if (plan.chunks > 1 && scratch == nullptr) return cudaErrorInvalidValue;
+  const uint64_t threads = plan.tasks * 32;
+  const unsigned block = 128;
+  const uint64_t blocks = (threads + block - 1) / block;
+  if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
+  const unsigned g = static_cast<unsigned>(blocks);
+  if (rec) {
+    renderKernel<1><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
+  } else if (stats) {
+    renderKernel<2><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats);
+  } else {
+    renderKernel<0><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || plan.chunks == 1) return e;
+  const size_t count = static_cast<size_t>(P) * eye.N;
+  combineChunksKernel<<<static_cast<unsigned>((count + 255) / 256), 256, 0, stream>>>(scratch, plan.chunks, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, int h, int mode, cudaStream_t stream) {
+  if (w <= 0 || h <= 0) return cudaSuccess;
+  dim3 grid((w + 127) / 128, h);
+  projectKernel<<<grid, 128, 0, stream>>>(sums, N, frame, w, h, mode);
+  return cudaGetLastError();
+}
+
+}  // namespace cr

@@ -1,0 +1,389 @@
+"""Seeded synthetic scenes, eyes and pose trajectories for the renderer.
+
+Everything is written as real glTF 2.0 + .eye files so the same inputs feed
+the C ABI (loadGlTFscene) and the CPU oracle.  Vertex colours are VEC4 float
+COLOR_0, the only colour form the reference shades from vertices besides
+u8/u16 VEC4 (libEyeRenderer3/MulticamScene.cpp:415-516).
+
+Workloads (all seeded from SEED with numpy's PCG64):
+  * small scene: 2-triangle grey ground (20 m square) + 64 axis-aligned boxes,
+    simple_sky; 1000-ommatidium Fibonacci-sphere eye of radius 1 mm,
+    acceptance 3 deg, 32 samples, one pose 0.5 m above the origin.
+  * terrain scene: 512 x 512-cell value-noise heightfield over 200 m
+    (2 m amplitude, 6 octaves) + 2000 cones of 32 triangles; 6000-ommatidium
+    sinewave-droplet eye (eyeGenerator/SinewaveDropletCoordinate.cpp:33-60),
+    acceptance 1.5-4 deg, 256 samples; 1024-pose random walk
+    (0.1 m steps, yaw noise 10 deg).
+"""
+import base64
+import json
+import math
+import os
+
+import numpy as np
+
+SEED = 20261203
+DEG = math.pi / 180.0
+
+
+# ---------------------------------------------------------------------------
+# File writers
+# ---------------------------------------------------------------------------
+def write_eye(path, pos, dirs, aa, fpo):
+    """Writes a .eye file: 8 space-separated floats per line
+    (data/eyes/eye-specification.txt), printed with 9 significant digits so
+    every float32 round-trips exactly."""
+    pos = np.asarray(pos, np.float32)
+    dirs = np.asarray(dirs, np.float32)
+    aa = np.broadcast_to(np.asarray(aa, np.float32), (len(pos),))
+    fpo = np.broadcast_to(np.asarray(fpo, np.float32), (len(pos),))
+    with open(path, "w") as f:
+        for i in range(len(pos)):
+            vals = [pos[i, 0], pos[i, 1], pos[i, 2], dirs[i, 0], dirs[i, 1], dirs[i, 2], aa[i], fpo[i]]
+            f.write(" ".join("%.9g" % float(v) for v in vals) + "\n")
+
+
+def read_eye(path):
+    """Reads a .eye file into an (N, 8) float32 array."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            toks = [t for t in line.split(" ") if t != ""]
+            rows.append([float(t) for t in toks[:8]])
+    return np.asarray(rows, np.float32).reshape(-1, 8)
+
+
+class GltfBuilder:
+    """Accumulates meshes/cameras into one glTF document with one buffer."""
+
+    def __init__(self):
+        self.blob = bytearray()
+        self.accessors = []
+        self.views = []
+        self.meshes = []
+        self.nodes = []
+        self.cameras = []
+        self.materials = []
+        self.scene_extras = {}
+
+    def _view(self, data):
+        while len(self.blob) % 16:
+            self.blob.append(0)
+        off = len(self.blob)
+        self.blob += data
+        self.views.append({"buffer": 0, "byteOffset": off, "byteLength": len(data)})
+        return len(self.views) - 1
+
+    def accessor(self, arr, comp_type, typ, minmax=False):
+        arr = np.ascontiguousarray(arr)
+        view = self._view(arr.tobytes())
+        count = arr.shape[0] if typ != "SCALAR" else arr.size
+        acc = {"bufferView": view, "componentType": comp_type, "count": int(count), "type": typ}
+        if minmax:
+            acc["min"] = [float(v) for v in arr.min(axis=0)]
+            acc["max"] = [float(v) for v in arr.max(axis=0)]
+        self.accessors.append(acc)
+        return len(self.accessors) - 1
+
+    def material(self, rgba, name="mat"):
+        self.materials.append({"name": name, "pbrMetallicRoughness": {"baseColorFactor": [float(c) for c in rgba]}})
+        return len(self.materials) - 1
+
+    def mesh(self, name, positions, indices, colours=None, material=None, translation=None, rotation=None,
+             scale=None, matrix=None, index_type=None, colour_type=5126, extras=None):
+        positions = np.asarray(positions, np.float32).reshape(-1, 3)
+        attrs = {"POSITION": self.accessor(positions, 5126, "VEC3", minmax=True)}
+        if colours is not None:
+            colours = np.asarray(colours)
+            if colour_type == 5126:
+                attrs["COLOR_0"] = self.accessor(colours.astype(np.float32), 5126, "VEC4" if colours.shape[1] == 4 else "VEC3")
+            elif colour_type == 5123:
+                attrs["COLOR_0"] = self.accessor(colours.astype(np.uint16), 5123, "VEC4")
+            else:
+                attrs["COLOR_0"] = self.accessor(colours.astype(np.uint8), 5121, "VEC4")
+        indices = np.asarray(indices).reshape(-1)
+        if index_type is None:
+            index_type = 5123 if positions.shape[0] <= 65535 else 5125
+        idx_dtype = {5121: np.uint8, 5123: np.uint16, 5125: np.uint32}[index_type]
+        prim = {"attributes": attrs, "indices": self.accessor(indices.astype(idx_dtype), index_type, "SCALAR")}
+        if material is not None:
+            prim["material"] = material
+        mesh = {"name": name, "primitives": [prim]}
+        if extras:
+            mesh["extras"] = extras
+        self.meshes.append(mesh)
+        node = {"name": name, "mesh": len(self.meshes) - 1}
+        for key, val in (("translation", translation), ("rotation", rotation), ("scale", scale), ("matrix", matrix)):
+            if val is not None:
+                node[key] = [float(v) for v in val]
+        self.nodes.append(node)
+        return len(self.nodes) - 1
+
+    def compound_camera(self, name, eye_file, projection="single_dimension_fast", translation=None, rotation=None):
+        self.cameras.append({"name": name, "type": "perspective",
+                             "perspective": {"yfov": 0.4, "znear": 0.1, "zfar": 100.0},
+                             "extras": {"compound-eye": "true", "compound-structure": eye_file,
+                                        "compound-projection": projection}})
+        node = {"name": name, "camera": len(self.cameras) - 1}
+        if translation is not None:
+            node["translation"] = [float(v) for v in translation]
+        if rotation is not None:
+            node["rotation"] = [float(v) for v in rotation]
+        self.nodes.append(node)
+        return len(self.nodes) - 1
+
+    def perspective_camera(self, name, translation=None):
+        self.cameras.append({"name": name, "type": "perspective",
+                             "perspective": {"yfov": 0.4, "znear": 0.1, "zfar": 100.0}})
+        node = {"name": name, "camera": len(self.cameras) - 1}
+        if translation is not None:
+            node["translation"] = [float(v) for v in translation]
+        self.nodes.append(node)
+        return len(self.nodes) - 1
+
+    def write(self, path, embed=True):
+        doc = {"asset": {"version": "2.0", "generator": "compound-ray_gb300 scenes.py"},
+               "scene": 0,
+               "scenes": [{"name": "Scene", "nodes": list(range(len(self.nodes))), "extras": self.scene_extras}],
+               "nodes": self.nodes, "meshes": self.meshes, "accessors": self.accessors,
+               "bufferViews": self.views}
+        if self.cameras:
+            doc["cameras"] = self.cameras
+        if self.materials:
+            doc["materials"] = self.materials
+        if embed:
+            uri = "data:application/octet-stream;base64," + base64.b64encode(bytes(self.blob)).decode()
+        else:
+            binname = os.path.splitext(os.path.basename(path))[0] + ".bin"
+            with open(os.path.join(os.path.dirname(path) or ".", binname), "wb") as f:
+                f.write(bytes(self.blob))
+            uri = binname
+        doc["buffers"] = [{"byteLength": len(self.blob), "uri": uri}]
+        with open(path, "w") as f:
+            json.dump(doc, f)
+        return path
+
+
+# ---------------------------------------------------------------------------
+# Geometry helpers
+# ---------------------------------------------------------------------------
+def fibonacci_sphere(n):
+    """n unit vectors on a Fibonacci (golden-angle) spiral."""
+    i = np.arange(n, dtype=np.float64) + 0.5
+    y = 1.0 - 2.0 * i / n
+    r = np.sqrt(np.maximum(0.0, 1.0 - y * y))
+    phi = i * math.pi * (3.0 - math.sqrt(5.0))
+    return np.stack([r * np.cos(phi), y, r * np.sin(phi)], axis=1)
+
+
+def box_mesh(lo, hi):
+    """8 corners and 12 triangles of an axis-aligned box."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    v = np.array([[x0, y0, z0], [x1, y0, z0], [x1, y1, z0], [x0, y1, z0],
+                  [x0, y0, z1], [x1, y0, z1], [x1, y1, z1], [x0, y1, z1]], np.float64)
+    f = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4],
+                  [3, 7, 6], [3, 6, 2], [0, 4, 7], [0, 7, 3], [1, 2, 6], [1, 6, 5]], np.int64)
+    return v, f
+
+
+def value_noise(nx, nz, octaves, rng):
+    """Sum of `octaves` bilinearly interpolated lattice-noise layers on an
+    (nx, nz) vertex grid, frequency doubling and amplitude halving per octave;
+    normalised to [-1, 1]."""
+    h = np.zeros((nx, nz))
+    amp = 1.0
+    for o in range(octaves):
+        cells = 4 * (2 ** o)
+        lat = rng.uniform(-1.0, 1.0, size=(cells + 1, cells + 1))
+        u = np.linspace(0.0, cells, nx)
+        w = np.linspace(0.0, cells, nz)
+        i0 = np.minimum(np.floor(u).astype(int), cells - 1)
+        j0 = np.minimum(np.floor(w).astype(int), cells - 1)
+        fu = (u - i0)[:, None]
+        fw = (w - j0)[None, :]
+        fu = fu * fu * (3 - 2 * fu)
+        fw = fw * fw * (3 - 2 * fw)
+        a = lat[i0][:, j0]
+        b = lat[i0 + 1][:, j0]
+        c = lat[i0][:, j0 + 1]
+        d = lat[i0 + 1][:, j0 + 1]
+        h += amp * ((a * (1 - fu) + b * fu) * (1 - fw) + (c * (1 - fu) + d * fu) * fw)
+        amp *= 0.5
+    h -= h.min()
+    h /= max(h.max(), 1e-12)
+    return 2.0 * h - 1.0
+
+
+def cone_mesh(cx, cy, cz, radius, height, segments=16):
+    """Cone with `segments` side and `segments` base triangles."""
+    ang = np.arange(segments) * (2 * math.pi / segments)
+    ring = np.stack([cx + radius * np.cos(ang), np.full(segments, cy), cz + radius * np.sin(ang)], axis=1)
+    apex = np.array([[cx, cy + height, cz]])
+    centre = np.array([[cx, cy, cz]])
+    verts = np.concatenate([ring, apex, centre])
+    a, c = segments, segments + 1
+    tris = []
+    for k in range(segments):
+        k1 = (k + 1) % segments
+        tris.append([k, a, k1])
+        tris.append([k, k1, c])
+    return verts, np.array(tris, np.int64)
+
+
+def droplet_eye(n, rng, wavelength=1.0, size=0.002):
+    """Ommatidia on the sinewave-droplet surface y = sin(wavelength * r)
+    over the square [-0.5, 0.5]^2, with the surface normal construction of
+    eyeGenerator/SinewaveDropletCoordinate.cpp:33-60 (a point pulled 1% towards
+    the centre gives the radial tangent; crossing with the vertical twice
+    gives the normal).  Points are a jittered grid; the whole eye is scaled to
+    `size` metres."""
+    side = int(math.ceil(math.sqrt(n)))
+    gx, gz = np.meshgrid((np.arange(side) + 0.5) / side - 0.5, (np.arange(side) + 0.5) / side - 0.5, indexing="ij")
+    pts = np.stack([gx.ravel(), gz.ravel()], axis=1)
+    pts = pts[rng.permutation(len(pts))[:n]]
+    pts += rng.uniform(-0.4 / side, 0.4 / side, size=pts.shape)
+    r = np.linalg.norm(pts, axis=1)
+    pos = np.stack([pts[:, 0], np.sin(wavelength * r), pts[:, 1]], axis=1)
+    inner = pts * 0.99
+    ri = np.linalg.norm(inner, axis=1)
+    inner3 = np.stack([inner[:, 0], np.sin(wavelength * ri), inner[:, 1]], axis=1)
+    diff = inner3 - pos
+    diff /= np.linalg.norm(diff, axis=1, keepdims=True)
+    up = np.array([0.0, 1.0, 0.0])
+    temp = np.cross(up, diff)
+    temp /= np.linalg.norm(temp, axis=1, keepdims=True)
+    normal = np.cross(temp, diff)
+    normal /= np.linalg.norm(normal, axis=1, keepdims=True)
+    return pos * size, normal
+
+
+def rotation_about(axis, angle):
+    """3x3 rotation (row-major) about a unit axis (Rodrigues)."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    c, s = math.cos(angle), math.sin(angle)
+    k = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return c * np.eye(3) + s * k + (1 - c) * np.outer(a, a)
+
+
+def pose_rows(position, yaw):
+    """12-float pose (position, local x, y, z axes) for a yaw about world Y,
+    the frame setCameraPose(p, 0, yaw, 0) produces."""
+    r = rotation_about([0, 1, 0], yaw)
+    x, y, z = r[:, 0], r[:, 1], r[:, 2]
+    return np.concatenate([position, x, y, z]).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+def small_scene(outdir, seed=SEED, n_omm=1000, spp=32):
+    """Ground + 64 boxes + simple_sky and a Fibonacci-sphere eye.  Returns a
+    dict with the glTF path, eye path, pose (12 floats) and spp."""
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    g = GltfBuilder()
+    g.scene_extras = {"background-shader": "simple_sky"}
+    ground = np.array([[-10, 0, -10], [10, 0, -10], [10, 0, 10], [-10, 0, 10]], np.float64)
+    g.mesh("ground", ground, np.array([[0, 2, 1], [0, 3, 2]]), colours=np.tile([0.5, 0.5, 0.5, 1.0], (4, 1)))
+    verts, faces, cols = [], [], []
+    placed = 0
+    while placed < 64:
+        c = rng.uniform(-8.0, 8.0, size=2)
+        e = rng.uniform(0.2, 2.0, size=3)
+        col = np.concatenate([rng.uniform(0.0, 1.0, size=(8, 3)), np.ones((8, 1))], axis=1)
+        # Keep the eye (0, 0.5, 0) outside every box.
+        if abs(c[0]) < e[0] / 2 + 0.3 and abs(c[1]) < e[2] / 2 + 0.3:
+            continue
+        v, f = box_mesh([c[0] - e[0] / 2, 0.0, c[1] - e[2] / 2], [c[0] + e[0] / 2, e[1], c[1] + e[2] / 2])
+        faces.append(f + 8 * placed)
+        verts.append(v)
+        cols.append(col)
+        placed += 1
+    g.mesh("boxes", np.concatenate(verts), np.concatenate(faces), colours=np.concatenate(cols))
+    d = fibonacci_sphere(n_omm)
+    eye_path = os.path.join(outdir, "small.eye")
+    write_eye(eye_path, d * 0.001, d, 3.0 * DEG, 0.0)
+    g.compound_camera("insect-eye", "small.eye", translation=[0.0, 0.5, 0.0])
+    path = g.write(os.path.join(outdir, "small.gltf"), embed=True)
+    pose = pose_rows(np.array([0.0, 0.5, 0.0]), 0.0)
+    return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm}
+
+
+def terrain_height_fn(heights, extent):
+    """Bilinear lookup in the heightfield vertex grid (heights[i, j] at
+    x = -extent/2 + i*dx, z = -extent/2 + j*dz)."""
+    n = heights.shape[0] - 1
+    cell = extent / n
+
+    def h(x, z):
+        u = np.clip((x + extent / 2) / cell, 0, n - 1e-9)
+        w = np.clip((z + extent / 2) / cell, 0, n - 1e-9)
+        i, j = int(u), int(w)
+        fu, fw = u - i, w - j
+        return ((heights[i, j] * (1 - fu) + heights[i + 1, j] * fu) * (1 - fw)
+                + (heights[i, j + 1] * (1 - fu) + heights[i + 1, j + 1] * fu) * fw)
+    return h
+
+
+def terrain_scene(outdir, seed=SEED, cells=512, extent=200.0, cones=2000, n_omm=6000, spp=256, poses=1024,
+                  eye_height=0.5):
+    """Heightfield + cones and a droplet eye with a random-walk trajectory.
+    Returns a dict with paths, the (poses, 12) trajectory and spp."""
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    g = GltfBuilder()
+    g.scene_extras = {"background-shader": "simple_sky"}
+    n = cells + 1
+    heights = 2.0 * value_noise(n, n, 6, rng)
+    xs = np.linspace(-extent / 2, extent / 2, n)
+    X, Z = np.meshgrid(xs, xs, indexing="ij")
+    pos = np.stack([X.ravel(), heights.ravel(), Z.ravel()], axis=1)
+    t = (heights.ravel() + 2.0) / 4.0
+    low, mid, high = np.array([0.20, 0.35, 0.10]), np.array([0.45, 0.35, 0.20]), np.array([0.85, 0.85, 0.80])
+    col = np.where(t[:, None] < 0.5, low + (mid - low) * (t[:, None] / 0.5), mid + (high - mid) * ((t[:, None] - 0.5) / 0.5))
+    col = np.concatenate([col, np.ones((len(col), 1))], axis=1)
+    ii, jj = np.meshgrid(np.arange(cells), np.arange(cells), indexing="ij")
+    v00 = (ii * n + jj).ravel()
+    v10 = ((ii + 1) * n + jj).ravel()
+    v01 = (ii * n + jj + 1).ravel()
+    v11 = ((ii + 1) * n + jj + 1).ravel()
+    faces = np.stack([np.stack([v00, v01, v10], 1), np.stack([v10, v01, v11], 1)], axis=1).reshape(-1, 3)
+    g.mesh("terrain", pos, faces, colours=col, index_type=5125)
+    hfn = terrain_height_fn(heights, extent)
+    cv, cf, cc = [], [], []
+    for k in range(cones):
+        x, z = rng.uniform(-extent / 2 + 5, extent / 2 - 5, size=2)
+        hgt = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
+        rad = hgt * rng.uniform(0.1, 0.3)
+        v, f = cone_mesh(x, hfn(x, z) - 0.05, z, rad, hgt)
+        tt = (v[:, 1] - v[:, 1].min()) / max(hgt, 1e-6)
+        c = np.stack([0.05 + 0.2 * tt, 0.3 + 0.5 * tt, 0.05 + 0.1 * tt, np.ones_like(tt)], axis=1)
+        cf.append(f + sum(len(a) for a in cv))
+        cv.append(v)
+        cc.append(c)
+    g.mesh("plants", np.concatenate(cv), np.concatenate(cf), colours=np.concatenate(cc), index_type=5125)
+    epos, edir = droplet_eye(n_omm, rng)
+    aa = rng.uniform(1.5 * DEG, 4.0 * DEG, size=n_omm)
+    eye_path = os.path.join(outdir, "droplet.eye")
+    write_eye(eye_path, epos, edir, aa, 0.0)
+    g.compound_camera("droplet-eye", "droplet.eye", translation=[0.0, hfn(0.0, 0.0) + eye_height, 0.0])
+    path = g.write(os.path.join(outdir, "terrain.gltf"), embed=False)
+    traj = random_walk(hfn, poses, rng, eye_height=eye_height)
+    return {"gltf": path, "eye": eye_path, "poses": traj, "spp": spp, "n_omm": n_omm,
+            "triangles": int(len(faces) + 32 * cones)}
+
+
+def random_walk(hfn, count, rng, step=0.1, yaw_sd=10.0 * DEG, eye_height=0.5):
+    """(count, 12) poses: 0.1 m steps along the heading, heading noise N(0, 10 deg),
+    height = terrain + eye_height."""
+    out = np.zeros((count, 12), np.float32)
+    x = z = 0.0
+    yaw = rng.uniform(0, 2 * math.pi)
+    for i in range(count):
+        out[i] = pose_rows(np.array([x, hfn(x, z) + eye_height, z]), yaw)
+        yaw += rng.normal(0.0, yaw_sd)
+        x += step * math.sin(yaw)
+        z += step * math.cos(yaw)
+    return out

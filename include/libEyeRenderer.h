@@ -1,0 +1,140 @@
+/*
+ * libEyeRenderer3 — headless compound-eye renderer for one GB300 GPU.
+ *
+ * Drop-in C ABI for the reference's libEyeRenderer3
+ * (BrainsOnBoard/compound-ray, libEyeRenderer3/libEyeRenderer.h:16-67).
+ * Every reference entry point keeps its name, signature and meaning; each
+ * declaration below cites the reference declaration it replaces.  No window
+ * is opened when the library loads.  Errors never throw across the ABI:
+ * they set a message readable with crGetLastError() and the function returns
+ * its sentinel (the reference's own sentinels where it has one).
+ *
+ * The entry points prefixed "cr" have no counterpart in the reference; they
+ * expose the per-ommatidium fp32 colours, batched pose trajectories and the
+ * test/diagnostic views the parity tests need.
+ *
+ * Not thread-safe: one process-wide renderer, as in the reference.
+ */
+#ifndef LIB_EYE_RENDERER_3_H
+#define LIB_EYE_RENDERER_3_H
+
+#include <cstddef>
+#include <cstdint>
+#include <vector_types.h>
+
+/* Same layout as the reference's OmmatidiumPacket (libEyeRenderer.h:8-14). */
+struct OmmatidiumPacket {
+  float posX, posY, posZ;
+  float dirX, dirY, dirZ;
+  float acceptanceAngle;
+  float focalpointOffset;
+};
+
+extern "C" {
+/* ---- Configuration (libEyeRenderer.h:18-26) ---------------------------- */
+void setVerbosity(bool v);                /* libEyeRenderer.h:19 */
+void loadGlTFscene(const char* filepath); /* libEyeRenderer.h:20; replaces any scene loaded before */
+void stop(void);                          /* libEyeRenderer.h:21; frees every GPU resource */
+void setRenderSize(int w, int h);         /* libEyeRenderer.h:22 */
+double renderFrame(void);                 /* libEyeRenderer.h:23; ms, -1.0 on error */
+void displayFrame(void);                  /* libEyeRenderer.h:24; no display here: no-op */
+void saveFrameAs(char* ppmFilename);      /* libEyeRenderer.h:25; binary PPM, rows flipped */
+unsigned char* getFramePointer(void);     /* libEyeRenderer.h:26; h*w*4 bytes owned by the library */
+
+/* ---- Camera control (libEyeRenderer.h:28-49) --------------------------- */
+size_t getCameraCount(void);              /* :29 */
+void nextCamera(void);                    /* :30 */
+void previousCamera(void);                /* :31 */
+size_t getCurrentCameraIndex(void);       /* :32 */
+const char* getCurrentCameraName(void);   /* :33 */
+void gotoCamera(int index);               /* :34 */
+bool gotoCameraByName(char* name);        /* :35 */
+void setCameraPosition(float x, float y, float z);      /* :36 */
+void getCameraPosition(float& x, float& y, float& z);   /* :37 */
+void setCameraLocalSpace(float lxx, float lxy, float lxz, float lyx, float lyy, float lyz, float lzx, float lzy,
+                         float lzz);                    /* :39-41 */
+void rotateCameraAround(float angle, float axisX, float axisY, float axisZ);        /* :42 */
+void rotateCameraLocallyAround(float angle, float axisX, float axisY, float axisZ); /* :43 */
+void translateCamera(float x, float y, float z);                                    /* :44 */
+void translateCameraLocally(float x, float y, float z);                             /* :45 */
+void resetCameraPose(void);                                                         /* :47 */
+void setCameraPose(float posX, float posY, float posZ, float rotX, float rotY, float rotZ); /* :49 */
+
+/* ---- Compound-eye control (libEyeRenderer.h:53-61) --------------------- */
+bool isCompoundEyeActive(void);                          /* :53 */
+void setCurrentEyeSamplesPerOmmatidium(int s);           /* :54; resets the random streams */
+int getCurrentEyeSamplesPerOmmatidium(void);             /* :55; -1 if not compound */
+void changeCurrentEyeSamplesPerOmmatidiumBy(int s);      /* :56 */
+size_t getCurrentEyeOmmatidialCount(void);               /* :57; 0 if not compound */
+void setOmmatidia(OmmatidiumPacket* omms, size_t count); /* :59 */
+const char* getCurrentEyeDataPath(void);                 /* :60; "" if not compound */
+void setCurrentEyeShaderName(char* name);                /* :61 */
+
+/* ---- Scene queries (libEyeRenderer.h:64-66) ---------------------------- */
+bool isInsideHitGeometry(float x, float y, float z, char* name); /* :64 */
+float3 getGeometryMaxBounds(char* name);                        /* :65 */
+float3 getGeometryMinBounds(char* name);                        /* :66 */
+
+/* ---- Additions (no counterpart in the reference) ----------------------- */
+
+/* Copies the last error message (NUL-terminated, truncated to len) and
+ * returns its full length; 0 when no error is pending.  Reading clears it. */
+int crGetLastError(char* buf, size_t len);
+
+/* Per-ommatidium fp32 RGB of the last compound render of the current eye:
+ * N x 3 floats, each the sum over samples of colour/spp before the gamma
+ * and 8-bit conversion of getFramePointer (shaders.cu:341-347).  0 on success. */
+int getOmmatidialColoursF32(float* out);
+
+/* Renders `count` poses of the current compound eye as `count` consecutive
+ * frames (the random streams advance one frame per pose, exactly as `count`
+ * calls of renderFrame would) in batched launches.
+ * poses: count x 12 floats = position xyz, local x axis, local y axis,
+ *        local z axis (host memory).  out: count x N x 3 floats (host).
+ * Leaves the camera pose unchanged.  Returns 0 on success. */
+int crRenderPoses(const float* poses, size_t count, float* out);
+
+/* As crRenderPoses with device pointers: d_poses = count x 16 floats
+ * (position, x, y, z axes as float4 each, w ignored), d_out = count x N x 3.
+ * Runs asynchronously on the library stream (see crSetStream). */
+int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out);
+
+/* Diagnostic: renders `count` device poses (layout of crRenderPosesDevice)
+ * of the current eye and reports the mean BVH node visits and triangle tests
+ * per ray.  Advances the random streams like a render.  0 on success. */
+int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, double* trisPerRay);
+
+/* Makes the library launch on `stream` (a cudaStream_t; null = the library's
+ * own stream).  Returns 0 on success. */
+int crSetStream(void* stream);
+
+/* Blocks until the library stream is idle; returns 0 or -1 on a CUDA error. */
+int crSynchronize(void);
+
+/* Renders one frame of the current compound eye at the current pose and
+ * writes one 64-byte record per ray (N*spp, ommatidium-major, sample-minor):
+ * float normalDraw, uniformDraw, origin xyz, direction xyz, t, b1, b2;
+ * int32 hit id (-1 = miss); float r, g, b (unscaled shaded colour); pad.
+ * Advances the random streams by one frame like renderFrame.  0 on success. */
+int crRenderFrameRecorded(void* records);
+
+/* Flattened world-space scene: number of triangles, then per triangle 9
+ * floats of vertices, 12 floats of colours and one byte that is 1 when the
+ * triangle is shaded from vertex colours.  0 on success. */
+size_t crGetTriangleCount(void);
+int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexColour);
+
+/* Current camera's local frame (x, y, z axes; 9 floats).  0 on success. */
+int crGetCameraLocalSpace(float* axes9);
+
+/* Current eye's generator states (8 x N*spp words, layout of the device
+ * buffer).  0 on success; -1 when the streams are not initialised yet. */
+int crGetRandomStates(uint32_t* out);
+
+/* BVH statistics of the loaded scene: inner nodes, leaves, max depth. */
+int crGetBvhStats(uint32_t* innerNodes, uint32_t* leaves, uint32_t* maxDepth);
+}
+
+void* getWindowPointer(); /* libEyeRenderer.h:69; there is no window: returns null */
+
+#endif

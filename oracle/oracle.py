@@ -1,0 +1,154 @@
+"""Python side of the CPU oracle.  TEST INFRASTRUCTURE ONLY: imported by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker, never by the product.
+
+Parity status: unpinned against the reference's own outputs (the reference
+needs OptiX and a window and ships no golden renders); the oracle restates
+the reference's shader and scene arithmetic, see oracle.cpp and gltf_ref.py.
+"""
+import ctypes
+import os
+import subprocess
+from ctypes import c_double, c_float, c_int, c_size_t, c_uint32, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "oracle.cpp")
+
+
+def build(force=False):
+    """Compiles oracle.cpp with OpenMP (no contraction of float operations)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + ".tmp"
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+           SRC, "-o", tmp]
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + proc.stdout)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build())
+        f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        i32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        f64 = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        u8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+        L.orc_scene_create.argtypes = [f32, f32, u8, c_uint32]
+        L.orc_scene_create.restype = c_void_p
+        L.orc_scene_destroy.argtypes = [c_void_p]
+        L.orc_trace.argtypes = [c_void_p, f32, f32, f32, c_float, c_size_t, i32, f32, f32, f32, c_int]
+        L.orc_trace_f64.argtypes = [c_void_p, f32, f32, f32, c_double, c_size_t, c_void_p, i32, f64, f64, f64, c_int]
+        L.orc_shade.argtypes = [c_void_p, c_int, f32, i32, f32, f32, c_size_t, f32]
+        L.orc_gen_rays.argtypes = [f32, c_uint32, c_uint32, f32, f32, f32, f32]
+        L.orc_render_rays.argtypes = [c_void_p, c_int, f32, c_uint32, c_uint32, c_uint32, f32, f32, f32, c_int]
+        L.orc_render_draws.argtypes = [c_void_p, c_int, f32, c_uint32, c_uint32, c_uint32, f32, f32, f32, c_int]
+        L.orc_render_draws.restype = c_size_t
+        L.orc_make_color.argtypes = [f32, c_size_t, u8]
+        L.orc_max_threads.restype = c_int
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+class OracleScene:
+    """World-space triangles (T,3,3), colours (T,3,4), vertex-colour flags (T,)
+    and the miss shader id (0 = default_background, 1 = simple_sky)."""
+
+    def __init__(self, verts, colours, flags, miss):
+        self.verts = _f32(verts).reshape(-1, 9)
+        self.colours = _f32(colours).reshape(-1, 12)
+        self.flags = np.ascontiguousarray(flags, np.uint8).reshape(-1)
+        self.miss = int(miss)
+        self.T = len(self.flags)
+        self._h = lib().orc_scene_create(self.verts, self.colours, self.flags, self.T)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_scene_destroy(self._h)
+            self._h = None
+
+    def trace(self, org, dirs, tmin, tmax=1e16, threads=0):
+        org, dirs = _f32(org).reshape(-1, 3), _f32(dirs).reshape(-1, 3)
+        n = len(org)
+        tmin = _f32(np.broadcast_to(np.asarray(tmin, np.float32), (n,)))
+        hit = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        b1 = np.zeros(n, np.float32)
+        b2 = np.zeros(n, np.float32)
+        lib().orc_trace(self._h, org, dirs, tmin, tmax, n, hit, t, b1, b2, threads)
+        return hit, t, b1, b2
+
+    def trace_f64(self, org, dirs, tmin, hit32=None, tmax=1e16, threads=0):
+        org, dirs = _f32(org).reshape(-1, 3), _f32(dirs).reshape(-1, 3)
+        n = len(org)
+        tmin = _f32(np.broadcast_to(np.asarray(tmin, np.float32), (n,)))
+        hit = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float64)
+        e32 = np.zeros(n, np.float64)
+        e64 = np.zeros(n, np.float64)
+        h32 = None
+        if hit32 is not None:
+            hit32 = np.ascontiguousarray(hit32, np.int32)
+            h32 = hit32.ctypes.data
+        lib().orc_trace_f64(self._h, org, dirs, tmin, tmax, n, h32, hit, t, e32, e64, threads)
+        return hit, t, e32, e64
+
+    def shade(self, dirs, hit, b1, b2):
+        dirs = _f32(dirs).reshape(-1, 3)
+        n = len(dirs)
+        out = np.zeros((n, 3), np.float32)
+        lib().orc_shade(self._h, self.miss, dirs, np.ascontiguousarray(hit, np.int32), _f32(b1), _f32(b2), n, out)
+        return out
+
+    def render_rays(self, omm, spp, org, dirs, poses=1, threads=0):
+        omm = _f32(omm).reshape(-1, 8)
+        N = len(omm)
+        out = np.zeros((poses, N, 3), np.float32)
+        lib().orc_render_rays(self._h, self.miss, omm, N, spp, poses, _f32(org).reshape(-1),
+                              _f32(dirs).reshape(-1), out, threads)
+        return out
+
+    def render_draws(self, omm, spp, poses12, draws, threads=0):
+        omm = _f32(omm).reshape(-1, 8)
+        poses12 = _f32(poses12).reshape(-1, 12)
+        N, P = len(omm), len(poses12)
+        draws = _f32(draws).reshape(-1)
+        assert draws.size == 2 * P * N * spp
+        out = np.zeros((P, N, 3), np.float32)
+        lib().orc_render_draws(self._h, self.miss, omm, N, spp, P, poses12, draws, out, threads)
+        return out
+
+
+def gen_rays(omm, spp, pose12, draws):
+    omm = _f32(omm).reshape(-1, 8)
+    N = len(omm)
+    org = np.zeros((N * spp, 3), np.float32)
+    dirs = np.zeros((N * spp, 3), np.float32)
+    lib().orc_gen_rays(omm, N, spp, _f32(pose12).reshape(-1), _f32(draws).reshape(-1), org, dirs)
+    return org, dirs
+
+
+def make_color(sums):
+    sums = _f32(sums).reshape(-1, 3)
+    out = np.zeros((len(sums), 4), np.uint8)
+    lib().orc_make_color(sums, len(sums), out)
+    return out
+
+
+def max_threads():
+    return lib().orc_max_threads()

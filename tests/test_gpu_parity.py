@@ -1,0 +1,181 @@
+"""GPU parity: the sm_103a render path against the CPU oracle on identical rays.
+
+Bars (from the renderer's correctness contract):
+  * hit triangle ids, hit distances and barycentrics: bit-exact against the
+    oracle's float watertight search on the GPU's own rays;
+  * disagreements with the independent double-precision search only for rays
+    that pass within 1e-6 (barycentric) of a triangle edge;
+  * ray generation from the same draws: within 2e-6 absolute per direction
+    component (the GPU uses the fast sin/cos of the reference build);
+  * per-ray shaded colour and per-ommatidium RGB: within 1e-5 relative
+    (RTOL below, with an absolute floor of 1e-7 for near-black channels);
+  * 8-bit frame: within one step of the oracle's make_color of the same sums.
+"""
+import numpy as np
+import pytest
+
+import eyeRendererHelperFunctions as eh
+import gltf_ref
+import oracle
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+ATOL = 1e-7
+DIR_ATOL = 2e-6
+
+
+def _load(lib, path, spp):
+    lib.loadGlTFscene(path.encode())
+    assert eh.lastError(lib) == ""
+    eh.gotoFirstCompoundEye(lib)
+    lib.setCurrentEyeSamplesPerOmmatidium(spp)
+
+
+def _oracle(path):
+    ref = gltf_ref.load(path)
+    v, c, f = ref.arrays()
+    cams = [c for c in ref.cameras if c["kind"] == "compound"]
+    return ref, oracle.OracleScene(v, c, f, ref.miss), cams[0]["omm"]
+
+
+def _check_frame(lib, sc, omm, spp, pose12):
+    rec = eh.renderFrameRecorded(lib)
+    N = len(omm)
+    assert rec.shape == (N, spp)
+    org = rec["origin"].reshape(-1, 3)
+    dirs = rec["direction"].reshape(-1, 3)
+    tmin = np.repeat(omm[:, 7], spp)
+
+    # Ray generation from the GPU's own draws.
+    draws = np.stack([rec["normalDraw"].reshape(-1), rec["uniformDraw"].reshape(-1)], axis=1)
+    o2, d2 = oracle.gen_rays(omm, spp, pose12, draws)
+    np.testing.assert_allclose(d2, dirs, rtol=0, atol=DIR_ATOL)
+    np.testing.assert_allclose(o2, org, rtol=1e-6, atol=1e-7)
+
+    # Closest hits on identical rays: bit-exact.
+    hit, t, b1, b2 = sc.trace(org, dirs, tmin)
+    gh = rec["hitId"].reshape(-1)
+    assert np.array_equal(hit, gh), "hit ids differ on %d of %d rays" % ((hit != gh).sum(), len(gh))
+    m = hit >= 0
+    assert np.array_equal(t[m].view(np.uint32), rec["t"].reshape(-1)[m].view(np.uint32))
+    assert np.array_equal(b1[m].view(np.uint32), rec["b1"].reshape(-1)[m].view(np.uint32))
+    assert np.array_equal(b2[m].view(np.uint32), rec["b2"].reshape(-1)[m].view(np.uint32))
+
+    # Independent double-precision search: only near-edge rays may differ.
+    h64, t64, e32, e64 = sc.trace_f64(org, dirs, tmin, hit32=hit)
+    diff = hit != h64
+    near = (e32 < 1e-6) | (e64 < 1e-6)
+    assert not (diff & ~near).any(), "fp32/fp64 disagree away from edges on %d rays" % (diff & ~near).sum()
+
+    # Shading of the same hits.
+    rgb = sc.shade(dirs, hit, b1, b2)
+    np.testing.assert_allclose(rec["rgb"].reshape(-1, 3), rgb, rtol=RTOL, atol=ATOL)
+
+    # Per-ommatidium sums.
+    got = eh.getOmmatidialColours(lib)
+    want = sc.render_rays(omm, spp, org, dirs)[0]
+    np.testing.assert_allclose(got, want, rtol=RTOL, atol=ATOL)
+    return rec, got
+
+
+def test_small_scene_spp32(lib, small, small_ref):
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"]
+    _load(lib, small["gltf"], 32)
+    lib.setCameraPose(0.0, 0.5, 0.0, 0.0, 0.0, 0.0)
+    rec, sums = _check_frame(lib, sc, omm, 32, small["pose"])
+    assert (rec["hitId"] >= 0).any() and (rec["hitId"] < 0).any()  # both boxes/ground and sky seen
+
+    # 8-bit frame through the reference-facing readout.
+    n = len(omm)
+    name = b"single_dimension_fast"
+    lib.setCurrentEyeShaderName(name)
+    eh.setRenderSize(lib, n, 1)
+    lib.renderFrame()
+    frame = eh.getFrame(lib, n, 1)[0]
+    sums = eh.getOmmatidialColours(lib)
+    want = oracle.make_color(sums)
+    assert np.abs(frame.astype(int) - want.astype(int)).max() <= 1
+    assert (frame[:, 3] == 255).all()
+
+
+@pytest.mark.parametrize("spp", [1, 5, 100])
+def test_small_scene_other_sample_counts(lib, small, small_ref, spp):
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"]
+    _load(lib, small["gltf"], spp)
+    lib.setCameraPose(0.3, 0.6, -0.2, 0.1, 0.7, -0.05)
+    pos = eh.getCameraPosition(lib)
+    ls = np.zeros(9, np.float32)
+    lib.crGetCameraLocalSpace(ls)
+    pose12 = np.concatenate([pos, ls]).astype(np.float32)
+    _check_frame(lib, sc, omm, spp, pose12)
+
+
+def test_terrain_scene(lib, tmp_path):
+    info = scenes.terrain_scene(str(tmp_path), cells=64, extent=40.0, cones=60, n_omm=400, spp=64, poses=3)
+    ref, sc, omm = _oracle(info["gltf"])
+    _load(lib, info["gltf"], 64)
+    for p in info["poses"]:
+        lib.setCameraPosition(*[float(v) for v in p[:3]])
+        lib.setCameraLocalSpace(*[float(v) for v in p[3:]])
+        _check_frame(lib, sc, omm, 64, p)
+
+
+def test_batched_poses_equal_sequential_frames(lib, small):
+    """P poses in one batched launch == P renderFrame calls (bit-exact)."""
+    _load(lib, small["gltf"], 48)
+    rng = np.random.default_rng(3)
+    poses = []
+    for k in range(5):
+        yaw = rng.uniform(0, 6.28)
+        poses.append(scenes.pose_rows(np.array([rng.uniform(-1, 1), 0.5, rng.uniform(-1, 1)]), yaw))
+    poses = np.stack(poses)
+    seq = []
+    for p in poses:
+        lib.setCameraPosition(*[float(v) for v in p[:3]])
+        lib.setCameraLocalSpace(*[float(v) for v in p[3:]])
+        assert lib.renderFrame() >= 0
+        seq.append(eh.getOmmatidialColours(lib))
+    lib.setCurrentEyeSamplesPerOmmatidium(48)  # resets the random streams
+    batch = eh.renderPoses(lib, poses)
+    assert np.array_equal(batch, np.stack(seq))
+
+
+def test_random_stream_ids_and_persistence(lib, small):
+    """Stream id = sample * N + ommatidium (shaders.cu:669, 684); states
+    persist across frames and reset on a sample-count change."""
+    _load(lib, small["gltf"], 8)
+    lib.setCameraPose(0.0, 0.5, 0.0, 0.0, 0.0, 0.0)
+    one = eh.c_ommatidiumPacket(0.0, 0.0, 0.0, 0.3, 0.2, 0.9, 0.05, 0.0)
+    # Eye A: one ommatidium, 8 samples -> ids 0..7.
+    eh.setOmmatidiaFromPacketList(lib, [one])
+    lib.setCurrentEyeSamplesPerOmmatidium(8)
+    a1 = eh.renderFrameRecorded(lib)
+    a2 = eh.renderFrameRecorded(lib)
+    # Eye B: eight ommatidia, one sample -> ids 0..7.
+    eh.setOmmatidiaFromPacketList(lib, [one] * 8)
+    lib.setCurrentEyeSamplesPerOmmatidium(1)
+    b1 = eh.renderFrameRecorded(lib)
+    assert np.array_equal(a1["normalDraw"][0], b1["normalDraw"][:, 0])
+    assert np.array_equal(a1["uniformDraw"][0], b1["uniformDraw"][:, 0])
+    # Later frames continue the streams.
+    assert not np.array_equal(a1["normalDraw"], a2["normalDraw"])
+    # Same count again: records only; the streams are kept.
+    b2 = eh.renderFrameRecorded(lib)
+    assert np.array_equal(b2["normalDraw"][:, 0], a2["normalDraw"][0])
+    # A sample-count change resets them.
+    lib.setCurrentEyeSamplesPerOmmatidium(1)
+    b3 = eh.renderFrameRecorded(lib)
+    assert np.array_equal(b3["normalDraw"], b1["normalDraw"])
+
+
+def test_draw_distribution(lib, small):
+    _load(lib, small["gltf"], 64)
+    rec = eh.renderFrameRecorded(lib)
+    n = rec["normalDraw"].ravel().astype(np.float64)
+    u = rec["uniformDraw"].ravel().astype(np.float64)
+    assert abs(n.mean()) < 0.02 and abs(n.std() - 1.0) < 0.02
+    assert u.min() > 0.0 and u.max() <= 1.0 and abs(u.mean() - 0.5) < 0.01
