@@ -228,7 +228,10 @@ def run_ours(args):
         p16[:, 4 * k:4 * k + 3] = poses12[:, 3 * k:3 * k + 3]
     d_poses = torch.from_numpy(p16).to(dev)
     d_out = torch.empty((P, N, 3), dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: torch's default stream has the null handle, and the
+    # events below must sit on the stream the library launches on.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     lib.crSetStream(stream.cuda_stream)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
     chunks = [(s, min(POSES_PER_LAUNCH, P - s)) for s in range(0, P, POSES_PER_LAUNCH)]
