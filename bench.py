@@ -45,6 +45,7 @@ def parse_args():
     ap.add_argument("--poses", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target wall time of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     return ap.parse_args()
 
 
@@ -361,9 +362,33 @@ def hit_fraction(lib, eh):
     return float((rec["hitId"] >= 0).mean())
 
 
+def run_profile(args):
+    """Small case for kernel profiling: loads the workload and renders its
+    first --poses poses twice (the second launch is the one to capture);
+    no timing, statistics, end-to-end or CPU legs."""
+    import torch
+
+    torch.cuda.set_device(0)
+    import eyeRendererHelperFunctions as eh
+
+    lib = eh.loadRenderer()
+    lib.setVerbosity(False)
+    info = workload(1024)
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])
+    P = min(args.poses, POSES_PER_LAUNCH)
+    poses = info["poses"][:P]
+    for _ in range(2):
+        out = eh.renderPoses(lib, poses)
+    print(json.dumps({"profile_case": "first %d poses of the terrain trajectory" % P, "checksum": float(out.sum())}))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -809,6 +809,20 @@ int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexC
   return 0;
 }
 
+int crGetOmmatidia(float* out) {
+  return guarded(
+      "crGetOmmatidia",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (!out) throw std::runtime_error("null output");
+        const std::vector<Ommatidium>& o = r.scene.cameras[r.current].omm;
+        if (!o.empty()) std::memcpy(out, o.data(), o.size() * sizeof(Ommatidium));
+        return 0;
+      },
+      -1);
+}
+
 int crGetCameraLocalSpace(float* a) {
   return guarded(
       "crGetCameraLocalSpace",

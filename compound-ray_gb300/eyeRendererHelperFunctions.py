@@ -134,6 +134,8 @@ def configureExtras(eyeRenderer):
     L.crGetTriangleCount.restype = c_size_t
     L.crGetSceneTriangles.argtypes = [c_void_p, c_void_p, c_void_p]
     L.crGetSceneTriangles.restype = c_int
+    L.crGetOmmatidia.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crGetOmmatidia.restype = c_int
     L.crGetCameraLocalSpace.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crGetCameraLocalSpace.restype = c_int
     L.crGetRandomStates.argtypes = [ndpointer(np.uint32, flags="C_CONTIGUOUS")]
@@ -157,6 +159,8 @@ def getCameraPosition(eyeRenderer):
 def getFrame(eyeRenderer, width, height):
     """Copy of the current frame as an (height, width, 4) uint8 array."""
     ptr = eyeRenderer.getFramePointer()
+    if isinstance(ptr, np.ndarray):  # restype set by setRenderSize
+        return ptr.reshape(height, width, 4).copy()
     if not ptr:
         raise RuntimeError(lastError(eyeRenderer) or "getFramePointer returned null")
     return np.ctypeslib.as_array((c_ubyte * (width * height * 4)).from_address(ptr)).reshape(height, width, 4).copy()
@@ -198,6 +202,14 @@ def getSceneTriangles(eyeRenderer):
     if eyeRenderer.crGetSceneTriangles(verts.ctypes.data, cols.ctypes.data, flags.ctypes.data) != 0:
         raise RuntimeError(lastError(eyeRenderer))
     return verts, cols, flags
+
+
+def getOmmatidia(eyeRenderer):
+    """Current eye's ommatidium records as an (N, 8) float32 array."""
+    out = np.zeros((eyeRenderer.getCurrentEyeOmmatidialCount(), 8), np.float32)
+    if eyeRenderer.crGetOmmatidia(out) != 0:
+        raise RuntimeError(lastError(eyeRenderer))
+    return out
 
 
 def setCameraLocalSpace(eyeRenderer, npMatrix):

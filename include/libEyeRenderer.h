@@ -124,6 +124,10 @@ int crRenderFrameRecorded(void* records);
 size_t crGetTriangleCount(void);
 int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexColour);
 
+/* Current eye's ommatidium records as N x 8 floats (position, direction,
+ * acceptance angle, focal offset).  0 on success. */
+int crGetOmmatidia(float* out);
+
 /* Current camera's local frame (x, y, z axes; 9 floats).  0 on success. */
 int crGetCameraLocalSpace(float* axes9);
 

@@ -1,0 +1,147 @@
+"""The CPU oracle itself: internal consistency, the reference's documented
+quirks, and agreement with brute force and double precision."""
+import math
+
+import numpy as np
+
+import oracle
+import scenes
+
+
+def _draws(n, seed):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.standard_normal(n), 1.0 - rng.random(n)], axis=1).astype(np.float32)
+
+
+def test_float_search_vs_double_search(small, small_ref):
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"]
+    spp = 32
+    org, dirs = oracle.gen_rays(omm, spp, small["pose"], _draws(len(omm) * spp, 1))
+    hit, t, b1, b2 = sc.trace(org, dirs, 0.0)
+    h64, t64, e32, e64 = sc.trace_f64(org, dirs, 0.0, hit32=hit)
+    diff = hit != h64
+    assert not (diff & ~((e32 < 1e-6) | (e64 < 1e-6))).any()
+    m = hit >= 0
+    np.testing.assert_allclose(t[m], t64[m], rtol=1e-5)
+    assert 0.2 < m.mean() < 0.95  # boxes, ground and sky are all visible
+
+
+def test_bvh_search_equals_brute_force(tmp_path):
+    """The oracle's BVH result equals the exhaustive (t, id) minimum: one
+    triangle at a time through a one-triangle scene."""
+    info = scenes.small_scene(str(tmp_path), n_omm=50)
+    import gltf_ref
+
+    ref = gltf_ref.load(info["gltf"])
+    v, c, f = ref.arrays()
+    sc = oracle.OracleScene(v, c, f, ref.miss)
+    omm = ref.cameras[0]["omm"]
+    org, dirs = oracle.gen_rays(omm, 8, info["pose"], _draws(len(omm) * 8, 2))
+    hit, t, _, _ = sc.trace(org, dirs, 0.0)
+    best_t = np.full(len(org), np.inf, np.float32)
+    best_id = np.full(len(org), -1, np.int64)
+    for k in range(len(v)):
+        one = oracle.OracleScene(v[k:k + 1], c[k:k + 1], f[k:k + 1], ref.miss)
+        h, tk, _, _ = one.trace(org, dirs, 0.0)
+        better = (h >= 0) & ((tk < best_t) | ((tk == best_t) & (k < best_id)))
+        best_t[better] = tk[better]
+        best_id[better] = k
+    assert np.array_equal(np.where(best_id < 0, -1, best_id), hit)
+
+
+def test_perpendicular_axis_quirk():
+    """generateOffsetRay (shaders.cu:655-657) replaces the perpendicular axis
+    by (0,0,1) whenever its components sum to zero, i.e. whenever the
+    ommatidial axis has x == z -- not only for a vertical axis."""
+    pose = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32)
+    draws = np.array([[1.0, 0.0]], np.float32)  # splay by one sd, no twist
+    for axis in ([0.0, 1.0, 0.0], [0.5, 0.7071, 0.5], [0.3, 0.5, 0.3]):
+        omm = np.array([[0, 0, 0, *axis, 0.5, 0.0]], np.float32)
+        _, d = oracle.gen_rays(omm, 1, pose, draws)
+        a = np.asarray(axis, np.float64)
+        ang = 0.5 / 2.35482004503094938
+        # Rodrigues about (0,0,1)
+        k = np.array([0.0, 0.0, 1.0])
+        want = a * math.cos(ang) + np.cross(k, a) * math.sin(ang) + k * np.dot(k, a) * (1 - math.cos(ang))
+        np.testing.assert_allclose(d[0], want, atol=1e-6)
+    # a generic axis uses normalize(cross(up, axis))
+    axis = np.array([0.6, 0.0, 0.8])
+    omm = np.array([[0, 0, 0, *axis, 0.5, 0.0]], np.float32)
+    _, d = oracle.gen_rays(omm, 1, pose, draws)
+    k = np.cross([0, 1, 0], axis)
+    k /= np.linalg.norm(k)
+    ang = 0.5 / 2.35482004503094938
+    want = axis * math.cos(ang) + np.cross(k, axis) * math.sin(ang) + k * np.dot(k, axis) * (1 - math.cos(ang))
+    np.testing.assert_allclose(d[0], want, atol=1e-6)
+
+
+def test_ray_generation_properties():
+    """Unit axes stay unit directions; the splay angle follows the draw times
+    acceptance/2.35482; the twist only rotates about the axis; the origin
+    moves back along the axis by the focal offset."""
+    d = scenes.fibonacci_sphere(64)
+    omm = np.concatenate([d * 0.001, d, np.full((64, 1), 0.1), np.full((64, 1), 0.002)], axis=1).astype(np.float32)
+    pose = np.array([1, 2, 3, 1, 0, 0, 0, 1, 0, 0, 0, 1], np.float32)
+    dr = _draws(64 * 16, 5)
+    org, dirs = oracle.gen_rays(omm, 16, pose, dr)
+    np.testing.assert_allclose(np.linalg.norm(dirs, axis=1), 1.0, atol=1e-5)
+    ax = np.repeat(d, 16, axis=0)
+    dd = dirs.astype(np.float64)
+    ang = np.arctan2(np.linalg.norm(np.cross(dd, ax), axis=1), (dd * ax).sum(1))
+    np.testing.assert_allclose(ang, np.abs(dr[:, 0]) * 0.1 / 2.35482004503094938, atol=2e-6)
+    np.testing.assert_allclose(org, np.repeat(d * 0.001 - d * 0.002, 16, axis=0) + [1, 2, 3], atol=1e-6)
+
+
+def test_sky_and_make_color():
+    import gltf_ref  # noqa: F401
+
+    v = np.zeros((1, 3, 3), np.float32) + 1e6
+    sc = oracle.OracleScene(v, np.ones((1, 3, 4), np.float32), np.ones(1, np.uint8), 1)
+    dirs = np.array([[0, 1, 0], [0, -1, 0], [1, 0, 0], [0, 0.5, 0.5]], np.float32)
+    rgb = sc.shade(dirs, np.full(4, -1, np.int32), np.zeros(4, np.float32), np.zeros(4, np.float32))
+    upper = np.array([1, 31, 117]) / 255.0
+    lower = np.array([143, 179, 203]) / 255.0 * 0.8
+    np.testing.assert_allclose(rgb[0], upper, rtol=1e-6)
+    np.testing.assert_allclose(rgb[1], lower, rtol=1e-6)
+    np.testing.assert_allclose(rgb[2], lower, rtol=1e-6)
+    np.testing.assert_allclose(rgb[3], lower * 0.5 + upper * 0.5, rtol=1e-5)
+    # make_color: clamp, x^(1/2.2), *255, truncate, alpha 255
+    sums = np.array([[0.0, 1.0, 2.0], [-1.0, 0.5, 0.2176]], np.float32)
+    out = oracle.make_color(sums)
+    want = [[0, 255, 255, 255], [0, int(0.5 ** (1 / 2.2) * 255), int(np.float32(0.2176) ** (1 / 2.2) * 255), 255]]
+    assert out.tolist() == want
+    # default background: border lines are black
+    sc0 = oracle.OracleScene(v, np.ones((1, 3, 4), np.float32), np.ones(1, np.uint8), 0)
+    rgb = sc0.shade(np.array([[0.005, 0.7, 0.7], [0.6, 0.6, 0.52]], np.float32), np.full(2, -1, np.int32),
+                    np.zeros(2, np.float32), np.zeros(2, np.float32))
+    assert (rgb[0] == 0).all() and rgb[1, 0] > 0 and rgb[1, 2] == 0
+
+
+def test_vertex_colour_shading_is_linearised_after_interpolation():
+    v = np.array([[[0, 0, 5], [1, 0, 5], [0, 1, 5]]], np.float32)
+    col = np.array([[[0.2, 0.4, 0.6, 1], [0.8, 0.1, 0.3, 1], [0.5, 0.5, 0.5, 1]]], np.float32)
+    sc = oracle.OracleScene(v, col, np.ones(1, np.uint8), 1)
+    hit, t, b1, b2 = sc.trace(np.array([[0.25, 0.25, 0]], np.float32), np.array([[0, 0, 1]], np.float32), 0.0)
+    assert hit[0] == 0 and t[0] == 5.0
+    rgb = sc.shade(np.array([[0, 0, 1]], np.float32), hit, b1, b2)
+    w = np.array([1 - b1[0] - b2[0], b1[0], b2[0]])
+    want = (w[:, None] * col[0, :, :3]).sum(0) ** 2.2
+    np.testing.assert_allclose(rgb[0], want, rtol=1e-5)
+    flat = oracle.OracleScene(v, col, np.zeros(1, np.uint8), 1)
+    np.testing.assert_array_equal(flat.shade(np.array([[0, 0, 1]], np.float32), hit, b1, b2)[0], col[0, 0, :3])
+
+
+def test_render_reduction_is_sequential_sum(small, small_ref):
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"][:40]
+    spp = 7
+    org, dirs = oracle.gen_rays(omm, spp, small["pose"], _draws(40 * spp, 9))
+    out = sc.render_rays(omm, spp, org, dirs)[0]
+    hit, t, b1, b2 = sc.trace(org, dirs, 0.0)
+    rgb = sc.shade(dirs, hit, b1, b2).reshape(40, spp, 3)
+    scale = np.float32(1.0) / np.float32(spp)
+    acc = np.zeros((40, 3), np.float32)
+    for k in range(spp):
+        acc = (acc + rgb[:, k] * scale).astype(np.float32)
+    assert np.array_equal(out, acc)
