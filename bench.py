@@ -254,6 +254,16 @@ def run_ours(args):
     if lib.crSynchronize() != 0:
         raise RuntimeError(eh.lastError(lib))
 
+    # Autotune the render-kernel variant on the first poses (not timed; the
+    # library restores the random streams after every trial).
+    import ctypes
+
+    nvar = lib.crGetRenderVariantCount()
+    tune_ms = np.zeros(nvar, np.float32)
+    best = ctypes.c_int(0)
+    if lib.crAutotune(d_poses.data_ptr(), min(64, P), ctypes.byref(best), tune_ms) != 0:
+        raise RuntimeError(eh.lastError(lib))
+
     # Traversal statistics for the roofline's per-ray bytes (not timed).
     nodes = ctypes_double()
     tris = ctypes_double()
@@ -329,7 +339,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "terrain %d tris, droplet eye 6000 omm x 256 spp, %d-pose trajectory" % (info["triangles"], P),
                    "rays_per_step": rays_step, "eye_frames_per_step": P, "l2": "flushed (512 MB write) between steps",
-                   "poses_per_launch": POSES_PER_LAUNCH},
+                   "poses_per_launch": POSES_PER_LAUNCH,
+                   "autotune": {"variant": best.value, "ms_64_poses": [round(float(x), 3) for x in tune_ms]}},
         "eye_frames_per_s": value / (N * spp),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},

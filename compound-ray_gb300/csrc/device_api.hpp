@@ -16,7 +16,8 @@ struct DevScene {
   const float4* tris = nullptr;
   const float4* shade = nullptr;
   uint32_t triCount = 0;
-  int miss = 0;  // 0 = default_background, 1 = simple_sky
+  int miss = 0;         // 0 = default_background, 1 = simple_sky
+  float extent = 0.f;   // largest |coordinate| of any triangle vertex
 };
 
 // Device view of one compound eye.
@@ -79,6 +80,12 @@ cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t str
 cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* out,
                          float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
                          unsigned long long* stats = nullptr);
+
+// Tuning variants of the plain render kernel (see render.cu); the variant
+// is process-wide and picked by the autotuner in eye_renderer.cpp.
+int renderVariantCount();
+void setRenderVariant(int v);
+int renderVariant();
 
 // Projection of per-ommatidium sums into a w x h uchar4 frame.
 //  mode 0: single_dimension_fast (row 0, x < N), mode 1: single_dimension.

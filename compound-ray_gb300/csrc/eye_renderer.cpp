@@ -142,6 +142,9 @@ struct Renderer {
     dev.shade = shade.ptr;
     dev.triCount = static_cast<uint32_t>(scene.triangleCount());
     dev.miss = static_cast<int>(scene.miss);
+    float ext = 0.f;
+    for (float v : scene.triVerts) ext = std::max(ext, std::fabs(v));
+    dev.extent = ext;
     pendingBvh.reset();
   }
 
@@ -750,6 +753,74 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
       },
       -1);
 }
+
+int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant) {
+  return guarded(
+      "crAutotune",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (count == 0 || !d_poses) throw std::runtime_error("no poses");
+        EyeDev& e = r.syncEye(r.current);
+        r.ensureRng(e);
+        // Trial renders must not advance the eye's random streams: keep a
+        // copy of the states and put it back after every trial.
+        const size_t words = static_cast<size_t>(kRngPlanes) * e.N * e.spp;
+        DevBuf<uint32_t> saved;
+        saved.ensure(std::max<size_t>(1, words));
+        DevBuf<float> out;
+        out.ensure(std::max<size_t>(1, 3 * count * e.N));
+        cudaStream_t st = r.stream();
+        check(cudaMemcpyAsync(saved.ptr, e.rng.ptr, words * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st), "cudaMemcpy");
+        cudaEvent_t a, b;
+        check(cudaEventCreate(&a), "cudaEventCreate");
+        check(cudaEventCreate(&b), "cudaEventCreate");
+        const int prev = renderVariant();
+        int best = 0;
+        float bestMs = INFINITY;
+        for (int v = 0; v < renderVariantCount(); ++v) {
+          setRenderVariant(v);
+          float ms = INFINITY;
+          for (int rep = 0; rep < 2; ++rep) {  // first pass warms caches and code
+            check(cudaEventRecord(a, st), "cudaEventRecord");
+            r.renderDevicePoses(e, reinterpret_cast<const float4*>(d_poses), count, out.ptr, nullptr);
+            check(cudaEventRecord(b, st), "cudaEventRecord");
+            check(cudaEventSynchronize(b), "cudaEventSynchronize");
+            check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+            check(cudaMemcpyAsync(e.rng.ptr, saved.ptr, words * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
+                  "cudaMemcpy");
+          }
+          if (msPerVariant) msPerVariant[v] = ms;
+          if (ms < bestMs) {
+            bestMs = ms;
+            best = v;
+          }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        r.checkErrWord();
+        setRenderVariant(best);
+        (void)prev;
+        if (bestVariant) *bestVariant = best;
+        saved.release();
+        out.release();
+        return 0;
+      },
+      -1);
+}
+
+int crSetRenderVariant(int variant) {
+  if (variant < 0 || variant >= renderVariantCount()) {
+    setError("crSetRenderVariant: variant out of range");
+    return -1;
+  }
+  setRenderVariant(variant);
+  return 0;
+}
+
+int crGetRenderVariant(void) { return renderVariant(); }
+
+int crGetRenderVariantCount(void) { return renderVariantCount(); }
 
 int crSetStream(void* stream) {
   R().userStream = static_cast<cudaStream_t>(stream);

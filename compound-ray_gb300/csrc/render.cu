@@ -89,9 +89,20 @@ __device__ __forceinline__ float sel3(float x, float y, float z, int k) { return
 
 // Ray set up for the watertight triangle test (Woop, Benthin, Wald,
 // "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013) and the slab test.
+//
+// Slab planes are evaluated in fused form t = plane * idir + nox with
+// nox = -origin * idir.  Rounding of idir, nox and the fma is bounded by
+// 3 ulp of (|plane| + |origin|) * |idir|; every plane of the scene lies within
+// `extent` of the world origin, so shifting nox by
+//   slack = (extent + |origin|) * |idir| * 2^-21   (8 ulp of that bound)
+// towards the ray for the near plane and away from it for the far plane of
+// each axis keeps every box interval a superset of the exact one at no cost
+// per node: the two shifted nox values are chosen once per ray by the sign of
+// the direction.
 struct Ray {
-  float ox, oy, oz;
-  float idx, idy, idz;  // reciprocal direction for the slab test
+  float idx, idy, idz;
+  float loX, loY, loZ;  // nox shifted for the box's low plane of each axis
+  float hiX, hiY, hiZ;  // nox shifted for the high plane
   int kx, ky, kz;
   float nSx, nSy, Sz;  // -Sx, -Sy, Sz of the shear
   float okx, oky, okz;
@@ -103,14 +114,21 @@ __device__ __forceinline__ float safeRcp(float d) {
   return xdiv(1.0f, dd);
 }
 
-__device__ __forceinline__ Ray setupRay(v3 o, v3 d) {
+__device__ __forceinline__ void slabOffsets(float o, float id, float extent, float& lo, float& hi) {
+  const float nox = -o * id;
+  const float slack = (extent + fabsf(o)) * fabsf(id) * 4.76837158e-07f;
+  lo = id >= 0.0f ? nox - slack : nox + slack;
+  hi = id >= 0.0f ? nox + slack : nox - slack;
+}
+
+__device__ __forceinline__ Ray setupRay(v3 o, v3 d, float extent) {
   Ray r;
-  r.ox = o.x;
-  r.oy = o.y;
-  r.oz = o.z;
   r.idx = safeRcp(d.x);
   r.idy = safeRcp(d.y);
   r.idz = safeRcp(d.z);
+  slabOffsets(o.x, r.idx, extent, r.loX, r.hiX);
+  slabOffsets(o.y, r.idy, extent, r.loY, r.hiY);
+  slabOffsets(o.z, r.idz, extent, r.loZ, r.hiZ);
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = 0;
   float m = ax;
@@ -130,9 +148,9 @@ __device__ __forceinline__ Ray setupRay(v3 o, v3 d) {
   r.kx = kx;
   r.ky = ky;
   r.kz = kz;
-  r.nSx = xneg(xdiv(sel3(d.x, d.y, d.z, kx), dkz));
-  r.nSy = xneg(xdiv(sel3(d.x, d.y, d.z, ky), dkz));
   r.Sz = xdiv(1.0f, dkz);
+  r.nSx = xneg(xmul(sel3(d.x, d.y, d.z, kx), r.Sz));
+  r.nSy = xneg(xmul(sel3(d.x, d.y, d.z, ky), r.Sz));
   r.okx = sel3(o.x, o.y, o.z, kx);
   r.oky = sel3(o.x, o.y, o.z, ky);
   r.okz = sel3(o.x, o.y, o.z, kz);
@@ -197,15 +215,26 @@ __device__ __forceinline__ void testTriangle(const Ray& r, float4 v0, float4 v1,
 }
 
 constexpr int kStackSize = 64;
-// Relative widening of slab intervals so that rounding never culls a box
-// holding a hit the triangle test would accept.
-constexpr float kSlabPad = 4.76837158e-07f;  // 2^-21
 
-__device__ __forceinline__ void slab(float lo, float hi, float o, float id, float& tn, float& tf) {
-  const float a = (lo - o) * id;
-  const float b = (hi - o) * id;
-  tn = fminf(a, b);
-  tf = fmaxf(a, b);
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// Entry/exit distances of one child box (planes lo/hi per axis).
+__device__ __forceinline__ void childSpan(const Ray& r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                          float tmin, float tmax, float& tn, float& tf) {
+  const float ax = fmaf(lx, r.idx, r.loX), bx = fmaf(hx, r.idx, r.hiX);
+  const float ay = fmaf(ly, r.idy, r.loY), by = fmaf(hy, r.idy, r.hiY);
+  const float az = fmaf(lz, r.idz, r.loZ), bz = fmaf(hz, r.idz, r.hiZ);
+  tn = max3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
+  tf = min3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
 }
 
 // Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
@@ -227,21 +256,9 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
       const float4 n1 = __ldg(n + 1);
       const float4 n2 = __ldg(n + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4*>(n + 3));
-      float a0, b0, a1, b1, a2, b2;
-      slab(n0.x, n0.y, r.ox, r.idx, a0, b0);
-      slab(n0.z, n0.w, r.oy, r.idy, a1, b1);
-      slab(n2.x, n2.y, r.oz, r.idz, a2, b2);
-      float tn0 = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
-      float tf0 = fminf(fminf(b0, b1), fminf(b2, h.t));
-      slab(n1.x, n1.y, r.ox, r.idx, a0, b0);
-      slab(n1.z, n1.w, r.oy, r.idy, a1, b1);
-      slab(n2.z, n2.w, r.oz, r.idz, a2, b2);
-      float tn1 = fmaxf(fmaxf(a0, a1), fmaxf(a2, tmin));
-      float tf1 = fminf(fminf(b0, b1), fminf(b2, h.t));
-      tn0 = fmaf(-fabsf(tn0), kSlabPad, tn0);
-      tf0 = fmaf(fabsf(tf0), kSlabPad, tf0);
-      tn1 = fmaf(-fabsf(tn1), kSlabPad, tn1);
-      tf1 = fmaf(fabsf(tf1), kSlabPad, tf1);
+      float tn0, tf0, tn1, tf1;
+      childSpan(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tmin, h.t, tn0, tf0);
+      childSpan(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tmin, h.t, tn1, tf1);
       const bool hit0 = tn0 <= tf0;
       const bool hit1 = tn1 <= tf1;
       if (hit0 && hit1) {
@@ -356,9 +373,11 @@ __global__ void rngInitKernel(DevEye eye, uint32_t* errFlag) {
 __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 
 // kMode: 0 = render, 1 = render and record every ray, 2 = render and count
-// node visits / triangle tests into stats[0..1].
-template <int kMode>
-__global__ void __launch_bounds__(128) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
+// node visits / triangle tests into stats[0..1].  kMinBlocks: resident
+// 128-thread blocks per SM the register allocation is sized for (the
+// autotuner's occupancy knob).
+template <int kMode, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
                                                     uint32_t P, WarpPlan plan, float* __restrict__ out,
                                                     float* __restrict__ scratch, uint32_t* errFlag,
                                                     RayRecord* __restrict__ rec, unsigned long long* stats) {
@@ -409,7 +428,7 @@ __global__ void __launch_bounds__(128) renderKernel(DevScene sc, DevEye eye, con
       const v3 org = mk(P0.x, P0.y, P0.z) + mk(X.x, X.y, X.z) * relPos.x + mk(Y.x, Y.y, Y.z) * relPos.y +
                      mk(Z.x, Z.y, Z.z) * relPos.z;
       const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
-      const Ray ray = setupRay(org, dir);
+      const Ray ray = setupRay(org, dir, sc.extent);
       Hit h;
       traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
       v3 c;
@@ -538,6 +557,14 @@ size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P) {
   return static_cast<size_t>(P) * N * p.chunks * 3;
 }
 
+// Occupancy variant of the plain render kernel: 0, 1, 2 = register budgets
+// for 5, 6 and 8 resident 128-thread blocks per SM.
+static int g_renderVariant = 0;
+
+int renderVariantCount() { return 3; }
+void setRenderVariant(int v) { g_renderVariant = (v >= 0 && v < 3) ? v : 0; }
+int renderVariant() { return g_renderVariant; }
+
 cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t stream) {
   const size_t total = static_cast<size_t>(eye.N) * eye.spp;
   if (total == 0) return cudaSuccess;
@@ -558,11 +585,21 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
   if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
   const unsigned g = static_cast<unsigned>(blocks);
   if (rec) {
-    renderKernel<1><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
+    renderKernel<1, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
   } else if (stats) {
-    renderKernel<2><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats);
+    renderKernel<2, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats);
   } else {
-    renderKernel<0><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+    switch (g_renderVariant) {
+      case 1:
+        renderKernel<0, 6><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        break;
+      case 2:
+        renderKernel<0, 8><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        break;
+      default:
+        renderKernel<0, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        break;
+    }
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || plan.chunks == 1) return e;

@@ -126,6 +126,12 @@ def configureExtras(eyeRenderer):
     L.crRenderPosesDevice.restype = c_int
     L.crMeasureTraversal.argtypes = [c_void_p, c_size_t, POINTER(c_double), POINTER(c_double)]
     L.crMeasureTraversal.restype = c_int
+    L.crAutotune.argtypes = [c_void_p, c_size_t, POINTER(c_int), ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crAutotune.restype = c_int
+    L.crSetRenderVariant.argtypes = [c_int]
+    L.crSetRenderVariant.restype = c_int
+    L.crGetRenderVariant.restype = c_int
+    L.crGetRenderVariantCount.restype = c_int
     L.crSetStream.argtypes = [c_void_p]
     L.crSetStream.restype = c_int
     L.crSynchronize.restype = c_int

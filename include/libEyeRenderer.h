@@ -104,6 +104,16 @@ int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out);
  * per ray.  Advances the random streams like a render.  0 on success. */
 int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, double* trisPerRay);
 
+/* Autotuner: times every variant of the render kernel on `count` device
+ * poses of the current eye (layout of crRenderPosesDevice), keeps the
+ * fastest for the rest of the process and reports it (and, if msPerVariant
+ * is not null, crGetRenderVariantCount() timings).  The eye's random streams
+ * are restored after every trial, so tuning changes no result.  0 on success. */
+int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant);
+int crSetRenderVariant(int variant);
+int crGetRenderVariant(void);
+int crGetRenderVariantCount(void);
+
 /* Makes the library launch on `stream` (a cudaStream_t; null = the library's
  * own stream).  Returns 0 on success. */
 int crSetStream(void* stream);

@@ -163,9 +163,9 @@ WRay setupW(const float* o, const float* d) {
   r.kx = kx;
   r.ky = ky;
   r.kz = kz;
-  r.nSx = -(d[kx] / d[kz]);
-  r.nSy = -(d[ky] / d[kz]);
   r.Sz = 1.0f / d[kz];
+  r.nSx = -(d[kx] * r.Sz);
+  r.nSy = -(d[ky] * r.Sz);
   return r;
 }
 

@@ -189,3 +189,35 @@ def test_draw_distribution(lib, small):
     u = rec["uniformDraw"].ravel().astype(np.float64)
     assert abs(n.mean()) < 0.02 and abs(n.std() - 1.0) < 0.02
     assert u.min() > 0.0 and u.max() <= 1.0 and abs(u.mean() - 0.5) < 0.01
+
+
+def test_autotune_changes_no_result(lib, small):
+    """Every kernel variant renders the same bits, and tuning leaves the
+    random streams where they were."""
+    import ctypes
+
+    import torch
+
+    _load(lib, small["gltf"], 64)
+    poses = np.stack([scenes.pose_rows(np.array([0.1 * k, 0.5, 0.0]), 0.3 * k) for k in range(4)])
+    p16 = np.zeros((4, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = poses[:, 3 * k:3 * k + 3]
+    d = torch.from_numpy(p16).cuda()
+    torch.cuda.synchronize()
+    ms = np.zeros(lib.crGetRenderVariantCount(), np.float32)
+    best = ctypes.c_int(-1)
+    assert lib.crAutotune(d.data_ptr(), 4, ctypes.byref(best), ms) == 0, eh.lastError(lib)
+    assert 0 <= best.value < len(ms) and (ms > 0).all()
+    outs = []
+    for v in range(len(ms)):
+        assert lib.crSetRenderVariant(v) == 0
+        lib.setCurrentEyeSamplesPerOmmatidium(64)  # same streams for every variant
+        outs.append(eh.renderPoses(lib, poses))
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    # tuning did not advance the streams: a fresh eye renders the same frames
+    lib.setCurrentEyeSamplesPerOmmatidium(64)
+    assert lib.crAutotune(d.data_ptr(), 4, ctypes.byref(best), ms) == 0
+    assert np.array_equal(eh.renderPoses(lib, poses), outs[0])
+    lib.crSetRenderVariant(best.value)
