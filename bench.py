@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target wall time of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
+    ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     return ap.parse_args()
 
 
@@ -388,6 +389,8 @@ def run_profile(args):
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])
+    if lib.crSetRenderVariant(args.variant) != 0:
+        raise RuntimeError(eh.lastError(lib))
     P = min(args.poses, POSES_PER_LAUNCH)
     poses = info["poses"][:P]
     for _ in range(2):
