@@ -87,6 +87,12 @@ int renderVariantCount();
 void setRenderVariant(int v);
 int renderVariant();
 
+// Fixed device array used as render scratch by the allocation-free entry
+// point: its capacity in floats, and its address on the current device
+// (looked up on the first call per device).
+size_t noAllocScratchFloats();
+cudaError_t noAllocScratch(float** ptr);
+
 // Projection of per-ommatidium sums into a w x h uchar4 frame.
 //  mode 0: single_dimension_fast (row 0, x < N), mode 1: single_dimension.
 cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, int h, int mode,

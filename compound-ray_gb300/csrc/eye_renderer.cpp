@@ -754,6 +754,52 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
       -1);
 }
 
+// Same work as crRenderPosesDevice for callers that cannot allocate device
+// memory when they render: the chunk partials go to the library's fixed
+// device array instead of a library-allocated buffer, and the call makes no
+// cudaMalloc/cudaFree.  The eye's device state (scene, ommatidia, random
+// streams, error word) must already exist, i.e. the current eye must have been
+// rendered once through an allocating entry point with its present ommatidium
+// and sample counts; otherwise the call fails without doing anything.
+int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out) {
+  return guarded(
+      "crRenderPosesDeviceNoAlloc",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+        if (count == 0) return 0;
+        if (!d_poses || !d_out) throw std::runtime_error("null pose or output pointer");
+        const Camera& c = r.scene.cameras[r.current];
+        const uint32_t N = static_cast<uint32_t>(c.omm.size());
+        const uint32_t spp = static_cast<uint32_t>(std::max(1, c.spp));
+        const size_t perPose = renderScratchFloats(N, spp, 1);
+        const size_t cap = noAllocScratchFloats();
+        if (perPose > cap)
+          throw std::runtime_error("an eye of " + std::to_string(N) + " ommatidia x " + std::to_string(spp) +
+                                   " samples needs " + std::to_string(perPose) +
+                                   " floats of scratch per pose; the allocation-free path holds at most " +
+                                   std::to_string(cap) + " floats (16 MiB)");
+        EyeDev& e = r.eyes[r.current];
+        if (r.pendingBvh || !e.omm.ptr || !e.rng.ptr || e.N != N || e.spp != spp || !r.err.ptr)
+          throw std::runtime_error(
+              "the eye's device state is not set up: render it once with renderFrame, crRenderPoses or "
+              "crRenderPosesDevice before using the allocation-free entry point");
+        float* scratch = nullptr;
+        check(noAllocScratch(&scratch), "cudaGetSymbolAddress");
+        r.ensureRng(e);
+        const size_t batch = perPose ? std::min<size_t>(kMaxPosesPerLaunch, cap / perPose) : kMaxPosesPerLaunch;
+        const float4* poses = reinterpret_cast<const float4*>(d_poses);
+        for (size_t first = 0; first < count; first += batch) {
+          const uint32_t P = static_cast<uint32_t>(std::min(batch, count - first));
+          check(launchRender(r.dev, r.devEye(e), poses + 4 * first, P, d_out + 3 * first * N, perPose ? scratch : nullptr,
+                             r.err.ptr, nullptr, r.stream()),
+                "render launch");
+        }
+        return 0;
+      },
+      -1);
+}
+
 int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant) {
   return guarded(
       "crAutotune",

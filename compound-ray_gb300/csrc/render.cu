@@ -616,3 +616,48 @@ cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, i
 }
 
 }  // namespace cr
+
+// ---------------------------------------------------------------------------
+// Scratch for the allocation-free entry point.
+//
+// The chunk partials of a render with more than 32 samples per ommatidium
+// normally live in a buffer the library allocates.  For callers that must
+// not allocate device memory at call time, the same partials can live in
+// this fixed array instead.  It is part of the module image, so every GPU
+// that loads the library holds its 16 MiB until the process exits.  Every
+// call of the allocation-free entry point uses the same array; calls that
+// overlap on the GPU (different streams, or several host threads) race on
+// it.  Nothing in it needs clearing: each partial is written before it is
+// read within the same call.
+// ---------------------------------------------------------------------------
+namespace cr {
+
+constexpr size_t kNoAllocScratchFloats = size_t(4) << 20;  // 16 MiB of float
+static __device__ __align__(256) float g_noAllocScratch[kNoAllocScratchFloats];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+float* s_noAllocScratch[kNoAllocMaxDevices] = {};
+}  // namespace
+
+size_t noAllocScratchFloats() { return kNoAllocScratchFloats; }
+
+// Device address of the array on the current device.  In host code the
+// array's name only stands for it, so the address is looked up once per
+// device, with that device current, and cached.
+cudaError_t noAllocScratch(float** ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  if (!s_noAllocScratch[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noAllocScratch);
+    if (e != cudaSuccess) return e;
+    s_noAllocScratch[dev] = static_cast<float*>(p);
+  }
+  *ptr = s_noAllocScratch[dev];
+  return cudaSuccess;
+}
+
+}  // namespace cr

@@ -124,6 +124,8 @@ def configureExtras(eyeRenderer):
     L.crRenderPoses.restype = c_int
     L.crRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDevice.restype = c_int
+    L.crRenderPosesDeviceNoAlloc.argtypes = [c_void_p, c_size_t, c_void_p]
+    L.crRenderPosesDeviceNoAlloc.restype = c_int
     L.crMeasureTraversal.argtypes = [c_void_p, c_size_t, POINTER(c_double), POINTER(c_double)]
     L.crMeasureTraversal.restype = c_int
     L.crAutotune.argtypes = [c_void_p, c_size_t, POINTER(c_int), ndpointer(np.float32, flags="C_CONTIGUOUS")]

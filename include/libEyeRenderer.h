@@ -99,6 +99,25 @@ int crRenderPoses(const float* poses, size_t count, float* out);
  * Runs asynchronously on the library stream (see crSetStream). */
 int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out);
 
+/* No counterpart in the reference.  crRenderPosesDevice for callers that
+ * cannot allocate device memory at render time -- e.g. code running while a
+ * CUDA stream is being captured into a graph, real-time loops that cannot
+ * take cudaMalloc's implicit synchronisation, or hosts whose device memory is
+ * owned by another allocator.  The call makes no cudaMalloc or cudaFree: the
+ * per-chunk partial sums go to a fixed 16 MiB device array inside the
+ * library (held by every GPU that loads it until exit) instead of a
+ * library-allocated buffer.  Limits and rules:
+ *  - an eye needing more than 4 Mi floats of scratch per pose
+ *    (N * ceil(spp/32) * 3 when spp > 32) is rejected with an error;
+ *  - the current eye must already have been rendered once through an
+ *    allocating entry point with its present ommatidium and sample counts,
+ *    so that its device state exists;
+ *  - the first call on each device looks up the array's device address; make
+ *    that first call before any stream capture;
+ *  - every call shares the array: calls that overlap on the GPU race.
+ * Results are identical to crRenderPosesDevice's.  0 on success. */
+int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out);
+
 /* Diagnostic: renders `count` device poses (layout of crRenderPosesDevice)
  * of the current eye and reports the mean BVH node visits and triangle tests
  * per ray.  Advances the random streams like a render.  0 on success. */
