@@ -154,19 +154,34 @@ struct Builder {
   }
 };
 
+// Centre and half-extent of a box such that [c - e, c + e] contains [lo, hi]
+// exactly: e is computed in double and rounded up.
+void centreExtent(const Box& b, float* c, float* e) {
+  for (int k = 0; k < 3; ++k) {
+    c[k] = 0.5f * b.lo[k] + 0.5f * b.hi[k];
+    const double need = std::max(static_cast<double>(b.hi[k]) - c[k], static_cast<double>(c[k]) - b.lo[k]);
+    float ef = static_cast<float>(need);
+    if (static_cast<double>(ef) < need) ef = std::nextafter(ef, INFINITY);
+    e[k] = ef;
+  }
+}
+
 void packNode(float* dst, const Box& a, const Box& b, int32_t c0, int32_t c1) {
-  dst[0] = a.lo[0];
-  dst[1] = a.hi[0];
-  dst[2] = a.lo[1];
-  dst[3] = a.hi[1];
-  dst[4] = b.lo[0];
-  dst[5] = b.hi[0];
-  dst[6] = b.lo[1];
-  dst[7] = b.hi[1];
-  dst[8] = a.lo[2];
-  dst[9] = a.hi[2];
-  dst[10] = b.lo[2];
-  dst[11] = b.hi[2];
+  float ca[3], ea[3], cb[3], eb[3];
+  centreExtent(a, ca, ea);
+  centreExtent(b, cb, eb);
+  dst[0] = ca[0];
+  dst[1] = ca[1];
+  dst[2] = ca[2];
+  dst[3] = ea[0];
+  dst[4] = ea[1];
+  dst[5] = ea[2];
+  dst[6] = cb[0];
+  dst[7] = cb[1];
+  dst[8] = cb[2];
+  dst[9] = eb[0];
+  dst[10] = eb[1];
+  dst[11] = eb[2];
   std::memcpy(&dst[12], &c0, 4);
   std::memcpy(&dst[13], &c1, 4);
   dst[14] = 0.f;

@@ -1,10 +1,11 @@
 // Two-wide bounding volume hierarchy built on the host with binned SAH.
 //
 // Device layout (all little-endian, 16-byte aligned):
-//   node i = 4 x float4 (64 B):
-//     [0] = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//     [1] = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//     [2] = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   node i = 4 x float4 (64 B), child boxes as centre c and half-extent e
+//   with [c - e, c + e] containing the exact box:
+//     [0] = (c0.cx, c0.cy, c0.cz, c0.ex)
+//     [1] = (c0.ey, c0.ez, c1.cx, c1.cy)
+//     [2] = (c1.cz, c1.ex, c1.ey, c1.ez)
 //     [3] = (int child0, int child1, 0, 0)
 //   child >= 0 is an inner node index; child < 0 is a leaf whose bitwise
 //   complement packs (first triangle << 3) | (count - 1), count in 1..8.

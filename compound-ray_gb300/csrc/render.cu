@@ -90,45 +90,47 @@ __device__ __forceinline__ float sel3(float x, float y, float z, int k) { return
 // Ray set up for the watertight triangle test (Woop, Benthin, Wald,
 // "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013) and the slab test.
 //
-// Slab planes are evaluated in fused form t = plane * idir + nox with
-// nox = -origin * idir.  Rounding of idir, nox and the fma is bounded by
-// 3 ulp of (|plane| + |origin|) * |idir|; every plane of the scene lies within
-// `extent` of the world origin, so shifting nox by
+// Child boxes are stored as centre c and half-extent e.  Per axis the entry
+// and exit distances are
+//   mid = c * idir + nox            (nox = -origin * idir, one fma)
+//   half = e * |idir| + slack       (one fma, |.| is an operand modifier)
+//   near = mid - half, far = mid + half
+// which puts the slab test on the fma pipe instead of min/max on the ALU pipe.
+// idir comes from the hardware reciprocal approximation (<= 1 ulp).  All
+// rounding (idir, nox, the two fmas, the add) stays within 5 ulp of
+// (|c| + |e| + |origin|) * |idir|; every plane of the scene lies within
+// `extent` of the world origin, so
 //   slack = (extent + |origin|) * |idir| * 2^-21   (8 ulp of that bound)
-// towards the ray for the near plane and away from it for the far plane of
-// each axis keeps every box interval a superset of the exact one at no cost
-// per node: the two shifted nox values are chosen once per ray by the sign of
-// the direction.
+// makes every computed box interval a superset of the exact one: no box
+// holding a hit the triangle test would accept is ever culled.
 struct Ray {
   float idx, idy, idz;
-  float loX, loY, loZ;  // nox shifted for the box's low plane of each axis
-  float hiX, hiY, hiZ;  // nox shifted for the high plane
+  float nox, noy, noz;
+  float slx, sly, slz;
   int kx, ky, kz;
   float nSx, nSy, Sz;  // -Sx, -Sy, Sz of the shear
   float okx, oky, okz;
 };
 
-__device__ __forceinline__ float safeRcp(float d) {
+__device__ __forceinline__ float rcpApprox(float d) {
   const float tiny = 1e-20f;
   const float dd = fabsf(d) < tiny ? copysignf(tiny, d) : d;
-  return xdiv(1.0f, dd);
-}
-
-__device__ __forceinline__ void slabOffsets(float o, float id, float extent, float& lo, float& hi) {
-  const float nox = -o * id;
-  const float slack = (extent + fabsf(o)) * fabsf(id) * 4.76837158e-07f;
-  lo = id >= 0.0f ? nox - slack : nox + slack;
-  hi = id >= 0.0f ? nox + slack : nox - slack;
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dd));
+  return r;
 }
 
 __device__ __forceinline__ Ray setupRay(v3 o, v3 d, float extent) {
   Ray r;
-  r.idx = safeRcp(d.x);
-  r.idy = safeRcp(d.y);
-  r.idz = safeRcp(d.z);
-  slabOffsets(o.x, r.idx, extent, r.loX, r.hiX);
-  slabOffsets(o.y, r.idy, extent, r.loY, r.hiY);
-  slabOffsets(o.z, r.idz, extent, r.loZ, r.hiZ);
+  r.idx = rcpApprox(d.x);
+  r.idy = rcpApprox(d.y);
+  r.idz = rcpApprox(d.z);
+  r.nox = -o.x * r.idx;
+  r.noy = -o.y * r.idy;
+  r.noz = -o.z * r.idz;
+  r.slx = (extent + fabsf(o.x)) * fabsf(r.idx) * 4.76837158e-07f;
+  r.sly = (extent + fabsf(o.y)) * fabsf(r.idy) * 4.76837158e-07f;
+  r.slz = (extent + fabsf(o.z)) * fabsf(r.idz) * 4.76837158e-07f;
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = 0;
   float m = ax;
@@ -227,14 +229,14 @@ __device__ __forceinline__ float min3(float a, float b, float c) {
   return r;
 }
 
-// Entry/exit distances of one child box (planes lo/hi per axis).
-__device__ __forceinline__ void childSpan(const Ray& r, float lx, float hx, float ly, float hy, float lz, float hz,
+// Entry/exit distances of one child box given as centre and half-extent.
+__device__ __forceinline__ void childSpan(const Ray& r, float cx, float cy, float cz, float ex, float ey, float ez,
                                           float tmin, float tmax, float& tn, float& tf) {
-  const float ax = fmaf(lx, r.idx, r.loX), bx = fmaf(hx, r.idx, r.hiX);
-  const float ay = fmaf(ly, r.idy, r.loY), by = fmaf(hy, r.idy, r.hiY);
-  const float az = fmaf(lz, r.idz, r.loZ), bz = fmaf(hz, r.idz, r.hiZ);
-  tn = max3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
-  tf = min3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+  const float mx = fmaf(cx, r.idx, r.nox), hx = fmaf(ex, fabsf(r.idx), r.slx);
+  const float my = fmaf(cy, r.idy, r.noy), hy = fmaf(ey, fabsf(r.idy), r.sly);
+  const float mz = fmaf(cz, r.idz, r.noz), hz = fmaf(ez, fabsf(r.idz), r.slz);
+  tn = max3(mx - hx, my - hy, fmaxf(mz - hz, tmin));
+  tf = min3(mx + hx, my + hy, fminf(mz + hz, tmax));
 }
 
 // Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
@@ -257,8 +259,8 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
       const float4 n2 = __ldg(n + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4*>(n + 3));
       float tn0, tf0, tn1, tf1;
-      childSpan(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tmin, h.t, tn0, tf0);
-      childSpan(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tmin, h.t, tn1, tf1);
+      childSpan(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, h.t, tn0, tf0);
+      childSpan(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, h.t, tn1, tf1);
       const bool hit0 = tn0 <= tf0;
       const bool hit1 = tn1 <= tf1;
       if (hit0 && hit1) {
