@@ -45,6 +45,7 @@ def parse_args():
     ap.add_argument("--poses", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target wall time of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-eye batching measurement")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     return ap.parse_args()
@@ -318,6 +319,8 @@ def run_ours(args):
         e2e_total = float(t.item())
     e2e_value = world * rays_step * args.steps / e2e_total
 
+    batch = None if args.no_batch else run_batch(lib, eh, args, stream)
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -353,12 +356,75 @@ def run_ours(args):
                      "kernel": "renderKernel<0> (+ combineChunksKernel)"},
         "clocks": clk,
     }
+    if batch:
+        line["batch_uneven"] = batch
     if not args.no_cpu_baseline:
         cb = cpu_baseline(info, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batch(lib, eh, args, stream):
+    """Uneven-eye batching: the small scene with 64 compound eyes
+    (ommatidia log-uniform 500-30000, spp from {16, 32, ..., 512},
+    acceptance 1-6 deg, 16 random poses each) in one persistent launch
+    replayed from a CUDA graph.  Reports rays/s over the timed launches and
+    the per-eye completion latency p50/p99 of the last launch."""
+    import ctypes
+
+    import torch
+
+    import scenes
+
+    d = os.path.join(tempfile.gettempdir(), "cr_bench_batch_%d" % scenes.SEED)
+    info = scenes.batch_scene(d)
+    lib.crSetStream(stream.cuda_stream)
+    lib.loadGlTFscene(info["gltf"].encode())
+    err = eh.lastError(lib)
+    if err:
+        raise RuntimeError(err)
+    n_eyes, P = len(info["n"]), info["poses"].shape[1]
+    first = info["first_batch_camera"]
+    cams = np.arange(first, first + n_eyes, dtype=np.int32)
+    for i, c in enumerate(cams):
+        lib.gotoCamera(int(c))
+        lib.setCurrentEyeSamplesPerOmmatidium(int(info["spp"][i]))
+    p12 = info["poses"].reshape(-1, 12)
+    p16 = np.zeros((len(p12), 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = p12[:, 3 * k:3 * k + 3]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_poses = torch.from_numpy(p16).to(dev)
+    d_out = torch.empty(sum(3 * P * n for n in info["n"]), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    h = lib.crBatchCreate(cams, n_eyes, P, d_poses.data_ptr(), d_out.data_ptr())
+    if h <= 0:
+        raise RuntimeError(eh.lastError(lib))
+    for _ in range(max(1, args.warmup)):
+        if lib.crBatchLaunch(h) != 0:
+            raise RuntimeError(eh.lastError(lib))
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        if lib.crBatchLaunch(h) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    lat = np.zeros(n_eyes, np.float32)
+    total = ctypes.c_float(0.0)
+    if lib.crBatchLatencies(h, lat, ctypes.byref(total)) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    lib.crBatchDestroy(h)
+    rays = int(sum(n * s for n, s in zip(info["n"], info["spp"])) * P)
+    return {"eyes": n_eyes, "poses_per_eye": P, "rays_per_launch": rays, "launch_ms": statistics.mean(ms),
+            "rays_per_s": rays / (statistics.mean(ms) / 1000.0),
+            "eye_latency_ms_p50": float(np.percentile(lat, 50)), "eye_latency_ms_p99": float(np.percentile(lat, 99)),
+            "graph": "one persistent work-queue kernel (+ chunk sums) replayed from a CUDA graph"}
 
 
 def ctypes_double():

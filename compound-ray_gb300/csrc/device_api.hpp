@@ -87,6 +87,28 @@ int renderVariantCount();
 void setRenderVariant(int v);
 int renderVariant();
 
+// One eye of a batched launch (device table entry).
+struct BatchEye {
+  DevEye eye;
+  const float4* poses;  // P poses of this eye
+  float* out;           // P x N x 3
+  float* scratch;       // P x N x chunks x 3, or null when chunks == 1
+  WarpPlan plan;
+  uint32_t P;
+};
+
+// Resident blocks per SM of the batch kernel for a render variant.
+int batchBlocksPerSM(int variant);
+
+// Persistent launch over all eyes' warp tasks (taskBase: nEyes ascending
+// task offsets) followed by the chunk sums of the eyes with chunks > 1
+// (cellBase: nEyes ascending offsets into their P*N cells).  ctrl must hold
+// 2 + nEyes words, set to {0, ~0, 0...} before the launch.
+cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsigned long long* taskBase,
+                        const unsigned long long* cellBase, uint32_t nEyes, unsigned long long totalTasks,
+                        unsigned long long totalCells, unsigned long long* ctrl, uint32_t* errFlag, int variant,
+                        int gridBlocks, cudaStream_t stream);
+
 // Fixed device array used as render scratch by the allocation-free entry
 // point: its capacity in floats, and its address on the current device
 // (looked up on the first call per device).

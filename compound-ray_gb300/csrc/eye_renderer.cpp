@@ -16,6 +16,7 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -74,6 +75,8 @@ struct EyeDev {
 
 constexpr uint32_t kMaxPosesPerLaunch = 256;
 
+void releaseBatches();
+
 struct Renderer {
   SceneData scene;
   bool loaded = false;
@@ -95,6 +98,8 @@ struct Renderer {
   cudaStream_t ownStream = nullptr;
   cudaStream_t userStream = nullptr;
   bool verbose = true;
+  // Bumped whenever device buffers an existing batch points into may change.
+  uint64_t generation = 0;
 
   cudaStream_t stream() {
     if (userStream) return userStream;
@@ -103,6 +108,8 @@ struct Renderer {
   }
 
   void releaseAll() {
+    ++generation;
+    releaseBatches();
     for (EyeDev& e : eyes) e.release();
     eyes.clear();
     nodes.release();
@@ -199,6 +206,7 @@ struct Renderer {
         e.sums.release();
         e.sums.ensure(std::max<size_t>(1, 3 * static_cast<size_t>(N)));
       }
+      ++generation;
       e.rng.release();
       e.rng.ensure(std::max<size_t>(1, static_cast<size_t>(kRngPlanes) * N * spp));
       e.N = N;
@@ -267,6 +275,42 @@ struct Renderer {
 Renderer& R() {
   static Renderer r;
   return r;
+}
+
+// A batch of eyes recorded as one CUDA graph (see crBatchCreate).
+struct Batch {
+  std::vector<int> cams;
+  size_t P = 0;
+  std::vector<size_t> outOffset;  // floats, per camera
+  DevBuf<BatchEye> table;
+  DevBuf<unsigned long long> taskBase, cellBase, ctrl;
+  DevBuf<float> scratch;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long totalTasks = 0, totalCells = 0;
+  int variant = 0, grid = 0;
+  uint64_t generation = 0;
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    table.release();
+    taskBase.release();
+    cellBase.release();
+    ctrl.release();
+    scratch.release();
+  }
+};
+
+std::map<int, Batch>& batches() {
+  static std::map<int, Batch> b;
+  return b;
+}
+
+void releaseBatches() {
+  for (auto& kv : batches()) kv.second.release();
+  batches().clear();
 }
 
 thread_local std::string g_lastError;
@@ -557,6 +601,7 @@ void setCurrentEyeSamplesPerOmmatidium(int s) {
     r.scene.cameras[r.current].spp = std::max(1, s);
     // Reallocating the generator states resets them (CompoundEye.cpp:171-179).
     EyeDev& e = r.eyes[r.current];
+    ++r.generation;
     e.rng.release();
     e.spp = 0;
     e.configured = false;
@@ -592,6 +637,7 @@ void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
     if (count != c.omm.size()) {
       // A count change reallocates every eye buffer and resets the streams
       // (CompoundEye.cpp:35-48); the same count only copies the records in.
+      ++r.generation;
       e.release();
     } else if (e.omm.ptr && count) {
       check(cudaMemcpyAsync(e.omm.ptr, v.data(), sizeof(Ommatidium) * count, cudaMemcpyHostToDevice, r.stream()),
@@ -752,6 +798,148 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
         return 0;
       },
       -1);
+}
+
+// Batched rendering of many eyes (the compound cameras of the scene) in one
+// persistent launch, recorded once into a CUDA graph and replayed.
+int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float* d_poses, float* d_out) {
+  return guarded(
+      "crBatchCreate",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.loaded) throw std::runtime_error("no scene loaded");
+        if (!cams || nCams == 0 || posesPerCam == 0 || !d_poses || !d_out)
+          throw std::runtime_error("empty batch or null pointer");
+        Batch b;
+        b.cams.assign(cams, cams + nCams);
+        b.P = posesPerCam;
+        std::vector<BatchEye> table(nCams);
+        std::vector<unsigned long long> tb(nCams), cb(nCams);
+        size_t outOff = 0, scratchFloats = 0;
+        for (size_t i = 0; i < nCams; ++i) {
+          const int ci = cams[i];
+          if (ci < 0 || static_cast<size_t>(ci) >= r.scene.cameras.size() ||
+              r.scene.cameras[static_cast<size_t>(ci)].kind != CameraKind::Compound)
+            throw std::runtime_error("camera " + std::to_string(ci) + " is not a compound eye");
+          for (size_t j = 0; j < i; ++j)
+            if (cams[j] == ci) throw std::runtime_error("camera " + std::to_string(ci) + " appears twice");
+          EyeDev& e = r.syncEye(static_cast<size_t>(ci));
+          r.ensureRng(e);
+          BatchEye& be = table[i];
+          be.eye = r.devEye(e);
+          be.poses = reinterpret_cast<const float4*>(d_poses) + 4 * posesPerCam * i;
+          be.out = d_out + outOff;
+          be.plan = planWarps(e.N, e.spp);
+          be.P = static_cast<uint32_t>(posesPerCam);
+          be.scratch = nullptr;
+          tb[i] = b.totalTasks;
+          cb[i] = b.totalCells;
+          b.outOffset.push_back(outOff);
+          outOff += 3 * posesPerCam * e.N;
+          b.totalTasks += e.N ? be.plan.tasks * 1ull : 0ull;
+          if (be.plan.chunks > 1 && e.N) {
+            scratchFloats += renderScratchFloats(e.N, e.spp, static_cast<uint32_t>(posesPerCam));
+            b.totalCells += static_cast<unsigned long long>(posesPerCam) * e.N;
+          }
+        }
+        if (scratchFloats) b.scratch.ensure(scratchFloats);
+        size_t so = 0;
+        for (size_t i = 0; i < nCams; ++i)
+          if (table[i].plan.chunks > 1 && table[i].eye.N) {
+            table[i].scratch = b.scratch.ptr + so;
+            so += renderScratchFloats(table[i].eye.N, table[i].eye.spp, static_cast<uint32_t>(posesPerCam));
+          }
+        b.table.ensure(nCams);
+        b.taskBase.ensure(nCams);
+        b.cellBase.ensure(nCams);
+        b.ctrl.ensure(2 + nCams);
+        cudaStream_t st = r.stream();
+        check(cudaMemcpyAsync(b.table.ptr, table.data(), nCams * sizeof(BatchEye), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+        check(cudaMemcpyAsync(b.taskBase.ptr, tb.data(), nCams * sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
+              "cudaMemcpy");
+        check(cudaMemcpyAsync(b.cellBase.ptr, cb.data(), nCams * sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
+              "cudaMemcpy");
+        uint32_t* err = r.errWord();
+        check(cudaStreamSynchronize(st), "batch set-up");
+        int dev = 0, sms = 0;
+        check(cudaGetDevice(&dev), "cudaGetDevice");
+        check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+        b.variant = renderVariant();
+        b.grid = sms * std::max(1, batchBlocksPerSM(b.variant));
+        // Record: reset the counters, the persistent launch, the chunk sums.
+        check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        cudaError_t ce = cudaMemsetAsync(b.ctrl.ptr, 0, (2 + nCams) * sizeof(unsigned long long), st);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(b.ctrl.ptr + 1, 0xff, sizeof(unsigned long long), st);
+        if (ce == cudaSuccess)
+          ce = launchBatch(r.dev, b.table.ptr, b.taskBase.ptr, b.cellBase.ptr, static_cast<uint32_t>(nCams),
+                           b.totalTasks, b.totalCells, b.ctrl.ptr, err, b.variant, b.grid, st);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(st, &g);
+        check(ce, "batch capture");
+        check(ee, "cudaStreamEndCapture");
+        b.graph = g;
+        check(cudaGraphInstantiate(&b.exec, b.graph, 0), "cudaGraphInstantiate");
+        b.generation = r.generation;
+        int id = 1;
+        while (batches().count(id)) ++id;
+        batches()[id] = std::move(b);
+        return id;
+      },
+      -1);
+}
+
+int crBatchLaunch(int handle) {
+  return guarded(
+      "crBatchLaunch",
+      [&]() -> int {
+        auto it = batches().find(handle);
+        if (it == batches().end()) throw std::runtime_error("unknown batch handle");
+        if (it->second.generation != R().generation)
+          throw std::runtime_error("batch invalidated by a change of scene or eye configuration; recreate it");
+        check(cudaGraphLaunch(it->second.exec, R().stream()), "cudaGraphLaunch");
+        return 0;
+      },
+      -1);
+}
+
+int crBatchLatencies(int handle, float* msPerCam, float* totalMs) {
+  return guarded(
+      "crBatchLatencies",
+      [&]() -> int {
+        auto it = batches().find(handle);
+        if (it == batches().end()) throw std::runtime_error("unknown batch handle");
+        Batch& b = it->second;
+        Renderer& r = R();
+        std::vector<unsigned long long> h(2 + b.cams.size());
+        check(cudaMemcpyAsync(h.data(), b.ctrl.ptr, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                              r.stream()),
+              "cudaMemcpy");
+        r.checkErrWord();
+        unsigned long long last = 0;
+        for (size_t i = 0; i < b.cams.size(); ++i) {
+          const unsigned long long done = h[2 + i];
+          last = std::max(last, done);
+          if (msPerCam) msPerCam[i] = done > h[1] ? static_cast<float>((done - h[1]) * 1e-6) : 0.f;
+        }
+        if (totalMs) *totalMs = last > h[1] ? static_cast<float>((last - h[1]) * 1e-6) : 0.f;
+        return 0;
+      },
+      -1);
+}
+
+size_t crBatchOutputOffset(int handle, size_t camIndex) {
+  auto it = batches().find(handle);
+  if (it == batches().end() || camIndex >= it->second.outOffset.size()) return 0;
+  return it->second.outOffset[camIndex];
+}
+
+int crBatchDestroy(int handle) {
+  auto it = batches().find(handle);
+  if (it == batches().end()) return -1;
+  cudaStreamSynchronize(R().stream());
+  it->second.release();
+  batches().erase(it);
+  return 0;
 }
 
 // Same work as crRenderPosesDevice for callers that cannot allocate device

@@ -378,17 +378,16 @@ __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 // node visits / triangle tests into stats[0..1].  kMinBlocks: resident
 // 128-thread blocks per SM the register allocation is sized for (the
 // autotuner's occupancy knob).
-template <int kMode, int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
-                                                    uint32_t P, WarpPlan plan, float* __restrict__ out,
-                                                    float* __restrict__ scratch, uint32_t* errFlag,
-                                                    RayRecord* __restrict__ rec, unsigned long long* stats) {
+// One warp task: up to 32 samples of one ommatidium (or whole ommatidia when
+// spp < 32) for all P poses.  Called by whole warps.
+template <int kMode>
+__device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye, const float4* __restrict__ poses,
+                                           uint32_t P, const WarpPlan& plan, uint64_t task, float* __restrict__ out,
+                                           float* __restrict__ scratch, uint32_t* errFlag,
+                                           RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests) {
   constexpr bool kRecord = kMode == 1;
   constexpr bool kCount = kMode == 2;
-  uint32_t nodeVisits = 0, triTests = 0;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint64_t task = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  if (task >= plan.tasks) return;  // whole warps exit together
   const uint32_t group = static_cast<uint32_t>(task / plan.chunks);
   const uint32_t chunk = static_cast<uint32_t>(task % plan.chunks);
   const uint32_t o = group * plan.ommPerWarp + lane / plan.segWidth;
@@ -478,6 +477,19 @@ __global__ void __launch_bounds__(128, kMinBlocks) renderKernel(DevScene sc, Dev
     }
   }
   if (valid) storeState(eye.rng, plane, sidx, st);
+}
+
+template <int kMode, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
+                                                    uint32_t P, WarpPlan plan, float* __restrict__ out,
+                                                    float* __restrict__ scratch, uint32_t* errFlag,
+                                                    RayRecord* __restrict__ rec, unsigned long long* stats) {
+  constexpr bool kCount = kMode == 2;
+  uint32_t nodeVisits = 0, triTests = 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t task = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (task >= plan.tasks) return;  // whole warps exit together
+  renderTask<kMode>(sc, eye, poses, P, plan, task, out, scratch, errFlag, rec, nodeVisits, triTests);
   if (kCount) {
     unsigned long long nv = nodeVisits, tt = triTests;
     for (int m = 16; m >= 1; m >>= 1) {
@@ -531,6 +543,77 @@ __global__ void projectKernel(const float* __restrict__ sums, uint32_t N, uchar4
   if (N == 0) return;
   const uint32_t o = static_cast<uint32_t>((static_cast<uint64_t>(x) * N) / static_cast<uint64_t>(w));
   frame[static_cast<size_t>(y) * w + x] = makeColour(sums[3 * o], sums[3 * o + 1], sums[3 * o + 2]);
+}
+
+// ---------------------------------------------------------------------------
+// Batched rendering of many eyes in one persistent launch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Index of the last entry with base <= key in an ascending table.
+template <typename T>
+__device__ __forceinline__ uint32_t lastAtMost(const T* base, uint32_t n, uint64_t key) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (static_cast<uint64_t>(base[mid]) <= key) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Persistent kernel over the warp tasks of every eye of a batch: each warp
+// takes the next task from a global counter until none are left.  Task t
+// belongs to the last eye whose taskBase <= t; the eyes' tasks are laid out
+// one eye after another.  ctrl[0] = task counter, ctrl[1] = earliest start
+// (ns), ctrl[2 + e] = completion time of eye e's last task (ns).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) batchKernel(DevScene sc, const BatchEye* __restrict__ eyes,
+                                                               const unsigned long long* __restrict__ taskBase,
+                                                               uint32_t nEyes, unsigned long long totalTasks,
+                                                               unsigned long long* ctrl, uint32_t* errFlag) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t nv = 0, tt = 0;
+  bool first = true;
+  for (;;) {
+    unsigned long long task = 0;
+    if (lane == 0) task = atomicAdd(&ctrl[0], 1ull);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= totalTasks) break;
+    if (first && lane == 0) atomicMin(&ctrl[1], globalTimerNs());
+    first = false;
+    const uint32_t e = lastAtMost(taskBase, nEyes, task);
+    const BatchEye be = eyes[e];
+    renderTask<0>(sc, be.eye, be.poses, be.P, be.plan, task - taskBase[e], be.out, be.scratch, errFlag, nullptr, nv,
+                  tt);
+    if (lane == 0) atomicMax(&ctrl[2 + e], globalTimerNs());
+  }
+}
+
+// Chunk sums of every eye with more than 32 samples: cell c belongs to the
+// last eye whose cellBase <= c.
+__global__ void batchCombineKernel(const BatchEye* __restrict__ eyes, const unsigned long long* __restrict__ cellBase,
+                                   uint32_t nEyes, unsigned long long totalCells) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= totalCells) return;
+  const uint32_t e = lastAtMost(cellBase, nEyes, i);
+  const BatchEye& be = eyes[e];
+  const unsigned long long local = i - cellBase[e];
+  const uint32_t chunks = be.plan.chunks;
+  const float* src = be.scratch + local * chunks * 3;
+  float x = 0.f, y = 0.f, z = 0.f;
+  for (uint32_t c = 0; c < chunks; ++c) {
+    x += src[3 * c];
+    y += src[3 * c + 1];
+    z += src[3 * c + 2];
+  }
+  be.out[3 * local] = x;
+  be.out[3 * local + 1] = y;
+  be.out[3 * local + 2] = z;
 }
 
 }  // namespace
@@ -607,6 +690,40 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
   if (e != cudaSuccess || plan.chunks == 1) return e;
   const size_t count = static_cast<size_t>(P) * eye.N;
   combineChunksKernel<<<static_cast<unsigned>((count + 255) / 256), 256, 0, stream>>>(scratch, plan.chunks, count, out);
+  return cudaGetLastError();
+}
+
+int batchBlocksPerSM(int variant) {
+  int blocks = 0;
+  cudaError_t e;
+  switch (variant) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<6>, 128, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<8>, 128, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<5>, 128, 0); break;
+  }
+  return e == cudaSuccess ? blocks : 0;
+}
+
+cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsigned long long* taskBase,
+                        const unsigned long long* cellBase, uint32_t nEyes, unsigned long long totalTasks,
+                        unsigned long long totalCells, unsigned long long* ctrl, uint32_t* errFlag, int variant,
+                        int gridBlocks, cudaStream_t stream) {
+  if (nEyes == 0 || gridBlocks <= 0) return cudaSuccess;
+  switch (variant) {
+    case 1:
+      batchKernel<6><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
+      break;
+    case 2:
+      batchKernel<8><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
+      break;
+    default:
+      batchKernel<5><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
+      break;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || totalCells == 0) return e;
+  batchCombineKernel<<<static_cast<unsigned>((totalCells + 255) / 256), 256, 0, stream>>>(eyes, cellBase, nEyes,
+                                                                                            totalCells);
   return cudaGetLastError();
 }
 

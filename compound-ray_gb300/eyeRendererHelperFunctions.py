@@ -124,6 +124,16 @@ def configureExtras(eyeRenderer):
     L.crRenderPoses.restype = c_int
     L.crRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDevice.restype = c_int
+    L.crBatchCreate.argtypes = [ndpointer(np.int32, flags="C_CONTIGUOUS"), c_size_t, c_size_t, c_void_p, c_void_p]
+    L.crBatchCreate.restype = c_int
+    L.crBatchLaunch.argtypes = [c_int]
+    L.crBatchLaunch.restype = c_int
+    L.crBatchLatencies.argtypes = [c_int, ndpointer(np.float32, flags="C_CONTIGUOUS"), POINTER(c_float)]
+    L.crBatchLatencies.restype = c_int
+    L.crBatchOutputOffset.argtypes = [c_int, c_size_t]
+    L.crBatchOutputOffset.restype = c_size_t
+    L.crBatchDestroy.argtypes = [c_int]
+    L.crBatchDestroy.restype = c_int
     L.crRenderPosesDeviceNoAlloc.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDeviceNoAlloc.restype = c_int
     L.crMeasureTraversal.argtypes = [c_void_p, c_size_t, POINTER(c_double), POINTER(c_double)]

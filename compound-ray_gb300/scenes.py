@@ -387,3 +387,42 @@ def random_walk(hfn, count, rng, step=0.1, yaw_sd=10.0 * DEG, eye_height=0.5):
         x += step * math.sin(yaw)
         z += step * math.cos(yaw)
     return out
+
+
+def batch_scene(outdir, seed=SEED, n_eyes=64, poses_per_eye=16, n_min=500, n_max=30000,
+                spp_choices=tuple(range(16, 513, 16)), aa_deg=(1.0, 6.0)):
+    """The small scene (ground + 64 boxes, simple_sky) with `n_eyes` compound
+    cameras of uneven size: ommatidium counts log-uniform in [n_min, n_max]
+    on Fibonacci spheres of radius 1 mm, acceptance angles uniform in aa_deg,
+    per-eye sample counts drawn from spp_choices, and `poses_per_eye` random
+    poses per eye (0.5 m above the ground, random yaw, within +-8 m).
+    Returns a dict with the glTF path, per-eye N and spp, and the poses
+    (n_eyes, poses_per_eye, 12)."""
+    base = small_scene(outdir, seed=seed)
+    rng = np.random.default_rng(seed + 3)
+    with open(base["gltf"]) as f:
+        doc = json.load(f)
+    ns, spps = [], []
+    cams = doc.setdefault("cameras", [])
+    for e in range(n_eyes):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        aa = rng.uniform(aa_deg[0] * DEG, aa_deg[1] * DEG)
+        d = fibonacci_sphere(n)
+        name = "batch-eye-%02d.eye" % e
+        write_eye(os.path.join(outdir, name), d * 0.001, d, aa, 0.0)
+        cams.append({"name": "batch-eye-%02d" % e, "type": "perspective",
+                     "perspective": {"yfov": 0.4, "znear": 0.1, "zfar": 100.0},
+                     "extras": {"compound-eye": "true", "compound-structure": name,
+                                "compound-projection": "single_dimension_fast"}})
+        doc["nodes"].append({"name": "batch-eye-%02d" % e, "camera": len(cams) - 1, "translation": [0.0, 0.5, 0.0]})
+        doc["scenes"][0]["nodes"].append(len(doc["nodes"]) - 1)
+        ns.append(n)
+        spps.append(int(rng.choice(spp_choices)))
+    poses = np.zeros((n_eyes, poses_per_eye, 12), np.float32)
+    for e in range(n_eyes):
+        for k in range(poses_per_eye):
+            poses[e, k] = pose_rows(np.array([rng.uniform(-8, 8), 0.5, rng.uniform(-8, 8)]), rng.uniform(0, 2 * math.pi))
+    path = os.path.join(outdir, "batch.gltf")
+    with open(path, "w") as f:
+        json.dump(doc, f)
+    return {"gltf": path, "n": ns, "spp": spps, "poses": poses, "first_batch_camera": 1}

@@ -118,6 +118,26 @@ int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out);
  * Results are identical to crRenderPosesDevice's.  0 on success. */
 int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out);
 
+/* Batched rendering of several compound cameras of the scene in ONE
+ * persistent launch (work-queue kernel over every eye's warp tasks),
+ * recorded once into a CUDA graph and replayed by crBatchLaunch.
+ *  cams: nCams camera indices (each a compound eye, each at most once);
+ *  d_poses: device, nCams x posesPerCam poses of 16 floats, camera-major;
+ *  d_out: device, each camera's posesPerCam x N x 3 floats at float offset
+ *         crBatchOutputOffset(handle, i), cameras one after another.
+ * Each launch renders every camera's poses as consecutive frames of that
+ * camera (its random streams advance exactly as crRenderPosesDevice's
+ * would).  The eyes keep the sample counts and ommatidia they had at
+ * creation; any later change of the scene or of an eye invalidates the
+ * batch (crBatchLaunch then fails).  Returns a handle > 0, or -1. */
+int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float* d_poses, float* d_out);
+int crBatchLaunch(int handle);
+/* After a launch: per-camera completion time of its last warp task and of
+ * the whole batch, in ms from the start of the launch (synchronises). */
+int crBatchLatencies(int handle, float* msPerCam, float* totalMs);
+size_t crBatchOutputOffset(int handle, size_t camIndex);
+int crBatchDestroy(int handle);
+
 /* Diagnostic: renders `count` device poses (layout of crRenderPosesDevice)
  * of the current eye and reports the mean BVH node visits and triangle tests
  * per ray.  Advances the random streams like a render.  0 on success. */
