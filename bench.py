@@ -48,6 +48,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-eye batching measurement")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
+    ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
     return ap.parse_args()
 
 
@@ -216,6 +217,7 @@ def run_ours(args):
     lib = eh.loadRenderer()
     lib.setVerbosity(False)
     info = workload(args.poses)
+    lib.crSetBvhBuilder(args.builder)
     lib.loadGlTFscene(info["gltf"].encode())
     err = eh.lastError(lib)
     if err:
@@ -249,12 +251,21 @@ def run_ours(args):
             if events is not None:
                 events[i][1].record(stream)
 
-    # Warm-up (includes generator initialisation on the first call).
-    for _ in range(max(args.warmup, 1)):
+    # Warm-up.  The first call uploads the scene (building the BVH on the GPU
+    # when that builder is selected) and initialises the generators.
+    t_first = time.perf_counter()
+    step()
+    torch.cuda.synchronize()
+    first_ms = 1000.0 * (time.perf_counter() - t_first)
+    for _ in range(max(args.warmup, 1) - 1):
         step()
     torch.cuda.synchronize()
     if lib.crSynchronize() != 0:
         raise RuntimeError(eh.lastError(lib))
+    import ctypes as _ct
+
+    bvh_inner, bvh_leaves, bvh_depth = _ct.c_uint32(), _ct.c_uint32(), _ct.c_uint32()
+    lib.crGetBvhStats(_ct.byref(bvh_inner), _ct.byref(bvh_leaves), _ct.byref(bvh_depth))
 
     # Autotune the render-kernel variant on the first poses (not timed; the
     # library restores the random streams after every trial).
@@ -355,6 +366,9 @@ def run_ours(args):
                      "hit_fraction": hit_frac, "launch_ms": statistics.mean(full),
                      "kernel": "renderKernel<0> (+ combineChunksKernel)"},
         "clocks": clk,
+        "bvh": {"builder": "gpu-lbvh" if args.builder == 1 else "host-sah", "inner_nodes": bvh_inner.value,
+                "leaves": bvh_leaves.value, "max_depth": bvh_depth.value,
+                "first_step_ms_incl_upload_build_rng_init": first_ms},
     }
     if batch:
         line["batch_uneven"] = batch
@@ -452,6 +466,7 @@ def run_profile(args):
     lib = eh.loadRenderer()
     lib.setVerbosity(False)
     info = workload(1024)
+    lib.crSetBvhBuilder(args.builder)
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])

@@ -87,6 +87,17 @@ int renderVariantCount();
 void setRenderVariant(int v);
 int renderVariant();
 
+// GPU BVH construction (lbvh.cu): bytes of temporary device memory for T
+// triangles, and the build itself.  verts: 9 floats, colours: 12 floats,
+// flags: 1 byte per triangle (device).  centroidLo/Hi: host bounds of the
+// triangle-box centres.  nodes: (T-1) x 4 float4, tris/shade: T x 3 float4.
+// statsOut (host): inner nodes, leaf references, maximum leaf depth.
+// Requires T >= 9; synchronises the stream.
+size_t lbvhTempBytes(uint32_t T);
+cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_t* d_flags, uint32_t T,
+                      const float* centroidLo, const float* centroidHi, float4* d_nodes, float4* d_tris,
+                      float4* d_shade, void* d_temp, uint32_t* statsOut, cudaStream_t stream);
+
 // One eye of a batched launch (device table entry).
 struct BatchEye {
   DevEye eye;

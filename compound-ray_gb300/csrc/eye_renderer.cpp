@@ -83,6 +83,8 @@ struct Renderer {
   // The BVH is built on the host by loadGlTFscene and uploaded by the first
   // call that needs the GPU, so every host-side entry point works without one.
   std::unique_ptr<HostBvh> pendingBvh;
+  bool pendingGpuBuild = false;
+  int builder = 0;  // 0 = host binned SAH, 1 = GPU linear BVH (crSetBvhBuilder)
   BvhBuildStats bvhStats;
   DevBuf<float4> nodes, tris, shade;
   DevScene dev;
@@ -123,6 +125,7 @@ struct Renderer {
     hostFrame.clear();
     dev = DevScene{};
     pendingBvh.reset();
+    pendingGpuBuild = false;
     if (ownStream) cudaStreamDestroy(ownStream);
     ownStream = nullptr;
     loaded = false;
@@ -130,7 +133,54 @@ struct Renderer {
     current = 0;
   }
 
+  // GPU construction (lbvh.cu) from the flattened scene.
+  void buildOnDevice() {
+    const uint32_t T = static_cast<uint32_t>(scene.triangleCount());
+    DevBuf<float> v, c;
+    DevBuf<uint8_t> f;
+    DevBuf<char> temp;
+    v.ensure(scene.triVerts.size());
+    c.ensure(scene.triColours.size());
+    f.ensure(T);
+    temp.ensure(lbvhTempBytes(T));
+    nodes.ensure(4 * static_cast<size_t>(T - 1));
+    tris.ensure(3 * static_cast<size_t>(T));
+    shade.ensure(3 * static_cast<size_t>(T));
+    cudaStream_t st = stream();
+    check(cudaMemcpyAsync(v.ptr, scene.triVerts.data(), scene.triVerts.size() * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    check(cudaMemcpyAsync(c.ptr, scene.triColours.data(), scene.triColours.size() * 4, cudaMemcpyHostToDevice, st),
+          "cudaMemcpy");
+    check(cudaMemcpyAsync(f.ptr, scene.triUsesVertexColour.data(), T, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t t = 0; t < T; ++t)
+      for (int k = 0; k < 3; ++k) {
+        const float* p = &scene.triVerts[9 * static_cast<size_t>(t)];
+        const float a = std::min({p[k], p[3 + k], p[6 + k]}), b = std::max({p[k], p[3 + k], p[6 + k]});
+        const float cen = 0.5f * a + 0.5f * b;
+        lo[k] = std::min(lo[k], cen);
+        hi[k] = std::max(hi[k], cen);
+      }
+    uint32_t stats[3] = {0, 0, 0};
+    const cudaError_t e = buildLbvh(v.ptr, c.ptr, f.ptr, T, lo, hi, nodes.ptr, tris.ptr, shade.ptr, temp.ptr, stats, st);
+    v.release();
+    c.release();
+    f.release();
+    temp.release();
+    check(e, "GPU BVH build");
+    bvhStats.innerNodes = stats[0];
+    bvhStats.leaves = stats[1];
+    bvhStats.maxDepth = stats[2];
+    if (stats[2] + 2 > 64) throw std::runtime_error("GPU-built BVH deeper than the traversal stack");
+  }
+
   void ensureUploaded() {
+    if (pendingGpuBuild) {
+      buildOnDevice();
+      pendingGpuBuild = false;
+      pendingBvh.reset();
+      finishUpload();
+      return;
+    }
     if (!pendingBvh) return;
     const HostBvh& b = *pendingBvh;
     const size_t nn = b.nodes.size() / 4, nt = b.tris.size() / 4;
@@ -144,6 +194,11 @@ struct Renderer {
       check(cudaMemcpyAsync(shade.ptr, b.shade.data(), nt * sizeof(float4), cudaMemcpyHostToDevice, st), "cudaMemcpy");
     }
     check(cudaStreamSynchronize(st), "scene upload");
+    pendingBvh.reset();
+    finishUpload();
+  }
+
+  void finishUpload() {
     dev.nodes = nodes.ptr;
     dev.tris = tris.ptr;
     dev.shade = shade.ptr;
@@ -152,7 +207,6 @@ struct Renderer {
     float ext = 0.f;
     for (float v : scene.triVerts) ext = std::max(ext, std::fabs(v));
     dev.extent = ext;
-    pendingBvh.reset();
   }
 
   Camera& cam() {
@@ -358,10 +412,15 @@ void loadGlTFscene(const char* filepath) {
     Renderer& r = R();
     SceneData s;
     loadGltfScene(filepath, s, r.verbose);
+    // GPU construction needs a handful of triangles at least; tiny scenes
+    // always use the host builder.
+    const bool gpuBuild = r.builder == 1 && s.triangleCount() >= 16;
     std::unique_ptr<HostBvh> bvh(new HostBvh);
-    buildBvh(s.triVerts.data(), s.triColours.data(), s.triUsesVertexColour.data(),
-             static_cast<uint32_t>(s.triangleCount()), *bvh);
-    if (bvh->stats.maxDepth + 2 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
+    if (!gpuBuild) {
+      buildBvh(s.triVerts.data(), s.triColours.data(), s.triUsesVertexColour.data(),
+               static_cast<uint32_t>(s.triangleCount()), *bvh);
+      if (bvh->stats.maxDepth + 2 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
+    }
     const bool keepVerbose = r.verbose;
     cudaStream_t user = r.userStream;
     r.releaseAll();
@@ -370,6 +429,7 @@ void loadGlTFscene(const char* filepath) {
     r.scene = std::move(s);
     r.bvhStats = bvh->stats;
     r.pendingBvh = std::move(bvh);
+    r.pendingGpuBuild = gpuBuild;
     r.eyes.resize(r.scene.cameras.size());
     r.current = 0;
     r.loaded = true;
@@ -968,7 +1028,7 @@ int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out)
                                    " floats of scratch per pose; the allocation-free path holds at most " +
                                    std::to_string(cap) + " floats (16 MiB)");
         EyeDev& e = r.eyes[r.current];
-        if (r.pendingBvh || !e.omm.ptr || !e.rng.ptr || e.N != N || e.spp != spp || !r.err.ptr)
+        if (r.pendingBvh || r.pendingGpuBuild || !e.omm.ptr || !e.rng.ptr || e.N != N || e.spp != spp || !r.err.ptr)
           throw std::runtime_error(
               "the eye's device state is not set up: render it once with renderFrame, crRenderPoses or "
               "crRenderPosesDevice before using the allocation-free entry point");
@@ -1055,6 +1115,17 @@ int crSetRenderVariant(int variant) {
 int crGetRenderVariant(void) { return renderVariant(); }
 
 int crGetRenderVariantCount(void) { return renderVariantCount(); }
+
+int crSetBvhBuilder(int kind) {
+  if (kind != 0 && kind != 1) {
+    setError("crSetBvhBuilder: builder must be 0 (host SAH) or 1 (GPU linear BVH)");
+    return -1;
+  }
+  R().builder = kind;
+  return 0;
+}
+
+int crGetBvhBuilder(void) { return R().builder; }
 
 int crSetStream(void* stream) {
   R().userStream = static_cast<cudaStream_t>(stream);

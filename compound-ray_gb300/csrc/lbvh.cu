@@ -1,0 +1,377 @@
+// GPU BVH construction for the compound-eye renderer (linear BVH).
+//
+// Builds, on the device, the same BVH2 layout the render kernel traverses
+// (bvh.hpp) from world-space triangles, replacing the reference's OptiX
+// acceleration-structure builds (libEyeRenderer3/MulticamScene.cpp:1052-1428):
+//   1. 30-bit Morton codes of the triangle centroids in the centroid bounds;
+//   2. an LSD radix sort of (code, triangle) pairs, 8-bit digits, stable;
+//   3. the binary radix tree of Karras ("Maximizing Parallelism in the
+//      Construction of BVHs, Octrees, and k-d Trees", HPG 2012): internal
+//      node i covers a contiguous range of sorted triangles, equal codes are
+//      split by position;
+//   4. bottom-up boxes, one thread per leaf, the second thread to reach a
+//      node builds its box;
+//   5. subtrees of at most kLbvhLeaf triangles collapse into leaves (their
+//      triangles are contiguous in sorted order), and the node array and the
+//      leaf-ordered triangle and shading arrays are written out.
+// Internal node 0 is the root; node slots of collapsed subtrees stay unused.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_api.hpp"
+
+namespace cr {
+namespace {
+
+constexpr uint32_t kLbvhLeaf = 4;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRadix = 256;
+
+__device__ __forceinline__ uint32_t expandBits(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__global__ void mortonKernel(const float* __restrict__ verts, uint32_t T, float3 lo, float3 scale,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const float* v = verts + 9 * static_cast<size_t>(t);
+  float c[3];
+  for (int k = 0; k < 3; ++k) {
+    const float a = fminf(fminf(v[k], v[3 + k]), v[6 + k]);
+    const float b = fmaxf(fmaxf(v[k], v[3 + k]), v[6 + k]);
+    c[k] = 0.5f * a + 0.5f * b;
+  }
+  const float q[3] = {(c[0] - lo.x) * scale.x, (c[1] - lo.y) * scale.y, (c[2] - lo.z) * scale.z};
+  uint32_t m[3];
+  for (int k = 0; k < 3; ++k) m[k] = static_cast<uint32_t>(fminf(fmaxf(q[k], 0.0f), 1023.0f));
+  keys[t] = (expandBits(m[0]) << 2) | (expandBits(m[1]) << 1) | expandBits(m[2]);
+  vals[t] = t;
+}
+
+// Radix sort pass 1: per-tile digit counts, stored digit-major
+// (hist[d * tiles + tile]) so one exclusive scan gives global offsets.
+__global__ void radixCountKernel(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t tiles,
+                                 uint32_t* __restrict__ hist) {
+  __shared__ uint32_t cnt[kRadix];
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) cnt[d] = 0;
+  __syncthreads();
+  const size_t base = static_cast<size_t>(blockIdx.x) * kSortTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    const size_t i = base + static_cast<size_t>(r) * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[static_cast<size_t>(d) * tiles + blockIdx.x] = cnt[d];
+}
+
+// Exclusive scan of `count` words in place by one block (tiled).
+__global__ void scanKernel(uint32_t* data, uint32_t count) {
+  __shared__ uint32_t part[1024];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < count; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < count ? data[i] : 0u;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {
+      const uint32_t add = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+      __syncthreads();
+      part[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (i < count) data[i] = carry + part[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += part[1023];
+    __syncthreads();
+  }
+}
+
+// Radix sort pass 2: stable scatter.  The tile is processed in kSortItems
+// rounds of one key per thread, in order; within a round a key's rank is the
+// number of equal digits before it (earlier warps, then earlier lanes).
+__global__ void radixScatterKernel(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+                                   uint32_t n, int shift, uint32_t tiles, const uint32_t* __restrict__ offsets,
+                                   uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t run[kRadix];            // keys of this digit already placed by this tile
+  __shared__ uint32_t warpCnt[kWarps][kRadix];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+    run[d] = offsets[static_cast<size_t>(d) * tiles + blockIdx.x];
+  const size_t base = static_cast<size_t>(blockIdx.x) * kSortTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    for (int k = threadIdx.x; k < kWarps * kRadix; k += blockDim.x) (&warpCnt[0][0])[k] = 0;
+    __syncthreads();
+    const size_t i = base + static_cast<size_t>(r) * kSortThreads + threadIdx.x;
+    const bool ok = i < n;
+    const uint32_t key = ok ? keysIn[i] : 0u;
+    const uint32_t d = ok ? ((key >> shift) & (kRadix - 1)) : kRadix;  // kRadix = no digit
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = __popc(peers & ((1u << lane) - 1u));
+    if (ok && before == 0) warpCnt[warp][d] = __popc(peers);
+    __syncthreads();
+    // Exclusive prefix over warps, per digit, and advance the running base.
+    for (int dd = threadIdx.x; dd < kRadix; dd += blockDim.x) {
+      uint32_t acc = run[dd];
+      for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = warpCnt[w][dd];
+        warpCnt[w][dd] = acc;
+        acc += c;
+      }
+      run[dd] = acc;
+    }
+    __syncthreads();
+    if (ok) {
+      const uint32_t dst = warpCnt[warp][d] + before;
+      keysOut[dst] = key;
+      valsOut[dst] = valsIn[i];
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint32_t a = k[i], b = k[j];
+  if (a != b) return __clz(a ^ b);
+  return 32 + __clz(static_cast<uint32_t>(i) ^ static_cast<uint32_t>(j));
+}
+
+// Karras hierarchy.  Node ids: internal 0..n-2, leaf g -> n-1+g.
+__global__ void hierarchyKernel(const uint32_t* __restrict__ keys, int n, int* __restrict__ left,
+                                int* __restrict__ right, int* __restrict__ parent, int* __restrict__ first,
+                                int* __restrict__ last) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta(keys, n, i, j);
+  int s = 0;
+  int step = l;
+  do {
+    step = (step + 1) >> 1;
+    if (delta(keys, n, i, i + (s + step) * d) > dnode) s += step;
+  } while (step > 1);
+  const int g = i + s * d + (d < 0 ? -1 : 0);
+  const int lo = i < j ? i : j, hi = i < j ? j : i;
+  const int lc = (lo == g) ? (n - 1 + g) : g;
+  const int rc = (hi == g + 1) ? (n - 1 + g + 1) : (g + 1);
+  left[i] = lc;
+  right[i] = rc;
+  parent[lc] = i;
+  parent[rc] = i;
+  first[i] = lo;
+  last[i] = hi;
+}
+
+// Bottom-up boxes.  boxes: 6 floats per node id (lo xyz, hi xyz).  Each
+// leaf thread climbs; the first thread to reach a node stops there, the
+// second (which sees both children finished) builds the box and continues.
+__global__ void boxesKernel(const float* __restrict__ verts, const uint32_t* __restrict__ order, int n,
+                            const int* __restrict__ left, const int* __restrict__ right,
+                            const int* __restrict__ parent, float* boxes, unsigned* visits) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const float* v = verts + 9 * static_cast<size_t>(order[g]);
+  float* b = boxes + 6 * static_cast<size_t>(n - 1 + g);
+  for (int k = 0; k < 3; ++k) {
+    b[k] = fminf(fminf(v[k], v[3 + k]), v[6 + k]);
+    b[3 + k] = fmaxf(fmaxf(v[k], v[3 + k]), v[6 + k]);
+  }
+  int node = parent[n - 1 + g];
+  while (node >= 0) {
+    __threadfence();
+    if (atomicAdd(&visits[node], 1u) == 0u) return;
+    __threadfence();
+    const volatile float* a = boxes + 6 * static_cast<size_t>(left[node]);
+    const volatile float* c = boxes + 6 * static_cast<size_t>(right[node]);
+    float* o = boxes + 6 * static_cast<size_t>(node);
+    for (int k = 0; k < 3; ++k) {
+      o[k] = fminf(a[k], c[k]);
+      o[3 + k] = fmaxf(a[3 + k], c[3 + k]);
+    }
+    if (node == 0) return;
+    node = parent[node];
+  }
+}
+
+__device__ __forceinline__ void centreExtent(const float* b, float* c, float* e) {
+  for (int k = 0; k < 3; ++k) {
+    c[k] = 0.5f * b[k] + 0.5f * b[3 + k];
+    const double need = fmax(static_cast<double>(b[3 + k]) - c[k], static_cast<double>(c[k]) - b[k]);
+    e[k] = __double2float_ru(need);
+  }
+}
+
+__device__ __forceinline__ int count(int node, int n, const int* first, const int* last) {
+  return node >= n - 1 ? 1 : last[node] - first[node] + 1;
+}
+
+// Child reference in the render layout: inner node index, or leaf code.
+__device__ __forceinline__ int childRef(int c, int n, const int* first, const int* last) {
+  if (c >= n - 1) return ~static_cast<int>((static_cast<uint32_t>(c - (n - 1)) << 3) | 0u);
+  const int cnt = last[c] - first[c] + 1;
+  if (cnt <= static_cast<int>(kLbvhLeaf))
+    return ~static_cast<int>((static_cast<uint32_t>(first[c]) << 3) | static_cast<uint32_t>(cnt - 1));
+  return c;
+}
+
+__global__ void emitNodesKernel(int n, const int* __restrict__ left, const int* __restrict__ right,
+                                const int* __restrict__ first, const int* __restrict__ last,
+                                const float* __restrict__ boxes, float4* __restrict__ nodes, unsigned* stats) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  if (i != 0 && count(i, n, first, last) <= static_cast<int>(kLbvhLeaf)) return;
+  const int l = left[i], r = right[i];
+  float ca[3], ea[3], cb[3], eb[3];
+  centreExtent(boxes + 6 * static_cast<size_t>(l), ca, ea);
+  centreExtent(boxes + 6 * static_cast<size_t>(r), cb, eb);
+  const int rl = childRef(l, n, first, last), rr = childRef(r, n, first, last);
+  float4* o = nodes + 4 * static_cast<size_t>(i);
+  o[0] = make_float4(ca[0], ca[1], ca[2], ea[0]);
+  o[1] = make_float4(ea[1], ea[2], cb[0], cb[1]);
+  o[2] = make_float4(cb[2], eb[0], eb[1], eb[2]);
+  o[3] = make_float4(__int_as_float(rl), __int_as_float(rr), 0.f, 0.f);
+  atomicAdd(&stats[0], 1u);
+  atomicAdd(&stats[1], (rl < 0 ? 1u : 0u) + (rr < 0 ? 1u : 0u));
+}
+
+// Depth (in inner nodes above it) of every emitted leaf reference.
+__global__ void depthKernel(int n, const int* __restrict__ parent, const int* __restrict__ first,
+                            const int* __restrict__ last, unsigned* stats) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  // Only the deepest collapsed node above leaf g is referenced; walking from
+  // the Karras leaf counts at most the levels collapsed into that leaf too.
+  int node = parent[n - 1 + g];
+  unsigned depth = 0;
+  bool collapsed = true;
+  while (node >= 0) {
+    if (collapsed && node != 0 && count(node, n, first, last) <= static_cast<int>(kLbvhLeaf)) {
+      node = parent[node];
+      continue;
+    }
+    collapsed = false;
+    ++depth;
+    node = node == 0 ? -1 : parent[node];
+  }
+  atomicMax(&stats[2], depth);
+}
+
+__global__ void gatherKernel(const float* __restrict__ verts, const float* __restrict__ colours,
+                             const uint8_t* __restrict__ flags, const uint32_t* __restrict__ order, uint32_t T,
+                             float4* __restrict__ tris, float4* __restrict__ shade) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= T) return;
+  const uint32_t t = order[p];
+  const float* v = verts + 9 * static_cast<size_t>(t);
+  const float* c = colours + 12 * static_cast<size_t>(t);
+  tris[3 * static_cast<size_t>(p)] = make_float4(v[0], v[1], v[2], __uint_as_float(t));
+  tris[3 * static_cast<size_t>(p) + 1] = make_float4(v[3], v[4], v[5], 0.f);
+  tris[3 * static_cast<size_t>(p) + 2] = make_float4(v[6], v[7], v[8], 0.f);
+  shade[3 * static_cast<size_t>(p)] = make_float4(c[0], c[1], c[2], flags[t] ? 1.0f : 0.0f);
+  shade[3 * static_cast<size_t>(p) + 1] = make_float4(c[4], c[5], c[6], c[7]);
+  shade[3 * static_cast<size_t>(p) + 2] = make_float4(c[8], c[9], c[10], c[11]);
+}
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+size_t lbvhTempBytes(uint32_t T) {
+  const size_t n = T;
+  const size_t tiles = (n + kSortTile - 1) / kSortTile;
+  size_t b = 0;
+  b += 4 * align256(n * 4);                    // keys, vals, keysAlt, valsAlt
+  b += align256(tiles * kRadix * 4);           // histogram
+  b += 5 * align256(2 * n * 4);                // left, right, parent, first, last (over-sized)
+  b += align256(2 * n * 6 * 4);                // boxes of all node ids
+  b += align256(n * 4);                        // visit counters
+  b += align256(16);                           // stats
+  return b;
+}
+
+cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_t* d_flags, uint32_t T,
+                      const float* centroidLo, const float* centroidHi, float4* d_nodes, float4* d_tris,
+                      float4* d_shade, void* d_temp, uint32_t* statsOut, cudaStream_t stream) {
+  if (T < 2 * kLbvhLeaf + 1) return cudaErrorInvalidValue;  // tiny scenes use the host builder
+  const size_t n = T;
+  const uint32_t tiles = static_cast<uint32_t>((n + kSortTile - 1) / kSortTile);
+  char* p = static_cast<char*>(d_temp);
+  auto take = [&](size_t bytes) {
+    char* q = p;
+    p += align256(bytes);
+    return q;
+  };
+  uint32_t* keys = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint32_t* vals = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint32_t* keys2 = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint32_t* vals2 = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint32_t* hist = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(tiles) * kRadix * 4));
+  int* left = reinterpret_cast<int*>(take(2 * n * 4));
+  int* right = reinterpret_cast<int*>(take(2 * n * 4));
+  int* parent = reinterpret_cast<int*>(take(2 * n * 4));
+  int* first = reinterpret_cast<int*>(take(2 * n * 4));
+  int* last = reinterpret_cast<int*>(take(2 * n * 4));
+  float* boxes = reinterpret_cast<float*>(take(2 * n * 6 * 4));
+  unsigned* visits = reinterpret_cast<unsigned*>(take(n * 4));
+  unsigned* stats = reinterpret_cast<unsigned*>(take(16));
+
+  float3 lo = make_float3(centroidLo[0], centroidLo[1], centroidLo[2]);
+  float3 sc;
+  const float ext[3] = {centroidHi[0] - centroidLo[0], centroidHi[1] - centroidLo[1], centroidHi[2] - centroidLo[2]};
+  sc.x = ext[0] > 0.f ? 1024.0f / ext[0] : 0.f;
+  sc.y = ext[1] > 0.f ? 1024.0f / ext[1] : 0.f;
+  sc.z = ext[2] > 0.f ? 1024.0f / ext[2] : 0.f;
+  const unsigned g = static_cast<unsigned>((n + 255) / 256);
+  mortonKernel<<<g, 256, 0, stream>>>(d_verts, T, lo, sc, keys, vals);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+  for (int shift = 0; shift < 30; shift += 8) {
+    radixCountKernel<<<tiles, kSortThreads, 0, stream>>>(kin, T, shift, tiles, hist);
+    scanKernel<<<1, 1024, 0, stream>>>(hist, tiles * kRadix);
+    radixScatterKernel<<<tiles, kSortThreads, 0, stream>>>(kin, vin, T, shift, tiles, hist, kout, vout);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    uint32_t* t = kin;
+    kin = kout;
+    kout = t;
+    t = vin;
+    vin = vout;
+    vout = t;
+  }
+  e = cudaMemsetAsync(parent, 0xff, 2 * n * 4, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(visits, 0, n * 4, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(stats, 0, 16, stream);
+  if (e != cudaSuccess) return e;
+  const unsigned gi = static_cast<unsigned>((n - 1 + 255) / 256);
+  hierarchyKernel<<<gi, 256, 0, stream>>>(kin, static_cast<int>(n), left, right, parent, first, last);
+  boxesKernel<<<g, 256, 0, stream>>>(d_verts, vin, static_cast<int>(n), left, right, parent, boxes, visits);
+  emitNodesKernel<<<gi, 256, 0, stream>>>(static_cast<int>(n), left, right, first, last, boxes, d_nodes, stats);
+  depthKernel<<<g, 256, 0, stream>>>(static_cast<int>(n), parent, first, last, stats);
+  gatherKernel<<<g, 256, 0, stream>>>(d_verts, d_colours, d_flags, vin, T, d_tris, d_shade);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(statsOut, stats, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(stream);
+}
+
+}  // namespace cr

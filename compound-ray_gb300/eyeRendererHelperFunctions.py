@@ -124,6 +124,9 @@ def configureExtras(eyeRenderer):
     L.crRenderPoses.restype = c_int
     L.crRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDevice.restype = c_int
+    L.crSetBvhBuilder.argtypes = [c_int]
+    L.crSetBvhBuilder.restype = c_int
+    L.crGetBvhBuilder.restype = c_int
     L.crBatchCreate.argtypes = [ndpointer(np.int32, flags="C_CONTIGUOUS"), c_size_t, c_size_t, c_void_p, c_void_p]
     L.crBatchCreate.restype = c_int
     L.crBatchLaunch.argtypes = [c_int]

@@ -153,6 +153,13 @@ int crSetRenderVariant(int variant);
 int crGetRenderVariant(void);
 int crGetRenderVariantCount(void);
 
+/* BVH builder for scenes loaded afterwards: 0 = host binned SAH (default),
+ * 1 = GPU linear BVH (Morton codes, radix sort, Karras hierarchy) built at
+ * the first render.  Results are identical either way (the closest hit does
+ * not depend on the tree); only speed differs.  0 on success. */
+int crSetBvhBuilder(int kind);
+int crGetBvhBuilder(void);
+
 /* Makes the library launch on `stream` (a cudaStream_t; null = the library's
  * own stream).  Returns 0 on success. */
 int crSetStream(void* stream);

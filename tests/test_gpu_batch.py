@@ -67,3 +67,4 @@ def test_batch_equals_per_eye_renders(lib, tmp_path):
     assert "invalidated" in eh.lastError(lib)
     assert lib.crBatchDestroy(h) == 0
     assert lib.crBatchLaunch(h) == -1
+    assert "unknown batch handle" in eh.lastError(lib)

@@ -14,6 +14,8 @@ Bars (from the renderer's correctness contract):
     and near the zenith d(asin y)/dy amplifies their last-bit differences;
   * 8-bit frame: within one step of the oracle's make_color of the same sums.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -31,6 +33,7 @@ DIR_ATOL = 2e-6
 
 
 def _load(lib, path, spp):
+    eh.lastError(lib)  # drop any message a previous test left behind
     lib.loadGlTFscene(path.encode())
     assert eh.lastError(lib) == ""
     eh.gotoFirstCompoundEye(lib)
@@ -221,3 +224,34 @@ def test_autotune_changes_no_result(lib, small):
     assert lib.crAutotune(d.data_ptr(), 4, ctypes.byref(best), ms) == 0
     assert np.array_equal(eh.renderPoses(lib, poses), outs[0])
     lib.crSetRenderVariant(best.value)
+
+
+@pytest.mark.parametrize("size", ["small", "terrain"])
+def test_gpu_built_bvh_renders_identical_bits(lib, small, tmp_path, size):
+    """The GPU linear BVH and the host SAH BVH give bit-identical renders:
+    the closest hit is the (t, id) minimum whatever the tree."""
+    if size == "small":
+        path, spp, poses = small["gltf"], 32, np.stack([small["pose"]])
+    else:
+        info = scenes.terrain_scene(str(tmp_path), cells=96, extent=40.0, cones=80, n_omm=300, spp=64, poses=4)
+        path, spp, poses = info["gltf"], 64, info["poses"]
+    outs = []
+    stats = []
+    for builder in (0, 1):
+        assert lib.crSetBvhBuilder(builder) == 0
+        _load(lib, path, spp)
+        outs.append(eh.renderPoses(lib, poses))
+        inner, leaves, depth = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        assert lib.crGetBvhStats(ctypes.byref(inner), ctypes.byref(leaves), ctypes.byref(depth)) == 0
+        stats.append((inner.value, leaves.value, depth.value))
+    lib.crSetBvhBuilder(0)
+    assert np.array_equal(outs[0], outs[1])
+    assert stats[1][0] > 0 and stats[1][1] > stats[1][0] and 0 < stats[1][2] < 62
+    # and the GPU-built tree passes the full per-ray parity check
+    assert lib.crSetBvhBuilder(1) == 0
+    ref, sc, omm = _oracle(path)
+    _load(lib, path, spp)
+    lib.setCameraPosition(*[float(v) for v in poses[0][:3]])
+    lib.setCameraLocalSpace(*[float(v) for v in poses[0][3:]])
+    _check_frame(lib, sc, omm, spp, poses[0])
+    lib.crSetBvhBuilder(0)

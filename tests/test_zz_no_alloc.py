@@ -59,6 +59,7 @@ def test_no_alloc_matches_allocating_entry_point(lib, tmp_path):
     import torch
 
     lib.setVerbosity(False)
+    eh.lastError(lib)  # start from a clean error state whatever ran before
     lib.loadGlTFscene(_scene(tmp_path).encode())
     assert eh.lastError(lib) == ""
     spp, P, N = 100, 6, 300  # spp > 32: the render uses chunk scratch
