@@ -336,9 +336,12 @@ cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_
   float3 lo = make_float3(centroidLo[0], centroidLo[1], centroidLo[2]);
   float3 sc;
   const float ext[3] = {centroidHi[0] - centroidLo[0], centroidHi[1] - centroidLo[1], centroidHi[2] - centroidLo[2]};
-  sc.x = ext[0] > 0.f ? 1024.0f / ext[0] : 0.f;
-  sc.y = ext[1] > 0.f ? 1024.0f / ext[1] : 0.f;
-  sc.z = ext[2] > 0.f ? 1024.0f / ext[2] : 0.f;
+  // One scale for all axes (the bounding cube): a flat scene then spends its
+  // top-level splits on its long axes instead of cutting its thin axis as
+  // often as the others, which would make sibling boxes overlap.
+  const float big = fmaxf(fmaxf(ext[0], ext[1]), ext[2]);
+  const float s = big > 0.f ? 1023.0f / big : 0.f;
+  sc.x = sc.y = sc.z = s;
   const unsigned g = static_cast<unsigned>((n + 255) / 256);
   mortonKernel<<<g, 256, 0, stream>>>(d_verts, T, lo, sc, keys, vals);
   cudaError_t e = cudaGetLastError();
