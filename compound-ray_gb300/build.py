@@ -20,8 +20,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["render.cu", "lbvh.cu"]
-CPP_SOURCES = ["gltf.cpp", "bvh.cpp", "eye_renderer.cpp"]
+CU_SOURCES = ["render.cu", "lbvh.cu", "mlp.cu"]
+CPP_SOURCES = ["gltf.cpp", "bvh.cpp", "denoiser.cpp", "eye_renderer.cpp"]
 
 
 def _run(cmd):

@@ -1,0 +1,272 @@
+// Host side of the learned per-ommatidium denoiser; see denoiser.hpp.
+#include "denoiser.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <numeric>
+#include <random>
+#include <stdexcept>
+
+namespace cr {
+namespace {
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string("denoiser ") + what + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+T* dalloc(size_t n) {
+  void* p = nullptr;
+  ck(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)), "cudaMalloc");
+  return static_cast<T*>(p);
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+constexpr uint32_t kMagic = 0x4e445243;  // checkpoint tag
+constexpr uint32_t kVersion = 1;
+
+}  // namespace
+
+void Denoiser::release() {
+  for (void* p : {static_cast<void*>(params_), static_cast<void*>(grads_), static_cast<void*>(m_), static_cast<void*>(v_),
+                  wbf_, Xb_, static_cast<void*>(baseb_), static_cast<void*>(targetb_), static_cast<void*>(zs_), h_[0],
+                  h_[1], h_[2], dz_[0], dz_[1], dz_[2], static_cast<void*>(y_), static_cast<void*>(dyf_), dyb_,
+                  static_cast<void*>(lossSum_), static_cast<void*>(idx_), X_, static_cast<void*>(base_),
+                  static_cast<void*>(target_)})
+    dfree(p);
+  params_ = grads_ = m_ = v_ = nullptr;
+  wbf_ = Xb_ = nullptr;
+  baseb_ = targetb_ = zs_ = y_ = dyf_ = lossSum_ = nullptr;
+  for (int i = 0; i < 3; ++i) h_[i] = dz_[i] = nullptr;
+  dyb_ = nullptr;
+  idx_ = nullptr;
+  X_ = nullptr;
+  base_ = target_ = nullptr;
+  cap_ = 0;
+  rows_ = rowCap_ = 0;
+  adamT_ = 0;
+}
+
+void Denoiser::init(uint32_t seed, cudaStream_t s) {
+  release();
+  params_ = dalloc<float>(kParams);
+  grads_ = dalloc<float>(kParams);
+  m_ = dalloc<float>(kParams);
+  v_ = dalloc<float>(kParams);
+  wbf_ = dalloc<uint16_t>(kParams);
+  std::vector<float> h(kParams, 0.f);
+  std::mt19937 rng(seed);
+  auto fill = [&](size_t off, int fanIn, int fanOut, float scale) {
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.0f / static_cast<float>(fanIn)) * scale);
+    for (size_t i = 0; i < size_t(fanIn) * fanOut; ++i) h[off + i] = nd(rng);
+  };
+  fill(offW1, kFeatureWidth, kHidden, 1.f);
+  fill(offW2, kHidden, kHidden, 1.f);
+  fill(offW3, kHidden, kHidden, 1.f);
+  fill(offW4, kHidden, kOut, 0.1f);
+  ck(cudaMemcpyAsync(params_, h.data(), kParams * 4, cudaMemcpyHostToDevice, s), "upload");
+  ck(cudaMemsetAsync(m_, 0, kParams * 4, s), "memset");
+  ck(cudaMemsetAsync(v_, 0, kParams * 4, s), "memset");
+  ck(toBf16(params_, wbf_, kParams, s), "bf16 copy");
+  ck(cudaStreamSynchronize(s), "init");
+  adamT_ = 0;
+}
+
+void Denoiser::ensureBatch(int rows) {
+  if (rows <= cap_) return;
+  for (void* p : {Xb_, static_cast<void*>(baseb_), static_cast<void*>(targetb_), static_cast<void*>(zs_), h_[0], h_[1],
+                  h_[2], dz_[0], dz_[1], dz_[2], static_cast<void*>(y_), static_cast<void*>(dyf_), dyb_,
+                  static_cast<void*>(lossSum_), static_cast<void*>(idx_)})
+    dfree(p);
+  cap_ = rows;
+  const size_t r = static_cast<size_t>(rows);
+  Xb_ = dalloc<uint16_t>(r * kFeatureWidth);
+  baseb_ = dalloc<float>(r * 3);
+  targetb_ = dalloc<float>(r * 3);
+  zs_ = dalloc<float>(r * kHidden);
+  for (int i = 0; i < 3; ++i) {
+    h_[i] = dalloc<uint16_t>(r * kHidden);
+    dz_[i] = dalloc<uint16_t>(r * kHidden);
+  }
+  y_ = dalloc<float>(r * kOut);
+  dyf_ = dalloc<float>(r * kOut);
+  dyb_ = dalloc<uint16_t>(r * kOut);
+  lossSum_ = dalloc<float>(1);
+  idx_ = dalloc<uint32_t>(r);
+}
+
+void Denoiser::forward(const void* X, int rows, cudaStream_t s) {
+  const uint16_t* w = static_cast<const uint16_t*>(wbf_);
+  ck(gemmBf16(1, rows, kHidden, kFeatureWidth, X, kFeatureWidth, false, w + offW1, kHidden, false, zs_, h_[0], kHidden,
+              params_ + offB1, nullptr, s),
+     "layer 1");
+  ck(gemmBf16(1, rows, kHidden, kHidden, h_[0], kHidden, false, w + offW2, kHidden, false, zs_, h_[1], kHidden,
+              params_ + offB2, nullptr, s),
+     "layer 2");
+  ck(gemmBf16(1, rows, kHidden, kHidden, h_[1], kHidden, false, w + offW3, kHidden, false, zs_, h_[2], kHidden,
+              params_ + offB3, nullptr, s),
+     "layer 3");
+  ck(gemmBf16(3, rows, kOut, kHidden, h_[2], kHidden, false, w + offW4, kOut, false, y_, nullptr, kOut,
+              params_ + offB4, nullptr, s),
+     "layer 4");
+}
+
+float Denoiser::forwardBackward(const void* X, const float* base, const float* target, int rows, bool wantLoss,
+                                cudaStream_t s) {
+  const uint16_t* w = static_cast<const uint16_t*>(wbf_);
+  forward(X, rows, s);
+  if (wantLoss) ck(cudaMemsetAsync(lossSum_, 0, 4, s), "memset");
+  ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, wantLoss ? lossSum_ : nullptr, s), "loss");
+  // Output layer.
+  ck(gemmBf16(0, kHidden, kOut, rows, h_[2], kHidden, true, dyb_, kOut, false, grads_ + offW4, nullptr, kOut, nullptr,
+              nullptr, s),
+     "dW4");
+  ck(colSumF32(dyf_, rows, kOut, kOut, grads_ + offB4, s), "db4");
+  ck(gemmBf16(2, rows, kHidden, kOut, dyb_, kOut, false, w + offW4, kOut, true, nullptr, dz_[2], kHidden, nullptr, h_[2],
+              s),
+     "dZ3");
+  // Hidden layers 3, 2, 1.
+  const size_t offW[3] = {offW1, offW2, offW3};
+  const size_t offB[3] = {offB1, offB2, offB3};
+  for (int l = 2; l >= 0; --l) {
+    const void* in = l == 0 ? X : h_[l - 1];
+    const int kin = l == 0 ? kFeatureWidth : kHidden;
+    ck(gemmBf16(0, kin, kHidden, rows, in, kin, true, dz_[l], kHidden, false, grads_ + offW[l], nullptr, kHidden,
+                nullptr, nullptr, s),
+       "dW");
+    ck(colSumBf16(dz_[l], rows, kHidden, kHidden, grads_ + offB[l], s), "db");
+    if (l > 0)
+      ck(gemmBf16(2, rows, kHidden, kHidden, dz_[l], kHidden, false, w + offW[l], kHidden, true, nullptr, dz_[l - 1],
+                  kHidden, nullptr, h_[l - 1], s),
+         "dZ");
+  }
+  if (!wantLoss) return 0.f;
+  float e2 = 0.f;
+  ck(cudaMemcpyAsync(&e2, lossSum_, 4, cudaMemcpyDeviceToHost, s), "loss readback");
+  ck(cudaStreamSynchronize(s), "step");
+  return e2 / (3.0f * static_cast<float>(rows));
+}
+
+void Denoiser::addRows(const void* X, const float* base, const float* target, size_t rows, cudaStream_t s) {
+  if (rows_ + rows > rowCap_) {
+    const size_t cap = std::max(rows_ + rows, rowCap_ * 2);
+    void* nX = dalloc<uint16_t>(cap * kFeatureWidth);
+    float* nb = dalloc<float>(cap * 3);
+    float* nt = dalloc<float>(cap * 3);
+    if (rows_) {
+      ck(cudaMemcpyAsync(nX, X_, rows_ * kFeatureWidth * 2, cudaMemcpyDeviceToDevice, s), "copy");
+      ck(cudaMemcpyAsync(nb, base_, rows_ * 12, cudaMemcpyDeviceToDevice, s), "copy");
+      ck(cudaMemcpyAsync(nt, target_, rows_ * 12, cudaMemcpyDeviceToDevice, s), "copy");
+    }
+    ck(cudaStreamSynchronize(s), "grow");
+    dfree(X_);
+    dfree(base_);
+    dfree(target_);
+    X_ = nX;
+    base_ = nb;
+    target_ = nt;
+    rowCap_ = cap;
+  }
+  ck(cudaMemcpyAsync(static_cast<uint16_t*>(X_) + rows_ * kFeatureWidth, X, rows * kFeatureWidth * 2,
+                     cudaMemcpyDeviceToDevice, s),
+     "append");
+  ck(cudaMemcpyAsync(base_ + rows_ * 3, base, rows * 12, cudaMemcpyDeviceToDevice, s), "append");
+  ck(cudaMemcpyAsync(target_ + rows_ * 3, target, rows * 12, cudaMemcpyDeviceToDevice, s), "append");
+  rows_ += rows;
+}
+
+void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s) {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  if (rows_ == 0) throw std::runtime_error("no training rows");
+  batch = static_cast<int>(std::min<size_t>(static_cast<size_t>(batch), rows_));
+  ensureBatch(batch);
+  std::mt19937 rng(seed);
+  std::vector<uint32_t> perm(rows_);
+  std::iota(perm.begin(), perm.end(), 0u);
+  std::shuffle(perm.begin(), perm.end(), rng);
+  size_t cursor = 0;
+  for (int st = 0; st < steps; ++st) {
+    if (cursor + static_cast<size_t>(batch) > rows_) {
+      std::shuffle(perm.begin(), perm.end(), rng);
+      cursor = 0;
+    }
+    ck(cudaMemcpyAsync(idx_, perm.data() + cursor, static_cast<size_t>(batch) * 4, cudaMemcpyHostToDevice, s), "idx");
+    cursor += static_cast<size_t>(batch);
+    ck(gatherRows(X_, base_, target_, idx_, batch, Xb_, baseb_, targetb_, s), "gather");
+    const bool want = loss != nullptr;
+    const float l = forwardBackward(Xb_, baseb_, targetb_, batch, want, s);
+    if (loss) loss[st] = l;
+    ++adamT_;
+    ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr, 0.9f, 0.999f, 1e-8f, adamT_, wbf_, s), "adam");
+  }
+  ck(cudaStreamSynchronize(s), "train");
+}
+
+void Denoiser::infer(const void* X, const float* base, size_t rows, float* out, cudaStream_t s) {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  const size_t chunk = 1 << 16;
+  ensureBatch(static_cast<int>(std::min(rows, chunk)));
+  for (size_t r0 = 0; r0 < rows; r0 += chunk) {
+    const int r = static_cast<int>(std::min(chunk, rows - r0));
+    forward(static_cast<const uint16_t*>(X) + r0 * kFeatureWidth, r, s);
+    ck(mlpLoss(y_, kOut, base + 3 * r0, nullptr, r, out + 3 * r0, nullptr, nullptr, nullptr, s), "prediction");
+  }
+}
+
+float Denoiser::gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost,
+                         float* paramsHost, cudaStream_t s) {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  ensureBatch(rows);
+  const float l = forwardBackward(X, base, target, rows, true, s);
+  if (gradsHost) ck(cudaMemcpyAsync(gradsHost, grads_, kParams * 4, cudaMemcpyDeviceToHost, s), "grads");
+  if (paramsHost) ck(cudaMemcpyAsync(paramsHost, params_, kParams * 4, cudaMemcpyDeviceToHost, s), "params");
+  ck(cudaStreamSynchronize(s), "gradient");
+  return l;
+}
+
+// Checkpoint: magic, version, parameter count, Adam step, then the fp32
+// parameters and the two Adam moment vectors.
+void Denoiser::save(const std::string& path, cudaStream_t s) {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  std::vector<float> p(kParams), m(kParams), v(kParams);
+  ck(cudaMemcpyAsync(p.data(), params_, kParams * 4, cudaMemcpyDeviceToHost, s), "save");
+  ck(cudaMemcpyAsync(m.data(), m_, kParams * 4, cudaMemcpyDeviceToHost, s), "save");
+  ck(cudaMemcpyAsync(v.data(), v_, kParams * 4, cudaMemcpyDeviceToHost, s), "save");
+  ck(cudaStreamSynchronize(s), "save");
+  std::ofstream f(path, std::ios::binary);
+  if (!f.is_open()) throw std::runtime_error("cannot write '" + path + "'");
+  const uint32_t hdr[4] = {kMagic, kVersion, static_cast<uint32_t>(kParams), static_cast<uint32_t>(adamT_)};
+  f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+  f.write(reinterpret_cast<const char*>(p.data()), kParams * 4);
+  f.write(reinterpret_cast<const char*>(m.data()), kParams * 4);
+  f.write(reinterpret_cast<const char*>(v.data()), kParams * 4);
+  if (!f.good()) throw std::runtime_error("short write to '" + path + "'");
+}
+
+void Denoiser::load(const std::string& path, cudaStream_t s) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f.is_open()) throw std::runtime_error("cannot read '" + path + "'");
+  uint32_t hdr[4] = {0, 0, 0, 0};
+  f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
+  if (hdr[0] != kMagic || hdr[1] != kVersion || hdr[2] != kParams)
+    throw std::runtime_error("'" + path + "' is not a denoiser checkpoint of this layout");
+  std::vector<float> p(kParams), m(kParams), v(kParams);
+  f.read(reinterpret_cast<char*>(p.data()), kParams * 4);
+  f.read(reinterpret_cast<char*>(m.data()), kParams * 4);
+  f.read(reinterpret_cast<char*>(v.data()), kParams * 4);
+  if (!f.good()) throw std::runtime_error("truncated checkpoint '" + path + "'");
+  if (!ready()) init(0, s);
+  ck(cudaMemcpyAsync(params_, p.data(), kParams * 4, cudaMemcpyHostToDevice, s), "load");
+  ck(cudaMemcpyAsync(m_, m.data(), kParams * 4, cudaMemcpyHostToDevice, s), "load");
+  ck(cudaMemcpyAsync(v_, v.data(), kParams * 4, cudaMemcpyHostToDevice, s), "load");
+  ck(toBf16(params_, wbf_, kParams, s), "bf16 copy");
+  ck(cudaStreamSynchronize(s), "load");
+  adamT_ = static_cast<int>(hdr[3]);
+}
+
+}  // namespace cr

@@ -1,0 +1,96 @@
+// Host side of the learned per-ommatidium denoiser (kernels in mlp.cu).
+//
+// Network: kFeatureWidth -> 128 -> 128 -> 128 -> 3 (output padded to 8),
+// ReLU hidden layers, predicting a correction added to the 8-sample mean.
+// fp32 master weights with Adam moments, bf16 working copies; every GEMM is
+// bf16 x bf16 with fp32 accumulation.  Parameter vector layout (floats):
+//   W1 [112 x 128] row-major (in x out), b1 [128], W2 [128 x 128], b2,
+//   W3 [128 x 128], b3, W4 [128 x 8], b4 [8].
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "device_api.hpp"
+
+namespace cr {
+
+class Denoiser {
+ public:
+  static constexpr int kHidden = 128;
+  static constexpr int kOut = 8;  // 3 used
+  static constexpr size_t offW1 = 0;
+  static constexpr size_t offB1 = offW1 + size_t(kFeatureWidth) * kHidden;
+  static constexpr size_t offW2 = offB1 + kHidden;
+  static constexpr size_t offB2 = offW2 + size_t(kHidden) * kHidden;
+  static constexpr size_t offW3 = offB2 + kHidden;
+  static constexpr size_t offB3 = offW3 + size_t(kHidden) * kHidden;
+  static constexpr size_t offW4 = offB3 + kHidden;
+  static constexpr size_t offB4 = offW4 + size_t(kHidden) * kOut;
+  static constexpr size_t kParams = offB4 + kOut;
+
+  ~Denoiser() { release(); }
+  void release();
+
+  // He-normal initialisation from `seed` (output layer scaled by 0.1).
+  void init(uint32_t seed, cudaStream_t s);
+  bool ready() const { return params_ != nullptr; }
+
+  // Appends rows to the training set (device arrays: X bf16 rows x 112,
+  // base and target fp32 rows x 3; copied).
+  void addRows(const void* X, const float* base, const float* target, size_t rows, cudaStream_t s);
+  size_t rows() const { return rows_; }
+  void clearRows() { rows_ = 0; }
+
+  // `steps` Adam steps on minibatches of `batch` rows drawn by a seeded
+  // shuffle of the training set; returns the mean squared error of each step
+  // in `loss` (host, `steps` floats) if given.
+  void train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s);
+
+  // Prediction for `rows` feature rows (device): out = base + net(X)[:, :3].
+  void infer(const void* X, const float* base, size_t rows, float* out, cudaStream_t s);
+
+  // One forward/backward on the given rows with the current weights:
+  // returns the loss and copies gradients and parameters to the host.
+  float gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost, float* paramsHost,
+                 cudaStream_t s);
+
+  void save(const std::string& path, cudaStream_t s);
+  void load(const std::string& path, cudaStream_t s);
+
+ private:
+  void ensureBatch(int rows);
+  float forwardBackward(const void* X, const float* base, const float* target, int rows, bool wantLoss,
+                        cudaStream_t s);
+  void forward(const void* X, int rows, cudaStream_t s);
+
+  float* params_ = nullptr;
+  float* grads_ = nullptr;
+  float* m_ = nullptr;
+  float* v_ = nullptr;
+  void* wbf_ = nullptr;  // bf16 copy of params_
+  int adamT_ = 0;
+  // batch work buffers
+  int cap_ = 0;
+  void* Xb_ = nullptr;
+  float* baseb_ = nullptr;
+  float* targetb_ = nullptr;
+  float* zs_ = nullptr;
+  void* h_[3] = {nullptr, nullptr, nullptr};
+  void* dz_[3] = {nullptr, nullptr, nullptr};
+  float* y_ = nullptr;
+  float* dyf_ = nullptr;
+  void* dyb_ = nullptr;
+  float* lossSum_ = nullptr;
+  uint32_t* idx_ = nullptr;
+  // training set
+  void* X_ = nullptr;
+  float* base_ = nullptr;
+  float* target_ = nullptr;
+  size_t rows_ = 0, rowCap_ = 0;
+};
+
+}  // namespace cr

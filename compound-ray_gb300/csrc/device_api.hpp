@@ -81,6 +81,39 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
                          float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
                          unsigned long long* stats = nullptr);
 
+// Per-ommatidium sample statistics of a feature render (spp <= 32), each the
+// mean over the samples: colour (3), squared colour (3), hit flag, hit
+// distance (0 on a miss), hit-triangle normal facing the ray in the eye's
+// frame (3, 0 on a miss).  stats: P x N x kFeatureStats floats.
+constexpr int kFeatureStats = 11;
+cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
+                           uint32_t* errFlag, cudaStream_t stream);
+
+// Denoiser network (mlp.cu).  Feature rows are kFeatureWidth bf16 values:
+// kFeatBlock values of the ommatidium itself then of its kNeighbours nearest
+// neighbours, zero padded.
+constexpr int kNeighbours = 6;
+constexpr int kFeatBlock = 15;
+constexpr int kFeatureWidth = 112;
+static_assert(kFeatBlock * (kNeighbours + 1) <= kFeatureWidth, "feature row too narrow");
+
+// bf16 GEMM C[M x N] = A[M x K] * B[K x N] (see mlp.cu for layouts/modes).
+cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
+                     bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
+                     cudaStream_t stream);
+cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream);
+cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream);
+cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
+                    void* dyb, float* lossSum, cudaStream_t stream);
+cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
+                     int t, void* wb, cudaStream_t stream);
+cudaError_t toBf16(const float* in, void* out, size_t n, cudaStream_t stream);
+cudaError_t nearestOmmatidia(const float4* omm, uint32_t N, int* nb, cudaStream_t stream);
+cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P, void* X,
+                             float* base, cudaStream_t stream);
+cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
+                       float* baseo, float* targeto, cudaStream_t stream);
+
 // Tuning variants of the plain render kernel (see render.cu); the variant
 // is process-wide and picked by the autotuner in eye_renderer.cpp.
 int renderVariantCount();

@@ -25,6 +25,7 @@
 #include "../../include/libEyeRenderer.h"
 #include "bvh.hpp"
 #include "device_api.hpp"
+#include "denoiser.hpp"
 #include "scene.hpp"
 
 namespace cr {
@@ -1115,6 +1116,242 @@ int crSetRenderVariant(int variant) {
 int crGetRenderVariant(void) { return renderVariant(); }
 
 int crGetRenderVariantCount(void) { return renderVariantCount(); }
+
+// ---------------------------------------------------------------------------
+// Learned denoiser (denoiser.hpp): the network is process-wide; its feature
+// render uses its own random streams (spp of the feature render) so that the
+// camera's own streams are untouched.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace cr {
+namespace {
+
+struct DenoiseState {
+  Denoiser net;
+  size_t cam = static_cast<size_t>(-1);
+  uint64_t generation = ~0ull;
+  DevBuf<int> nb;
+  DevBuf<uint32_t> featRng, targetRng;
+  uint32_t featSpp = 0, targetSpp = 0;
+  bool featReady = false, targetReady = false;
+  DevBuf<float> stats, base, out, scratch;
+  DevBuf<uint16_t> X;
+  DevBuf<float4> poses;
+};
+
+DenoiseState& DS() {
+  static DenoiseState d;
+  return d;
+}
+
+// Ties the denoiser's per-eye state (neighbour table, streams) to the
+// current eye, rebuilding it when the eye or its buffers changed.
+EyeDev& denoiseEye(Renderer& r, DenoiseState& d) {
+  if (!r.compoundActive()) throw std::runtime_error("current camera is not a compound eye");
+  EyeDev& e = r.syncEye(r.current);
+  if (d.cam != r.current || d.generation != r.generation) {
+    d.cam = r.current;
+    d.generation = r.generation;
+    d.nb.release();
+    d.nb.ensure(std::max<size_t>(1, static_cast<size_t>(kNeighbours) * e.N));
+    check(nearestOmmatidia(e.omm.ptr, e.N, d.nb.ptr, r.stream()), "neighbour search");
+    d.featReady = d.targetReady = false;
+    d.featSpp = d.targetSpp = 0;
+  }
+  return e;
+}
+
+DevEye streamsFor(Renderer& r, EyeDev& e, DevBuf<uint32_t>& rng, uint32_t& haveSpp, bool& ready, uint32_t spp) {
+  DevEye d;
+  d.omm = e.omm.ptr;
+  d.N = e.N;
+  d.spp = spp;
+  if (haveSpp != spp || !ready) {
+    rng.release();
+    rng.ensure(std::max<size_t>(1, static_cast<size_t>(kRngPlanes) * e.N * spp));
+    d.rng = rng.ptr;
+    check(launchRngInit(d, r.errWord(), r.stream()), "rng init launch");
+    haveSpp = spp;
+    ready = true;
+  }
+  d.rng = rng.ptr;
+  return d;
+}
+
+// Feature rows (and 8-sample means) of `count` device poses of the current eye.
+void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dposes, size_t count, uint32_t featSpp) {
+  if (featSpp < 1 || featSpp > 32) throw std::runtime_error("feature renders use 1 to 32 samples per ommatidium");
+  const DevEye fe = streamsFor(r, e, d.featRng, d.featSpp, d.featReady, featSpp);
+  d.stats.ensure(std::max<size_t>(1, count * e.N * kFeatureStats));
+  d.X.ensure(std::max<size_t>(1, count * e.N * kFeatureWidth));
+  d.base.ensure(std::max<size_t>(1, count * e.N * 3));
+  for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
+    const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+    check(launchFeatures(r.dev, fe, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
+                         r.stream()),
+          "feature render");
+  }
+  check(assembleFeatures(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, static_cast<uint32_t>(count), d.X.ptr, d.base.ptr,
+                         r.stream()),
+        "feature rows");
+}
+
+void uploadPoses12(DevBuf<float4>& dst, const float* poses12, size_t count, cudaStream_t s) {
+  std::vector<float> p16(16 * count, 0.f);
+  for (size_t i = 0; i < count; ++i)
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) p16[16 * i + 4 * k + c] = poses12[12 * i + 3 * k + c];
+  dst.ensure(std::max<size_t>(1, 4 * count));
+  check(cudaMemcpyAsync(dst.ptr, p16.data(), p16.size() * 4, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+}
+
+}  // namespace
+}  // namespace cr
+
+extern "C" {
+
+int crDenoiserInit(int seed) {
+  return guarded(
+      "crDenoiserInit",
+      [&]() -> int {
+        DS().net.init(static_cast<uint32_t>(seed), R().stream());
+        return 0;
+      },
+      -1);
+}
+
+size_t crDenoiserParamCount(void) { return Denoiser::kParams; }
+
+int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSpp, int targetSpp) {
+  return guarded(
+      "crDenoiserAddTrainingPoses",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit first");
+        if (!poses12 || count == 0) throw std::runtime_error("no poses");
+        if (targetSpp < 1) throw std::runtime_error("target sample count must be positive");
+        EyeDev& e = denoiseEye(r, d);
+        uploadPoses12(d.poses, poses12, count, r.stream());
+        denoiseFeatures(r, d, e, d.poses.ptr, count, static_cast<uint32_t>(featureSpp));
+        const DevEye te = streamsFor(r, e, d.targetRng, d.targetSpp, d.targetReady, static_cast<uint32_t>(targetSpp));
+        d.out.ensure(std::max<size_t>(1, count * e.N * 3));
+        for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
+          const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+          const size_t need = renderScratchFloats(e.N, te.spp, P);
+          if (need) d.scratch.ensure(need);
+          check(launchRender(r.dev, te, d.poses.ptr + 4 * first, P, d.out.ptr + 3 * first * e.N,
+                             need ? d.scratch.ptr : nullptr, r.errWord(), nullptr, r.stream()),
+                "target render");
+        }
+        d.net.addRows(d.X.ptr, d.base.ptr, d.out.ptr, count * e.N, r.stream());
+        r.checkErrWord();
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserTrain(int steps, int batch, float lr, int seed, float* lossHistory) {
+  return guarded(
+      "crDenoiserTrain",
+      [&]() -> int {
+        DS().net.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+size_t crDenoiserTrainingRows(void) { return DS().net.rows(); }
+
+int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out) {
+  return guarded(
+      "crDenoiserRenderPosesDevice",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit or crDenoiserLoad first");
+        if (count == 0) return 0;
+        if (!d_poses || !d_out) throw std::runtime_error("null pointer");
+        EyeDev& e = denoiseEye(r, d);
+        denoiseFeatures(r, d, e, reinterpret_cast<const float4*>(d_poses), count, static_cast<uint32_t>(featureSpp));
+        d.net.infer(d.X.ptr, d.base.ptr, count * e.N, d_out, r.stream());
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserRenderPoses(const float* poses12, size_t count, int featureSpp, float* out) {
+  return guarded(
+      "crDenoiserRenderPoses",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!poses12 || !out) throw std::runtime_error("null pointer");
+        if (count == 0) return 0;
+        EyeDev& e = denoiseEye(r, d);
+        uploadPoses12(d.poses, poses12, count, r.stream());
+        DevBuf<float> o;
+        o.ensure(std::max<size_t>(1, count * e.N * 3));
+        if (crDenoiserRenderPosesDevice(reinterpret_cast<const float*>(d.poses.ptr), count, featureSpp, o.ptr) != 0)
+          throw std::runtime_error(g_lastError);
+        check(cudaMemcpyAsync(out, o.ptr, count * e.N * 12, cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        r.checkErrWord();
+        o.release();
+        return 0;
+      },
+      -1);
+}
+
+float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* target, int rows, float* grads,
+                         float* params) {
+  return guarded(
+      "crDenoiserGradient",
+      [&]() -> float {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit first");
+        if (rows <= 0 || !xBf16 || !base || !target) throw std::runtime_error("empty input");
+        DevBuf<uint16_t> X;
+        DevBuf<float> b, t;
+        X.ensure(static_cast<size_t>(rows) * kFeatureWidth);
+        b.ensure(static_cast<size_t>(rows) * 3);
+        t.ensure(static_cast<size_t>(rows) * 3);
+        cudaStream_t s = r.stream();
+        check(cudaMemcpyAsync(X.ptr, xBf16, static_cast<size_t>(rows) * kFeatureWidth * 2, cudaMemcpyHostToDevice, s),
+              "cudaMemcpy");
+        check(cudaMemcpyAsync(b.ptr, base, static_cast<size_t>(rows) * 12, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(t.ptr, target, static_cast<size_t>(rows) * 12, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        const float l = d.net.gradient(X.ptr, b.ptr, t.ptr, rows, grads, params, s);
+        X.release();
+        b.release();
+        t.release();
+        return l;
+      },
+      -1.0f);
+}
+
+int crDenoiserSave(const char* path) {
+  return guarded(
+      "crDenoiserSave",
+      [&]() -> int {
+        if (!path) throw std::runtime_error("null path");
+        DS().net.save(path, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserLoad(const char* path) {
+  return guarded(
+      "crDenoiserLoad",
+      [&]() -> int {
+        if (!path) throw std::runtime_error("null path");
+        DS().net.load(path, R().stream());
+        return 0;
+      },
+      -1);
+}
 
 int crSetBvhBuilder(int kind) {
   if (kind != 0 && kind != 1) {

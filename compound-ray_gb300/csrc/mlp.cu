@@ -1,0 +1,381 @@
+// Learned per-ommatidium denoiser: a 4-layer MLP (width 128, ReLU) trained
+// and run on the GPU with BF16 tensor-core GEMMs accumulating in FP32.
+//
+// The denoiser maps an 8-sample estimate of an ommatidium and of its six
+// nearest neighbours (sample statistics from the feature render, the
+// ommatidial axis and acceptance angle) to a correction of the 8-sample mean
+// colour; the target is a high-sample render of the same pose.  Everything
+// here is device code driven by the host class in denoiser.cpp:
+//   gemmKernel       C = A * B with bf16 operands (mma.sync m16n8k16, fp32
+//                    accumulators) and fused epilogues (bias, ReLU, ReLU
+//                    derivative mask, plain fp32 store);
+//   colSumKernel     bias gradients;
+//   lossKernel       residual prediction, squared error and its gradient;
+//   adamKernel       Adam on fp32 master weights, refreshing the bf16 copy;
+//   knnKernel        six nearest ommatidia by axis direction;
+//   featureKernel    assembles the 112-wide bf16 feature rows.
+// The GEMMs are 128 wide: the network is launch- and latency-bound, not
+// tensor-throughput-bound, so the warp-level mma.sync instruction is used.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_api.hpp"
+
+namespace cr {
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 32;
+constexpr int kPad = 8;  // bf16 elements of padding per smem row
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return static_cast<uint32_t>(__bfloat16_as_ushort(lo)) | (static_cast<uint32_t>(__bfloat16_as_ushort(hi)) << 16);
+}
+
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[M x N] = A[M x K] * B[K x N].
+//  A: aTrans ? stored K x M row-major (A[m][k] = A[k*lda + m]) : M x K (A[m*lda + k]).
+//  B: bTrans ? stored N x K row-major (B[k][n] = B[n*ldb + k]) : K x N (B[k*ldb + n]).
+// Epilogue (mode):
+//  0: Cf[m*ldc+n] = acc
+//  1: Cf = acc + bias[n]; Hb[m*ldc+n] = bf16(max(Cf, 0))        (hidden layer forward)
+//  2: Hb[m*ldc+n] = bf16(acc * (mask[m*ldc+n] > 0))             (back through ReLU)
+//  3: Cf = acc + bias[n]                                       (output layer)
+template <int kMode>
+__global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+                                                  bool aTrans, const __nv_bfloat16* __restrict__ B, int ldb,
+                                                  bool bTrans, float* __restrict__ Cf, __nv_bfloat16* __restrict__ Hb,
+                                                  int ldc, const float* __restrict__ bias,
+                                                  const __nv_bfloat16* __restrict__ mask) {
+  __shared__ __nv_bfloat16 As[BM][BK + kPad];
+  __shared__ __nv_bfloat16 Bs[BN][BK + kPad];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 1, wn = warp & 1;  // 2 x 2 warps of 32 x 32
+  const int g = lane >> 2, q = lane & 3;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += 128) {
+      const int r = e / BK, c = e % BK;
+      const int m = m0 + r, k = k0 + c;
+      __nv_bfloat16 v = zero;
+      if (m < M && k < K) v = aTrans ? A[static_cast<size_t>(k) * lda + m] : A[static_cast<size_t>(m) * lda + k];
+      As[r][c] = v;
+    }
+    for (int e = tid; e < BN * BK; e += 128) {
+      const int r = e / BK, c = e % BK;
+      const int n = n0 + r, k = k0 + c;
+      __nv_bfloat16 v = zero;
+      if (n < N && k < K) v = bTrans ? B[static_cast<size_t>(n) * ldb + k] : B[static_cast<size_t>(k) * ldb + n];
+      Bs[r][c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bf[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r0 = wm * 32 + i * 16 + g;
+        const int c0 = kk + q * 2;
+        af[i][0] = pack2(As[r0][c0], As[r0][c0 + 1]);
+        af[i][1] = pack2(As[r0 + 8][c0], As[r0 + 8][c0 + 1]);
+        af[i][2] = pack2(As[r0][c0 + 8], As[r0][c0 + 9]);
+        af[i][3] = pack2(As[r0 + 8][c0 + 8], As[r0 + 8][c0 + 9]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nr = wn * 32 + j * 8 + g;
+        const int c0 = kk + q * 2;
+        bf[j][0] = pack2(Bs[nr][c0], Bs[nr][c0 + 1]);
+        bf[j][1] = pack2(Bs[nr][c0 + 8], Bs[nr][c0 + 9]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma16816(acc[i][j], af[i], bf[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm * 32 + i * 16 + g + (r >= 2 ? 8 : 0);
+        const int n = n0 + wn * 32 + j * 8 + q * 2 + (r & 1);
+        if (m >= M || n >= N) continue;
+        const size_t o = static_cast<size_t>(m) * ldc + n;
+        float v = acc[i][j][r];
+        if (kMode == 0) {
+          Cf[o] = v;
+        } else if (kMode == 1) {
+          v += bias[n];
+          Cf[o] = v;
+          Hb[o] = __float2bfloat16(fmaxf(v, 0.f));
+        } else if (kMode == 2) {
+          Hb[o] = __float2bfloat16(__bfloat162float(mask[o]) > 0.f ? v : 0.f);
+        } else {
+          Cf[o] = v + bias[n];
+        }
+      }
+}
+
+// out[n] = sum over m of in[m*ld + n], for bf16 or fp32 input.
+template <typename T>
+__global__ void colSumKernel(const T* __restrict__ in, int M, int N, int ld, float* __restrict__ out) {
+  const int n = blockIdx.x;
+  float s = 0.f;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    if constexpr (sizeof(T) == 2) s += __bfloat162float(in[static_cast<size_t>(m) * ld + n]);
+    else s += in[static_cast<size_t>(m) * ld + n];
+  }
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = red[0];
+}
+
+// Prediction = base + y[:, :3]; squared error against target; gradient of
+// the mean squared error w.r.t. y (fp32 and bf16 copies, padded columns 0).
+__global__ void lossKernel(const float* __restrict__ y, int ldy, const float* __restrict__ base,
+                           const float* __restrict__ target, int rows, float* __restrict__ pred,
+                           float* __restrict__ dyf, __nv_bfloat16* __restrict__ dyb, float* __restrict__ lossSum) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  float e2 = 0.f;
+  if (r < rows) {
+    const float scale = 2.0f / (3.0f * static_cast<float>(rows));
+    for (int c = 0; c < ldy; ++c) {
+      float g = 0.f;
+      if (c < 3) {
+        const float p = base[3 * r + c] + y[static_cast<size_t>(r) * ldy + c];
+        if (pred) pred[3 * r + c] = p;
+        if (target) {
+          const float d = p - target[3 * r + c];
+          e2 += d * d;
+          g = scale * d;
+        }
+      }
+      if (dyf) dyf[static_cast<size_t>(r) * ldy + c] = g;
+      if (dyb) dyb[static_cast<size_t>(r) * ldy + c] = __float2bfloat16(g);
+    }
+  }
+  if (lossSum) {
+    for (int m = 16; m >= 1; m >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, m);
+    if ((threadIdx.x & 31) == 0) atomicAdd(lossSum, e2);
+  }
+}
+
+__global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                           float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2,
+                           __nv_bfloat16* __restrict__ wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  w[i] = wi;
+  if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+__global__ void toBf16Kernel(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, size_t n) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __float2bfloat16(in[i]);
+}
+
+// Six nearest ommatidia of each ommatidium by the angle between axes.
+__global__ void knnKernel(const float4* __restrict__ omm, uint32_t N, int* __restrict__ nb) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= N) return;
+  const float4 a = omm[2 * o], b = omm[2 * o + 1];
+  float ax = a.w, ay = b.x, az = b.y;
+  const float il = rsqrtf(fmaxf(ax * ax + ay * ay + az * az, 1e-30f));
+  ax *= il;
+  ay *= il;
+  az *= il;
+  float best[kNeighbours];
+  int idx[kNeighbours];
+  for (int k = 0; k < kNeighbours; ++k) {
+    best[k] = -2.f;
+    idx[k] = static_cast<int>(o);
+  }
+  for (uint32_t j = 0; j < N; ++j) {
+    if (j == o) continue;
+    const float4 c = omm[2 * j], d = omm[2 * j + 1];
+    const float l = rsqrtf(fmaxf(c.w * c.w + d.x * d.x + d.y * d.y, 1e-30f));
+    const float s = (ax * c.w + ay * d.x + az * d.y) * l;
+    if (s <= best[kNeighbours - 1]) continue;
+    int k = kNeighbours - 1;
+    while (k > 0 && best[k - 1] < s) {
+      best[k] = best[k - 1];
+      idx[k] = idx[k - 1];
+      --k;
+    }
+    best[k] = s;
+    idx[k] = static_cast<int>(j);
+  }
+  for (int k = 0; k < kNeighbours; ++k) nb[kNeighbours * o + k] = idx[k];
+}
+
+// Per-ommatidium feature block (kFeatBlock floats) from its statistics.
+__device__ __forceinline__ void featureBlock(const float* __restrict__ s, const float4* __restrict__ omm, uint32_t o,
+                                             float* f) {
+  const float m0 = s[0], m1 = s[1], m2 = s[2];
+  f[0] = m0;
+  f[1] = m1;
+  f[2] = m2;
+  f[3] = sqrtf(fmaxf(s[3] - m0 * m0, 0.f));
+  f[4] = sqrtf(fmaxf(s[4] - m1 * m1, 0.f));
+  f[5] = sqrtf(fmaxf(s[5] - m2 * m2, 0.f));
+  const float hit = s[6];
+  f[6] = hit;
+  const float depth = hit > 0.f ? s[7] / hit : 0.f;
+  f[7] = log1pf(depth) * 0.25f;
+  f[8] = s[8];
+  f[9] = s[9];
+  f[10] = s[10];
+  const float4 a = omm[2 * o], b = omm[2 * o + 1];
+  const float il = rsqrtf(fmaxf(a.w * a.w + b.x * b.x + b.y * b.y, 1e-30f));
+  f[11] = a.w * il;
+  f[12] = b.x * il;
+  f[13] = b.y * il;
+  f[14] = b.z * 10.0f;
+}
+
+// Feature rows: [own block, 6 neighbour blocks, zero padding] as bf16, and
+// the own 8-sample mean colour as the residual base (fp32).
+__global__ void featureKernel(const float* __restrict__ stats, const float4* __restrict__ omm,
+                              const int* __restrict__ nb, uint32_t N, uint32_t P, __nv_bfloat16* __restrict__ X,
+                              float* __restrict__ base) {
+  const size_t row = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= static_cast<size_t>(P) * N) return;
+  const uint32_t p = static_cast<uint32_t>(row / N), o = static_cast<uint32_t>(row % N);
+  __nv_bfloat16* x = X + row * kFeatureWidth;
+  float f[kFeatBlock];
+  const float* sp = stats + static_cast<size_t>(p) * N * kFeatureStats;
+  featureBlock(sp + static_cast<size_t>(o) * kFeatureStats, omm, o, f);
+  for (int k = 0; k < kFeatBlock; ++k) x[k] = __float2bfloat16(f[k]);
+  base[3 * row] = f[0];
+  base[3 * row + 1] = f[1];
+  base[3 * row + 2] = f[2];
+  for (int j = 0; j < kNeighbours; ++j) {
+    const uint32_t q = static_cast<uint32_t>(nb[kNeighbours * o + j]);
+    featureBlock(sp + static_cast<size_t>(q) * kFeatureStats, omm, q, f);
+    for (int k = 0; k < kFeatBlock; ++k) x[kFeatBlock * (j + 1) + k] = __float2bfloat16(f[k]);
+  }
+  for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) x[k] = __float2bfloat16(0.f);
+}
+
+__global__ void gatherRowsKernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ base,
+                                 const float* __restrict__ target, const uint32_t* __restrict__ idx, int rows,
+                                 __nv_bfloat16* __restrict__ Xo, float* __restrict__ baseo, float* __restrict__ targeto) {
+  const int r = blockIdx.x;
+  if (r >= rows) return;
+  const size_t src = idx[r];
+  for (int k = threadIdx.x; k < kFeatureWidth; k += blockDim.x)
+    Xo[static_cast<size_t>(r) * kFeatureWidth + k] = X[src * kFeatureWidth + k];
+  if (threadIdx.x < 3) {
+    baseo[3 * r + threadIdx.x] = base[3 * src + threadIdx.x];
+    targeto[3 * r + threadIdx.x] = target[3 * src + threadIdx.x];
+  }
+}
+
+}  // namespace
+
+cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
+                     bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
+                     cudaStream_t stream) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  auto a = static_cast<const __nv_bfloat16*>(A);
+  auto b = static_cast<const __nv_bfloat16*>(B);
+  auto h = static_cast<__nv_bfloat16*>(Hb);
+  auto mk = static_cast<const __nv_bfloat16*>(mask);
+  switch (mode) {
+    case 0: gemmKernel<0><<<grid, 128, 0, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk); break;
+    case 1: gemmKernel<1><<<grid, 128, 0, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk); break;
+    case 2: gemmKernel<2><<<grid, 128, 0, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk); break;
+    default: gemmKernel<3><<<grid, 128, 0, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream) {
+  colSumKernel<__nv_bfloat16><<<N, 256, 0, stream>>>(static_cast<const __nv_bfloat16*>(in), M, N, ld, out);
+  return cudaGetLastError();
+}
+
+cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream) {
+  colSumKernel<float><<<N, 256, 0, stream>>>(in, M, N, ld, out);
+  return cudaGetLastError();
+}
+
+cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
+                    void* dyb, float* lossSum, cudaStream_t stream) {
+  if (rows <= 0) return cudaSuccess;
+  lossKernel<<<(rows + 255) / 256, 256, 0, stream>>>(y, ldy, base, target, rows, pred, dyf,
+                                                      static_cast<__nv_bfloat16*>(dyb), lossSum);
+  return cudaGetLastError();
+}
+
+cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
+                     int t, void* wb, cudaStream_t stream) {
+  const float c1 = 1.f / (1.f - powf(b1, static_cast<float>(t)));
+  const float c2 = 1.f / (1.f - powf(b2, static_cast<float>(t)));
+  adamKernel<<<(n + 255) / 256, 256, 0, stream>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2,
+                                                   static_cast<__nv_bfloat16*>(wb));
+  return cudaGetLastError();
+}
+
+cudaError_t toBf16(const float* in, void* out, size_t n, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  toBf16Kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(in, static_cast<__nv_bfloat16*>(out), n);
+  return cudaGetLastError();
+}
+
+cudaError_t nearestOmmatidia(const float4* omm, uint32_t N, int* nb, cudaStream_t stream) {
+  if (N == 0) return cudaSuccess;
+  knnKernel<<<(N + 127) / 128, 128, 0, stream>>>(omm, N, nb);
+  return cudaGetLastError();
+}
+
+cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P, void* X,
+                             float* base, cudaStream_t stream) {
+  const size_t rows = static_cast<size_t>(P) * N;
+  if (rows == 0) return cudaSuccess;
+  featureKernel<<<static_cast<unsigned>((rows + 127) / 128), 128, 0, stream>>>(
+      stats, omm, nb, N, P, static_cast<__nv_bfloat16*>(X), base);
+  return cudaGetLastError();
+}
+
+cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
+                       float* baseo, float* targeto, cudaStream_t stream) {
+  if (rows <= 0) return cudaSuccess;
+  gatherRowsKernel<<<rows, 128, 0, stream>>>(static_cast<const __nv_bfloat16*>(X), base, target, idx, rows,
+                                             static_cast<__nv_bfloat16*>(Xo), baseo, targeto);
+  return cudaGetLastError();
+}
+
+}  // namespace cr

@@ -387,6 +387,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
                                            RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests) {
   constexpr bool kRecord = kMode == 1;
   constexpr bool kCount = kMode == 2;
+  constexpr bool kFeat = kMode == 3;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t group = static_cast<uint32_t>(task / plan.chunks);
   const uint32_t chunk = static_cast<uint32_t>(task % plan.chunks);
@@ -417,6 +418,9 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
 
   for (uint32_t p = 0; p < P; ++p) {
     v3 col = mk(0.f, 0.f, 0.f);
+    // Feature mode: per-sample squared colour, hit flag, hit distance and the
+    // hit triangle's normal in the eye's frame (facing the ray), all / spp.
+    float f2x = 0.f, f2y = 0.f, f2z = 0.f, fHit = 0.f, fT = 0.f, fnx = 0.f, fny = 0.f, fnz = 0.f;
     if (valid) {
       const float4* pp = poses + 4 * p;
       const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
@@ -461,12 +465,55 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
         R.pad = 0.f;
       }
       col = c * invSpp;
+      if (kFeat) {
+        f2x = c.x * c.x * invSpp;
+        f2y = c.y * c.y * invSpp;
+        f2z = c.z * c.z * invSpp;
+        if (h.id != 0xffffffffu) {
+          fHit = invSpp;
+          fT = h.t * invSpp;
+          const float4* t = sc.tris + 3 * h.pos;
+          const float4 a = __ldg(t), b = __ldg(t + 1), cc = __ldg(t + 2);
+          v3 n = normalize(cross(mk(b.x - a.x, b.y - a.y, b.z - a.z), mk(cc.x - a.x, cc.y - a.y, cc.z - a.z)));
+          if (dot(n, dir) > 0.f) n = n * -1.0f;
+          fnx = dot(n, mk(X.x, X.y, X.z)) * invSpp;
+          fny = dot(n, mk(Y.x, Y.y, Y.z)) * invSpp;
+          fnz = dot(n, mk(Z.x, Z.y, Z.z)) * invSpp;
+        }
+      }
     }
     // Segmented butterfly reduction over the samples of each ommatidium.
     for (uint32_t m = plan.segWidth >> 1; m >= 1u; m >>= 1) {
       col.x += __shfl_xor_sync(0xffffffffu, col.x, static_cast<int>(m));
       col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
       col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
+      if (kFeat) {
+        f2x += __shfl_xor_sync(0xffffffffu, f2x, static_cast<int>(m));
+        f2y += __shfl_xor_sync(0xffffffffu, f2y, static_cast<int>(m));
+        f2z += __shfl_xor_sync(0xffffffffu, f2z, static_cast<int>(m));
+        fHit += __shfl_xor_sync(0xffffffffu, fHit, static_cast<int>(m));
+        fT += __shfl_xor_sync(0xffffffffu, fT, static_cast<int>(m));
+        fnx += __shfl_xor_sync(0xffffffffu, fnx, static_cast<int>(m));
+        fny += __shfl_xor_sync(0xffffffffu, fny, static_cast<int>(m));
+        fnz += __shfl_xor_sync(0xffffffffu, fnz, static_cast<int>(m));
+      }
+    }
+    if (kFeat) {
+      if ((lane % plan.segWidth) == 0u && o < eye.N) {
+        float* dst = out + (static_cast<size_t>(p) * eye.N + o) * kFeatureStats;
+        dst[0] = col.x;
+        dst[1] = col.y;
+        dst[2] = col.z;
+        dst[3] = f2x;
+        dst[4] = f2y;
+        dst[5] = f2z;
+        dst[6] = fHit;
+        dst[7] = fT;
+        dst[8] = fnx;
+        dst[9] = fny;
+        dst[10] = fnz;
+      }
+      continue;
     }
     if ((lane % plan.segWidth) == 0u && o < eye.N) {
       float* dst = plan.chunks == 1 ? out + (static_cast<size_t>(p) * eye.N + o) * 3
@@ -690,6 +737,17 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
   if (e != cudaSuccess || plan.chunks == 1) return e;
   const size_t count = static_cast<size_t>(P) * eye.N;
   combineChunksKernel<<<static_cast<unsigned>((count + 255) / 256), 256, 0, stream>>>(scratch, plan.chunks, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
+                           uint32_t* errFlag, cudaStream_t stream) {
+  if (P == 0 || eye.N == 0) return cudaSuccess;
+  const WarpPlan plan = planWarps(eye.N, eye.spp);
+  if (plan.chunks != 1) return cudaErrorInvalidValue;  // feature renders use at most 32 samples
+  const uint64_t blocks = (plan.tasks * 32 + 127) / 128;
+  renderKernel<3, 5><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr,
+                                                                         errFlag, nullptr, nullptr);
   return cudaGetLastError();
 }
 

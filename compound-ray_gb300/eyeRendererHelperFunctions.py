@@ -124,6 +124,25 @@ def configureExtras(eyeRenderer):
     L.crRenderPoses.restype = c_int
     L.crRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDevice.restype = c_int
+    f32 = ndpointer(np.float32, flags="C_CONTIGUOUS")
+    L.crDenoiserInit.argtypes = [c_int]
+    L.crDenoiserInit.restype = c_int
+    L.crDenoiserParamCount.restype = c_size_t
+    L.crDenoiserAddTrainingPoses.argtypes = [f32, c_size_t, c_int, c_int]
+    L.crDenoiserAddTrainingPoses.restype = c_int
+    L.crDenoiserTrainingRows.restype = c_size_t
+    L.crDenoiserTrain.argtypes = [c_int, c_int, c_float, c_int, c_void_p]
+    L.crDenoiserTrain.restype = c_int
+    L.crDenoiserRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p]
+    L.crDenoiserRenderPosesDevice.restype = c_int
+    L.crDenoiserRenderPoses.argtypes = [f32, c_size_t, c_int, f32]
+    L.crDenoiserRenderPoses.restype = c_int
+    L.crDenoiserGradient.argtypes = [ndpointer(np.uint16, flags="C_CONTIGUOUS"), f32, f32, c_int, f32, f32]
+    L.crDenoiserGradient.restype = c_float
+    L.crDenoiserSave.argtypes = [c_char_p]
+    L.crDenoiserSave.restype = c_int
+    L.crDenoiserLoad.argtypes = [c_char_p]
+    L.crDenoiserLoad.restype = c_int
     L.crSetBvhBuilder.argtypes = [c_int]
     L.crSetBvhBuilder.restype = c_int
     L.crGetBvhBuilder.restype = c_int

@@ -153,6 +153,36 @@ int crSetRenderVariant(int variant);
 int crGetRenderVariant(void);
 int crGetRenderVariantCount(void);
 
+/* ---- Learned per-ommatidium denoiser ------------------------------------
+ * A 4-layer MLP (feature row of 112 -> 128 -> 128 -> 128 -> 3, ReLU) that
+ * predicts a correction to an ommatidium's low-sample mean colour from the
+ * sample statistics (mean, spread, hit fraction, depth, normal), axis and
+ * acceptance angle of the ommatidium and of its 6 nearest ommatidia.  It is
+ * trained and run on the GPU with bf16 tensor-core GEMMs accumulating in
+ * fp32 and Adam on fp32 master weights.  Its feature renders use their own
+ * random streams; the camera's streams are not touched. */
+int crDenoiserInit(int seed);                 /* fresh He-initialised weights */
+size_t crDenoiserParamCount(void);
+/* Renders `count` host poses (12 floats each) of the current eye twice --
+ * a featureSpp-sample feature render and a targetSpp-sample plain render --
+ * and appends count x N (features, target) rows to the training set. */
+int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSpp, int targetSpp);
+size_t crDenoiserTrainingRows(void);
+/* `steps` Adam steps on shuffled minibatches; lossHistory: steps floats
+ * (mean squared error per step) or null. */
+int crDenoiserTrain(int steps, int batch, float lr, int seed, float* lossHistory);
+/* The learned form: featureSpp-sample render + network, count x N x 3. */
+int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out);
+int crDenoiserRenderPoses(const float* poses12, size_t count, int featureSpp, float* out);
+/* One forward/backward pass on host rows (x: rows x 112 bf16 bit patterns,
+ * base/target: rows x 3): returns the loss (-1 on error) and writes the
+ * gradients and the current parameters (crDenoiserParamCount floats each). */
+float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* target, int rows, float* grads,
+                         float* params);
+/* Checkpoint of the parameters and Adam moments (binary, with a header). */
+int crDenoiserSave(const char* path);
+int crDenoiserLoad(const char* path);
+
 /* BVH builder for scenes loaded afterwards: 0 = host binned SAH (default),
  * 1 = GPU linear BVH (Morton codes, radix sort, Karras hierarchy) built at
  * the first render.  Results are identical either way (the closest hit does

@@ -1,0 +1,74 @@
+"""Reference forward/backward of the denoiser MLP in numpy.  TEST
+INFRASTRUCTURE ONLY (the checker of the GPU training kernels).
+
+Same network and rounding points as the GPU path (compound-ray_gb300/csrc/
+denoiser.cpp): bf16 copies of the weights, bf16 hidden activations after
+ReLU, bf16 output gradient and bf16 back-propagated gradients after the ReLU
+mask; everything else accumulates in float64 here (fp32 on the GPU).
+"""
+import numpy as np
+
+FEAT = 112
+HID = 128
+OUT = 8
+OFF_W1 = 0
+OFF_B1 = OFF_W1 + FEAT * HID
+OFF_W2 = OFF_B1 + HID
+OFF_B2 = OFF_W2 + HID * HID
+OFF_W3 = OFF_B2 + HID
+OFF_B3 = OFF_W3 + HID * HID
+OFF_W4 = OFF_B3 + HID
+OFF_B4 = OFF_W4 + HID * OUT
+N_PARAMS = OFF_B4 + OUT
+
+
+def bf16(x):
+    """Round float32 values to bfloat16 (nearest even) and back."""
+    x = np.ascontiguousarray(x, np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    rounded = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return rounded.astype(np.uint32).view(np.float32)
+
+
+def bf16_bits(x):
+    x = np.ascontiguousarray(x, np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    return (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
+
+
+def unpack(params):
+    p = np.asarray(params, np.float32)
+    return (p[OFF_W1:OFF_B1].reshape(FEAT, HID), p[OFF_B1:OFF_W2], p[OFF_W2:OFF_B2].reshape(HID, HID),
+            p[OFF_B2:OFF_W3], p[OFF_W3:OFF_B3].reshape(HID, HID), p[OFF_B3:OFF_W4], p[OFF_W4:OFF_B4].reshape(HID, OUT),
+            p[OFF_B4:N_PARAMS])
+
+
+def forward_backward(params, X, base, target):
+    """Loss and gradient vector (layout of the parameter vector)."""
+    W1, b1, W2, b2, W3, b3, W4, b4 = unpack(params)
+    W1b, W2b, W3b, W4b = (bf16(w).astype(np.float64) for w in (W1, W2, W3, W4))
+    X = bf16(X).astype(np.float64)
+    H1 = bf16(np.maximum(X @ W1b + b1, 0).astype(np.float32)).astype(np.float64)
+    H2 = bf16(np.maximum(H1 @ W2b + b2, 0).astype(np.float32)).astype(np.float64)
+    H3 = bf16(np.maximum(H2 @ W3b + b3, 0).astype(np.float32)).astype(np.float64)
+    Y = H3 @ W4b + b4
+    rows = len(X)
+    pred = base + Y[:, :3]
+    diff = pred - target
+    loss = float((diff ** 2).mean())
+    dY = np.zeros((rows, OUT))
+    dY[:, :3] = 2.0 * diff / (3.0 * rows)
+    dYb = bf16(dY.astype(np.float32)).astype(np.float64)
+    g = np.zeros(N_PARAMS)
+    g[OFF_W4:OFF_B4] = (H3.T @ dYb).ravel()
+    g[OFF_B4:N_PARAMS] = dY.sum(0)
+    dZ3 = bf16(((dYb @ W4b.T) * (H3 > 0)).astype(np.float32)).astype(np.float64)
+    g[OFF_W3:OFF_B3] = (H2.T @ dZ3).ravel()
+    g[OFF_B3:OFF_W4] = dZ3.sum(0)
+    dZ2 = bf16(((dZ3 @ W3b.T) * (H2 > 0)).astype(np.float32)).astype(np.float64)
+    g[OFF_W2:OFF_B2] = (H1.T @ dZ2).ravel()
+    g[OFF_B2:OFF_W3] = dZ2.sum(0)
+    dZ1 = bf16(((dZ2 @ W2b.T) * (H1 > 0)).astype(np.float32)).astype(np.float64)
+    g[OFF_W1:OFF_B1] = (X.T @ dZ1).ravel()
+    g[OFF_B1:OFF_W2] = dZ1.sum(0)
+    return loss, g
