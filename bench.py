@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="target wall time of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-eye batching measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurement")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
@@ -331,6 +332,7 @@ def run_ours(args):
     e2e_value = world * rays_step * args.steps / e2e_total
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
+    learned = None if args.no_learned else run_learned(lib, eh, args, stream)
 
     if rank != 0:
         if world > 1:
@@ -372,6 +374,8 @@ def run_ours(args):
     }
     if batch:
         line["batch_uneven"] = batch
+    if learned:
+        line["learned_denoiser"] = learned
     if not args.no_cpu_baseline:
         cb = cpu_baseline(info, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -439,6 +443,102 @@ def run_batch(lib, eh, args, stream):
             "rays_per_s": rays / (statistics.mean(ms) / 1000.0),
             "eye_latency_ms_p50": float(np.percentile(lat, 50)), "eye_latency_ms_p99": float(np.percentile(lat, 99)),
             "graph": "one persistent work-queue kernel (+ chunk sums) replayed from a CUDA graph"}
+
+
+def run_learned(lib, eh, args, stream, train_poses=200, held_poses=1000, steps=3000, batch=4096):
+    """Learned denoiser on the small scene and its 1000-ommatidium eye:
+    trains on 200 random poses (200k ommatidium-frames: 8-sample features,
+    1024-sample targets), then on 1000 held-out poses reports the RMSE
+    against the 1024-sample plain render, the plain sample count that matches
+    it, and eye-frames/s of the learned form against the plain form at that
+    matched RMSE (both timed with CUDA events on device-resident poses)."""
+    import ctypes
+
+    import torch
+
+    import scenes
+
+    d = os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED)
+    info = scenes.small_scene(d)
+    lib.crSetStream(stream.cuda_stream)
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    N = lib.getCurrentEyeOmmatidialCount()
+    rng = np.random.default_rng(scenes.SEED + 11)
+
+    def poses(k):
+        return np.stack([scenes.pose_rows(np.array([rng.uniform(-7, 7), rng.uniform(0.2, 1.5), rng.uniform(-7, 7)]),
+                                          rng.uniform(0, 2 * math.pi)) for _ in range(k)]).astype(np.float32)
+
+    train, held = poses(train_poses), poses(held_poses)
+    t0 = time.perf_counter()
+    if lib.crDenoiserInit(1) != 0 or lib.crDenoiserAddTrainingPoses(train, len(train), 8, 1024) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    t_data = time.perf_counter() - t0
+    loss = np.zeros(steps, np.float32)
+    t0 = time.perf_counter()
+    if lib.crDenoiserTrain(steps, batch, 1e-3, 3, loss.ctypes.data) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    t_train = time.perf_counter() - t0
+    p16 = np.zeros((held_poses, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_poses = torch.from_numpy(p16).to(dev)
+    d_out = torch.empty((held_poses, N, 3), dtype=torch.float32, device=dev)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    def learned():
+        if lib.crDenoiserRenderPosesDevice(d_poses.data_ptr(), held_poses, 8, d_out.data_ptr()) != 0:
+            raise RuntimeError(eh.lastError(lib))
+
+    ms_learned = timed(learned)
+    learned_img = d_out.cpu().numpy()
+
+    def plain(spp):
+        lib.setCurrentEyeSamplesPerOmmatidium(spp)
+
+        def run():
+            if lib.crRenderPosesDevice(d_poses.data_ptr(), held_poses, d_out.data_ptr()) != 0:
+                raise RuntimeError(eh.lastError(lib))
+        ms = timed(run, reps=1)
+        return ms, d_out.cpu().numpy()
+
+    _, ref = plain(1024)
+    rmse = lambda a: float(np.sqrt(((a - ref) ** 2).mean()))
+    sweep = {}
+    for spp in (8, 16, 32, 64, 128, 256, 512):
+        ms, img = plain(spp)
+        sweep[spp] = (rmse(img), ms)
+    r_learned = rmse(learned_img)
+    matched = None
+    for spp in sorted(sweep):
+        if sweep[spp][0] <= r_learned:
+            matched = spp
+            break
+    ms_matched = sweep[matched][1] if matched else None
+    fps_learned = held_poses / (ms_learned / 1000.0)
+    return {"scene": "small scene (770 tris), 1000-ommatidium eye", "train_ommatidium_frames": train_poses * N,
+            "held_out_poses": held_poses, "steps": steps, "batch": batch, "final_loss": float(loss[-100:].mean()),
+            "data_s": t_data, "train_s": t_train, "rmse_learned_8spp": r_learned, "rmse_plain_8spp": sweep[8][0],
+            "rmse_plain_by_spp": {str(k): round(v[0], 6) for k, v in sweep.items()},
+            "target_rmse": 1.0 / 255.0, "matched_plain_spp": matched,
+            "eye_frames_per_s_learned": fps_learned,
+            "eye_frames_per_s_plain_matched": (held_poses / (ms_matched / 1000.0)) if ms_matched else None,
+            "speedup_vs_plain_at_matched_rmse": (ms_matched / ms_learned) if ms_matched else None}
 
 
 def ctypes_double():

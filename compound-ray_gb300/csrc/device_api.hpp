@@ -163,5 +163,13 @@ cudaError_t noAllocScratch(float** ptr);
 //  mode 0: single_dimension_fast (row 0, x < N), mode 1: single_dimension.
 cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, int h, int mode,
                           cudaStream_t stream);
+// Spherical projections (kind: 0 positionwise, 1 orientationwise, 2 split
+// orientationwise, 3 orientationwise ids, 4 positionwise ids); lenScratch
+// holds 2 * N floats.
+cudaError_t launchSpherical(const float4* omm, float* lenScratch, uint32_t N, const float* sums, uchar4* frame, int w,
+                            int h, int kind, cudaStream_t stream);
+// raw_ommatidial_samples from a recorded frame (N x spp records).
+cudaError_t launchRawSamples(const RayRecord* rec, uint32_t N, uint32_t spp, uchar4* frame, int w, int h,
+                             cudaStream_t stream);
 
 }  // namespace cr

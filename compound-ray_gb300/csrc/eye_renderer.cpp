@@ -313,17 +313,35 @@ struct Renderer {
     }
   }
 
-  void project(EyeDev& e, const std::string& shader) {
+  // Compound projection shaders by name (the reference's
+  // "__raygen__compound_projection_" programs without the prefix).
+  static int projectionKind(const std::string& shader) {
+    if (shader == "single_dimension_fast") return 0;
+    if (shader == "single_dimension") return 1;
+    if (shader == "spherical_positionwise") return 10;
+    if (shader == "spherical_orientationwise") return 11;
+    if (shader == "spherical_split_orientationwise") return 12;
+    if (shader == "spherical_orientationwise_ids") return 13;
+    if (shader == "spherical_positionwise_ids") return 14;
+    if (shader == "raw_ommatidial_samples") return 20;
+    throw std::runtime_error("unknown compound projection '" + shader + "'");
+  }
+
+  void project(EyeDev& e, const std::string& shader, const RayRecord* rec) {
     ensureFrame();
-    int mode = -1;
-    if (shader == "single_dimension_fast") mode = 0;
-    else if (shader == "single_dimension") mode = 1;
-    if (mode < 0) {
-      throw std::runtime_error("compound projection '" + shader +
-                               "' is not implemented; use single_dimension_fast or single_dimension "
-                               "(per-ommatidium colours are still available from getOmmatidialColoursF32)");
+    const int kind = projectionKind(shader);
+    if (kind < 10) {
+      check(launchProject(e.sums.ptr, e.N, frame.ptr, width, height, kind, stream()), "projection launch");
+    } else if (kind < 20) {
+      DevBuf<float> len;
+      len.ensure(std::max<size_t>(1, 2 * static_cast<size_t>(e.N)));
+      check(launchSpherical(e.omm.ptr, len.ptr, e.N, e.sums.ptr, frame.ptr, width, height, kind - 10, stream()),
+            "projection launch");
+      check(cudaStreamSynchronize(stream()), "projection");
+      len.release();
+    } else {
+      check(launchRawSamples(rec, e.N, e.spp, frame.ptr, width, height, stream()), "projection launch");
     }
-    check(launchProject(e.sums.ptr, e.N, frame.ptr, width, height, mode, stream()), "projection launch");
   }
 };
 
@@ -476,9 +494,18 @@ double renderFrame(void) {
           Renderer::packPose(c, p16);
           r.poses.ensure(4);
           check(cudaMemcpyAsync(r.poses.ptr, p16, sizeof(p16), cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
-          r.renderDevicePoses(e, r.poses.ptr, 1, e.sums.ptr, nullptr);
+          // raw_ommatidial_samples shows individual samples: that projection
+          // renders through the recording variant, which keeps them.
+          const bool raw = Renderer::projectionKind(c.projection) == 20;
+          DevBuf<RayRecord> rec;
+          if (raw) rec.ensure(std::max<size_t>(1, static_cast<size_t>(e.N) * e.spp));
+          r.renderDevicePoses(e, r.poses.ptr, 1, e.sums.ptr, raw ? rec.ptr : nullptr);
           e.haveSums = true;
-          r.project(e, c.projection);
+          r.project(e, c.projection, rec.ptr);
+          if (raw) {
+            check(cudaStreamSynchronize(r.stream()), "projection");
+            rec.release();
+          }
         } else {
           throw std::runtime_error("camera '" + c.name +
                                    "' is not a compound eye; only compound eyes are rendered by this library");

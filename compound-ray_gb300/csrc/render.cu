@@ -592,6 +592,83 @@ __global__ void projectKernel(const float* __restrict__ sums, uint32_t N, uchar4
   frame[static_cast<size_t>(y) * w + x] = makeColour(sums[3 * o], sums[3 * o + 1], sums[3 * o + 2]);
 }
 
+// Spherical projections (shaders.cu:412-640): every pixel maps to a point on
+// the unit sphere and shows the ommatidium whose position (or direction)
+// makes the smallest angle with it, the first such ommatidium on ties.
+//  kind 0 positionwise, 1 orientationwise, 2 split orientationwise (the left
+//  half of the image considers only ommatidia with position.x < 0, the right
+//  half those with x > 0; ommatidium 0 is the starting candidate either way),
+//  3 orientationwise ids, 4 positionwise ids (index in RGBA, base 256).
+// The candidate lengths are precomputed per ommatidium (len), identical to
+// recomputing them per pixel.
+__global__ void sphericalKernel(const float4* __restrict__ omm, const float* __restrict__ len, uint32_t N,
+                                const float* __restrict__ sums, uchar4* frame, int w, int h, int kind) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= w || y >= h || N == 0) return;
+  const float ux = static_cast<float>(x) / static_cast<float>(w), uy = static_cast<float>(y) / static_cast<float>(h);
+  float dx, dy;
+  if (kind == 2) {
+    const float sx = ux * 2.0f;
+    const float sub = sx > 1.0f ? 1.0f : 0.f;
+    dx = (sx - sub) * 2.0f - 1.0f;
+    dy = uy * 2.0f - 1.0f;
+  } else {
+    dx = 2.0f * ux - 1.0f;
+    dy = 2.0f * uy - 1.0f;
+  }
+  const float ax = dx * -CR_PI_F + CR_PI_F / 2.0f, ay = dy * (CR_PI_F / 2.0f);
+  const float cosY = cosf(ay);
+  const v3 p = mk(cosf(ax) * cosY, sinf(ay), sinf(ax) * cosY);
+  const float lp = sqrtf(dot(p, p));
+  const bool byPos = (kind == 0 || kind == 4);
+  auto vec = [&](uint32_t i) {
+    const float4 a = __ldg(omm + 2 * i), b = __ldg(omm + 2 * i + 1);
+    return byPos ? mk(a.x, a.y, a.z) : mk(a.w, b.x, b.y);
+  };
+  float best = acosf(dot(vec(0), p) / (len[byPos ? 0 : N] * lp));
+  uint32_t bi = 0;
+  for (uint32_t i = 1; i < N; ++i) {
+    const float ang = acosf(dot(vec(i), p) / (len[byPos ? i : N + i] * lp));
+    bool ok = ang < best;
+    if (kind == 2) {
+      const float px = __ldg(omm + 2 * i).x;
+      ok = ok && ((px > 0.f && ux > 0.5f) || (px < 0.f && ux < 0.5f));
+    }
+    if (ok) {
+      best = ang;
+      bi = i;
+    }
+  }
+  uchar4 c;
+  if (kind >= 3) c = make_uchar4(static_cast<uint8_t>(bi >> 24), static_cast<uint8_t>((bi >> 16) & 0xff),
+                                 static_cast<uint8_t>((bi >> 8) & 0xff), static_cast<uint8_t>(bi & 0xff));
+  else c = makeColour(sums[3 * bi], sums[3 * bi + 1], sums[3 * bi + 2]);
+  frame[static_cast<size_t>(y) * w + x] = c;
+}
+
+__global__ void lengthsKernel(const float4* __restrict__ omm, uint32_t N, float* len) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float4 a = omm[2 * i], b = omm[2 * i + 1];
+  const v3 pos = mk(a.x, a.y, a.z), dir = mk(a.w, b.x, b.y);
+  len[i] = sqrtf(dot(pos, pos));
+  len[N + i] = sqrtf(dot(dir, dir));
+}
+
+// raw_ommatidial_samples (shaders.cu:354-369): pixel (x, y) with x < N and
+// y < spp shows sample y of ommatidium x, scaled by 1/spp.
+__global__ void rawSamplesKernel(const RayRecord* __restrict__ rec, uint32_t N, uint32_t spp, uchar4* frame, int w,
+                                 int h) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= w || y >= h) return;
+  if (static_cast<uint32_t>(y) >= spp || static_cast<uint32_t>(x) >= N) return;
+  const RayRecord& r = rec[static_cast<size_t>(x) * spp + y];
+  const float inv = 1.0f / static_cast<float>(spp);
+  frame[static_cast<size_t>(y) * w + x] = makeColour(r.r * inv, r.g * inv, r.b * inv);
+}
+
 // ---------------------------------------------------------------------------
 // Batched rendering of many eyes in one persistent launch.
 // ---------------------------------------------------------------------------
@@ -782,6 +859,23 @@ cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsig
   if (e != cudaSuccess || totalCells == 0) return e;
   batchCombineKernel<<<static_cast<unsigned>((totalCells + 255) / 256), 256, 0, stream>>>(eyes, cellBase, nEyes,
                                                                                             totalCells);
+  return cudaGetLastError();
+}
+
+cudaError_t launchSpherical(const float4* omm, float* lenScratch, uint32_t N, const float* sums, uchar4* frame, int w,
+                            int h, int kind, cudaStream_t stream) {
+  if (w <= 0 || h <= 0 || N == 0) return cudaSuccess;
+  lengthsKernel<<<(N + 255) / 256, 256, 0, stream>>>(omm, N, lenScratch);
+  dim3 grid((w + 127) / 128, h);
+  sphericalKernel<<<grid, 128, 0, stream>>>(omm, lenScratch, N, sums, frame, w, h, kind);
+  return cudaGetLastError();
+}
+
+cudaError_t launchRawSamples(const RayRecord* rec, uint32_t N, uint32_t spp, uchar4* frame, int w, int h,
+                             cudaStream_t stream) {
+  if (w <= 0 || h <= 0) return cudaSuccess;
+  dim3 grid((w + 127) / 128, h);
+  rawSamplesKernel<<<grid, 128, 0, stream>>>(rec, N, spp, frame, w, h);
   return cudaGetLastError();
 }
 

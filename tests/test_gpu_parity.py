@@ -255,3 +255,66 @@ def test_gpu_built_bvh_renders_identical_bits(lib, small, tmp_path, size):
     lib.setCameraLocalSpace(*[float(v) for v in poses[0][3:]])
     _check_frame(lib, sc, omm, spp, poses[0])
     lib.crSetBvhBuilder(0)
+
+
+def _sphere_points(w, h, split=False):
+    x = np.arange(w, dtype=np.float32) / np.float32(w)
+    y = np.arange(h, dtype=np.float32) / np.float32(h)
+    ux, uy = np.meshgrid(x, y)
+    if split:
+        sx = ux * 2.0
+        dx = (sx - (sx > 1.0)) * 2.0 - 1.0
+    else:
+        dx = 2.0 * ux - 1.0
+    dy = 2.0 * uy - 1.0
+    ax = dx * -np.pi + np.pi / 2
+    ay = dy * (np.pi / 2)
+    p = np.stack([np.cos(ax) * np.cos(ay), np.sin(ay), np.sin(ax) * np.cos(ay)], axis=-1)
+    return p, ux
+
+
+@pytest.mark.parametrize("kind", ["spherical_orientationwise_ids", "spherical_positionwise_ids",
+                                  "spherical_orientationwise", "spherical_split_orientationwise"])
+def test_spherical_projections(lib, small, small_ref, kind):
+    """Voronoi projections of shaders.cu:412-640: each pixel shows the
+    ommatidium with the smallest angle to its sphere point (first on ties)."""
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"].astype(np.float64)
+    _load(lib, small["gltf"], 32)
+    w, h = 96, 48
+    lib.setCurrentEyeShaderName(kind.encode())
+    eh.setRenderSize(lib, w, h)
+    assert lib.renderFrame() >= 0, eh.lastError(lib)
+    frame = eh.getFrame(lib, w, h).astype(np.int64)
+    p, ux = _sphere_points(w, h, split="split" in kind)
+    v = omm[:, 0:3] if "positionwise" in kind else omm[:, 3:6]
+    cosang = (p.reshape(-1, 3) @ v.T) / np.linalg.norm(v, axis=1)[None, :]
+    ang = np.arccos(np.clip(cosang, -1, 1))
+    if "split" in kind:
+        ok = ((omm[None, :, 0] > 0) & (ux.reshape(-1, 1) > 0.5)) | ((omm[None, :, 0] < 0) & (ux.reshape(-1, 1) < 0.5))
+        ok[:, 0] = True  # ommatidium 0 is the starting candidate whatever its side
+        ang = np.where(ok, ang, np.inf)
+    want = ang.argmin(axis=1)
+    srt = np.sort(ang, axis=1)
+    clear = (srt[:, 1] - srt[:, 0]) > 1e-4  # pixels not on a Voronoi boundary
+    if kind.endswith("_ids"):
+        got = (frame[..., 0] << 24) | (frame[..., 1] << 16) | (frame[..., 2] << 8) | frame[..., 3]
+        got = got.reshape(-1)
+        assert (got[clear] == want[clear]).all()
+        assert clear.mean() > 0.9
+    else:
+        sums = eh.getOmmatidialColours(lib)
+        colours = oracle.make_color(sums)[want]
+        d = np.abs(frame.reshape(-1, 4) - colours.astype(np.int64))[clear]
+        assert d.max() <= 1
+
+
+def test_raw_samples_projection(lib, small):
+    _load(lib, small["gltf"], 8)
+    n = lib.getCurrentEyeOmmatidialCount()
+    lib.setCurrentEyeShaderName(b"raw_ommatidial_samples")
+    eh.setRenderSize(lib, n, 12)
+    assert lib.renderFrame() >= 0, eh.lastError(lib)
+    frame = eh.getFrame(lib, n, 12)
+    assert (frame[:8, :, 3] == 255).all() and (frame[8:] == 0).all()
+    assert frame[:8, :, :3].any()
