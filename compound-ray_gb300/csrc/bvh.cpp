@@ -190,7 +190,7 @@ void packNode(float* dst, const Box& a, const Box& b, int32_t c0, int32_t c1) {
 
 }  // namespace
 
-void buildBvh(const float* verts, const float* colours, const uint8_t* usesVertexColour, uint32_t triCount,
+void buildBvh(const float* verts, const float* colours, const uint8_t* shading, uint32_t triCount,
               HostBvh& out) {
   out = HostBvh{};
   if (triCount == 0) return;
@@ -262,7 +262,7 @@ void buildBvh(const float* verts, const float* colours, const uint8_t* usesVerte
     std::memcpy(&d[3], &t, 4);
     float* s = &out.shade[12 * static_cast<size_t>(j)];
     std::memcpy(s, &colours[12 * static_cast<size_t>(t)], 12 * sizeof(float));
-    s[3] = usesVertexColour[t] ? 1.0f : 0.0f;
+    s[3] = static_cast<float>(shading[t]);
   }
   out.stats = b.stats;
 }

@@ -11,8 +11,9 @@
 //   complement packs (first triangle << 3) | (count - 1), count in 1..8.
 //   triangle j (BVH order) = 3 x float4: (v0, id) (v1, 0) (v2, 0) where id is
 //   the original global triangle id stored as integer bits.
-//   shade j = 3 x float4 colours at v0, v1, v2; c0.w holds 1.0 when the
-//   triangle uses vertex colours and 0.0 for a material base colour.
+//   shade j = the triangle's 3 x float4 colour record (material colour,
+//   vertex colours, or (u, v, texture, 0) per vertex) with c0.w replaced by
+//   the shading kind as a float: 0 base colour, 1 vertex colours, 2 texture.
 // Node 0 is the root and is always an inner node.
 #pragma once
 
@@ -37,8 +38,8 @@ struct HostBvh {
 };
 
 // verts: 9 floats per triangle (world space); colours: 12 floats per triangle;
-// usesVertexColour: 1 byte per triangle.
-void buildBvh(const float* verts, const float* colours, const uint8_t* usesVertexColour, uint32_t triCount,
+// shading: 1 byte per triangle (the scene's kShade* kind).
+void buildBvh(const float* verts, const float* colours, const uint8_t* shading, uint32_t triCount,
               HostBvh& out);
 
 constexpr int kMaxLeafSize = 8;

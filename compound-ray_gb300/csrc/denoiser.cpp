@@ -68,7 +68,7 @@ void Denoiser::init(uint32_t seed, cudaStream_t s) {
   fill(offW1, kFeatureWidth, kHidden, 1.f);
   fill(offW2, kHidden, kHidden, 1.f);
   fill(offW3, kHidden, kHidden, 1.f);
-  fill(offW4, kHidden, kOut, 0.1f);
+  fill(offW4, kHidden, kOut, 0.01f);  // start close to the 8-sample mean
   ck(cudaMemcpyAsync(params_, h.data(), kParams * 4, cudaMemcpyHostToDevice, s), "upload");
   ck(cudaMemsetAsync(m_, 0, kParams * 4, s), "memset");
   ck(cudaMemsetAsync(v_, 0, kParams * 4, s), "memset");
@@ -202,7 +202,10 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
     const float l = forwardBackward(Xb_, baseb_, targetb_, batch, want, s);
     if (loss) loss[st] = l;
     ++adamT_;
-    ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr, 0.9f, 0.999f, 1e-8f, adamT_, wbf_, s), "adam");
+    // half-cosine decay of the step size over this call, down to 5%
+    const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
+    ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr * decay, 0.9f, 0.999f, 1e-8f, adamT_, wbf_, s),
+       "adam");
   }
   ck(cudaStreamSynchronize(s), "train");
 }
@@ -216,6 +219,13 @@ void Denoiser::infer(const void* X, const float* base, size_t rows, float* out, 
     forward(static_cast<const uint16_t*>(X) + r0 * kFeatureWidth, r, s);
     ck(mlpLoss(y_, kOut, base + 3 * r0, nullptr, r, out + 3 * r0, nullptr, nullptr, nullptr, s), "prediction");
   }
+}
+
+MlpWeights Denoiser::weights() const {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  const __nv_bfloat16* w = static_cast<const __nv_bfloat16*>(wbf_);
+  return MlpWeights{w + offW1, w + offW2, w + offW3, w + offW4,
+                    params_ + offB1, params_ + offB2, params_ + offB3, params_ + offB4};
 }
 
 float Denoiser::gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost,

@@ -20,8 +20,8 @@ namespace cr {
 
 class Denoiser {
  public:
-  static constexpr int kHidden = 128;
-  static constexpr int kOut = 8;  // 3 used
+  static constexpr int kHidden = kMlpHidden;
+  static constexpr int kOut = kMlpOut;  // 3 used
   static constexpr size_t offW1 = 0;
   static constexpr size_t offB1 = offW1 + size_t(kFeatureWidth) * kHidden;
   static constexpr size_t offW2 = offB1 + kHidden;
@@ -50,8 +50,13 @@ class Denoiser {
   // in `loss` (host, `steps` floats) if given.
   void train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s);
 
-  // Prediction for `rows` feature rows (device): out = base + net(X)[:, :3].
+  // Prediction for `rows` feature rows (device): out = base + net(X)[:, :3],
+  // layer by layer.
   void infer(const void* X, const float* base, size_t rows, float* out, cudaStream_t s);
+
+  // Current bf16 weights and fp32 biases (device pointers) for the fused
+  // inference kernel.
+  MlpWeights weights() const;
 
   // One forward/backward on the given rows with the current weights:
   // returns the loss and copies gradients and parameters to the host.

@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace cr {
@@ -18,7 +19,20 @@ struct DevScene {
   uint32_t triCount = 0;
   int miss = 0;         // 0 = default_background, 1 = simple_sky
   float extent = 0.f;   // largest |coordinate| of any triangle vertex
+  // Base-colour textures: RGBA8 texels (r in the low byte) of all textures,
+  // and per texture (first texel, width, height, 0).
+  const uint32_t* texels = nullptr;
+  const int4* texTable = nullptr;
 };
+
+// Samples one width x height RGBA8 texture at n (u, v) coordinates twice:
+// with the render kernel's own bilinear filter (rgbaSoft) and with a
+// hardware texture object in the reference's sampler state (wrap
+// addressing, linear filtering, normalised coordinates, texels read as
+// value / 255; MulticamScene.cpp:800-833) (rgbaHard).  Host buffers, n x 4
+// floats out; allocates and synchronises (a check, not a render path).
+cudaError_t sampleTextureBoth(const uint32_t* texels, int width, int height, const float* uv, int n, float* rgbaSoft,
+                              float* rgbaHard);
 
 // Device view of one compound eye.
 //  omm: N ommatidium records of 32 bytes (2 x float4).
@@ -26,11 +40,21 @@ struct DevScene {
 //       32-bit words (d, v0..v4, boxmuller_flag, boxmuller_extra); the state
 //       of (ommatidium o, sample s) sits at index o*spp + s and holds the
 //       stream curand_init(42, s*N + o, 0) (shaders.cu:669-695).
+//  order: null, or a permutation of the N ommatidia giving the order in
+//       which warp segments take them (neighbouring directions together, so
+//       the rays of a warp stay coherent when it holds several ommatidia);
+//       results are indexed by ommatidium and do not depend on it.
 struct DevEye {
   const float4* omm = nullptr;
   uint32_t N = 0;
   uint32_t spp = 1;
   uint32_t* rng = nullptr;
+  const uint32_t* order = nullptr;
+  // draws: null (each warp draws its samples' random numbers pose after pose
+  //       from the states it holds), or P x N x spp (normal, uniform) pairs
+  //       of a launch, generated up front so that the poses of the launch can
+  //       be spread over several warps (renderDrawBytes).
+  float2* draws = nullptr;
 };
 
 // One pose = 4 x float4: position, local x axis, local y axis, local z axis
@@ -64,8 +88,15 @@ struct WarpPlan {
   uint32_t ommPerWarp;   // 32 / segWidth
   uint32_t chunks;       // warp segments per ommatidium (spp > 32)
   uint64_t tasks;        // warp tasks per pose batch
+  uint32_t poseSplits = 1;     // pose ranges the batch is cut into (pre-drawn launches)
+  uint32_t posesPerSplit = 0;  // poses per range (0: all)
 };
 WarpPlan planWarps(uint32_t N, uint32_t spp);
+
+// Bytes of DevEye::draws worth providing for a P-pose launch of an
+// N-ommatidium, spp-sample eye: non-zero only when the eye alone has too few
+// samples to fill the GPU, so that its poses are better spread over warps.
+size_t renderDrawBytes(uint32_t N, uint32_t spp, uint32_t P);
 
 // Floats of scratch needed by launchRender for P poses (0 when spp <= 32).
 size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P);
@@ -95,6 +126,21 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
 constexpr int kNeighbours = 6;
 constexpr int kFeatBlock = 15;
 constexpr int kFeatureWidth = 112;
+constexpr int kMlpHidden = 128;
+constexpr int kMlpOut = 8;  // 3 used
+
+// bf16 weight matrices W[in x out] (row-major) and fp32 biases of the
+// denoiser network.
+struct MlpWeights {
+  const __nv_bfloat16* w1;
+  const __nv_bfloat16* w2;
+  const __nv_bfloat16* w3;
+  const __nv_bfloat16* w4;
+  const float* b1;
+  const float* b2;
+  const float* b3;
+  const float* b4;
+};
 static_assert(kFeatBlock * (kNeighbours + 1) <= kFeatureWidth, "feature row too narrow");
 
 // bf16 GEMM C[M x N] = A[M x K] * B[K x N] (see mlp.cu for layouts/modes).
@@ -111,6 +157,11 @@ cudaError_t toBf16(const float* in, void* out, size_t n, cudaStream_t stream);
 cudaError_t nearestOmmatidia(const float4* omm, uint32_t N, int* nb, cudaStream_t stream);
 cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P, void* X,
                              float* base, cudaStream_t stream);
+// Fused prediction for P poses of an N-ommatidium eye straight from the
+// feature-render statistics: out (P x N x 3) = own mean colour + network
+// output, bit-identical to assembleFeatures + the layer-by-layer forward.
+cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
+                          const MlpWeights& w, float* out, cudaStream_t stream);
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
                        float* baseo, float* targeto, cudaStream_t stream);
 

@@ -59,6 +59,7 @@ struct DevBuf {
 
 struct EyeDev {
   DevBuf<float4> omm;
+  DevBuf<uint32_t> order;  // warp-segment order of the ommatidia (directionOrder)
   DevBuf<uint32_t> rng;
   DevBuf<float> sums;  // N x 3 of the last frame
   uint32_t N = 0, spp = 0;
@@ -66,6 +67,7 @@ struct EyeDev {
   bool haveSums = false;
   void release() {
     omm.release();
+    order.release();
     rng.release();
     sums.release();
     N = spp = 0;
@@ -75,6 +77,36 @@ struct EyeDev {
 };
 
 constexpr uint32_t kMaxPosesPerLaunch = 256;
+
+// Order in which warp segments take an eye's ommatidia: by the 30-bit Morton
+// code of the unit axis direction mapped into the cube [0, 1)^3 (ties by
+// index), so a warp holding several ommatidia traces neighbouring directions.
+std::vector<uint32_t> directionOrder(const std::vector<Ommatidium>& omm) {
+  auto spread = [](uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+  };
+  std::vector<std::pair<uint32_t, uint32_t>> keys(omm.size());
+  for (size_t i = 0; i < omm.size(); ++i) {
+    const f3 d = omm[i].dir;
+    const double len = std::sqrt(double(d.x) * d.x + double(d.y) * d.y + double(d.z) * d.z);
+    uint32_t q[3] = {0, 0, 0};
+    const double c[3] = {d.x, d.y, d.z};
+    for (int k = 0; k < 3; ++k) {
+      const double u = len > 0 ? 0.5 + 0.5 * c[k] / len : 0.5;
+      q[k] = static_cast<uint32_t>(std::min(1023.0, std::max(0.0, std::floor(u * 1024.0))));
+    }
+    keys[i] = {spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2), static_cast<uint32_t>(i)};
+  }
+  std::sort(keys.begin(), keys.end());
+  std::vector<uint32_t> out(omm.size());
+  for (size_t i = 0; i < omm.size(); ++i) out[i] = keys[i].second;
+  return out;
+}
 
 void releaseBatches();
 
@@ -88,6 +120,8 @@ struct Renderer {
   int builder = 0;  // 0 = host binned SAH, 1 = GPU linear BVH (crSetBvhBuilder)
   BvhBuildStats bvhStats;
   DevBuf<float4> nodes, tris, shade;
+  DevBuf<uint32_t> texels;
+  DevBuf<int4> texTable;
   DevScene dev;
   std::vector<EyeDev> eyes;  // parallel to scene.cameras
   size_t current = 0;
@@ -96,6 +130,7 @@ struct Renderer {
   std::vector<uchar4> hostFrame;
   DevBuf<float4> poses;
   DevBuf<float> scratch;
+  DevBuf<float2> draws;  // pre-drawn random numbers of small-eye launches
   DevBuf<float> batchOut;
   DevBuf<uint32_t> err;
   cudaStream_t ownStream = nullptr;
@@ -118,9 +153,12 @@ struct Renderer {
     nodes.release();
     tris.release();
     shade.release();
+    texels.release();
+    texTable.release();
     frame.release();
     poses.release();
     scratch.release();
+    draws.release();
     batchOut.release();
     err.release();
     hostFrame.clear();
@@ -151,7 +189,7 @@ struct Renderer {
     check(cudaMemcpyAsync(v.ptr, scene.triVerts.data(), scene.triVerts.size() * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
     check(cudaMemcpyAsync(c.ptr, scene.triColours.data(), scene.triColours.size() * 4, cudaMemcpyHostToDevice, st),
           "cudaMemcpy");
-    check(cudaMemcpyAsync(f.ptr, scene.triUsesVertexColour.data(), T, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    check(cudaMemcpyAsync(f.ptr, scene.triShading.data(), T, cudaMemcpyHostToDevice, st), "cudaMemcpy");
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t t = 0; t < T; ++t)
       for (int k = 0; k < 3; ++k) {
@@ -205,6 +243,20 @@ struct Renderer {
     dev.shade = shade.ptr;
     dev.triCount = static_cast<uint32_t>(scene.triangleCount());
     dev.miss = static_cast<int>(scene.miss);
+    if (!scene.textures.empty()) {
+      std::vector<int4> table;
+      for (const Texture& t : scene.textures) table.push_back(make_int4(static_cast<int>(t.offset), t.width, t.height, 0));
+      texels.ensure(scene.texels.size());
+      texTable.ensure(table.size());
+      cudaStream_t st = stream();
+      check(cudaMemcpyAsync(texels.ptr, scene.texels.data(), scene.texels.size() * 4, cudaMemcpyHostToDevice, st),
+            "cudaMemcpy");
+      check(cudaMemcpyAsync(texTable.ptr, table.data(), table.size() * sizeof(int4), cudaMemcpyHostToDevice, st),
+            "cudaMemcpy");
+      check(cudaStreamSynchronize(st), "texture upload");
+    }
+    dev.texels = texels.ptr;
+    dev.texTable = texTable.ptr;
     float ext = 0.f;
     for (float v : scene.triVerts) ext = std::max(ext, std::fabs(v));
     dev.extent = ext;
@@ -270,6 +322,16 @@ struct Renderer {
       e.haveSums = false;
       if (N) check(cudaMemcpyAsync(e.omm.ptr, c.omm.data(), sizeof(Ommatidium) * N, cudaMemcpyHostToDevice, stream()),
                    "cudaMemcpy");
+      if (countChanged) {
+        e.order.release();
+        e.order.ensure(std::max<size_t>(1, N));
+      }
+      if (N) {
+        const std::vector<uint32_t> ord = directionOrder(c.omm);
+        check(cudaMemcpyAsync(e.order.ptr, ord.data(), 4 * static_cast<size_t>(N), cudaMemcpyHostToDevice, stream()),
+              "cudaMemcpy");
+        check(cudaStreamSynchronize(stream()), "eye upload");
+      }
     }
     return e;
   }
@@ -280,6 +342,7 @@ struct Renderer {
     d.N = e.N;
     d.spp = e.spp;
     d.rng = e.rng.ptr;
+    d.order = e.order.ptr;
     return d;
   }
 
@@ -307,10 +370,23 @@ struct Renderer {
       const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
       const size_t need = renderScratchFloats(e.N, e.spp, P);
       if (need) scratch.ensure(need);
-      check(launchRender(dev, devEye(e), d_poses + 4 * first, P, d_out + 3 * first * e.N, need ? scratch.ptr : nullptr,
+      DevEye de = devEye(e);
+      withDraws(de, P, !rec && !stats);
+      check(launchRender(dev, de, d_poses + 4 * first, P, d_out + 3 * first * e.N, need ? scratch.ptr : nullptr,
                          errWord(), rec, stream(), stats),
             "render launch");
     }
+  }
+
+  // Gives a P-pose launch of a small eye a buffer for its pre-drawn random
+  // numbers, so that its poses spread over more warps (renderDrawBytes).
+  void withDraws(DevEye& de, uint32_t P, bool allowed) {
+    de.draws = nullptr;
+    if (!allowed) return;
+    const size_t bytes = renderDrawBytes(de.N, de.spp, P);
+    if (!bytes) return;
+    draws.ensure(bytes / sizeof(float2));
+    de.draws = draws.ptr;
   }
 
   // Compound projection shaders by name (the reference's
@@ -436,7 +512,7 @@ void loadGlTFscene(const char* filepath) {
     const bool gpuBuild = r.builder == 1 && s.triangleCount() >= 16;
     std::unique_ptr<HostBvh> bvh(new HostBvh);
     if (!gpuBuild) {
-      buildBvh(s.triVerts.data(), s.triColours.data(), s.triUsesVertexColour.data(),
+      buildBvh(s.triVerts.data(), s.triColours.data(), s.triShading.data(),
                static_cast<uint32_t>(s.triangleCount()), *bvh);
       if (bvh->stats.maxDepth + 2 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
     }
@@ -730,6 +806,8 @@ void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
     } else if (e.omm.ptr && count) {
       check(cudaMemcpyAsync(e.omm.ptr, v.data(), sizeof(Ommatidium) * count, cudaMemcpyHostToDevice, r.stream()),
             "cudaMemcpy");
+      const std::vector<uint32_t> ord = directionOrder(v);
+      check(cudaMemcpyAsync(e.order.ptr, ord.data(), 4 * count, cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
       check(cudaStreamSynchronize(r.stream()), "ommatidia upload");
     }
     c.omm = std::move(v);
@@ -1192,6 +1270,7 @@ EyeDev& denoiseEye(Renderer& r, DenoiseState& d) {
 DevEye streamsFor(Renderer& r, EyeDev& e, DevBuf<uint32_t>& rng, uint32_t& haveSpp, bool& ready, uint32_t spp) {
   DevEye d;
   d.omm = e.omm.ptr;
+  d.order = e.order.ptr;
   d.N = e.N;
   d.spp = spp;
   if (haveSpp != spp || !ready) {
@@ -1207,18 +1286,25 @@ DevEye streamsFor(Renderer& r, EyeDev& e, DevBuf<uint32_t>& rng, uint32_t& haveS
 }
 
 // Feature rows (and 8-sample means) of `count` device poses of the current eye.
-void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dposes, size_t count, uint32_t featSpp) {
+// Feature render of `count` poses into d.stats; with `rows`, also the
+// feature rows and residual bases (d.X, d.base) the training set and the
+// layer-by-layer path use.
+void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dposes, size_t count, uint32_t featSpp,
+                     bool rows = true) {
   if (featSpp < 1 || featSpp > 32) throw std::runtime_error("feature renders use 1 to 32 samples per ommatidium");
   const DevEye fe = streamsFor(r, e, d.featRng, d.featSpp, d.featReady, featSpp);
   d.stats.ensure(std::max<size_t>(1, count * e.N * kFeatureStats));
-  d.X.ensure(std::max<size_t>(1, count * e.N * kFeatureWidth));
-  d.base.ensure(std::max<size_t>(1, count * e.N * 3));
   for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
     const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
-    check(launchFeatures(r.dev, fe, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
+    DevEye de = fe;
+    r.withDraws(de, P, true);
+    check(launchFeatures(r.dev, de, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
                          r.stream()),
           "feature render");
   }
+  if (!rows) return;
+  d.X.ensure(std::max<size_t>(1, count * e.N * kFeatureWidth));
+  d.base.ensure(std::max<size_t>(1, count * e.N * 3));
   check(assembleFeatures(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, static_cast<uint32_t>(count), d.X.ptr, d.base.ptr,
                          r.stream()),
         "feature rows");
@@ -1301,8 +1387,14 @@ int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureS
         if (count == 0) return 0;
         if (!d_poses || !d_out) throw std::runtime_error("null pointer");
         EyeDev& e = denoiseEye(r, d);
-        denoiseFeatures(r, d, e, reinterpret_cast<const float4*>(d_poses), count, static_cast<uint32_t>(featureSpp));
-        d.net.infer(d.X.ptr, d.base.ptr, count * e.N, d_out, r.stream());
+        denoiseFeatures(r, d, e, reinterpret_cast<const float4*>(d_poses), count, static_cast<uint32_t>(featureSpp),
+                        false);
+        for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
+          const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+          check(inferDenoiser(d.stats.ptr + first * e.N * kFeatureStats, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(),
+                              d_out + 3 * first * e.N, r.stream()),
+                "denoiser inference");
+        }
         return 0;
       },
       -1);
@@ -1325,6 +1417,51 @@ int crDenoiserRenderPoses(const float* poses12, size_t count, int featureSpp, fl
         check(cudaMemcpyAsync(out, o.ptr, count * e.N * 12, cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
         r.checkErrWord();
         o.release();
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserFeatureRows(const float* poses12, size_t count, int featureSpp, uint16_t* xBf16, float* base) {
+  return guarded(
+      "crDenoiserFeatureRows",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!poses12 || !xBf16 || !base) throw std::runtime_error("null pointer");
+        if (count == 0) return 0;
+        EyeDev& e = denoiseEye(r, d);
+        uploadPoses12(d.poses, poses12, count, r.stream());
+        denoiseFeatures(r, d, e, d.poses.ptr, count, static_cast<uint32_t>(featureSpp));
+        const size_t rows = count * e.N;
+        check(cudaMemcpyAsync(xBf16, d.X.ptr, rows * kFeatureWidth * 2, cudaMemcpyDeviceToHost, r.stream()),
+              "cudaMemcpy");
+        check(cudaMemcpyAsync(base, d.base.ptr, rows * 12, cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        r.checkErrWord();
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserPredictRows(const uint16_t* xBf16, const float* base, size_t rows, float* out) {
+  return guarded(
+      "crDenoiserPredictRows",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit or crDenoiserLoad first");
+        if (rows == 0) return 0;
+        if (!xBf16 || !base || !out) throw std::runtime_error("null pointer");
+        DevBuf<uint16_t> x;
+        DevBuf<float> b, o;
+        x.ensure(rows * kFeatureWidth);
+        b.ensure(rows * 3);
+        o.ensure(rows * 3);
+        check(cudaMemcpyAsync(x.ptr, xBf16, rows * kFeatureWidth * 2, cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
+        check(cudaMemcpyAsync(b.ptr, base, rows * 12, cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
+        d.net.infer(x.ptr, b.ptr, rows, o.ptr, r.stream());
+        check(cudaMemcpyAsync(out, o.ptr, rows * 12, cudaMemcpyDeviceToHost, r.stream()), "cudaMemcpy");
+        check(cudaStreamSynchronize(r.stream()), "prediction");
         return 0;
       },
       -1);
@@ -1436,7 +1573,7 @@ int crRenderFrameRecorded(void* records) {
 
 size_t crGetTriangleCount(void) { return R().loaded ? R().scene.triangleCount() : 0; }
 
-int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexColour) {
+int crGetSceneTriangles(float* verts, float* colours, unsigned char* shading) {
   Renderer& r = R();
   if (!r.loaded) {
     setError("crGetSceneTriangles: no scene loaded");
@@ -1445,8 +1582,39 @@ int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexC
   const SceneData& s = r.scene;
   if (verts) std::memcpy(verts, s.triVerts.data(), s.triVerts.size() * sizeof(float));
   if (colours) std::memcpy(colours, s.triColours.data(), s.triColours.size() * sizeof(float));
-  if (usesVertexColour) std::memcpy(usesVertexColour, s.triUsesVertexColour.data(), s.triUsesVertexColour.size());
+  if (shading) std::memcpy(shading, s.triShading.data(), s.triShading.size());
   return 0;
+}
+
+size_t crGetTextureCount(void) { return R().loaded ? R().scene.textures.size() : 0; }
+size_t crGetTexelCount(void) { return R().loaded ? R().scene.texels.size() : 0; }
+
+int crGetSceneTextures(int* table, unsigned int* texels) {
+  Renderer& r = R();
+  if (!r.loaded) {
+    setError("crGetSceneTextures: no scene loaded");
+    return -1;
+  }
+  const SceneData& s = r.scene;
+  if (table)
+    for (size_t i = 0; i < s.textures.size(); ++i) {
+      table[3 * i] = static_cast<int>(s.textures[i].offset);
+      table[3 * i + 1] = s.textures[i].width;
+      table[3 * i + 2] = s.textures[i].height;
+    }
+  if (texels && !s.texels.empty()) std::memcpy(texels, s.texels.data(), s.texels.size() * sizeof(uint32_t));
+  return 0;
+}
+
+int crCompareTextureSampling(const unsigned int* texels, int width, int height, const float* uv, int n,
+                             float* rgbaRenderer, float* rgbaHardware) {
+  return guarded(
+      "crCompareTextureSampling",
+      [&]() -> int {
+        check(sampleTextureBoth(texels, width, height, uv, n, rgbaRenderer, rgbaHardware), "texture sampling");
+        return 0;
+      },
+      -1);
 }
 
 int crGetOmmatidia(float* out) {

@@ -16,6 +16,18 @@
 //    unsigned byte (:415-516), normalised by 1, 65535 or 255 at shading time
 //    (cuda/LocalGeometry.h:105-156); otherwise the material baseColorFactor
 //    (default white, cuda/MaterialData.h:42) is used;
+//  * without vertex colours, a material "baseColorTexture" replaces the base
+//    colour by the texture sampled at the TEXCOORD_0 coordinates (float
+//    VEC2; without them the coordinates are the hit's barycentrics b1, b2)
+//    (shaders.cu:801-805, cuda/LocalGeometry.h:88-103).  The texture's
+//    sampler is not consulted: the reference translates the glTF wrap and
+//    filter enums to CUDA modes and then compares those CUDA modes with the
+//    GL enums again (:605-623, :800-828), which never match, so every
+//    texture samples with wrap addressing and linear filtering on
+//    normalised coordinates;
+//  * every image is decoded up front to RGBA8 (forced four components,
+//    tiny_gltf.h:2305-2389); 16-bit images are refused, as the reference's
+//    upload into a uchar4 array with a 16-bit pitch fails (:753-795);
 //  * the scene extra "background-shader" picks the miss shader (:555-565).
 //
 // Transforms are composed and applied in double precision and the world
@@ -32,6 +44,7 @@
 #include <stdexcept>
 
 #include "json.hpp"
+#include "png.hpp"
 #include "scene.hpp"
 
 namespace cr {
@@ -141,6 +154,7 @@ struct Model {
   Json doc;
   std::string dir;
   std::vector<std::vector<uint8_t>> buffers;
+  std::vector<int> textureImage;  // glTF texture -> SceneData::textures index
 };
 
 // A read-only view of one accessor.
@@ -362,18 +376,22 @@ struct Loader {
     whi = f3{static_cast<float>(mx[0]), static_cast<float>(mx[1]), static_cast<float>(mx[2])};
   }
 
-  void baseColour(int matIdx, float* rgba) const {
+  // Material base colour factor, and the scene texture index of its base
+  // colour texture (-1 when it has none).
+  int baseColour(int matIdx, float* rgba) const {
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 1.0f;
-    if (matIdx < 0) return;
+    if (matIdx < 0) return -1;
+    if (static_cast<size_t>(matIdx) >= m.doc["materials"].size()) throw std::runtime_error("material index out of range");
     const Json& mat = m.doc["materials"][static_cast<size_t>(matIdx)];
     const Json& pbr = mat["pbrMetallicRoughness"];
     const Json& f = pbr["baseColorFactor"];
     if (f.isArray() && f.size() == 4)
       for (size_t k = 0; k < 4; ++k) rgba[k] = static_cast<float>(f[k].asNumber());
-    if (pbr.has("baseColorTexture"))
-      std::cerr << "WARNING: material " << matIdx
-                << " has a base colour texture; textures are not sampled, the base colour factor is used instead."
-                << std::endl;
+    if (!pbr.has("baseColorTexture")) return -1;
+    const int t = pbr["baseColorTexture"].integer("index", -1);
+    if (t < 0 || static_cast<size_t>(t) >= m.textureImage.size())
+      throw std::runtime_error("material " + std::to_string(matIdx) + ": base colour texture index out of range");
+    return m.textureImage[static_cast<size_t>(t)];
   }
 
   void addMesh(const Json& mesh, const double* xf) {
@@ -420,7 +438,16 @@ struct Loader {
       }
       mp.colourType = ctype;
       float base[4];
-      baseColour(prim.integer("material", -1), base);
+      const int matTex = baseColour(prim.integer("material", -1), base);
+      const int tex = ctype == -1 ? matTex : -1;  // vertex colours take precedence
+      Accessor ta;
+      bool hasUv = false;
+      if (tex >= 0 && attrs.has("TEXCOORD_0")) {
+        ta = accessor(m, attrs.integer("TEXCOORD_0", -1));
+        if (ta.compType == 5121) throw std::runtime_error("gltf accessor component type not supported");
+        if (ta.compType != 5126 || ta.comps != 2) throw std::runtime_error("TEXCOORD_0 must be float VEC2");
+        hasUv = true;
+      }
 
       // Indices (u8 / u16 / u32); a primitive without indices has no triangles,
       // as a build input with zero index triplets in the reference.
@@ -441,6 +468,16 @@ struct Loader {
           s.triVerts.push_back(w.x);
           s.triVerts.push_back(w.y);
           s.triVerts.push_back(w.z);
+          if (tex >= 0) {
+            // (u, v, texture, 0); the default coordinates (0,0) (1,0) (0,1)
+            // interpolate to exactly (b1, b2).
+            if (hasUv && vi >= ta.count) throw std::runtime_error("texture coordinate index out of range");
+            cols[k * 4 + 0] = hasUv ? ta.getF(vi, 0) : (k == 1 ? 1.0f : 0.0f);
+            cols[k * 4 + 1] = hasUv ? ta.getF(vi, 1) : (k == 2 ? 1.0f : 0.0f);
+            cols[k * 4 + 2] = static_cast<float>(tex);
+            cols[k * 4 + 3] = 0.0f;
+            continue;
+          }
           for (int q = 0; q < 4; ++q) {
             float v = base[q];
             if (ctype == 5126) v = ca.getF(vi, q);
@@ -450,7 +487,7 @@ struct Loader {
           }
         }
         s.triColours.insert(s.triColours.end(), cols, cols + 12);
-        s.triUsesVertexColour.push_back(ctype != -1 ? 1 : 0);
+        s.triShading.push_back(ctype != -1 ? kShadeVertexColour : tex >= 0 ? kShadeTexture : kShadeBaseColour);
       }
       mp.triCount = static_cast<uint32_t>(triCount);
       s.meshes.push_back(mp);
@@ -528,6 +565,63 @@ void loadGltfScene(const std::string& path, SceneData& out, bool verbose) {
     }
   }
   SceneData s;
+  // Images (all of them, used or not) then textures, which name an image.
+  size_t imgIdx = 0;
+  for (const Json& im : m.doc["images"].items()) {
+    const std::string where = "image " + std::to_string(imgIdx++) + " '" + im.str("name") + "'";
+    std::vector<uint8_t> bytes;
+    const std::string uri = im.str("uri");
+    if (uri.rfind("data:", 0) == 0) {
+      const size_t comma = uri.find(',');
+      if (comma == std::string::npos || uri.find(";base64") == std::string::npos)
+        throw std::runtime_error(where + ": unsupported data URI");
+      bytes = base64Decode(uri, comma + 1);
+    } else if (!uri.empty()) {
+      const std::string raw = readFile(m.dir + uri);
+      bytes.assign(raw.begin(), raw.end());
+    } else if (im.has("bufferView")) {
+      const size_t bvi = static_cast<size_t>(im.integer("bufferView", -1));
+      if (bvi >= m.doc["bufferViews"].size()) throw std::runtime_error(where + ": bufferView out of range");
+      const Json& bv = m.doc["bufferViews"][bvi];
+      const int bufIdx = bv.integer("buffer", -1);
+      if (bufIdx < 0 || static_cast<size_t>(bufIdx) >= m.buffers.size())
+        throw std::runtime_error(where + ": bufferView buffer out of range");
+      const std::vector<uint8_t>& buf = m.buffers[static_cast<size_t>(bufIdx)];
+      const size_t off = static_cast<size_t>(bv.num("byteOffset", 0)), len = static_cast<size_t>(bv.num("byteLength", 0));
+      if (off + len > buf.size()) throw std::runtime_error(where + ": bufferView past the end of its buffer");
+      bytes.assign(buf.begin() + static_cast<std::ptrdiff_t>(off), buf.begin() + static_cast<std::ptrdiff_t>(off + len));
+    } else {
+      throw std::runtime_error(where + ": no uri or bufferView");
+    }
+    if (!isPng(bytes.data(), bytes.size())) throw std::runtime_error(where + ": only PNG images are supported");
+    Image img;
+    try {
+      img = decodePng(bytes.data(), bytes.size());
+    } catch (const std::exception& e) {
+      throw std::runtime_error(where + ": " + e.what());
+    }
+    if (img.bits == 16) throw std::runtime_error(where + ": 16-bit images are not supported");
+    Texture t;
+    t.offset = static_cast<uint32_t>(s.texels.size());
+    t.width = img.width;
+    t.height = img.height;
+    const size_t n = static_cast<size_t>(img.width) * static_cast<size_t>(img.height);
+    if (s.texels.size() + n > 0xFFFFFFFFull) throw std::runtime_error(where + ": texture memory exceeds 2^32 texels");
+    for (size_t i = 0; i < n; ++i) {
+      const uint8_t* p = &img.rgba[4 * i];
+      s.texels.push_back(static_cast<uint32_t>(p[0]) | (static_cast<uint32_t>(p[1]) << 8) |
+                         (static_cast<uint32_t>(p[2]) << 16) | (static_cast<uint32_t>(p[3]) << 24));
+    }
+    s.textures.push_back(t);
+    if (verbose)
+      std::cerr << "Processing " << where << "\n\t(" << img.width << "x" << img.height << ")x4\n\tbits: 8" << std::endl;
+  }
+  for (const Json& tx : m.doc["textures"].items()) {
+    const int src = tx.integer("source", -1);
+    if (src < 0 || static_cast<size_t>(src) >= s.textures.size())
+      throw std::runtime_error("texture " + std::to_string(m.textureImage.size()) + ": source image out of range");
+    m.textureImage.push_back(src);
+  }
   for (const Json& sc : m.doc["scenes"].items()) {
     const std::string bg = sc["extras"].str("background-shader");
     if (!bg.empty()) s.missName = bg;

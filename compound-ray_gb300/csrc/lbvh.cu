@@ -285,7 +285,7 @@ __global__ void gatherKernel(const float* __restrict__ verts, const float* __res
   tris[3 * static_cast<size_t>(p)] = make_float4(v[0], v[1], v[2], __uint_as_float(t));
   tris[3 * static_cast<size_t>(p) + 1] = make_float4(v[3], v[4], v[5], 0.f);
   tris[3 * static_cast<size_t>(p) + 2] = make_float4(v[6], v[7], v[8], 0.f);
-  shade[3 * static_cast<size_t>(p)] = make_float4(c[0], c[1], c[2], flags[t] ? 1.0f : 0.0f);
+  shade[3 * static_cast<size_t>(p)] = make_float4(c[0], c[1], c[2], static_cast<float>(flags[t]));
   shade[3 * static_cast<size_t>(p) + 1] = make_float4(c[4], c[5], c[6], c[7]);
   shade[3 * static_cast<size_t>(p) + 2] = make_float4(c[8], c[9], c[10], c[11]);
 }

@@ -19,6 +19,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "device_api.hpp"
@@ -239,53 +240,240 @@ __global__ void knnKernel(const float4* __restrict__ omm, uint32_t N, int* __res
   for (int k = 0; k < kNeighbours; ++k) nb[kNeighbours * o + k] = idx[k];
 }
 
-// Per-ommatidium feature block (kFeatBlock floats) from its statistics.
-__device__ __forceinline__ void featureBlock(const float* __restrict__ s, const float4* __restrict__ omm, uint32_t o,
-                                             float* f) {
-  const float m0 = s[0], m1 = s[1], m2 = s[2];
-  f[0] = m0;
-  f[1] = m1;
-  f[2] = m2;
-  f[3] = sqrtf(fmaxf(s[3] - m0 * m0, 0.f));
-  f[4] = sqrtf(fmaxf(s[4] - m1 * m1, 0.f));
-  f[5] = sqrtf(fmaxf(s[5] - m2 * m2, 0.f));
-  const float hit = s[6];
-  f[6] = hit;
-  const float depth = hit > 0.f ? s[7] / hit : 0.f;
-  f[7] = log1pf(depth) * 0.25f;
-  f[8] = s[8];
-  f[9] = s[9];
-  f[10] = s[10];
-  const float4 a = omm[2 * o], b = omm[2 * o + 1];
-  const float il = rsqrtf(fmaxf(a.w * a.w + b.x * b.x + b.y * b.y, 1e-30f));
-  f[11] = a.w * il;
-  f[12] = b.x * il;
-  f[13] = b.y * il;
-  f[14] = b.z * 10.0f;
+// Feature rows.  Block 0 describes the ommatidium itself:
+//   0-2 mean colour, 3-5 colour standard deviation x 4, 6 hit fraction,
+//   7 log(1 + mean hit distance) / 4, 8-10 mean facing normal, 11-13 axis
+//   direction (eye frame), 14 acceptance angle x 10 (radians).
+// Blocks 1..6 describe the neighbours relative to it:
+//   0-2 (neighbour mean - own mean) x 4, 3-5 neighbour deviation x 4,
+//   6 hit-fraction difference, 7 log-distance difference, 8-10 neighbour
+//   normal, 11-12 neighbour axis offset in the own axis' tangent frame and
+//   13 its length, all in units of the own acceptance angle, 14 acceptance
+//   angle ratio.
+// Colour differences are formed in fp32 before the bf16 rounding.
+struct OmmStats {
+  float m[3], sd[3], hit, logDepth, n[3];
+};
+
+__device__ __forceinline__ OmmStats ommStats(const float* __restrict__ s) {
+  OmmStats r;
+  for (int k = 0; k < 3; ++k) {
+    r.m[k] = s[k];
+    r.sd[k] = sqrtf(fmaxf(s[3 + k] - s[k] * s[k], 0.f));
+    r.n[k] = s[8 + k];
+  }
+  r.hit = s[6];
+  const float depth = r.hit > 0.f ? s[7] / r.hit : 0.f;
+  r.logDepth = log1pf(depth) * 0.25f;
+  return r;
 }
 
-// Feature rows: [own block, 6 neighbour blocks, zero padding] as bf16, and
-// the own 8-sample mean colour as the residual base (fp32).
+__device__ __forceinline__ float3 ommAxis(const float4* __restrict__ omm, uint32_t o, float& aa) {
+  const float4 a = omm[2 * o], b = omm[2 * o + 1];
+  const float il = rsqrtf(fmaxf(a.w * a.w + b.x * b.x + b.y * b.y, 1e-30f));
+  aa = b.z;
+  return make_float3(a.w * il, b.x * il, b.y * il);
+}
+
+// One feature row (row = pose * N + ommatidium): the own block when
+// `withSelf`, neighbour blocks [jBegin, jEnd) and, when jEnd is the last
+// neighbour, the zero padding; the residual base (own mean colour) when
+// `base` is given.
+__device__ __forceinline__ void featureRow(const float* __restrict__ stats, const float4* __restrict__ omm,
+                                           const int* __restrict__ nb, uint32_t N, size_t row, bool withSelf,
+                                           int jBegin, int jEnd, __nv_bfloat16* __restrict__ x,
+                                           float* __restrict__ base) {
+  const uint32_t p = static_cast<uint32_t>(row / N), o = static_cast<uint32_t>(row % N);
+  const float* sp = stats + static_cast<size_t>(p) * N * kFeatureStats;
+  const OmmStats me = ommStats(sp + static_cast<size_t>(o) * kFeatureStats);
+  float aa;
+  const float3 d = ommAxis(omm, o, aa);
+  float f[kFeatBlock];
+  if (withSelf) {
+    for (int k = 0; k < 3; ++k) {
+      f[k] = me.m[k];
+      f[3 + k] = me.sd[k] * 4.0f;
+      f[8 + k] = me.n[k];
+    }
+    f[6] = me.hit;
+    f[7] = me.logDepth;
+    f[11] = d.x;
+    f[12] = d.y;
+    f[13] = d.z;
+    f[14] = aa * 10.0f;
+    for (int k = 0; k < kFeatBlock; ++k) x[k] = __float2bfloat16(f[k]);
+  }
+  if (base) {
+    base[3 * row] = me.m[0];
+    base[3 * row + 1] = me.m[1];
+    base[3 * row + 2] = me.m[2];
+  }
+  if (jBegin >= jEnd) return;
+  const float inva = 1.0f / fmaxf(aa, 1e-6f);
+  // tangent frame of the own axis
+  float3 t1 = fabsf(d.y) < 0.9f ? make_float3(d.z, 0.f, -d.x) : make_float3(0.f, -d.z, d.y);
+  const float il = rsqrtf(fmaxf(t1.x * t1.x + t1.y * t1.y + t1.z * t1.z, 1e-30f));
+  t1 = make_float3(t1.x * il, t1.y * il, t1.z * il);
+  const float3 t2 = make_float3(d.y * t1.z - d.z * t1.y, d.z * t1.x - d.x * t1.z, d.x * t1.y - d.y * t1.x);
+  for (int j = jBegin; j < jEnd; ++j) {
+    const uint32_t q = static_cast<uint32_t>(nb[kNeighbours * o + j]);
+    const OmmStats ns = ommStats(sp + static_cast<size_t>(q) * kFeatureStats);
+    float qa;
+    const float3 e = ommAxis(omm, q, qa);
+    for (int k = 0; k < 3; ++k) {
+      f[k] = (ns.m[k] - me.m[k]) * 4.0f;
+      f[3 + k] = ns.sd[k] * 4.0f;
+      f[8 + k] = ns.n[k];
+    }
+    f[6] = ns.hit - me.hit;
+    f[7] = ns.logDepth - me.logDepth;
+    const float3 g = make_float3(e.x - d.x, e.y - d.y, e.z - d.z);
+    const float u = (g.x * t1.x + g.y * t1.y + g.z * t1.z) * inva, v = (g.x * t2.x + g.y * t2.y + g.z * t2.z) * inva;
+    f[11] = u;
+    f[12] = v;
+    f[13] = sqrtf(u * u + v * v);
+    f[14] = qa * inva;
+    for (int k = 0; k < kFeatBlock; ++k) x[kFeatBlock * (j + 1) + k] = __float2bfloat16(f[k]);
+  }
+  if (jEnd == kNeighbours)
+    for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) x[k] = __float2bfloat16(0.f);
+}
+
 __global__ void featureKernel(const float* __restrict__ stats, const float4* __restrict__ omm,
                               const int* __restrict__ nb, uint32_t N, uint32_t P, __nv_bfloat16* __restrict__ X,
                               float* __restrict__ base) {
   const size_t row = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (row >= static_cast<size_t>(P) * N) return;
-  const uint32_t p = static_cast<uint32_t>(row / N), o = static_cast<uint32_t>(row % N);
-  __nv_bfloat16* x = X + row * kFeatureWidth;
-  float f[kFeatBlock];
-  const float* sp = stats + static_cast<size_t>(p) * N * kFeatureStats;
-  featureBlock(sp + static_cast<size_t>(o) * kFeatureStats, omm, o, f);
-  for (int k = 0; k < kFeatBlock; ++k) x[k] = __float2bfloat16(f[k]);
-  base[3 * row] = f[0];
-  base[3 * row + 1] = f[1];
-  base[3 * row + 2] = f[2];
-  for (int j = 0; j < kNeighbours; ++j) {
-    const uint32_t q = static_cast<uint32_t>(nb[kNeighbours * o + j]);
-    featureBlock(sp + static_cast<size_t>(q) * kFeatureStats, omm, q, f);
-    for (int k = 0; k < kFeatBlock; ++k) x[kFeatBlock * (j + 1) + k] = __float2bfloat16(f[k]);
+  featureRow(stats, omm, nb, N, row, true, 0, kNeighbours, X + row * kFeatureWidth, base);
+}
+
+// ---------------------------------------------------------------------------
+// Fused inference: feature rows, the four layers and the residual sum for
+// tiles of 128 rows, with all weights resident in shared memory.  A
+// persistent grid (one block per SM) stages the weights once, transposed to
+// [out][in] so every B fragment is one 32-bit shared load; each of the 8
+// warps owns 16 rows and keeps all 128 hidden outputs of a layer in
+// registers (16 m16n8 tiles), so activations never leave the SM.  The
+// k-steps run in the same order as gemmKernel's, so a row's prediction is
+// bit-identical to the layer-by-layer path.
+// ---------------------------------------------------------------------------
+constexpr int kInferRows = 128;
+constexpr int kInferThreads = 256;
+constexpr int kS1 = kFeatureWidth + 8;  // padded row strides (bf16 elements)
+constexpr int kSH = kMlpHidden + 8;
+constexpr size_t kInferSmem = (size_t(kMlpHidden) * kS1 + 2 * size_t(kMlpHidden) * kSH + size_t(kMlpOut) * kSH +
+                               size_t(kInferRows) * kSH) * 2 +
+                              (3 * kMlpHidden + kMlpOut) * 4;
+
+// One hidden layer for the warp's 16 rows, in place: h[16 x K] -> h[16 x 128].
+template <int K, int kStrideW>
+__device__ __forceinline__ void hiddenLayer(__nv_bfloat16* h, const __nv_bfloat16* wt, const float* bias, int lane) {
+  const int g = lane >> 2, q = lane & 3;
+  float acc[kMlpHidden / 8][4];
+#pragma unroll
+  for (int j = 0; j < kMlpHidden / 8; ++j)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[j][r] = 0.f;
+#pragma unroll
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint32_t a[4];
+    const __nv_bfloat16* hr = h + g * kSH + k0 + 2 * q;
+    a[0] = *reinterpret_cast<const uint32_t*>(hr);
+    a[1] = *reinterpret_cast<const uint32_t*>(hr + 8 * kSH);
+    a[2] = *reinterpret_cast<const uint32_t*>(hr + 8);
+    a[3] = *reinterpret_cast<const uint32_t*>(hr + 8 * kSH + 8);
+#pragma unroll
+    for (int j = 0; j < kMlpHidden / 8; ++j) {
+      const __nv_bfloat16* wr = wt + (j * 8 + g) * kStrideW + k0 + 2 * q;
+      uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
+      mma16816(acc[j], a, b);
+    }
   }
-  for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) x[k] = __float2bfloat16(0.f);
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < kMlpHidden / 8; ++j) {
+    const int c = j * 8 + 2 * q;
+    const float v0 = acc[j][0] + bias[c], v1 = acc[j][1] + bias[c + 1];
+    const float v2 = acc[j][2] + bias[c], v3 = acc[j][3] + bias[c + 1];
+    *reinterpret_cast<uint32_t*>(h + g * kSH + c) =
+        pack2(__float2bfloat16(fmaxf(v0, 0.f)), __float2bfloat16(fmaxf(v1, 0.f)));
+    *reinterpret_cast<uint32_t*>(h + (g + 8) * kSH + c) =
+        pack2(__float2bfloat16(fmaxf(v2, 0.f)), __float2bfloat16(fmaxf(v3, 0.f)));
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1)
+    inferKernel(const float* __restrict__ stats, const float4* __restrict__ omm, const int* __restrict__ nb,
+                uint32_t N, uint64_t rows, MlpWeights w, float* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __nv_bfloat16* w1t = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* w2t = w1t + kMlpHidden * kS1;
+  __nv_bfloat16* w3t = w2t + kMlpHidden * kSH;
+  __nv_bfloat16* w4t = w3t + kMlpHidden * kSH;
+  __nv_bfloat16* h = w4t + kMlpOut * kSH;
+  float* b1 = reinterpret_cast<float*>(h + kInferRows * kSH);
+  float* b2 = b1 + kMlpHidden;
+  float* b3 = b2 + kMlpHidden;
+  float* b4 = b3 + kMlpHidden;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // Stage the weights transposed: wt[n][k] = W[k][n].
+  for (int e = tid; e < kFeatureWidth * kMlpHidden; e += kInferThreads)
+    w1t[(e % kMlpHidden) * kS1 + e / kMlpHidden] = w.w1[e];
+  for (int e = tid; e < kMlpHidden * kMlpHidden; e += kInferThreads) {
+    w2t[(e % kMlpHidden) * kSH + e / kMlpHidden] = w.w2[e];
+    w3t[(e % kMlpHidden) * kSH + e / kMlpHidden] = w.w3[e];
+  }
+  for (int e = tid; e < kMlpHidden * kMlpOut; e += kInferThreads) w4t[(e % kMlpOut) * kSH + e / kMlpOut] = w.w4[e];
+  for (int e = tid; e < kMlpHidden; e += kInferThreads) {
+    b1[e] = w.b1[e];
+    b2[e] = w.b2[e];
+    b3[e] = w.b3[e];
+  }
+  if (tid < kMlpOut) b4[tid] = w.b4[tid];
+  const uint64_t tiles = (rows + kInferRows - 1) / kInferRows;
+  const int g = lane >> 2, q = lane & 3;
+  __nv_bfloat16* hw = h + warp * 16 * kSH;
+  for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    __syncthreads();  // weights staged / previous tile's rows consumed
+    {
+      const int r = tid >> 1, half = tid & 1;
+      const uint64_t row = tile * kInferRows + r;
+      __nv_bfloat16* x = h + r * kSH;
+      if (row < rows) {
+        featureRow(stats, omm, nb, N, row, half == 0, half == 0 ? 0 : 3, half == 0 ? 3 : kNeighbours, x, nullptr);
+      } else {
+        for (int k = half; k < kFeatureWidth; k += 2) x[k] = __float2bfloat16(0.f);
+      }
+    }
+    __syncthreads();
+    hiddenLayer<kFeatureWidth, kS1>(hw, w1t, b1, lane);
+    hiddenLayer<kMlpHidden, kSH>(hw, w2t, b2, lane);
+    hiddenLayer<kMlpHidden, kSH>(hw, w3t, b3, lane);
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k0 = 0; k0 < kMlpHidden; k0 += 16) {
+      uint32_t a[4];
+      const __nv_bfloat16* hr = hw + g * kSH + k0 + 2 * q;
+      a[0] = *reinterpret_cast<const uint32_t*>(hr);
+      a[1] = *reinterpret_cast<const uint32_t*>(hr + 8 * kSH);
+      a[2] = *reinterpret_cast<const uint32_t*>(hr + 8);
+      a[3] = *reinterpret_cast<const uint32_t*>(hr + 8 * kSH + 8);
+      const __nv_bfloat16* wr = w4t + g * kSH + k0 + 2 * q;
+      uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
+      mma16816(acc, a, b);
+    }
+    // acc: rows g / g+8, output columns 2q, 2q+1; columns 0..2 are colours.
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int c = 2 * q + (r & 1);
+      const uint64_t row = tile * kInferRows + warp * 16 + g + (r >= 2 ? 8 : 0);
+      if (c < 3 && row < rows) {
+        const float y = acc[r] + b4[c];
+        out[3 * row + c] = stats[row * kFeatureStats + c] + y;
+      }
+    }
+  }
 }
 
 __global__ void gatherRowsKernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ base,
@@ -367,6 +555,28 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
   if (rows == 0) return cudaSuccess;
   featureKernel<<<static_cast<unsigned>((rows + 127) / 128), 128, 0, stream>>>(
       stats, omm, nb, N, P, static_cast<__nv_bfloat16*>(X), base);
+  return cudaGetLastError();
+}
+
+cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
+                          const MlpWeights& w, float* out, cudaStream_t stream) {
+  const uint64_t rows = static_cast<uint64_t>(N) * P;
+  if (rows == 0) return cudaSuccess;
+  static int smCount = 0;
+  static bool attrSet = false;
+  if (!attrSet) {
+    cudaError_t e = cudaFuncSetAttribute(inferKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kInferSmem));
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    attrSet = true;
+  }
+  const uint64_t tiles = (rows + kInferRows - 1) / kInferRows;
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(tiles, static_cast<uint64_t>(smCount)));
+  inferKernel<<<grid, kInferThreads, kInferSmem, stream>>>(stats, omm, nb, N, rows, w, out);
   return cudaGetLastError();
 }
 

@@ -305,6 +305,62 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ v3 linearize(v3 c) { return mk(powf(c.x, 2.2f), powf(c.y, 2.2f), powf(c.z, 2.2f)); }
 
+// One wrapped texel index along an axis of n texels.
+__device__ __forceinline__ int wrapIndex(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// Texel-space position along one axis: wrap to [0, 1] (frac), scale, move to
+// texel centres; i = first texel, A = weight of the second in 1/256 steps,
+// rounded half up (the texture unit's 8-bit fractional filter weight).
+__device__ __forceinline__ void texAxis(float u, int n, int& i, int& A) {
+  float f = __fsub_rn(u, floorf(u));
+  if (!(f >= 0.0f && f <= 1.0f)) f = 0.0f;  // NaN / infinite coordinates
+  const float xb = __fsub_rn(__fmul_rn(f, static_cast<float>(n)), 0.5f);
+  const float fl = floorf(xb);
+  i = static_cast<int>(fl);
+  A = static_cast<int>(floorf(__fadd_rn(__fmul_rn(__fsub_rn(xb, fl), 256.0f), 0.5f)));
+}
+
+// x / 256 rounded to the nearest integer, ties to even.
+__device__ __forceinline__ uint32_t div256Even(uint32_t x) {
+  const uint32_t q = x >> 8, r = x & 255u;
+  return q + ((r > 128u || (r == 128u && (q & 1u))) ? 1u : 0u);
+}
+
+// Bilinear lookup in integer arithmetic: the four corner weights are the
+// products of the per-axis weights rounded to 1/256, the result
+// sum(w * texel) / (256 * 255) rounded once to float.
+__device__ __forceinline__ float4 sampleTexture(const uint32_t* __restrict__ tx, int4 t, float u, float v) {
+  int i, j, A, B;
+  texAxis(u, t.y, i, A);
+  texAxis(v, t.z, j, B);
+  const int i0 = wrapIndex(i, t.y), i1 = wrapIndex(i + 1, t.y);
+  const int j0 = wrapIndex(j, t.z), j1 = wrapIndex(j + 1, t.z);
+  const uint32_t* row0 = tx + static_cast<uint32_t>(t.x) + static_cast<uint32_t>(j0) * static_cast<uint32_t>(t.y);
+  const uint32_t* row1 = tx + static_cast<uint32_t>(t.x) + static_cast<uint32_t>(j1) * static_cast<uint32_t>(t.y);
+  const uint32_t T00 = __ldg(row0 + i0), T10 = __ldg(row0 + i1), T01 = __ldg(row1 + i0), T11 = __ldg(row1 + i1);
+  const uint32_t a = static_cast<uint32_t>(A), b = static_cast<uint32_t>(B);
+  const uint32_t w00 = div256Even((256u - a) * (256u - b)), w10 = div256Even(a * (256u - b));
+  const uint32_t w01 = div256Even((256u - a) * b), w11 = div256Even(a * b);
+  float r[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t s = 8u * k;
+    const uint32_t acc = w00 * ((T00 >> s) & 255u) + w10 * ((T10 >> s) & 255u) + w01 * ((T01 >> s) & 255u) +
+                         w11 * ((T11 >> s) & 255u);
+    r[k] = __fdiv_rn(static_cast<float>(acc), 65280.0f);
+  }
+  return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// Barycentric interpolation of one texture coordinate, (1-b1-b2) p0 + b1 p1
+// + b2 p2 evaluated left to right with rounded operations.
+__device__ __forceinline__ float lerpUv(float w0, float b1, float b2, float p0, float p1, float p2) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(w0, p0), __fmul_rn(b1, p1)), __fmul_rn(b2, p2));
+}
+
 __device__ __forceinline__ v3 shadeHit(const DevScene& sc, uint32_t pos, float b1, float b2) {
   const float4* s = sc.shade + 3 * pos;
   const float4 c0 = __ldg(s);
@@ -312,6 +368,12 @@ __device__ __forceinline__ v3 shadeHit(const DevScene& sc, uint32_t pos, float b
   const float4 c1 = __ldg(s + 1);
   const float4 c2 = __ldg(s + 2);
   const float w0 = 1.0f - b1 - b2;
+  if (c0.w == 2.0f) {  // base colour texture at the interpolated (u, v)
+    const float u = lerpUv(w0, b1, b2, c0.x, c1.x, c2.x);
+    const float v = lerpUv(w0, b1, b2, c0.y, c1.y, c2.y);
+    const float4 T = sampleTexture(sc.texels, __ldg(sc.texTable + static_cast<int>(c0.z)), u, v);
+    return linearize(mk(T.x, T.y, T.z));
+  }
   const v3 C = mk(w0 * c0.x + b1 * c1.x + b2 * c2.x, w0 * c0.y + b1 * c1.y + b2 * c2.y, w0 * c0.z + b1 * c1.z + b2 * c2.z);
   return linearize(C);
 }
@@ -372,6 +434,24 @@ __global__ void rngInitKernel(DevEye eye, uint32_t* errFlag) {
   storeState(eye.rng, total, idx, st);
 }
 
+// The random numbers of P consecutive frames for every (ommatidium, sample)
+// stream, in the order the render kernel would draw them (one normal, then
+// one uniform per frame), into draws[(p * N + o) * spp + s]; the states
+// advance by P frames, exactly as a render of the P poses would leave them.
+__global__ void drawsKernel(DevEye eye, uint32_t P) {
+  const size_t total = static_cast<size_t>(eye.N) * eye.spp;
+  const size_t idx = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  curandState st;
+  loadState(eye.rng, total, idx, st);
+  for (uint32_t p = 0; p < P; ++p) {
+    const float nd = curand_normal(&st);
+    const float ud = curand_uniform(&st);
+    eye.draws[static_cast<size_t>(p) * total + idx] = make_float2(nd, ud);
+  }
+  storeState(eye.rng, total, idx, st);
+}
+
 __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 
 // kMode: 0 = render, 1 = render and record every ray, 2 = render and count
@@ -389,11 +469,20 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   constexpr bool kCount = kMode == 2;
   constexpr bool kFeat = kMode == 3;
   const uint32_t lane = threadIdx.x & 31u;
+  uint32_t p0 = 0, p1 = P;
+  if (plan.poseSplits > 1) {
+    const uint64_t perSplit = plan.tasks / plan.poseSplits;
+    const uint32_t split = static_cast<uint32_t>(task / perSplit);
+    task %= perSplit;
+    p0 = split * plan.posesPerSplit;
+    p1 = min(P, p0 + plan.posesPerSplit);
+  }
   const uint32_t group = static_cast<uint32_t>(task / plan.chunks);
   const uint32_t chunk = static_cast<uint32_t>(task % plan.chunks);
-  const uint32_t o = group * plan.ommPerWarp + lane / plan.segWidth;
+  const uint32_t slot = group * plan.ommPerWarp + lane / plan.segWidth;
+  const uint32_t o = (eye.order && slot < eye.N) ? __ldg(eye.order + slot) : slot;
   const uint32_t s = chunk * 32u + lane % plan.segWidth;
-  const bool valid = o < eye.N && s < eye.spp;
+  const bool valid = slot < eye.N && s < eye.spp;
   const size_t plane = static_cast<size_t>(eye.N) * eye.spp;
   const size_t sidx = static_cast<size_t>(o) * eye.spp + s;
 
@@ -401,7 +490,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   v3 axis = mk(0.f, 1.f, 0.f), relPos = mk(0.f, 0.f, 0.f), perp = mk(0.f, 0.f, 1.f);
   float sd = 0.f, fpo = 0.f;
   if (valid) {
-    loadState(eye.rng, plane, sidx, st);
+    if (!eye.draws) loadState(eye.rng, plane, sidx, st);
     const float4 a = __ldg(eye.omm + 2 * o);
     const float4 b = __ldg(eye.omm + 2 * o + 1);
     axis = mk(a.w, b.x, b.y);
@@ -416,7 +505,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   }
   const float invSpp = 1.0f / static_cast<float>(eye.spp);
 
-  for (uint32_t p = 0; p < P; ++p) {
+  for (uint32_t p = p0; p < p1; ++p) {
     v3 col = mk(0.f, 0.f, 0.f);
     // Feature mode: per-sample squared colour, hit flag, hit distance and the
     // hit triangle's normal in the eye's frame (facing the ray), all / spp.
@@ -424,8 +513,15 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
     if (valid) {
       const float4* pp = poses + 4 * p;
       const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
-      const float nd = curand_normal(&st);
-      const float ud = curand_uniform(&st);
+      float nd, ud;
+      if (eye.draws) {
+        const float2 dr = eye.draws[(static_cast<size_t>(p) * eye.N + o) * eye.spp + s];
+        nd = dr.x;
+        ud = dr.y;
+      } else {
+        nd = curand_normal(&st);
+        ud = curand_uniform(&st);
+      }
       const float splayAngle = nd * sd;
       const float axisAngle = ud * CR_PI_F;
       const v3 splayed = rotatePoint(axis, splayAngle, perp);
@@ -523,7 +619,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       dst[2] = col.z;
     }
   }
-  if (valid) storeState(eye.rng, plane, sidx, st);
+  if (valid && !eye.draws) storeState(eye.rng, plane, sidx, st);
 }
 
 template <int kMode, int kMinBlocks>
@@ -740,7 +836,76 @@ __global__ void batchCombineKernel(const BatchEye* __restrict__ eyes, const unsi
   be.out[3 * local + 2] = z;
 }
 
+// The render kernel's texture filter and the hardware sampler side by side.
+__global__ void textureCheckKernel(const uint32_t* __restrict__ tx, int4 t, cudaTextureObject_t obj,
+                                   const float2* __restrict__ uv, int n, float4* __restrict__ soft,
+                                   float4* __restrict__ hard) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float2 c = uv[k];
+  soft[k] = sampleTexture(tx, t, c.x, c.y);
+  hard[k] = tex2D<float4>(obj, c.x, c.y);
+}
+
 }  // namespace
+
+cudaError_t sampleTextureBoth(const uint32_t* texels, int width, int height, const float* uv, int n, float* rgbaSoft,
+                              float* rgbaHard) {
+  if (width <= 0 || height <= 0 || n < 0 || !texels || (n > 0 && (!uv || !rgbaSoft || !rgbaHard)))
+    return cudaErrorInvalidValue;
+  if (n == 0) return cudaSuccess;
+  const size_t texBytes = static_cast<size_t>(width) * static_cast<size_t>(height) * 4;
+  uint32_t* dTex = nullptr;
+  float2* dUv = nullptr;
+  float4* dOut = nullptr;
+  cudaArray_t arr = nullptr;
+  cudaTextureObject_t obj = 0;
+  cudaError_t e = cudaMalloc(&dTex, texBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&dUv, static_cast<size_t>(n) * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&dOut, static_cast<size_t>(n) * 2 * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMemcpy(dTex, texels, texBytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dUv, uv, static_cast<size_t>(n) * sizeof(float2), cudaMemcpyHostToDevice);
+  // The reference's texture: a uchar4 array behind a sampler with wrap
+  // addressing, linear filtering, normalised-float reads and normalised
+  // coordinates (MulticamScene.cpp:753-833).
+  const cudaChannelFormatDesc cd = cudaCreateChannelDesc<uchar4>();
+  if (e == cudaSuccess) e = cudaMallocArray(&arr, &cd, static_cast<size_t>(width), static_cast<size_t>(height));
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DToArray(arr, 0, 0, texels, static_cast<size_t>(width) * 4, static_cast<size_t>(width) * 4,
+                            static_cast<size_t>(height), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeNormalizedFloat;
+    td.normalizedCoords = 1;
+    td.maxAnisotropy = 1;
+    td.maxMipmapLevelClamp = 99;
+    td.minMipmapLevelClamp = 0;
+    td.mipmapFilterMode = cudaFilterModePoint;
+    td.borderColor[0] = 1.0f;
+    td.sRGB = 0;
+    e = cudaCreateTextureObject(&obj, &rd, &td, nullptr);
+  }
+  if (e == cudaSuccess) {
+    const int4 t = make_int4(0, width, height, 0);
+    textureCheckKernel<<<(n + 127) / 128, 128>>>(dTex, t, obj, dUv, n, dOut, dOut + n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(rgbaSoft, dOut, static_cast<size_t>(n) * sizeof(float4), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(rgbaHard, dOut + n, static_cast<size_t>(n) * sizeof(float4), cudaMemcpyDeviceToHost);
+  if (obj) cudaDestroyTextureObject(obj);
+  if (arr) cudaFreeArray(arr);
+  cudaFree(dOut);
+  cudaFree(dUv);
+  cudaFree(dTex);
+  return e;
+}
 
 WarpPlan planWarps(uint32_t N, uint32_t spp) {
   WarpPlan p;
@@ -758,6 +923,29 @@ WarpPlan planWarps(uint32_t N, uint32_t spp) {
   const uint64_t groups = (static_cast<uint64_t>(N) + p.ommPerWarp - 1) / p.ommPerWarp;
   p.tasks = groups * p.chunks;
   return p;
+}
+
+namespace {
+constexpr uint64_t kFillWarps = 16384;  // warps that keep every SM busy (152 SMs x 8 blocks x 4 warps, x3)
+
+// Cuts the poses of a pre-drawn launch into ranges so that about kFillWarps
+// warp tasks exist.
+WarpPlan splitPoses(WarpPlan plan, uint32_t P) {
+  if (P < 2 || plan.tasks >= kFillWarps / 2) return plan;
+  uint64_t S = (kFillWarps + plan.tasks - 1) / plan.tasks;
+  if (S > P) S = P;
+  const uint32_t pps = static_cast<uint32_t>((P + S - 1) / S);
+  plan.posesPerSplit = pps;
+  plan.poseSplits = (P + pps - 1) / pps;
+  plan.tasks *= plan.poseSplits;
+  return plan;
+}
+}  // namespace
+
+size_t renderDrawBytes(uint32_t N, uint32_t spp, uint32_t P) {
+  const WarpPlan plan = splitPoses(planWarps(N, spp), P);
+  if (plan.poseSplits <= 1) return 0;
+  return static_cast<size_t>(P) * N * spp * sizeof(float2);
 }
 
 size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P) {
@@ -786,8 +974,15 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
                          float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
                          unsigned long long* stats) {
   if (P == 0 || eye.N == 0) return cudaSuccess;
-  const WarpPlan plan = planWarps(eye.N, eye.spp);
+  WarpPlan plan = planWarps(eye.N, eye.spp);
   if (plan.chunks > 1 && scratch == nullptr) return cudaErrorInvalidValue;
+  if (eye.draws) {
+    const size_t total = static_cast<size_t>(eye.N) * eye.spp;
+    drawsKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(eye, P);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    plan = splitPoses(plan, P);
+  }
   const uint64_t threads = plan.tasks * 32;
   const unsigned block = 128;
   const uint64_t blocks = (threads + block - 1) / block;
@@ -820,8 +1015,15 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
 cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
                            uint32_t* errFlag, cudaStream_t stream) {
   if (P == 0 || eye.N == 0) return cudaSuccess;
-  const WarpPlan plan = planWarps(eye.N, eye.spp);
+  WarpPlan plan = planWarps(eye.N, eye.spp);
   if (plan.chunks != 1) return cudaErrorInvalidValue;  // feature renders use at most 32 samples
+  if (eye.draws) {
+    const size_t total = static_cast<size_t>(eye.N) * eye.spp;
+    drawsKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(eye, P);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    plan = splitPoses(plan, P);
+  }
   const uint64_t blocks = (plan.tasks * 32 + 127) / 128;
   renderKernel<3, 5><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr,
                                                                          errFlag, nullptr, nullptr);

@@ -73,14 +73,31 @@ struct HitboxMesh {
 
 enum class MissShader { DefaultBackground = 0, SimpleSky = 1 };
 
+// How a triangle's hit colour is found (shaders.cu:788-811).
+enum : uint8_t {
+  kShadeBaseColour = 0,    // material base colour factor as is
+  kShadeVertexColour = 1,  // pow(barycentric mix of the vertex colours, 2.2)
+  kShadeTexture = 2,       // pow(bilinear sample of the base colour texture, 2.2)
+};
+
+// One base-colour texture: width x height RGBA8 texels starting at texel
+// `offset` of SceneData::texels, row 0 first.
+struct Texture {
+  uint32_t offset = 0;
+  int width = 0, height = 0;
+};
+
 struct SceneData {
   // World-space triangles, 9 floats each (v0, v1, v2).
   std::vector<float> triVerts;
-  // Per triangle: three float4 colours (vertex colours) or the material base
-  // colour repeated; flag 1 = vertex colours (shaded as pow(c, 2.2) of the
-  // barycentric mix), 0 = material base colour as is (shaders.cu:788-811).
-  std::vector<float> triColours;  // 12 floats per triangle
-  std::vector<uint8_t> triUsesVertexColour;
+  // Per triangle 12 floats, three float4 at v0, v1, v2, by shading kind:
+  //   kShadeBaseColour:   the material base colour repeated,
+  //   kShadeVertexColour: the vertex colours,
+  //   kShadeTexture:      (u, v, texture index, 0) at each vertex.
+  std::vector<float> triColours;
+  std::vector<uint8_t> triShading;  // one kShade* per triangle
+  std::vector<uint32_t> texels;     // RGBA8 (r in the low byte) of every texture
+  std::vector<Texture> textures;
   std::vector<MeshPrim> meshes;
   std::vector<HitboxMesh> hitboxes;
   std::vector<Camera> cameras;
@@ -88,7 +105,7 @@ struct SceneData {
   std::string missName = "default_background";
   f3 sceneMin, sceneMax;
 
-  size_t triangleCount() const { return triUsesVertexColour.size(); }
+  size_t triangleCount() const { return triShading.size(); }
 };
 
 // Loads a .gltf (ASCII glTF 2.0) file; throws std::runtime_error on failure.

@@ -132,6 +132,14 @@ def configureExtras(eyeRenderer):
     L.crDenoiserAddTrainingPoses.restype = c_int
     L.crDenoiserTrainingRows.restype = c_size_t
     L.crDenoiserTrain.argtypes = [c_int, c_int, c_float, c_int, c_void_p]
+    L.crDenoiserFeatureRows.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int,
+                                        ndpointer(np.uint16, flags="C_CONTIGUOUS"),
+                                        ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crDenoiserFeatureRows.restype = c_int
+    L.crDenoiserPredictRows.argtypes = [ndpointer(np.uint16, flags="C_CONTIGUOUS"),
+                                        ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t,
+                                        ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crDenoiserPredictRows.restype = c_int
     L.crDenoiserTrain.restype = c_int
     L.crDenoiserRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p]
     L.crDenoiserRenderPosesDevice.restype = c_int
@@ -174,6 +182,15 @@ def configureExtras(eyeRenderer):
     L.crGetTriangleCount.restype = c_size_t
     L.crGetSceneTriangles.argtypes = [c_void_p, c_void_p, c_void_p]
     L.crGetSceneTriangles.restype = c_int
+    L.crGetTextureCount.restype = c_size_t
+    L.crGetTexelCount.restype = c_size_t
+    L.crGetSceneTextures.argtypes = [c_void_p, c_void_p]
+    L.crGetSceneTextures.restype = c_int
+    L.crCompareTextureSampling.argtypes = [ndpointer(np.uint32, flags="C_CONTIGUOUS"), c_int, c_int,
+                                           ndpointer(np.float32, flags="C_CONTIGUOUS"), c_int,
+                                           ndpointer(np.float32, flags="C_CONTIGUOUS"),
+                                           ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crCompareTextureSampling.restype = c_int
     L.crGetOmmatidia.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crGetOmmatidia.restype = c_int
     L.crGetCameraLocalSpace.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS")]
@@ -242,6 +259,28 @@ def getSceneTriangles(eyeRenderer):
     if eyeRenderer.crGetSceneTriangles(verts.ctypes.data, cols.ctypes.data, flags.ctypes.data) != 0:
         raise RuntimeError(lastError(eyeRenderer))
     return verts, cols, flags
+
+
+def getSceneTextures(eyeRenderer):
+    """Decoded textures: (K, 3) int32 table of (first texel, width, height)
+    and the RGBA8 texels as uint32 (red in the low byte)."""
+    k, n = eyeRenderer.crGetTextureCount(), eyeRenderer.crGetTexelCount()
+    table = np.zeros((k, 3), np.int32)
+    texels = np.zeros(n, np.uint32)
+    if eyeRenderer.crGetSceneTextures(table.ctypes.data, texels.ctypes.data) != 0:
+        raise RuntimeError(lastError(eyeRenderer))
+    return table, texels
+
+
+def compareTextureSampling(eyeRenderer, texels, width, height, uv):
+    """(renderer filter, hardware texture unit) lookups, each (n, 4)."""
+    texels = np.ascontiguousarray(texels, np.uint32).reshape(-1)
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    soft = np.zeros((len(uv), 4), np.float32)
+    hard = np.zeros((len(uv), 4), np.float32)
+    if eyeRenderer.crCompareTextureSampling(texels, int(width), int(height), uv.reshape(-1), len(uv), soft, hard) != 0:
+        raise RuntimeError(lastError(eyeRenderer))
+    return soft, hard
 
 
 def getOmmatidia(eyeRenderer):

@@ -19,6 +19,8 @@ import base64
 import json
 import math
 import os
+import struct
+import zlib
 
 import numpy as np
 
@@ -53,6 +55,90 @@ def read_eye(path):
     return np.asarray(rows, np.float32).reshape(-1, 8)
 
 
+def _png_chunk(kind, body):
+    return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+    return np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+
+
+def _filter_rows(rows, bpp, filters):
+    """PNG scanline filtering (ISO/IEC 15948 section 9): row y uses filter
+    filters[y % len(filters)]."""
+    out = bytearray()
+    prev = np.zeros(rows.shape[1], np.int32)
+    for y in range(rows.shape[0]):
+        cur = rows[y].astype(np.int32)
+        a = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]]) if bpp < len(cur) else np.zeros_like(cur)
+        c = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]]) if bpp < len(cur) else np.zeros_like(cur)
+        f = filters[y % len(filters)]
+        pred = [np.zeros_like(cur), a, prev, (a + prev) >> 1, _paeth(a, prev, c)][f]
+        out.append(f)
+        out += ((cur - pred) & 0xFF).astype(np.uint8).tobytes()
+        prev = cur
+    return bytes(out)
+
+
+def _pack_rows(samples, depth):
+    """(h, w*channels) integer samples -> (h, stride) bytes at `depth` bits."""
+    samples = np.asarray(samples)
+    if depth == 8:
+        return samples.astype(np.uint8)
+    if depth == 16:
+        return samples.astype(">u2").view(np.uint8).reshape(samples.shape[0], -1)
+    per = 8 // depth
+    h, n = samples.shape
+    padded = np.zeros((h, -(-n // per) * per), np.uint8)
+    padded[:, :n] = samples
+    out = np.zeros((h, padded.shape[1] // per), np.uint8)
+    for k in range(per):
+        out |= (padded[:, k::per] << (8 - depth * (k + 1))).astype(np.uint8)
+    return out
+
+
+def png_bytes(samples, colour_type=6, depth=8, palette=None, trns=None, filters=(0, 1, 2, 3, 4), interlace=False,
+              level=6):
+    """Encodes an (h, w, channels) integer array as a PNG file (colour type
+    0 grey, 2 RGB, 3 palette index, 4 grey+alpha, 6 RGBA) at the given bit
+    depth, cycling the scanline filters, optionally Adam7-interlaced."""
+    samples = np.asarray(samples)
+    if samples.ndim == 2:
+        samples = samples[:, :, None]
+    h, w, ch = samples.shape
+    bpp = max(1, ch * depth // 8)
+    raw = bytearray()
+    if interlace:
+        for x0, y0, dx, dy in ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+                               (0, 1, 1, 2)):
+            sub_img = samples[y0::dy, x0::dx]
+            if sub_img.size == 0:
+                continue
+            raw += _filter_rows(_pack_rows(sub_img.reshape(sub_img.shape[0], -1), depth), bpp, filters)
+    else:
+        raw += _filter_rows(_pack_rows(samples.reshape(h, -1), depth), bpp, filters)
+    out = b"\x89PNG\r\n\x1a\n"
+    out += _png_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, colour_type, 0, 0, 1 if interlace else 0))
+    if palette is not None:
+        out += _png_chunk(b"PLTE", np.asarray(palette, np.uint8).tobytes())
+    if trns is not None:
+        out += _png_chunk(b"tRNS", bytes(trns))
+    comp = zlib.compress(bytes(raw), level)
+    # Split the image data over two IDAT chunks (decoders must join them).
+    half = len(comp) // 2
+    out += _png_chunk(b"IDAT", comp[:half]) + _png_chunk(b"IDAT", comp[half:])
+    out += _png_chunk(b"IEND", b"")
+    return out
+
+
+def rgba_words(rgba):
+    """(h, w, 4) uint8 -> (h*w,) uint32 with red in the low byte."""
+    rgba = np.asarray(rgba, np.uint8).reshape(-1, 4).astype(np.uint32)
+    return rgba[:, 0] | (rgba[:, 1] << 8) | (rgba[:, 2] << 16) | (rgba[:, 3] << 24)
+
+
 class GltfBuilder:
     """Accumulates meshes/cameras into one glTF document with one buffer."""
 
@@ -64,7 +150,44 @@ class GltfBuilder:
         self.nodes = []
         self.cameras = []
         self.materials = []
+        self.images = []
+        self.image_files = {}
+        self.textures = []
+        self.samplers = []
         self.scene_extras = {}
+
+    def image(self, data, how="data", name="img"):
+        """Adds an image from encoded bytes: as a data URI, a bufferView or
+        an external file written next to the glTF."""
+        if how == "data":
+            self.images.append({"name": name, "uri": "data:image/png;base64," + base64.b64encode(data).decode()})
+        elif how == "bufferView":
+            self.images.append({"name": name, "bufferView": self._view(data), "mimeType": "image/png"})
+        else:
+            fname = "%s_%d.png" % (name, len(self.images))
+            self.image_files[fname] = data
+            self.images.append({"name": name, "uri": fname})
+        return len(self.images) - 1
+
+    def texture(self, image, wrap=None, nearest=False):
+        """A texture of an image; `wrap` / `nearest` add a sampler (which
+        the reference ends up ignoring)."""
+        tex = {"source": image}
+        if wrap is not None or nearest:
+            smp = {}
+            if wrap is not None:
+                smp["wrapS"] = smp["wrapT"] = wrap
+            if nearest:
+                smp["minFilter"] = smp["magFilter"] = 9728
+            self.samplers.append(smp)
+            tex["sampler"] = len(self.samplers) - 1
+        self.textures.append(tex)
+        return len(self.textures) - 1
+
+    def textured_material(self, texture, rgba=(1, 1, 1, 1), name="texmat"):
+        self.materials.append({"name": name, "pbrMetallicRoughness": {
+            "baseColorFactor": [float(c) for c in rgba], "baseColorTexture": {"index": int(texture)}}})
+        return len(self.materials) - 1
 
     def _view(self, data):
         while len(self.blob) % 16:
@@ -90,9 +213,11 @@ class GltfBuilder:
         return len(self.materials) - 1
 
     def mesh(self, name, positions, indices, colours=None, material=None, translation=None, rotation=None,
-             scale=None, matrix=None, index_type=None, colour_type=5126, extras=None):
+             scale=None, matrix=None, index_type=None, colour_type=5126, extras=None, texcoords=None):
         positions = np.asarray(positions, np.float32).reshape(-1, 3)
         attrs = {"POSITION": self.accessor(positions, 5126, "VEC3", minmax=True)}
+        if texcoords is not None:
+            attrs["TEXCOORD_0"] = self.accessor(np.asarray(texcoords, np.float32).reshape(-1, 2), 5126, "VEC2")
         if colours is not None:
             colours = np.asarray(colours)
             if colour_type == 5126:
@@ -151,6 +276,12 @@ class GltfBuilder:
             doc["cameras"] = self.cameras
         if self.materials:
             doc["materials"] = self.materials
+        for key in ("images", "textures", "samplers"):
+            if getattr(self, key):
+                doc[key] = getattr(self, key)
+        for fname, data in self.image_files.items():
+            with open(os.path.join(os.path.dirname(path) or ".", fname), "wb") as f:
+                f.write(data)
         if embed:
             uri = "data:application/octet-stream;base64," + base64.b64encode(bytes(self.blob)).decode()
         else:
@@ -311,6 +442,82 @@ def small_scene(outdir, seed=SEED, n_omm=1000, spp=32):
     return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm}
 
 
+def textured_scene(outdir, seed=SEED, n_omm=1000, spp=32):
+    """Textured variant of the small scene: a ground quad with an RGB noise
+    texture repeated through wrapped coordinates in [-3.3, 4.7], 24 boxes
+    with textures of the other PNG forms (palette, 4-bit grey, grey+alpha,
+    RGBA, Adam7-interlaced; no TEXCOORD_0, so they sample at the hit's
+    barycentrics), 4 boxes with vertex colours under a textured material
+    (vertex colours win) and 4 plain boxes; simple_sky.  Images are stored
+    as data URIs, bufferViews and external files.  Returns the small-scene
+    dict plus the decoded RGBA arrays of the images in order."""
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(seed + 7)
+    g = GltfBuilder()
+    g.scene_extras = {"background-shader": "simple_sky"}
+    images = []
+
+    def add_image(rgba_expected, data, how):
+        images.append(np.asarray(rgba_expected, np.uint8))
+        return g.texture(g.image(data, how=how, name="tex%d" % len(images)))
+
+    # 64 x 48 RGB noise, every filter type, data URI
+    rgb = rng.integers(0, 256, size=(48, 64, 3), dtype=np.uint8)
+    t_ground = add_image(np.concatenate([rgb, np.full((48, 64, 1), 255, np.uint8)], axis=2),
+                         png_bytes(rgb, colour_type=2), "data")
+    # 16 x 16 palette of 12 colours with tRNS, bufferView
+    pal = rng.integers(0, 256, size=(12, 3), dtype=np.uint8)
+    idx = rng.integers(0, 12, size=(16, 16), dtype=np.uint8)
+    trns = rng.integers(0, 256, size=5, dtype=np.uint8)
+    alpha = np.full(12, 255, np.uint8)
+    alpha[:5] = trns
+    t_pal = add_image(np.concatenate([pal[idx], alpha[idx][:, :, None]], axis=2),
+                      png_bytes(idx, colour_type=3, palette=pal, trns=trns.tobytes()), "bufferView")
+    # 20 x 12 4-bit grey, external file
+    grey4 = rng.integers(0, 16, size=(12, 20), dtype=np.uint8)
+    g8 = (grey4.astype(np.int32) * 17).astype(np.uint8)
+    t_grey = add_image(np.stack([g8, g8, g8, np.full_like(g8, 255)], axis=2),
+                       png_bytes(grey4, colour_type=0, depth=4), "file")
+    # 9 x 7 grey + alpha
+    ga = rng.integers(0, 256, size=(7, 9, 2), dtype=np.uint8)
+    t_ga = add_image(np.stack([ga[:, :, 0]] * 3 + [ga[:, :, 1]], axis=2), png_bytes(ga, colour_type=4), "data")
+    # 33 x 17 RGBA, Adam7 interlaced, with a sampler (ignored: wrap + linear)
+    rgba = rng.integers(0, 256, size=(17, 33, 4), dtype=np.uint8)
+    t_rgba = add_image(rgba, png_bytes(rgba, colour_type=6, interlace=True), "data")
+    g.samplers.append({"wrapS": 33071, "wrapT": 33648, "magFilter": 9728, "minFilter": 9728})
+    g.textures[t_rgba]["sampler"] = len(g.samplers) - 1
+
+    ground = np.array([[-10, 0, -10], [10, 0, -10], [10, 0, 10], [-10, 0, 10]], np.float64)
+    uv = np.array([[-3.3, -3.3], [4.7, -3.3], [4.7, 4.7], [-3.3, 4.7]], np.float32)
+    g.mesh("ground", ground, np.array([[0, 2, 1], [0, 3, 2]]), material=g.textured_material(t_ground),
+           texcoords=uv)
+    box_tex = [t_pal, t_grey, t_ga, t_rgba]
+    mats = [g.textured_material(t) for t in box_tex]
+    plain = g.material([0.8, 0.3, 0.2, 1.0])
+    placed = 0
+    while placed < 32:
+        c = rng.uniform(-8.0, 8.0, size=2)
+        e = rng.uniform(0.2, 2.0, size=3)
+        if abs(c[0]) < e[0] / 2 + 0.3 and abs(c[1]) < e[2] / 2 + 0.3:
+            continue
+        v, f = box_mesh([c[0] - e[0] / 2, 0.0, c[1] - e[2] / 2], [c[0] + e[0] / 2, e[1], c[1] + e[2] / 2])
+        if placed < 24:
+            g.mesh("tbox%d" % placed, v, f, material=mats[placed % 4])
+        elif placed < 28:
+            col = np.concatenate([rng.uniform(0.0, 1.0, size=(8, 3)), np.ones((8, 1))], axis=1)
+            g.mesh("cbox%d" % placed, v, f, colours=col, material=mats[placed % 4])
+        else:
+            g.mesh("pbox%d" % placed, v, f, material=plain)
+        placed += 1
+    d = fibonacci_sphere(n_omm)
+    eye_path = os.path.join(outdir, "textured.eye")
+    write_eye(eye_path, d * 0.001, d, 3.0 * DEG, 0.0)
+    g.compound_camera("insect-eye", "textured.eye", translation=[0.0, 0.5, 0.0])
+    path = g.write(os.path.join(outdir, "textured.gltf"), embed=True)
+    pose = pose_rows(np.array([0.0, 0.5, 0.0]), 0.0)
+    return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm, "images": images}
+
+
 def terrain_height_fn(heights, extent):
     """Bilinear lookup in the heightfield vertex grid (heights[i, j] at
     x = -extent/2 + i*dx, z = -extent/2 + j*dz)."""
@@ -372,7 +579,17 @@ def terrain_scene(outdir, seed=SEED, cells=512, extent=200.0, cones=2000, n_omm=
     path = g.write(os.path.join(outdir, "terrain.gltf"), embed=False)
     traj = random_walk(hfn, poses, rng, eye_height=eye_height)
     return {"gltf": path, "eye": eye_path, "poses": traj, "spp": spp, "n_omm": n_omm,
-            "triangles": int(len(faces) + 32 * cones)}
+            "triangles": int(len(faces) + 32 * cones), "height_fn": hfn, "extent": extent, "eye_height": eye_height}
+
+
+def random_poses(hfn, count, rng, half_width, eye_height=0.5):
+    """(count, 12) independent poses: x, z uniform in +-half_width, height
+    terrain + eye_height, uniform yaw."""
+    out = np.zeros((count, 12), np.float32)
+    for i in range(count):
+        x, z = rng.uniform(-half_width, half_width, size=2)
+        out[i] = pose_rows(np.array([x, hfn(x, z) + eye_height, z]), rng.uniform(0, 2 * math.pi))
+    return out
 
 
 def random_walk(hfn, count, rng, step=0.1, yaw_sd=10.0 * DEG, eye_height=0.5):

@@ -168,12 +168,21 @@ size_t crDenoiserParamCount(void);
  * and appends count x N (features, target) rows to the training set. */
 int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSpp, int targetSpp);
 size_t crDenoiserTrainingRows(void);
-/* `steps` Adam steps on shuffled minibatches; lossHistory: steps floats
+/* `steps` Adam steps on shuffled minibatches, the step size decaying from
+ * lr by a half cosine to 5% of it over the call; lossHistory: steps floats
  * (mean squared error per step) or null. */
 int crDenoiserTrain(int steps, int batch, float lr, int seed, float* lossHistory);
-/* The learned form: featureSpp-sample render + network, count x N x 3. */
+/* The learned form: featureSpp-sample render + network, count x N x 3
+ * (one fused feature + network kernel after the feature render). */
 int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out);
 int crDenoiserRenderPoses(const float* poses12, size_t count, int featureSpp, float* out);
+/* The feature render's rows for host poses: x count*N x 112 bf16 bit
+ * patterns, base count*N x 3 (own mean colour); advances the feature
+ * streams like a learned render.  And the layer-by-layer prediction of host
+ * rows, base + network(x), rows x 3.  Test access, no reference
+ * counterpart. */
+int crDenoiserFeatureRows(const float* poses12, size_t count, int featureSpp, uint16_t* xBf16, float* base);
+int crDenoiserPredictRows(const uint16_t* xBf16, const float* base, size_t rows, float* out);
 /* One forward/backward pass on host rows (x: rows x 112 bf16 bit patterns,
  * base/target: rows x 3): returns the loss (-1 on error) and writes the
  * gradients and the current parameters (crDenoiserParamCount floats each). */
@@ -205,10 +214,30 @@ int crSynchronize(void);
 int crRenderFrameRecorded(void* records);
 
 /* Flattened world-space scene: number of triangles, then per triangle 9
- * floats of vertices, 12 floats of colours and one byte that is 1 when the
- * triangle is shaded from vertex colours.  0 on success. */
+ * floats of vertices, 12 floats of colour record and one shading byte:
+ * 0 = material base colour (record = the colour three times), 1 = vertex
+ * colours (record = the three vertex colours), 2 = base colour texture
+ * (record = (u, v, texture index, 0) per vertex).  0 on success.
+ * No counterpart in the reference (test and tooling access). */
 size_t crGetTriangleCount(void);
-int crGetSceneTriangles(float* verts, float* colours, unsigned char* usesVertexColour);
+int crGetSceneTriangles(float* verts, float* colours, unsigned char* shading);
+
+/* Decoded base colour textures of the loaded scene: texture count, total
+ * texel count, then per texture (first texel, width, height) as 3 ints and
+ * all texels as RGBA8 words (red in the low byte), row 0 first.  0 on
+ * success.  No counterpart in the reference. */
+size_t crGetTextureCount(void);
+size_t crGetTexelCount(void);
+int crGetSceneTextures(int* table, unsigned int* texels);
+
+/* Samples a width x height RGBA8 texture at n (u, v) pairs with the
+ * renderer's bilinear filter (rgbaRenderer) and with a CUDA texture object
+ * in the reference's sampler state (rgbaHardware; wrap, linear filter,
+ * normalised coordinates and reads; libEyeRenderer3/MulticamScene.cpp:800-833),
+ * n x 4 floats each.  Host buffers; allocates and synchronises.  0 on
+ * success.  No counterpart in the reference (sampling check). */
+int crCompareTextureSampling(const unsigned int* texels, int width, int height, const float* uv, int n,
+                             float* rgbaRenderer, float* rgbaHardware);
 
 /* Current eye's ommatidium records as N x 8 floats (position, direction,
  * acceptance angle, focal offset).  0 on success. */

@@ -12,6 +12,13 @@ Restates libEyeRenderer3/MulticamScene.cpp:
   * COLOR_0 shaded from vertices only when VEC4 float / u16 / u8
     (:415-516, cuda/LocalGeometry.h:105-156), else the material
     baseColorFactor (default white, cuda/MaterialData.h:42);
+  * without vertex colours a material baseColorTexture gives texture
+    shading at TEXCOORD_0 (float VEC2) or at the barycentrics
+    (shaders.cu:801-805, cuda/LocalGeometry.h:88-103); records (u, v,
+    texture, 0) per vertex with the default coordinates (0,0) (1,0) (0,1);
+  * every image decoded to RGBA8 as a forced 4-component load would
+    (tiny_gltf.h:2305-2389), here with Python's zlib and the PNG
+    specification's unfiltering and Adam7 passes; 16-bit images refused;
   * background shader from the scene extras (:555-565).
 Transforms are composed and applied in float64 with the same operation order
 as the library's loader and rounded once to float32 (the reference composes
@@ -22,6 +29,8 @@ import ctypes
 import ctypes.util
 import json
 import os
+import struct
+import zlib
 
 import numpy as np
 
@@ -105,11 +114,100 @@ def _extra_true(extras, key):
     return False
 
 
+def _unfilter(data, pos, h, stride, bpp):
+    out = np.zeros((h, stride), np.int32)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        f = data[pos]
+        line = np.frombuffer(data, np.uint8, stride, pos + 1).astype(np.int32)
+        pos += stride + 1
+        cur = np.zeros(stride, np.int32)
+        for i in range(stride):
+            a = cur[i - bpp] if i >= bpp else 0
+            b = prev[i]
+            c = prev[i - bpp] if i >= bpp else 0
+            if f == 0:
+                p = 0
+            elif f == 1:
+                p = a
+            elif f == 2:
+                p = b
+            elif f == 3:
+                p = (a + b) >> 1
+            elif f == 4:
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            else:
+                raise ValueError("bad PNG filter")
+            cur[i] = (line[i] + p) & 0xFF
+        out[y] = cur
+        prev = cur
+    return out, pos
+
+
+def decode_png(data):
+    """PNG -> (h, w, 4) uint8 with a forced four-channel expansion."""
+    assert data[:8] == b"\x89PNG\r\n\x1a\n", "not a PNG image"
+    pos, idat, palette, trns = 8, b"", None, b""
+    while pos + 8 <= len(data):
+        n, kind = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8: pos + 8 + n]
+        if kind == b"IHDR":
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body[:13])
+        elif kind == b"PLTE":
+            palette = np.frombuffer(body, np.uint8).reshape(-1, 3)
+        elif kind == b"tRNS":
+            trns = body
+        elif kind == b"IDAT":
+            idat += body
+        elif kind == b"IEND":
+            break
+        pos += 12 + n
+    if depth == 16:
+        raise ValueError("16-bit images are not supported")
+    raw = zlib.decompress(idat)
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    img = np.zeros((h, w, 4), np.uint8)
+    img[:, :, 3] = 255
+    passes = [(0, 0, 1, 1)] if not interlace else [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4),
+                                                    (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+    at = 0
+    for x0, y0, dx, dy in passes:
+        pw, ph = (w - x0 + dx - 1) // dx if x0 < w else 0, (h - y0 + dy - 1) // dy if y0 < h else 0
+        if pw == 0 or ph == 0:
+            continue
+        stride = (pw * ch * depth + 7) // 8
+        rows, at = _unfilter(raw, at, ph, stride, max(1, ch * depth // 8))
+        if depth == 8:
+            s = rows[:, : pw * ch].reshape(ph, pw, ch)
+        else:
+            bits = np.unpackbits(rows.astype(np.uint8), axis=1)[:, : pw * depth].reshape(ph, pw, depth)
+            s = (bits * (1 << np.arange(depth - 1, -1, -1))).sum(axis=2)[:, :, None]
+            if ctype == 0:
+                s = s * (255 // ((1 << depth) - 1))
+        sub_img = np.zeros((ph, pw, 4), np.uint8)
+        sub_img[:, :, 3] = 255
+        if ctype == 3:
+            sub_img[:, :, :3] = palette[s[:, :, 0]]
+            alpha = np.full(len(palette), 255, np.uint8)
+            alpha[: len(trns)] = np.frombuffer(trns, np.uint8)[: len(palette)]
+            sub_img[:, :, 3] = alpha[s[:, :, 0]]
+        elif ctype in (0, 4):
+            sub_img[:, :, :3] = s[:, :, :1]
+            if ctype == 4:
+                sub_img[:, :, 3] = s[:, :, 1]
+        else:
+            sub_img[:, :, :ch] = s
+        img[y0::dy, x0::dx] = sub_img
+    return img
+
+
 class RefScene:
     def __init__(self):
         self.verts = []
         self.colours = []
         self.flags = []
+        self.images = []  # (h, w, 4) uint8 per image
         self.meshes = []  # (name, tri offset, tri count)
         self.cameras = []
         self.hitboxes = []
@@ -127,6 +225,18 @@ class RefScene:
         else:
             v, c, f = np.zeros((0, 3, 3), np.float32), np.zeros((0, 3, 4), np.float32), np.zeros(0, np.uint8)
         return v, c, f
+
+    def textures(self):
+        """(table (K,3) of first texel / width / height, uint32 texels)."""
+        table, words, off = [], [], 0
+        for im in self.images:
+            h, w = im.shape[:2]
+            table.append((off, w, h))
+            q = im.reshape(-1, 4).astype(np.uint32)
+            words.append(q[:, 0] | (q[:, 1] << 8) | (q[:, 2] << 16) | (q[:, 3] << 24))
+            off += w * h
+        t = np.array(table, np.int32).reshape(-1, 3)
+        return t, (np.concatenate(words) if words else np.zeros(0, np.uint32))
 
 
 def load(path):
@@ -157,6 +267,19 @@ def load(path):
         return np.ascontiguousarray(rows).view(dt).reshape(count, nc), a
 
     sc = RefScene()
+    for im in doc.get("images", []):
+        uri = im.get("uri", "")
+        if uri.startswith("data:"):
+            data = base64.b64decode(uri.split(",", 1)[1])
+        elif uri:
+            with open(gdir + uri, "rb") as fh:
+                data = fh.read()
+        else:
+            bv = doc["bufferViews"][im["bufferView"]]
+            o = bv.get("byteOffset", 0)
+            data = bytes(buffers[bv["buffer"]][o: o + bv["byteLength"]])
+        sc.images.append(decode_png(data))
+    tex_image = [t["source"] for t in doc.get("textures", [])]
     for s in doc.get("scenes", []):
         bg = (s.get("extras") or {}).get("background-shader", "")
         if isinstance(bg, str) and bg:
@@ -231,10 +354,14 @@ def load(path):
                 world = np.stack([wx, wy, wz], axis=1).astype(np.float32)
                 base = np.ones(4, np.float32)
                 mat = prim.get("material", -1)
+                tex = -1
                 if mat is not None and mat >= 0:
-                    bcf = doc["materials"][mat].get("pbrMetallicRoughness", {}).get("baseColorFactor")
+                    pbr = doc["materials"][mat].get("pbrMetallicRoughness", {})
+                    bcf = pbr.get("baseColorFactor")
                     if bcf is not None:
                         base = np.array([np.float32(v) for v in bcf], np.float32)
+                    if "baseColorTexture" in pbr:
+                        tex = tex_image[pbr["baseColorTexture"]["index"]]
                 flag = 0
                 vcol = np.tile(base, (len(pos), 1))
                 if "COLOR_0" in prim["attributes"]:
@@ -247,8 +374,21 @@ def load(path):
                             vcol = col.astype(np.float32) / np.float32(65535.0)
                         else:
                             vcol = col.astype(np.float32) / np.float32(255.0)
+                if flag == 0 and tex >= 0:
+                    flag = 2
+                    if "TEXCOORD_0" in prim["attributes"]:
+                        uv, _ = accessor(prim["attributes"]["TEXCOORD_0"])
+                        rec = np.zeros((len(tri), 3, 4), np.float32)
+                        rec[:, :, :2] = uv.astype(np.float32)[tri]
+                    else:
+                        rec = np.zeros((len(tri), 3, 4), np.float32)
+                        rec[:, 1, 0] = 1.0
+                        rec[:, 2, 1] = 1.0
+                    rec[:, :, 2] = tex
+                    sc.colours.append(rec)
+                else:
+                    sc.colours.append(vcol[tri])
                 sc.verts.append(world[tri])
-                sc.colours.append(vcol[tri])
                 sc.flags.append(np.full(len(tri), flag, np.uint8))
                 sc.meshes.append((mesh.get("name", ""), off, len(tri)))
         else:

@@ -72,3 +72,19 @@ def forward_backward(params, X, base, target):
     g[OFF_W1:OFF_B1] = (X.T @ dZ1).ravel()
     g[OFF_B1:OFF_W2] = dZ1.sum(0)
     return loss, g
+
+
+def from_bits(bits):
+    """bf16 bit patterns -> float32."""
+    return (np.asarray(bits, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def predict(params, X, base):
+    """base + network(X)[:, :3] with the GPU path's rounding points."""
+    W1, b1, W2, b2, W3, b3, W4, b4 = unpack(params)
+    W1b, W2b, W3b, W4b = (bf16(w).astype(np.float64) for w in (W1, W2, W3, W4))
+    X = bf16(X).astype(np.float64)
+    H1 = bf16(np.maximum(X @ W1b + b1, 0).astype(np.float32)).astype(np.float64)
+    H2 = bf16(np.maximum(H1 @ W2b + b2, 0).astype(np.float32)).astype(np.float64)
+    H3 = bf16(np.maximum(H2 @ W3b + b3, 0).astype(np.float32)).astype(np.float64)
+    return base + (H3 @ W4b + b4)[:, :3]

@@ -10,6 +10,11 @@
 //   ray generation ........ libEyeRenderer3/shaders.cu:648-709
 //   closest hit (no light)  libEyeRenderer3/shaders.cu:779-811,
 //                           cuda/LocalGeometry.h:55-156
+//   base colour textures .. libEyeRenderer3/MulticamScene.cpp:753-833 (a
+//                           uchar4 array read as value/255 through a wrap /
+//                           linear / normalised-coordinate sampler), filtered
+//                           by the texture unit's documented bilinear rule
+//                           with weights in 1/256 steps
 //   miss programs ......... libEyeRenderer3/shaders.cu:740-756
 //   sample scaling/sum .... libEyeRenderer3/shaders.cu:730, 341-347
 //   make_color ............ libEyeRenderer3/shaders.cu:180-189
@@ -60,7 +65,9 @@ struct Scene {
   uint32_t T = 0;
   std::vector<float> v;   // 9 per triangle
   std::vector<float> c;   // 12 per triangle
-  std::vector<uint8_t> f; // vertex-colour flag
+  std::vector<uint8_t> f; // shading kind: 0 base colour, 1 vertex colours, 2 texture
+  std::vector<uint32_t> texels;  // RGBA8, red in the low byte
+  std::vector<int32_t> texTable; // per texture: first texel, width, height
   // BVH: nodes with a box and either two children or a triangle range.
   struct Node {
     double lo[3], hi[3];
@@ -326,10 +333,64 @@ double edgeDistance(const Scene& s, uint32_t t, const float* of, const float* df
 // ---------------------------------------------------------------------------
 // Shading (lighting off).
 // ---------------------------------------------------------------------------
+// Bilinear texture lookup: wrap u to [0, 1] (frac), x = u * width - 0.5,
+// first texel floor(x), weight A of the second = frac(x) in 1/256 steps
+// rounded half up, both texel indices wrapped; the corner weights are the
+// products of the axis weights rounded to 1/256 (ties to even) and the value
+// sum(w * texel) / (256 * 255).  This restates the texture unit's documented
+// bilinear rule with 8-bit fractional weights; on one-axis filtering it
+// matches the unit's output to 2^-16, on two axes to a mean of about 2e-5.
+void texAxis(float u, int n, int& i, int& A) {
+  float f = u - std::floor(u);
+  if (!(f >= 0.0f && f <= 1.0f)) f = 0.0f;
+  const float xb = f * static_cast<float>(n) - 0.5f;
+  const float fl = std::floor(xb);
+  i = static_cast<int>(fl);
+  A = static_cast<int>(std::floor((xb - fl) * 256.0f + 0.5f));
+}
+
+int wrapIndex(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+uint32_t div256Even(uint32_t x) {
+  const uint32_t q = x >> 8, r = x & 255u;
+  return q + ((r > 128u || (r == 128u && (q & 1u))) ? 1u : 0u);
+}
+
+void sampleTexture(const uint32_t* tx, int width, int height, float u, float v, float* rgba) {
+  int i, j, A, B;
+  texAxis(u, width, i, A);
+  texAxis(v, height, j, B);
+  const int i0 = wrapIndex(i, width), i1 = wrapIndex(i + 1, width);
+  const int j0 = wrapIndex(j, height), j1 = wrapIndex(j + 1, height);
+  const uint32_t T[4] = {tx[static_cast<size_t>(j0) * width + i0], tx[static_cast<size_t>(j0) * width + i1],
+                         tx[static_cast<size_t>(j1) * width + i0], tx[static_cast<size_t>(j1) * width + i1]};
+  const uint32_t a = static_cast<uint32_t>(A), b = static_cast<uint32_t>(B);
+  const uint32_t w[4] = {div256Even((256u - a) * (256u - b)), div256Even(a * (256u - b)), div256Even((256u - a) * b),
+                         div256Even(a * b)};
+  for (int k = 0; k < 4; ++k) {
+    uint32_t acc = 0;
+    for (int q = 0; q < 4; ++q) acc += w[q] * ((T[q] >> (8 * k)) & 255u);
+    rgba[k] = static_cast<float>(acc) / 65280.0f;
+  }
+}
+
 V3 shadeHit(const Scene& s, uint32_t t, float b1, float b2) {
   const float* c = &s.c[12 * t];
   if (!s.f[t]) return mk(c[0], c[1], c[2]);
   const float w0 = 1.0f - b1 - b2;
+  if (s.f[t] == 2) {
+    // UV = (1-b1-b2) UV0 + b1 UV1 + b2 UV2 (cuda/LocalGeometry.h:88-103).
+    const float u = w0 * c[0] + b1 * c[4] + b2 * c[8];
+    const float v = w0 * c[1] + b1 * c[5] + b2 * c[9];
+    const int tex = static_cast<int>(c[2]);
+    const int32_t* e = &s.texTable[3 * static_cast<size_t>(tex)];
+    float rgba[4];
+    sampleTexture(&s.texels[static_cast<size_t>(e[0])], e[1], e[2], u, v, rgba);
+    return mk(std::pow(rgba[0], 2.2f), std::pow(rgba[1], 2.2f), std::pow(rgba[2], 2.2f));
+  }
   const V3 C = mk(w0 * c[0] + b1 * c[4] + b2 * c[8], w0 * c[1] + b1 * c[5] + b2 * c[9], w0 * c[2] + b1 * c[6] + b2 * c[10]);
   return mk(std::pow(C.x, 2.2f), std::pow(C.y, 2.2f), std::pow(C.z, 2.2f));
 }
@@ -383,6 +444,19 @@ void setThreads(int threads) {
 }  // namespace
 
 extern "C" {
+
+// Base colour textures of a scene: the texels of all textures and per
+// texture (first texel, width, height).
+void orc_scene_set_textures(void* h, const uint32_t* texels, size_t nTexels, const int32_t* table, uint32_t nTex) {
+  Scene* s = static_cast<Scene*>(h);
+  s->texels.assign(texels, texels + nTexels);
+  s->texTable.assign(table, table + 3 * static_cast<size_t>(nTex));
+}
+
+// n lookups of one texture at (u, v) pairs: n x 4 floats.
+void orc_sample_texture(const uint32_t* texels, int width, int height, const float* uv, size_t n, float* rgba) {
+  for (size_t i = 0; i < n; ++i) sampleTexture(texels, width, height, uv[2 * i], uv[2 * i + 1], rgba + 4 * i);
+}
 
 void* orc_scene_create(const float* verts, const float* colours, const uint8_t* flags, uint32_t T) {
   Scene* s = new Scene;

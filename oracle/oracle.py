@@ -56,6 +56,9 @@ def lib():
         L.orc_render_draws.argtypes = [c_void_p, c_int, f32, c_uint32, c_uint32, c_uint32, f32, f32, f32, c_int]
         L.orc_render_draws.restype = c_size_t
         L.orc_make_color.argtypes = [f32, c_size_t, u8]
+        u32 = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+        L.orc_scene_set_textures.argtypes = [c_void_p, u32, c_size_t, i32, c_uint32]
+        L.orc_sample_texture.argtypes = [u32, c_int, c_int, f32, c_size_t, f32]
         L.orc_max_threads.restype = c_int
         _lib = L
     return _lib
@@ -66,16 +69,24 @@ def _f32(a):
 
 
 class OracleScene:
-    """World-space triangles (T,3,3), colours (T,3,4), vertex-colour flags (T,)
-    and the miss shader id (0 = default_background, 1 = simple_sky)."""
+    """World-space triangles (T,3,3), colour records (T,3,4), shading kinds
+    (T,) (0 base colour, 1 vertex colours, 2 texture with (u, v, texture, 0)
+    records), the miss shader id (0 = default_background, 1 = simple_sky) and
+    optionally the textures: (table (K,3) of first texel / width / height,
+    RGBA8 texels as uint32)."""
 
-    def __init__(self, verts, colours, flags, miss):
+    def __init__(self, verts, colours, flags, miss, textures=None):
         self.verts = _f32(verts).reshape(-1, 9)
         self.colours = _f32(colours).reshape(-1, 12)
         self.flags = np.ascontiguousarray(flags, np.uint8).reshape(-1)
         self.miss = int(miss)
         self.T = len(self.flags)
         self._h = lib().orc_scene_create(self.verts, self.colours, self.flags, self.T)
+        if textures is not None:
+            table = np.ascontiguousarray(textures[0], np.int32).reshape(-1)
+            texels = np.ascontiguousarray(textures[1], np.uint32).reshape(-1)
+            self._tex = (table, texels)
+            lib().orc_scene_set_textures(self._h, texels, texels.size, table, table.size // 3)
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -141,6 +152,17 @@ def gen_rays(omm, spp, pose12, draws):
     dirs = np.zeros((N * spp, 3), np.float32)
     lib().orc_gen_rays(omm, N, spp, _f32(pose12).reshape(-1), _f32(draws).reshape(-1), org, dirs)
     return org, dirs
+
+
+def sample_texture(texels, width, height, uv):
+    """Bilinear lookups of one RGBA8 texture (uint32 texels, red in the low
+    byte) at (n, 2) coordinates: (n, 4) float32."""
+    texels = np.ascontiguousarray(texels, np.uint32).reshape(-1)
+    assert texels.size == width * height
+    uv = _f32(uv).reshape(-1, 2)
+    out = np.zeros((len(uv), 4), np.float32)
+    lib().orc_sample_texture(texels, int(width), int(height), uv.reshape(-1), len(uv), out)
+    return out
 
 
 def make_color(sums):

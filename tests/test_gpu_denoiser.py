@@ -35,25 +35,65 @@ def test_gradients_match_reference(lib, rows):
         assert rel < 2e-2, "%s gradient relative error %.3g" % (name, rel)
 
 
-def test_training_beats_the_plain_low_sample_render(lib, tmp_path):
-    info = scenes.small_scene(str(tmp_path), n_omm=400)
+def test_fused_inference_matches_layer_path(lib, tmp_path):
+    """The learned render's fused feature + network kernel against the
+    feature rows and the layer-by-layer GEMM path (bit for bit), and against
+    the numpy forward pass (float64 accumulation)."""
+    info = scenes.terrain_scene(str(tmp_path), cells=64, extent=40.0, cones=50, n_omm=700, poses=4)
     lib.loadGlTFscene(info["gltf"].encode())
     assert eh.lastError(lib) == ""
     eh.gotoFirstCompoundEye(lib)
+    n = lib.getCurrentEyeOmmatidialCount()
+    rng = np.random.default_rng(2)
+    poses = scenes.random_poses(info["height_fn"], 3, rng, 10.0)
+    assert lib.crDenoiserInit(4) == 0
+    assert lib.crDenoiserAddTrainingPoses(poses, 3, 8, 64) == 0, eh.lastError(lib)
+    assert lib.crDenoiserTrain(50, 512, 1e-3, 1, None) == 0, eh.lastError(lib)
+    rows = 3 * n
+    X = np.zeros((rows, mlp_ref.FEAT), np.uint16)
+    base = np.zeros((rows, 3), np.float32)
+    # Reload to restart the feature streams before each of the two renders.
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    assert lib.crDenoiserFeatureRows(poses, 3, 8, X, base) == 0, eh.lastError(lib)
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    fused = np.zeros((3, n, 3), np.float32)
+    assert lib.crDenoiserRenderPoses(poses, 3, 8, fused) == 0, eh.lastError(lib)
+    layered = np.zeros((rows, 3), np.float32)
+    assert lib.crDenoiserPredictRows(X, base, rows, layered) == 0, eh.lastError(lib)
+    assert np.array_equal(fused.reshape(-1, 3).view(np.uint32), layered.view(np.uint32))
+    assert (X[:, 105:] == 0).all()
+    params = np.zeros(mlp_ref.N_PARAMS, np.float32)
+    grads = np.zeros(mlp_ref.N_PARAMS, np.float32)
+    assert lib.crDenoiserGradient(X[:64].copy(), base[:64].copy(), base[:64].copy(), 64, grads, params) >= 0
+    want = mlp_ref.predict(params, mlp_ref.from_bits(X), base)
+    # fp32 sums on the GPU against float64 here: bf16 roundings of hidden
+    # activations may land one step apart, so compare against the size of
+    # the correction itself.
+    scale = np.abs(want - base).max() + 1e-6
+    err = np.abs(layered - want)
+    assert err.max() <= 0.05 * scale and err.mean() <= 0.005 * scale, (err.max(), err.mean(), scale)
+
+
+def test_training_beats_the_plain_low_sample_render(lib, tmp_path):
+    # A terrain with an eye whose acceptance cones overlap their neighbours'
+    # (droplet eye, 1500 ommatidia, 1.5-4 deg), as in the denoiser workload.
+    info = scenes.terrain_scene(str(tmp_path), cells=128, extent=60.0, cones=300, n_omm=1500, poses=8)
+    lib.loadGlTFscene(info["gltf"].encode())
+    assert eh.lastError(lib) == ""
+    eh.gotoFirstCompoundEye(lib)
+    n = lib.getCurrentEyeOmmatidialCount()
     rng = np.random.default_rng(5)
-
-    def poses(k):
-        return np.stack([scenes.pose_rows(np.array([rng.uniform(-6, 6), 0.5, rng.uniform(-6, 6)]),
-                                          rng.uniform(0, 2 * np.pi)) for _ in range(k)])
-
-    train, held = poses(40), poses(6)
+    train = scenes.random_poses(info["height_fn"], 300, rng, 20.0)
+    held = scenes.random_poses(info["height_fn"], 6, rng, 20.0)
     assert lib.crDenoiserInit(1) == 0
     assert lib.crDenoiserAddTrainingPoses(train, len(train), 8, 256) == 0, eh.lastError(lib)
-    assert lib.crDenoiserTrainingRows() == 40 * 400
-    loss = np.zeros(600, np.float32)
-    assert lib.crDenoiserTrain(600, 1024, 2e-3, 3, loss.ctypes.data) == 0, eh.lastError(lib)
+    assert lib.crDenoiserTrainingRows() == len(train) * n
+    loss = np.zeros(2000, np.float32)
+    assert lib.crDenoiserTrain(2000, 4096, 1e-3, 3, loss.ctypes.data) == 0, eh.lastError(lib)
     assert loss[-50:].mean() < 0.5 * loss[:20].mean()
-    learned = np.zeros((6, 400, 3), np.float32)
+    learned = np.zeros((6, n, 3), np.float32)
     assert lib.crDenoiserRenderPoses(held, 6, 8, learned) == 0, eh.lastError(lib)
     # plain renders of the held-out poses: 8 samples, and 1024 as the reference
     lib.setCurrentEyeSamplesPerOmmatidium(8)

@@ -157,6 +157,40 @@ def test_batched_poses_equal_sequential_frames(lib, small):
     assert np.array_equal(batch, np.stack(seq))
 
 
+@pytest.mark.parametrize("spp,prior", [(8, 0), (8, 3), (4, 1), (32, 2)])
+def test_spread_poses_equal_sequential_frames(lib, small, spp, prior):
+    """Small eyes render their poses from random numbers drawn up front and
+    spread over many warps: after `prior` frames (an odd count leaves a
+    cached Box-Muller normal in every state) a 40-pose launch equals 40
+    renderFrame calls, bit for bit, and leaves the same generator states."""
+    _load(lib, small["gltf"], spp)
+    rng = np.random.default_rng(spp + prior)
+    poses = np.stack([scenes.pose_rows(np.array([rng.uniform(-2, 2), rng.uniform(0.3, 1.2), rng.uniform(-2, 2)]),
+                                       rng.uniform(0, 6.28)) for _ in range(40)])
+    n = lib.getCurrentEyeOmmatidialCount()
+    states = np.zeros(8 * n * spp, np.uint32)
+
+    def frames(ps):
+        out = []
+        for p in ps:
+            lib.setCameraPosition(*[float(v) for v in p[:3]])
+            lib.setCameraLocalSpace(*[float(v) for v in p[3:]])
+            assert lib.renderFrame() >= 0
+            out.append(eh.getOmmatidialColours(lib))
+        return np.stack(out) if out else None
+
+    frames(poses[:prior])
+    seq = frames(poses)
+    assert lib.crGetRandomStates(states) == 0
+    seq_states = states.copy()
+    lib.setCurrentEyeSamplesPerOmmatidium(spp)  # resets the random streams
+    frames(poses[:prior])
+    batch = eh.renderPoses(lib, poses)
+    assert lib.crGetRandomStates(states) == 0
+    assert np.array_equal(batch, seq)
+    assert np.array_equal(states, seq_states)
+
+
 def test_random_stream_ids_and_persistence(lib, small):
     """Stream id = sample * N + ommatidium (shaders.cu:669, 684); states
     persist across frames and reset on a sample-count change."""
