@@ -518,6 +518,49 @@ def textured_scene(outdir, seed=SEED, n_omm=1000, spp=32):
     return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm, "images": images}
 
 
+def fixture_scene(npz, variant, outdir):
+    """Rebuilds a flattened fixture scene (tests/golden/reference_test_scene.npz
+    layout) as glTF + .eye files: one mesh per material colour (shading kind
+    0) and one vertex-coloured mesh (kind 1), world-space vertices, and each
+    compound camera at its stored pose through a node matrix whose columns
+    are the local x, y and -z axes.  Returns the glTF path."""
+    os.makedirs(outdir, exist_ok=True)
+    z = np.load(npz) if isinstance(npz, str) else npz
+    v = z[variant + "__verts"]
+    c = z[variant + "__colours"]
+    f = z[variant + "__flags"]
+    g = GltfBuilder()
+    g.scene_extras = {"background-shader": "simple_sky" if int(z[variant + "__miss"]) == 1 else "default_background"}
+    flat = f == 0
+    if flat.any():
+        keys = c[flat][:, 0, :]
+        uniq, inv = np.unique(keys, axis=0, return_inverse=True)
+        tri_idx = np.where(flat)[0]
+        for m, col in enumerate(uniq):
+            sel = tri_idx[inv.reshape(-1) == m]
+            pos = v[sel].reshape(-1, 3).astype(np.float64)
+            g.mesh("flat%d" % m, pos, np.arange(len(pos)).reshape(-1, 3), material=g.material(col), index_type=5125)
+    if (f == 1).any():
+        sel = np.where(f == 1)[0]
+        pos = v[sel].reshape(-1, 3).astype(np.float64)
+        g.mesh("coloured", pos, np.arange(len(pos)).reshape(-1, 3), colours=c[sel].reshape(-1, 4), index_type=5125)
+    for k, name in enumerate(z[variant + "__cams"]):
+        key = "%s__cam%d" % (variant, k)
+        pose = z[key + "__pose"].astype(np.float64)
+        omm = z[key + "__omm"]
+        eye = os.path.join(outdir, "%s_cam%d.eye" % (variant, k))
+        write_eye(eye, omm[:, :3], omm[:, 3:6], omm[:, 6], omm[:, 7])
+        ls = pose[3:].reshape(3, 3)
+        cols = [ls[0], ls[1], -ls[2], pose[:3]]
+        matrix = [float(cols[j][i]) if i < 3 else (1.0 if j == 3 else 0.0) for j in range(4) for i in range(4)]
+        g.cameras.append({"name": str(name), "type": "perspective",
+                          "perspective": {"yfov": 0.4, "znear": 0.1, "zfar": 100.0},
+                          "extras": {"compound-eye": "true", "compound-structure": os.path.basename(eye),
+                                     "compound-projection": str(z[key + "__projection"])}})
+        g.nodes.append({"name": str(name), "camera": len(g.cameras) - 1, "matrix": matrix})
+    return g.write(os.path.join(outdir, variant + ".gltf"), embed=True)
+
+
 def terrain_height_fn(heights, extent):
     """Bilinear lookup in the heightfield vertex grid (heights[i, j] at
     x = -extent/2 + i*dx, z = -extent/2 + j*dz)."""
