@@ -61,6 +61,21 @@ def workload(poses):
     return info
 
 
+# From an ncu capture of renderKernel on one 256-pose launch of this workload
+# (variant 2): DRAM bytes read + written, and warp instructions per ray.
+RENDER_DRAM_BYTES_PER_LAUNCH = 54536704 + 187921408
+RENDER_WARP_INSTR_PER_RAY = 23060962816 / (256 * 6000 * 256)
+SM_COUNT = 152
+
+
+def sm_max_mhz():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        return 2070.0
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -349,6 +364,12 @@ def run_ours(args):
     launch_s = statistics.mean(full) / 1000.0
     achieved = per_ray * launch_n * N * spp / launch_s / 1e9
     peak, src = peaks()
+    # Issue-rate roofline: warp instructions per ray from an ncu capture of
+    # this kernel on this launch (smsp__inst_executed.sum / rays), against 4
+    # schedulers x 1 instruction per cycle on every SM at the maximum clock.
+    issue_per_ray = RENDER_WARP_INSTR_PER_RAY
+    issue_peak = 4.0 * SM_COUNT * sm_max_mhz() * 1e6
+    issue_achieved = issue_per_ray * launch_n * N * spp / launch_s
     clk = clocks.summary()
     line = {
         "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -363,7 +384,13 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},
         "gpu_launches": args.steps * len(chunks) * (2 if spp > 32 else 1),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": src,
+                     "traffic": RENDER_DRAM_BYTES_PER_LAUNCH if launch_n == POSES_PER_LAUNCH else None,
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one 256-pose launch (ncu); "
+                                     "the per-ray demand bytes above are served from L1/L2",
+                     "peak_source": src,
+                     "issue": {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
+                               "frac": issue_achieved / issue_peak, "instr_per_ray": issue_per_ray,
+                               "note": "the limiter: smsp__inst_executed.sum per ray from ncu x live rays/s"},
                      "bytes_per_ray": per_ray, "node_visits_per_ray": nodes.value, "tri_tests_per_ray": tris.value,
                      "hit_fraction": hit_frac, "launch_ms": statistics.mean(full),
                      "kernel": "renderKernel<0> (+ combineChunksKernel)"},
