@@ -47,6 +47,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-eye batching measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurement")
+    ap.add_argument("--no-adaptive", action="store_true", help="skip the sample-allocator measurement")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
@@ -348,6 +349,7 @@ def run_ours(args):
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
     learned = None if args.no_learned else run_learned(lib, eh, args, stream)
+    adaptive = None if args.no_adaptive else run_adaptive(lib, eh, args, stream)
 
     if rank != 0:
         if world > 1:
@@ -403,6 +405,8 @@ def run_ours(args):
         line["batch_uneven"] = batch
     if learned:
         line["learned_denoiser"] = learned
+    if adaptive:
+        line["learned_allocator"] = adaptive
     if not args.no_cpu_baseline:
         cb = cpu_baseline(info, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -565,6 +569,117 @@ def run_learned(lib, eh, args, stream, train_poses=1000, held_poses=1000, steps=
             "eye_frames_per_s_plain_1024": held_poses / (ms_1024 / 1000.0),
             "speedup_vs_plain_at_matched_rmse": (ms_matched / ms_learned) if ms_matched else None,
             "speedup_vs_plain_1024": ms_1024 / ms_learned}
+
+
+def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_steps=3000, den_steps=3000,
+                 batch=8192, threshold=1.0 / 512.0, seeds=8):
+    """Learned sample allocator plus denoiser at scale: a 2048 x 2048-cell
+    heightfield over 400 m with 20,000 cone plants (9.03 M triangles, GPU
+    linear BVH) and a 100,000-ommatidium panoramic eye (Fibonacci sphere,
+    acceptance U(0.5, 5) deg).  The allocator is trained on minimum-sample
+    labels (smallest count in 4..1024 whose colour standard deviation across
+    8 seeds is below 1/512) of `train_poses` random poses, the denoiser on the
+    same poses (8-sample features, 1024-sample targets); on `held_poses`
+    held-out random poses the adaptive learned render is compared with the
+    plain 1024-sample render: RMSE, rays and time (CUDA events)."""
+    import ctypes
+
+    import torch
+
+    import scenes
+
+    d = os.path.join(tempfile.gettempdir(), "cr_bench_large_%d" % scenes.SEED)
+    t0 = time.perf_counter()
+    info = scenes.terrain_scene(d, cells=2048, extent=400.0, cones=20000, n_omm=100000, poses=4,
+                                eye_kind="panoramic", aa_deg=(0.5, 5.0))
+    t_scene = time.perf_counter() - t0
+    lib.crSetStream(stream.cuda_stream)
+    lib.crSetBvhBuilder(1)
+    t0 = time.perf_counter()
+    lib.loadGlTFscene(info["gltf"].encode())
+    err = eh.lastError(lib)
+    if err:
+        raise RuntimeError(err)
+    eh.gotoFirstCompoundEye(lib)
+    N = lib.getCurrentEyeOmmatidialCount()
+    t_load = time.perf_counter() - t0
+    rng = np.random.default_rng(scenes.SEED + 21)
+    train = scenes.random_poses(info["height_fn"], train_poses, rng, 150.0)
+    held = scenes.random_poses(info["height_fn"], held_poses, rng, 150.0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    p16 = np.zeros((held_poses, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
+    d_poses = torch.from_numpy(p16).to(dev)
+    d_out = torch.empty((held_poses, N, 3), dtype=torch.float32, device=dev)
+    d_lev = torch.empty((held_poses, N), dtype=torch.uint8, device=dev)
+
+    t0 = time.perf_counter()
+    if lib.crAllocatorInit(3) != 0 or lib.crDenoiserInit(4) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    labels = np.zeros((train_poses, N), np.uint16)
+    for k in range(0, train_poses, 4):
+        lab = np.zeros((4, N), np.uint16)
+        if lib.crAllocatorAddTrainingPoses(train[k:k + 4], 4, 8, threshold, seeds, lab.ctypes.data) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        labels[k:k + 4] = lab
+    if lib.crDenoiserAddTrainingPoses(train, train_poses, 8, 1024) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if lib.crAllocatorTrain(alloc_steps, batch, 1e-3, 5, None) != 0 or \
+            lib.crDenoiserTrain(den_steps, batch, 1e-3, 6, None) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    rays = ctypes.c_double(0.0)
+
+    def adaptive():
+        if lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), held_poses, 8, d_out.data_ptr(), d_lev.data_ptr(),
+                                           ctypes.byref(rays)) != 0:
+            raise RuntimeError(eh.lastError(lib))
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    ms_adaptive = timed(adaptive)
+    img = d_out.cpu().numpy()
+    lev = d_lev.cpu().numpy()
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+
+    def plain():
+        if lib.crRenderPosesDevice(d_poses.data_ptr(), held_poses, d_out.data_ptr()) != 0:
+            raise RuntimeError(eh.lastError(lib))
+
+    ms_plain = timed(plain, reps=1)
+    ref = d_out.cpu().numpy()
+    rmse = float(np.sqrt(((img - ref) ** 2).mean()))
+    lib.crSetBvhBuilder(0)
+    rays_plain = float(held_poses) * N * 1024
+    lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
+    return {"scene": "heightfield 2048^2 cells + 20000 cones (%d tris, GPU LBVH), %d-ommatidium panoramic eye, "
+                     "acceptance 0.5-5 deg" % (info["triangles"], N),
+            "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
+            "label_histogram": lab_hist, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
+            "train_s": t_train, "rmse_vs_plain_1024": rmse, "target_rmse": 1.0 / 255.0,
+            "meets_target": rmse <= 1.0 / 255.0,
+            "rays_adaptive": rays.value, "rays_plain_1024": rays_plain, "ray_fraction": rays.value / rays_plain,
+            "fraction_feature_only": float((lev == 0xFF).mean()), "fraction_fallback_1024": float((lev == 0x88).mean()),
+            "ms_adaptive": ms_adaptive, "ms_plain_1024": ms_plain,
+            "eye_frames_per_s_adaptive": held_poses / (ms_adaptive / 1000.0),
+            "eye_frames_per_s_plain_1024": held_poses / (ms_plain / 1000.0),
+            "speedup_vs_plain_1024": ms_plain / ms_adaptive}
 
 
 def ctypes_double():

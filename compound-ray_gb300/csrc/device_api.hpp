@@ -159,9 +159,10 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
                              float* base, cudaStream_t stream);
 // Fused prediction for P poses of an N-ommatidium eye straight from the
 // feature-render statistics: out (P x N x 3) = own mean colour + network
-// output, bit-identical to assembleFeatures + the layer-by-layer forward.
+// output (or the network output alone when !residual), bit-identical to
+// assembleFeatures + the layer-by-layer forward.
 cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
-                          const MlpWeights& w, float* out, cudaStream_t stream);
+                          const MlpWeights& w, float* out, cudaStream_t stream, bool residual = true);
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
                        float* baseo, float* targeto, cudaStream_t stream);
 
@@ -203,6 +204,66 @@ cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsig
                         const unsigned long long* cellBase, uint32_t nEyes, unsigned long long totalTasks,
                         unsigned long long totalCells, unsigned long long* ctrl, uint32_t* errFlag, int variant,
                         int gridBlocks, cudaStream_t stream);
+
+// Adaptive sampling (render.cu).  An entry e = pose * N + ommatidium is
+// rendered at its bucket's sample count; buckets hold counts 4 << index.
+constexpr uint32_t kAdaptiveBuckets = 9;  // 4, 8, ..., 1024
+constexpr uint8_t kNoRender = 0xFF;        // level of an entry the feature render covers
+#ifdef __CUDACC__
+#define CR_HOST_DEVICE __host__ __device__
+#else
+#define CR_HOST_DEVICE
+#endif
+// Samples each lane traces per task (up to 8, for counts above 32) and warp
+// tasks per entry of a bucket with `spp` samples (a power of two).
+CR_HOST_DEVICE inline uint32_t adaptiveSamplesPerLane(uint32_t spp) {
+  return spp <= 32 ? 1u : (spp / 32 < 8 ? spp / 32 : 8u);
+}
+CR_HOST_DEVICE inline uint32_t adaptiveChunks(uint32_t spp) {
+  return spp <= 32 ? 1u : spp / (32u * adaptiveSamplesPerLane(spp));
+}
+struct AdaptiveBucket {
+  const uint32_t* entries = nullptr;  // count entry ids
+  uint64_t count = 0;
+  uint32_t spp = 0;
+  float* partials = nullptr;  // adaptivePartialFloats(count, spp) floats when spp > 32
+  uint64_t taskBase = 0;      // first warp task of the bucket
+};
+struct AdaptiveLaunch {
+  AdaptiveBucket b[kAdaptiveBuckets];
+  uint32_t nBuckets = 0;
+  uint64_t totalTasks = 0;
+};
+// Table of the non-empty buckets among nBuckets (entries, counts, spp and
+// partial buffers per bucket) with their warp-task offsets.
+AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* counts, const uint32_t* spp,
+                            float* const* partials, uint32_t nBuckets);
+size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
+// One launch over every bucket: sums[3e..3e+2] = mean sample colour of entry
+// e, samples drawn from the Philox4x32-10 stream (seed, e * 1024 + s).  rec:
+// null, or count x spp records of a single-bucket launch (tests).
+cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
+                           const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
+                           RayRecord* rec, cudaStream_t stream);
+// Minimum-sample labels: entries with label 0 get `spp` when the standard
+// deviation across the k renders outs[k][rows][3] is below thr in every channel.
+cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, float thr, uint16_t* label,
+                         cudaStream_t stream);
+// Per-entry bucket level from the allocator's prediction (rows x 3) and the
+// bucket sizes (counts: kAdaptiveBuckets words, zeroed by the caller).
+cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
+                           unsigned long long* counts, cudaStream_t stream);
+// Entry lists of rows = P x N entries, pose by pose and within a pose in the
+// eye's `order` (null: index order): bucket k's entries go to
+// entries[bucketBase[k]...] (bucketBase: device, kAdaptiveBuckets words);
+// scratch: scatterScratchWords(rows) words.
+size_t scatterScratchWords(uint64_t rows);
+cudaError_t launchScatterBuckets(const uint8_t* level, uint64_t rows, uint32_t N, const uint32_t* order,
+                                 const unsigned long long* bucketBase, unsigned long long* scratch, uint32_t* entries,
+                                 cudaStream_t stream);
+// Final colours of an adaptive render (see render.cu).
+cudaError_t launchAdaptiveFinish(const uint8_t* level, uint64_t rows, uint32_t featureSpp, const float* stats,
+                                 const float* learned, const float* sums, float* out, cudaStream_t stream);
 
 // Fixed device array used as render scratch by the allocation-free entry
 // point: its capacity in floats, and its address on the current device

@@ -1243,6 +1243,17 @@ struct DenoiseState {
   DevBuf<float> stats, base, out, scratch;
   DevBuf<uint16_t> X;
   DevBuf<float4> poses;
+  // Sample-count allocator: a second network of the same shape, trained on
+  // minimum-sample labels; and the adaptive render's buffers.
+  Denoiser alloc;
+  uint64_t adaptiveFrame = 0;  // frames rendered adaptively since the eye was bound (Philox seed offset)
+  DevBuf<float> pred, learned, sums, partials, labelOuts;
+  DevBuf<uint32_t> entries;
+  DevBuf<uint8_t> level;
+  DevBuf<uint16_t> labels;
+  DevBuf<unsigned long long> counts, tileScratch;
+  std::vector<uint16_t> lastLabels;
+  double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
 };
 
 DenoiseState& DS() {
@@ -1263,6 +1274,7 @@ EyeDev& denoiseEye(Renderer& r, DenoiseState& d) {
     check(nearestOmmatidia(e.omm.ptr, e.N, d.nb.ptr, r.stream()), "neighbour search");
     d.featReady = d.targetReady = false;
     d.featSpp = d.targetSpp = 0;
+    d.adaptiveFrame = 0;
   }
   return e;
 }
@@ -1335,6 +1347,8 @@ int crDenoiserInit(int seed) {
 }
 
 size_t crDenoiserParamCount(void) { return Denoiser::kParams; }
+
+void crDenoiserRelease(void) { DS().net.release(); }
 
 int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSpp, int targetSpp) {
   return guarded(
@@ -1512,6 +1526,243 @@ int crDenoiserLoad(const char* path) {
       [&]() -> int {
         if (!path) throw std::runtime_error("null path");
         DS().net.load(path, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+// ---- Learned sample allocator and adaptive rendering ----------------------
+
+int crAllocatorInit(int seed) {
+  return guarded(
+      "crAllocatorInit",
+      [&]() -> int {
+        DS().alloc.init(static_cast<uint32_t>(seed), R().stream());
+        return 0;
+      },
+      -1);
+}
+
+int crAllocatorAddTrainingPoses(const float* poses12, size_t count, int featureSpp, float threshold, int seeds,
+                                uint16_t* labelsOut) {
+  return guarded(
+      "crAllocatorAddTrainingPoses",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.alloc.ready()) throw std::runtime_error("call crAllocatorInit first");
+        if (!poses12 || count == 0) throw std::runtime_error("no poses");
+        if (seeds < 2 || seeds > 64) throw std::runtime_error("the label search needs 2 to 64 seeds");
+        if (!(threshold > 0.f)) throw std::runtime_error("threshold must be positive");
+        if (count > kMaxPosesPerLaunch) throw std::runtime_error("at most 256 poses per call");
+        EyeDev& e = denoiseEye(r, d);
+        cudaStream_t st = r.stream();
+        uploadPoses12(d.poses, poses12, count, st);
+        denoiseFeatures(r, d, e, d.poses.ptr, count, static_cast<uint32_t>(featureSpp));
+        const uint64_t rows = static_cast<uint64_t>(count) * e.N;
+        // Minimum-sample search: every entry rendered `seeds` times (independent
+        // streams) at 4, 8, ..., 1024 samples; the label is the first count at
+        // which the colour's standard deviation across the renders falls below
+        // the threshold in every channel (0 = none up to 1024).  Entries are
+        // listed pose by pose in the eye's direction order, for coherent warps.
+        const std::vector<uint32_t> ord = directionOrder(r.scene.cameras[r.current].omm);
+        std::vector<uint32_t> iota(rows);
+        for (uint64_t i = 0; i < rows; ++i)
+          iota[i] = static_cast<uint32_t>((i / e.N) * e.N + ord[static_cast<size_t>(i % e.N)]);
+        d.entries.ensure(rows);
+        check(cudaMemcpyAsync(d.entries.ptr, iota.data(), rows * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+        d.labels.ensure(rows);
+        check(cudaMemsetAsync(d.labels.ptr, 0, rows * 2, st), "cudaMemset");
+        d.labelOuts.ensure(static_cast<size_t>(seeds) * rows * 3);
+        d.partials.ensure(std::max<size_t>(1, adaptivePartialFloats(rows, 1024)));
+        for (uint32_t c = 4; c <= 1024; c *= 2) {
+          const uint32_t* ent = d.entries.ptr;
+          float* part = d.partials.ptr;
+          const AdaptiveLaunch L = planAdaptive(&ent, &rows, &c, &part, 1);
+          for (int k = 0; k < seeds; ++k)
+            check(launchAdaptive(r.dev, e.omm.ptr, e.N, d.poses.ptr, L, 0x5eed0000ull + static_cast<uint64_t>(k),
+                                 d.labelOuts.ptr + static_cast<size_t>(k) * rows * 3, r.errWord(), nullptr, st),
+                  "label render");
+          check(launchLabels(d.labelOuts.ptr, seeds, rows, c, threshold, d.labels.ptr, st), "labels");
+        }
+        d.lastLabels.assign(rows, 0);
+        check(cudaMemcpyAsync(d.lastLabels.data(), d.labels.ptr, rows * 2, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+        r.checkErrWord();
+        // Targets: log2(label) / 10 in all three outputs (label 0 -> 2048).
+        std::vector<float> target(rows * 3);
+        for (uint64_t i = 0; i < rows; ++i) {
+          const uint32_t lab = d.lastLabels[i] ? d.lastLabels[i] : 2048u;
+          const float l = std::log2(static_cast<float>(lab)) / 10.0f;
+          target[3 * i] = target[3 * i + 1] = target[3 * i + 2] = l;
+        }
+        DevBuf<float> t, zero;
+        t.ensure(rows * 3);
+        zero.ensure(rows * 3);
+        check(cudaMemcpyAsync(t.ptr, target.data(), rows * 12, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+        check(cudaMemsetAsync(zero.ptr, 0, rows * 12, st), "cudaMemset");
+        d.alloc.addRows(d.X.ptr, zero.ptr, t.ptr, rows, st);
+        check(cudaStreamSynchronize(st), "allocator rows");
+        if (labelsOut) std::memcpy(labelsOut, d.lastLabels.data(), rows * 2);
+        return 0;
+      },
+      -1);
+}
+
+int crAllocatorTrain(int steps, int batch, float lr, int seed, float* lossHistory) {
+  return guarded(
+      "crAllocatorTrain",
+      [&]() -> int {
+        DS().alloc.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+size_t crAllocatorTrainingRows(void) { return DS().alloc.rows(); }
+
+int crAllocatorSave(const char* path) {
+  return guarded(
+      "crAllocatorSave",
+      [&]() -> int {
+        if (!path) throw std::runtime_error("null path");
+        DS().alloc.save(path, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+int crAllocatorLoad(const char* path) {
+  return guarded(
+      "crAllocatorLoad",
+      [&]() -> int {
+        if (!path) throw std::runtime_error("null path");
+        DS().alloc.load(path, R().stream());
+        return 0;
+      },
+      -1);
+}
+
+int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out, uint8_t* d_level,
+                                double* raysTraced) {
+  return guarded(
+      "crAdaptiveRenderPosesDevice",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!d.alloc.ready()) throw std::runtime_error("call crAllocatorInit (and train) or crAllocatorLoad first");
+        if (count == 0) return 0;
+        if (!d_poses || !d_out) throw std::runtime_error("null pointer");
+        EyeDev& e = denoiseEye(r, d);
+        cudaStream_t st = r.stream();
+        const float4* poses = reinterpret_cast<const float4*>(d_poses);
+        const uint32_t fs = static_cast<uint32_t>(featureSpp);
+        double rays = 0;
+        for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
+          const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+          const uint64_t rows = static_cast<uint64_t>(P) * e.N;
+          denoiseFeatures(r, d, e, poses + 4 * first, P, fs, false);
+          rays += static_cast<double>(rows) * fs;
+          d.pred.ensure(rows * 3);
+          check(inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, d.alloc.weights(), d.pred.ptr, st, false),
+                "allocator inference");
+          const float* learned = nullptr;
+          if (d.net.ready()) {
+            d.learned.ensure(rows * 3);
+            check(inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d.learned.ptr, st),
+                  "denoiser inference");
+            learned = d.learned.ptr;
+          }
+          d.level.ensure(rows);
+          d.counts.ensure(kAdaptiveBuckets);
+          check(cudaMemsetAsync(d.counts.ptr, 0, kAdaptiveBuckets * 8, st), "cudaMemset");
+          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st), "allocation");
+          unsigned long long cnt[kAdaptiveBuckets];
+          check(cudaMemcpyAsync(cnt, d.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+          check(cudaStreamSynchronize(st), "allocation");
+          unsigned long long off[kAdaptiveBuckets];
+          uint64_t total = 0, partialFloats = 0;
+          for (uint32_t k = 0; k < kAdaptiveBuckets; ++k) {
+            off[k] = total;
+            total += cnt[k];
+            partialFloats += adaptivePartialFloats(cnt[k], 4u << k);
+            rays += static_cast<double>(cnt[k]) * static_cast<double>(4u << k);
+          }
+          d.sums.ensure(rows * 3);
+          if (total) {
+            d.entries.ensure(total);
+            d.partials.ensure(std::max<uint64_t>(1, partialFloats));
+            check(cudaMemcpyAsync(d.counts.ptr, off, sizeof(off), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+            d.tileScratch.ensure(scatterScratchWords(rows));
+            check(launchScatterBuckets(d.level.ptr, rows, e.N, e.order.ptr, d.counts.ptr, d.tileScratch.ptr,
+                                       d.entries.ptr, st),
+                  "bucket lists");
+            const uint32_t* ent[kAdaptiveBuckets];
+            uint64_t n[kAdaptiveBuckets];
+            uint32_t spp[kAdaptiveBuckets];
+            float* part[kAdaptiveBuckets];
+            uint64_t pf = 0;
+            for (uint32_t k = 0; k < kAdaptiveBuckets; ++k) {
+              ent[k] = d.entries.ptr + off[k];
+              n[k] = cnt[k];
+              spp[k] = 4u << k;
+              part[k] = d.partials.ptr + pf;
+              pf += adaptivePartialFloats(cnt[k], spp[k]);
+            }
+            const AdaptiveLaunch L = planAdaptive(ent, n, spp, part, kAdaptiveBuckets);
+            check(launchAdaptive(r.dev, e.omm.ptr, e.N, poses + 4 * first, L, 0xada90000ull + d.adaptiveFrame,
+                                 d.sums.ptr, r.errWord(), nullptr, st),
+                  "adaptive render");
+          }
+          check(launchAdaptiveFinish(d.level.ptr, rows, fs, d.stats.ptr, learned, d.sums.ptr, d_out + 3 * first * e.N,
+                                     st),
+                "adaptive finish");
+          if (d_level)
+            check(cudaMemcpyAsync(d_level + first * e.N, d.level.ptr, rows, cudaMemcpyDeviceToDevice, st),
+                  "cudaMemcpy");
+          d.adaptiveFrame += P;
+        }
+        d.lastRays = rays;
+        if (raysTraced) *raysTraced = rays;
+        return 0;
+      },
+      -1);
+}
+
+int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long long seed, void* records,
+                     float* sums) {
+  return guarded(
+      "crAdaptiveRecord",
+      [&]() -> int {
+        Renderer& r = R();
+        DenoiseState& d = DS();
+        if (!poses12 || !records || !sums) throw std::runtime_error("null pointer");
+        if (count == 0) return 0;
+        if (spp < 1 || spp > 1024 || (spp & (spp - 1))) throw std::runtime_error("spp must be a power of two <= 1024");
+        if (count > kMaxPosesPerLaunch) throw std::runtime_error("at most 256 poses per call");
+        EyeDev& e = denoiseEye(r, d);
+        cudaStream_t st = r.stream();
+        uploadPoses12(d.poses, poses12, count, st);
+        const uint64_t rows = static_cast<uint64_t>(count) * e.N;
+        std::vector<uint32_t> iota(rows);
+        for (uint64_t i = 0; i < rows; ++i) iota[i] = static_cast<uint32_t>(i);
+        DevBuf<uint32_t> ent;
+        DevBuf<float> part, s;
+        DevBuf<RayRecord> rec;
+        ent.ensure(rows);
+        s.ensure(rows * 3);
+        part.ensure(std::max<size_t>(1, adaptivePartialFloats(rows, static_cast<uint32_t>(spp))));
+        rec.ensure(rows * static_cast<uint64_t>(spp));
+        check(cudaMemcpyAsync(ent.ptr, iota.data(), rows * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+        const uint32_t* ep = ent.ptr;
+        float* pp = part.ptr;
+        const uint32_t c = static_cast<uint32_t>(spp);
+        const AdaptiveLaunch L = planAdaptive(&ep, &rows, &c, &pp, 1);
+        check(launchAdaptive(r.dev, e.omm.ptr, e.N, d.poses.ptr, L, seed, s.ptr, r.errWord(), rec.ptr, st),
+              "adaptive render");
+        check(cudaMemcpyAsync(records, rec.ptr, rows * spp * sizeof(RayRecord), cudaMemcpyDeviceToHost, st),
+              "cudaMemcpy");
+        check(cudaMemcpyAsync(sums, s.ptr, rows * 12, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+        r.checkErrWord();
         return 0;
       },
       -1);

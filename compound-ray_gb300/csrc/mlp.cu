@@ -71,15 +71,17 @@ __global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __n
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
   for (int k0 = 0; k0 < K; k0 += BK) {
+    // Tile loads walk the operand's contiguous dimension with consecutive
+    // threads (k for a row-major A / transposed B, m or n otherwise).
     for (int e = tid; e < BM * BK; e += 128) {
-      const int r = e / BK, c = e % BK;
+      const int r = aTrans ? e % BM : e / BK, c = aTrans ? e / BM : e % BK;
       const int m = m0 + r, k = k0 + c;
       __nv_bfloat16 v = zero;
       if (m < M && k < K) v = aTrans ? A[static_cast<size_t>(k) * lda + m] : A[static_cast<size_t>(m) * lda + k];
       As[r][c] = v;
     }
     for (int e = tid; e < BN * BK; e += 128) {
-      const int r = e / BK, c = e % BK;
+      const int r = bTrans ? e / BK : e % BN, c = bTrans ? e % BK : e / BN;
       const int n = n0 + r, k = k0 + c;
       __nv_bfloat16 v = zero;
       if (n < N && k < K) v = bTrans ? B[static_cast<size_t>(n) * ldb + k] : B[static_cast<size_t>(k) * ldb + n];
@@ -405,7 +407,7 @@ __device__ __forceinline__ void hiddenLayer(__nv_bfloat16* h, const __nv_bfloat1
 
 __global__ void __launch_bounds__(kInferThreads, 1)
     inferKernel(const float* __restrict__ stats, const float4* __restrict__ omm, const int* __restrict__ nb,
-                uint32_t N, uint64_t rows, MlpWeights w, float* __restrict__ out) {
+                uint32_t N, uint64_t rows, MlpWeights w, bool residual, float* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16* w1t = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* w2t = w1t + kMlpHidden * kS1;
@@ -470,7 +472,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       const uint64_t row = tile * kInferRows + warp * 16 + g + (r >= 2 ? 8 : 0);
       if (c < 3 && row < rows) {
         const float y = acc[r] + b4[c];
-        out[3 * row + c] = stats[row * kFeatureStats + c] + y;
+        out[3 * row + c] = residual ? stats[row * kFeatureStats + c] + y : y;
       }
     }
   }
@@ -559,7 +561,7 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
 }
 
 cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
-                          const MlpWeights& w, float* out, cudaStream_t stream) {
+                          const MlpWeights& w, float* out, cudaStream_t stream, bool residual) {
   const uint64_t rows = static_cast<uint64_t>(N) * P;
   if (rows == 0) return cudaSuccess;
   static int smCount = 0;
@@ -576,7 +578,7 @@ cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, 
   }
   const uint64_t tiles = (rows + kInferRows - 1) / kInferRows;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(tiles, static_cast<uint64_t>(smCount)));
-  inferKernel<<<grid, kInferThreads, kInferSmem, stream>>>(stats, omm, nb, N, rows, w, out);
+  inferKernel<<<grid, kInferThreads, kInferSmem, stream>>>(stats, omm, nb, N, rows, w, residual, out);
   return cudaGetLastError();
 }
 

@@ -1088,6 +1088,355 @@ cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, i
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Adaptive sampling: entries (pose, ommatidium) rendered at per-entry sample
+// counts, grouped into buckets of one power-of-two count each.
+// ---------------------------------------------------------------------------
+namespace {
+
+// One warp task of a bucket: up to 32 samples of one entry, or several whole
+// entries when the bucket's count is below 32 (the render kernel's plan).
+// Random numbers: Philox4x32-10 stream (seed, e * 1024 + s), one normal then
+// one uniform per sample (O(1) set-up per entry, unlike XORWOW's skip-ahead).
+__global__ void __launch_bounds__(128, 5)
+    adaptiveKernel(DevScene sc, const float4* __restrict__ omm, uint32_t N, const float4* __restrict__ poses,
+                   AdaptiveLaunch L, unsigned long long seed, float* __restrict__ sums, uint32_t* errFlag,
+                   RayRecord* __restrict__ rec) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // totalTasks < 2^31 (checked at launch)
+  if (task >= L.totalTasks) return;
+  uint32_t bi = 0;
+  while (bi + 1 < L.nBuckets && task >= L.b[bi + 1].taskBase) ++bi;
+  const AdaptiveBucket B = L.b[bi];
+  const uint32_t spp = B.spp;
+  const uint32_t segWidth = spp < 32u ? spp : 32u;
+  const uint32_t perWarp = 32u / segWidth;
+  const uint32_t spl = adaptiveSamplesPerLane(spp);
+  const uint32_t chunks = adaptiveChunks(spp);
+  const uint32_t t = task - static_cast<uint32_t>(B.taskBase);
+  const uint32_t group = t / chunks;
+  const uint32_t chunk = t - group * chunks;
+  const uint32_t i = group * perWarp + lane / segWidth;  // entry index within the bucket
+  const bool valid = i < B.count;
+  v3 col = mk(0.f, 0.f, 0.f);
+  uint32_t nodeVisits = 0, triTests = 0;
+  if (valid) {
+    const uint32_t e = B.entries[i];
+    const uint32_t p = e / N, o = e - p * N;
+    const float4 a = __ldg(omm + 2 * o), b = __ldg(omm + 2 * o + 1);
+    const v3 axis = mk(a.w, b.x, b.y);
+    const float fpo = b.w;
+    const float sd = b.z / FWHM_SD_RATIO;
+    v3 perp = cross(mk(0.0f, 1.0f, 0.0f), axis);
+    perp = (perp.x + perp.y + perp.z == 0.0f) ? mk(0.0f, 0.0f, 1.0f) : normalize(perp);
+    const v3 relPos = mk(a.x, a.y, a.z) - normalize(axis) * fpo;
+    const float4* pp = poses + 4 * p;
+    const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
+    const v3 org = mk(P0.x, P0.y, P0.z) + mk(X.x, X.y, X.z) * relPos.x + mk(Y.x, Y.y, Y.z) * relPos.y +
+                   mk(Z.x, Z.y, Z.z) * relPos.z;
+    const float invSpp = 1.0f / static_cast<float>(spp);
+    for (uint32_t j = 0; j < spl; ++j) {
+      const uint32_t s = chunk * 32u * spl + j * segWidth + lane % segWidth;
+      curandStatePhilox4_32_10_t st;
+      curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + s, 0ull, &st);
+      const float nd = curand_normal(&st);
+      const float ud = curand_uniform(&st);
+      const v3 splayed = rotatePoint(axis, nd * sd, perp);
+      const v3 rel = rotatePoint(splayed, ud * CR_PI_F, axis);
+      const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
+      const Ray ray = setupRay(org, dir, sc.extent);
+      Hit h;
+      traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+      v3 c;
+      float b1 = 0.f, b2 = 0.f;
+      if (h.id != 0xffffffffu) {
+        b1 = xdiv(h.V, h.det);
+        b2 = xdiv(h.W, h.det);
+        c = shadeHit(sc, h.pos, b1, b2);
+      } else {
+        c = shadeMiss(sc.miss, dir);
+      }
+      if (rec) {
+        RayRecord& R = rec[static_cast<size_t>(i) * spp + s];
+        R.normalDraw = nd;
+        R.uniformDraw = ud;
+        R.ox = org.x;
+        R.oy = org.y;
+        R.oz = org.z;
+        R.dx = dir.x;
+        R.dy = dir.y;
+        R.dz = dir.z;
+        R.t = h.id != 0xffffffffu ? h.t : -1.0f;
+        R.b1 = b1;
+        R.b2 = b2;
+        R.hitId = h.id != 0xffffffffu ? static_cast<int32_t>(h.id) : -1;
+        R.r = c.x;
+        R.g = c.y;
+        R.b = c.z;
+        R.pad = 0.f;
+      }
+      col = col + c * invSpp;
+    }
+  }
+  for (uint32_t m = segWidth >> 1; m >= 1u; m >>= 1) {
+    col.x += __shfl_xor_sync(0xffffffffu, col.x, static_cast<int>(m));
+    col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
+    col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
+  }
+  if ((lane % segWidth) == 0u && valid) {
+    float* dst = chunks == 1 ? sums + 3 * static_cast<size_t>(B.entries[i])
+                             : B.partials + (static_cast<size_t>(i) * chunks + chunk) * 3;
+    dst[0] = col.x;
+    dst[1] = col.y;
+    dst[2] = col.z;
+  }
+}
+
+// Chunk partials of one bucket summed in chunk order into the entries' sums.
+__global__ void adaptiveCombineKernel(AdaptiveBucket B, float* __restrict__ sums) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= B.count) return;
+  const uint32_t chunks = adaptiveChunks(B.spp);
+  const float* src = B.partials + i * chunks * 3;
+  float x = 0.f, y = 0.f, z = 0.f;
+  for (uint32_t c = 0; c < chunks; ++c) {
+    x += src[3 * c];
+    y += src[3 * c + 1];
+    z += src[3 * c + 2];
+  }
+  float* dst = sums + 3 * static_cast<size_t>(B.entries[i]);
+  dst[0] = x;
+  dst[1] = y;
+  dst[2] = z;
+}
+
+// Minimum-sample labels: for entries still unlabelled, the sample standard
+// deviation (n - 1) across the k renders of this sample count, per channel;
+// when every channel is below thr the entry's label becomes `spp`.
+__global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows, uint32_t spp, float thr,
+                            uint16_t* __restrict__ label) {
+  const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= rows || label[e] != 0) return;
+  float worst = 0.f;
+  for (int ch = 0; ch < 3; ++ch) {
+    float m = 0.f;
+    for (int j = 0; j < k; ++j) m += outs[(static_cast<size_t>(j) * rows + e) * 3 + ch];
+    m /= static_cast<float>(k);
+    float v = 0.f;
+    for (int j = 0; j < k; ++j) {
+      const float d = outs[(static_cast<size_t>(j) * rows + e) * 3 + ch] - m;
+      v += d * d;
+    }
+    worst = fmaxf(worst, sqrtf(v / static_cast<float>(k - 1)));
+  }
+  if (worst < thr) label[e] = static_cast<uint16_t>(spp);
+}
+
+// Bucket of every entry from the allocator's prediction l (mean of its three
+// outputs; the predicted count is 2^(10 l)): level = bucket index 0..8 of
+// 4 << index samples, 0x80 | 8 for a fallback entry (more than 1024 needed),
+// or kNoRender (at most featureSpp samples needed: the feature render suffices).
+__global__ void allocateKernel(const float* __restrict__ pred, uint64_t rows, uint32_t featureSpp,
+                               uint8_t* __restrict__ level, unsigned long long* __restrict__ counts) {
+  const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= rows) return;
+  const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
+  float kf = ceilf(l * 10.0f - 1e-3f);
+  if (!(kf >= 2.0f)) kf = 2.0f;  // also NaN
+  if (kf > 11.0f) kf = 11.0f;
+  const int k = static_cast<int>(kf);
+  uint8_t lv;
+  if ((1u << k) <= featureSpp) {
+    lv = kNoRender;
+  } else if (k == 11) {
+    lv = 0x80 | 8;
+  } else {
+    lv = static_cast<uint8_t>(k - 2);
+  }
+  level[e] = lv;
+  if (lv != kNoRender) atomicAdd(counts + (lv & 0x7f), 1ull);
+}
+
+// Ordered bucket lists in three steps, so that every bucket lists its
+// entries pose by pose and, within a pose, in the eye's direction order
+// (consecutive warps then trace neighbouring ommatidia of one pose):
+// per-block bucket counts over tiles of kScatterTile positions, an exclusive
+// scan over the tiles per bucket, and the placement with warp ballots.
+constexpr int kScatterTile = 1024;
+
+__device__ __forceinline__ int bucketOf(uint8_t lv) { return lv == kNoRender ? -1 : (lv & 0x7f); }
+
+// Entry at ordered position x (pose x / N, the (x % N)-th ommatidium of the order).
+__device__ __forceinline__ uint64_t entryAt(uint64_t x, uint32_t N, const uint32_t* __restrict__ order) {
+  const uint64_t p = x / N;
+  const uint32_t j = static_cast<uint32_t>(x % N);
+  return p * N + (order ? __ldg(order + j) : j);
+}
+
+__global__ void __launch_bounds__(kScatterTile) bucketCountKernel(const uint8_t* __restrict__ level, uint64_t rows,
+                                                                   uint32_t N, const uint32_t* __restrict__ order,
+                                                                   unsigned long long* __restrict__ tileCounts) {
+  __shared__ unsigned int cnt[kAdaptiveBuckets];
+  if (threadIdx.x < kAdaptiveBuckets) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t x = static_cast<uint64_t>(blockIdx.x) * kScatterTile + threadIdx.x;
+  const int k = x < rows ? bucketOf(level[entryAt(x, N, order)]) : -1;
+  if (k >= 0) atomicAdd(&cnt[k], 1u);
+  __syncthreads();
+  if (threadIdx.x < kAdaptiveBuckets)
+    tileCounts[static_cast<size_t>(blockIdx.x) * kAdaptiveBuckets + threadIdx.x] = cnt[threadIdx.x];
+}
+
+// One thread per bucket: tileCounts[t][k] becomes the first slot of tile t's
+// bucket-k entries (bucket k starting at bucketBase[k]).
+__global__ void bucketScanKernel(unsigned long long* __restrict__ tileCounts, uint64_t tiles,
+                                 const unsigned long long* __restrict__ bucketBase) {
+  const int k = threadIdx.x;
+  if (k >= static_cast<int>(kAdaptiveBuckets)) return;
+  unsigned long long run = bucketBase[k];
+  for (uint64_t t = 0; t < tiles; ++t) {
+    const unsigned long long c = tileCounts[t * kAdaptiveBuckets + k];
+    tileCounts[t * kAdaptiveBuckets + k] = run;
+    run += c;
+  }
+}
+
+__global__ void __launch_bounds__(kScatterTile) bucketPlaceKernel(const uint8_t* __restrict__ level, uint64_t rows,
+                                                                   uint32_t N, const uint32_t* __restrict__ order,
+                                                                   const unsigned long long* __restrict__ tileFirst,
+                                                                   uint32_t* __restrict__ entries) {
+  __shared__ unsigned int warpCnt[kScatterTile / 32][kAdaptiveBuckets];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t x = static_cast<uint64_t>(blockIdx.x) * kScatterTile + threadIdx.x;
+  const uint64_t e = x < rows ? entryAt(x, N, order) : 0;
+  const int k = x < rows ? bucketOf(level[e]) : -1;
+  unsigned int rank = 0;
+  for (int b = 0; b < static_cast<int>(kAdaptiveBuckets); ++b) {
+    const unsigned int m = __ballot_sync(0xffffffffu, k == b);
+    if (k == b) rank = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) warpCnt[warp][b] = __popc(m);
+  }
+  __syncthreads();
+  if (k < 0) return;
+  unsigned long long at = tileFirst[static_cast<size_t>(blockIdx.x) * kAdaptiveBuckets + k];
+  for (int w = 0; w < warp; ++w) at += warpCnt[w][k];
+  entries[at + rank] = static_cast<uint32_t>(e);
+}
+
+// Final colour of every entry: the denoised feature-render estimate where no
+// extra samples were needed; the sample-weighted mean of the feature render
+// and the adaptive render otherwise; the adaptive 1024-sample render alone
+// for fallback entries.
+__global__ void adaptiveFinishKernel(const uint8_t* __restrict__ level, uint64_t rows, uint32_t featureSpp,
+                                     const float* __restrict__ stats, const float* __restrict__ learned,
+                                     const float* __restrict__ sums, float* __restrict__ out) {
+  const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= rows) return;
+  const uint8_t lv = level[e];
+  for (int ch = 0; ch < 3; ++ch) {
+    float v;
+    if (lv == kNoRender) {
+      v = learned ? learned[3 * e + ch] : stats[e * kFeatureStats + ch];
+    } else if (lv & 0x80) {
+      v = sums[3 * e + ch];
+    } else {
+      const float c = static_cast<float>(4u << lv), f = static_cast<float>(featureSpp);
+      v = (f * stats[e * kFeatureStats + ch] + c * sums[3 * e + ch]) / (f + c);
+    }
+    out[3 * e + ch] = v;
+  }
+}
+
+}  // namespace
+
+AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* counts, const uint32_t* spp,
+                            float* const* partials, uint32_t nBuckets) {
+  AdaptiveLaunch L{};
+  uint64_t tasks = 0;
+  for (uint32_t k = 0; k < nBuckets && L.nBuckets < kAdaptiveBuckets; ++k) {
+    if (counts[k] == 0) continue;
+    AdaptiveBucket& B = L.b[L.nBuckets++];
+    B.entries = entries[k];
+    B.count = counts[k];
+    B.spp = spp[k];
+    B.partials = partials[k];
+    B.taskBase = tasks;
+    const uint64_t segWidth = spp[k] < 32 ? spp[k] : 32;
+    const uint64_t perWarp = 32 / segWidth, chunks = adaptiveChunks(spp[k]);
+    tasks += (counts[k] + perWarp - 1) / perWarp * chunks;
+  }
+  L.totalTasks = tasks;
+  return L;
+}
+
+size_t adaptivePartialFloats(uint64_t count, uint32_t spp) {
+  return adaptiveChunks(spp) > 1 ? count * adaptiveChunks(spp) * 3 : 0;
+}
+
+cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
+                           const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
+                           RayRecord* rec, cudaStream_t stream) {
+  if (L.totalTasks == 0) return cudaSuccess;
+  if (rec && L.nBuckets != 1) return cudaErrorInvalidValue;
+  for (uint32_t k = 0; k < L.nBuckets; ++k) {
+    const uint32_t c = L.b[k].spp;
+    if (c == 0 || c > 1024 || (c & (c - 1)) || L.b[k].count > 0xffffffffull || (adaptiveChunks(c) > 1 && !L.b[k].partials))
+      return cudaErrorInvalidValue;
+  }
+  if (L.totalTasks >= (1ull << 27)) return cudaErrorInvalidConfiguration;  // 32-bit thread ids
+  const uint64_t blocks = (L.totalTasks * 32 + 127) / 128;
+  adaptiveKernel<<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
+                                                                      rec);
+  cudaError_t e = cudaGetLastError();
+  for (uint32_t k = 0; k < L.nBuckets && e == cudaSuccess; ++k) {
+    if (adaptiveChunks(L.b[k].spp) == 1) continue;
+    adaptiveCombineKernel<<<static_cast<unsigned>((L.b[k].count + 255) / 256), 256, 0, stream>>>(L.b[k], sums);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, float thr, uint16_t* label,
+                         cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  labelKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(outs, k, rows, spp, thr, label);
+  return cudaGetLastError();
+}
+
+cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
+                           unsigned long long* counts, cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  allocateKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(pred, rows, featureSpp, level,
+                                                                                  counts);
+  return cudaGetLastError();
+}
+
+size_t scatterScratchWords(uint64_t rows) {
+  return ((rows + kScatterTile - 1) / kScatterTile) * kAdaptiveBuckets;
+}
+
+cudaError_t launchScatterBuckets(const uint8_t* level, uint64_t rows, uint32_t N, const uint32_t* order,
+                                 const unsigned long long* bucketBase, unsigned long long* scratch, uint32_t* entries,
+                                 cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  if (N == 0 || rows % N) return cudaErrorInvalidValue;
+  const uint64_t tiles = (rows + kScatterTile - 1) / kScatterTile;
+  if (tiles > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
+  bucketCountKernel<<<static_cast<unsigned>(tiles), kScatterTile, 0, stream>>>(level, rows, N, order, scratch);
+  bucketScanKernel<<<1, 32, 0, stream>>>(scratch, tiles, bucketBase);
+  bucketPlaceKernel<<<static_cast<unsigned>(tiles), kScatterTile, 0, stream>>>(level, rows, N, order, scratch,
+                                                                                entries);
+  return cudaGetLastError();
+}
+
+cudaError_t launchAdaptiveFinish(const uint8_t* level, uint64_t rows, uint32_t featureSpp, const float* stats,
+                                 const float* learned, const float* sums, float* out, cudaStream_t stream) {
+  if (rows == 0) return cudaSuccess;
+  adaptiveFinishKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(level, rows, featureSpp, stats,
+                                                                                        learned, sums, out);
+  return cudaGetLastError();
+}
+
 }  // namespace cr
 
 // ---------------------------------------------------------------------------

@@ -13,7 +13,7 @@ import ctypes
 import math
 import os
 from ctypes import (CDLL, POINTER, Structure, c_bool, c_char_p, c_double, c_float, c_int, c_size_t, c_ubyte,
-                    c_uint32, c_void_p)
+                    c_uint32, c_ulonglong, c_void_p)
 
 import numpy as np
 from numpy.ctypeslib import ndpointer
@@ -140,6 +140,24 @@ def configureExtras(eyeRenderer):
                                         ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t,
                                         ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crDenoiserPredictRows.restype = c_int
+    L.crDenoiserRelease.restype = None
+    L.crAllocatorInit.argtypes = [c_int]
+    L.crAllocatorInit.restype = c_int
+    L.crAllocatorAddTrainingPoses.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int, c_float,
+                                              c_int, c_void_p]
+    L.crAllocatorAddTrainingPoses.restype = c_int
+    L.crAllocatorTrain.argtypes = [c_int, c_int, c_float, c_int, c_void_p]
+    L.crAllocatorTrain.restype = c_int
+    L.crAllocatorTrainingRows.restype = c_size_t
+    L.crAllocatorSave.argtypes = [c_char_p]
+    L.crAllocatorSave.restype = c_int
+    L.crAllocatorLoad.argtypes = [c_char_p]
+    L.crAllocatorLoad.restype = c_int
+    L.crAdaptiveRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p, c_void_p, c_void_p]
+    L.crAdaptiveRenderPosesDevice.restype = c_int
+    L.crAdaptiveRecord.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int, c_ulonglong,
+                                   c_void_p, ndpointer(np.float32, flags="C_CONTIGUOUS")]
+    L.crAdaptiveRecord.restype = c_int
     L.crDenoiserTrain.restype = c_int
     L.crDenoiserRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p]
     L.crDenoiserRenderPosesDevice.restype = c_int

@@ -578,8 +578,10 @@ def terrain_height_fn(heights, extent):
 
 
 def terrain_scene(outdir, seed=SEED, cells=512, extent=200.0, cones=2000, n_omm=6000, spp=256, poses=1024,
-                  eye_height=0.5):
-    """Heightfield + cones and a droplet eye with a random-walk trajectory.
+                  eye_height=0.5, eye_kind="droplet", aa_deg=(1.5, 4.0)):
+    """Heightfield + cones and an eye with a random-walk trajectory: the
+    sinewave-droplet eye, or (eye_kind "panoramic") a Fibonacci sphere of
+    radius 1 mm looking in every direction.  Acceptance angles U(aa_deg).
     Returns a dict with paths, the (poses, 12) trajectory and spp."""
     os.makedirs(outdir, exist_ok=True)
     rng = np.random.default_rng(seed)
@@ -603,6 +605,7 @@ def terrain_scene(outdir, seed=SEED, cells=512, extent=200.0, cones=2000, n_omm=
     g.mesh("terrain", pos, faces, colours=col, index_type=5125)
     hfn = terrain_height_fn(heights, extent)
     cv, cf, cc = [], [], []
+    nv = 0
     for k in range(cones):
         x, z = rng.uniform(-extent / 2 + 5, extent / 2 - 5, size=2)
         hgt = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
@@ -610,15 +613,21 @@ def terrain_scene(outdir, seed=SEED, cells=512, extent=200.0, cones=2000, n_omm=
         v, f = cone_mesh(x, hfn(x, z) - 0.05, z, rad, hgt)
         tt = (v[:, 1] - v[:, 1].min()) / max(hgt, 1e-6)
         c = np.stack([0.05 + 0.2 * tt, 0.3 + 0.5 * tt, 0.05 + 0.1 * tt, np.ones_like(tt)], axis=1)
-        cf.append(f + sum(len(a) for a in cv))
+        cf.append(f + nv)
+        nv += len(v)
         cv.append(v)
         cc.append(c)
     g.mesh("plants", np.concatenate(cv), np.concatenate(cf), colours=np.concatenate(cc), index_type=5125)
-    epos, edir = droplet_eye(n_omm, rng)
-    aa = rng.uniform(1.5 * DEG, 4.0 * DEG, size=n_omm)
-    eye_path = os.path.join(outdir, "droplet.eye")
+    if eye_kind == "droplet":
+        epos, edir = droplet_eye(n_omm, rng)
+    else:
+        edir = fibonacci_sphere(n_omm)
+        epos = edir * 0.001
+    aa = rng.uniform(aa_deg[0] * DEG, aa_deg[1] * DEG, size=n_omm)
+    eye_name = "droplet" if eye_kind == "droplet" else "panoramic"
+    eye_path = os.path.join(outdir, eye_name + ".eye")
     write_eye(eye_path, epos, edir, aa, 0.0)
-    g.compound_camera("droplet-eye", "droplet.eye", translation=[0.0, hfn(0.0, 0.0) + eye_height, 0.0])
+    g.compound_camera(eye_name + "-eye", eye_name + ".eye", translation=[0.0, hfn(0.0, 0.0) + eye_height, 0.0])
     path = g.write(os.path.join(outdir, "terrain.gltf"), embed=False)
     traj = random_walk(hfn, poses, rng, eye_height=eye_height)
     return {"gltf": path, "eye": eye_path, "poses": traj, "spp": spp, "n_omm": n_omm,

@@ -163,6 +163,7 @@ int crGetRenderVariantCount(void);
  * random streams; the camera's streams are not touched. */
 int crDenoiserInit(int seed);                 /* fresh He-initialised weights */
 size_t crDenoiserParamCount(void);
+void crDenoiserRelease(void);                 /* drops the network (the adaptive render then uses feature means) */
 /* Renders `count` host poses (12 floats each) of the current eye twice --
  * a featureSpp-sample feature render and a targetSpp-sample plain render --
  * and appends count x N (features, target) rows to the training set. */
@@ -183,6 +184,42 @@ int crDenoiserRenderPoses(const float* poses12, size_t count, int featureSpp, fl
  * counterpart. */
 int crDenoiserFeatureRows(const float* poses12, size_t count, int featureSpp, uint16_t* xBf16, float* base);
 int crDenoiserPredictRows(const uint16_t* xBf16, const float* base, size_t rows, float* out);
+
+/* ---- Learned sample allocator and adaptive rendering ---------------------
+ * A second network of the denoiser's shape predicts, from the same
+ * featureSpp-sample features, how many samples each ommatidium needs:
+ * log2(count) / 10 in each output.  Training labels come from a
+ * minimum-sample search: every (pose, ommatidium) is rendered `seeds` times
+ * with independent streams at 4, 8, ..., 1024 samples, and its label is the
+ * first count at which the colour's standard deviation across the renders is
+ * below `threshold` in every channel (0 when none is, i.e. more than 1024).
+ * No counterpart in the reference. */
+int crAllocatorInit(int seed);
+/* count <= 256 host poses (12 floats); labelsOut: null or count x N words. */
+int crAllocatorAddTrainingPoses(const float* poses12, size_t count, int featureSpp, float threshold, int seeds,
+                                uint16_t* labelsOut);
+int crAllocatorTrain(int steps, int batch, float lr, int seed, float* lossHistory);
+size_t crAllocatorTrainingRows(void);
+int crAllocatorSave(const char* path);
+int crAllocatorLoad(const char* path);
+/* The adaptive learned form of `count` device poses (16 floats each) into
+ * d_out (count x N x 3): a featureSpp-sample feature render; the allocator's
+ * count c per (pose, ommatidium); where c <= featureSpp the denoised feature
+ * estimate (the feature mean when no denoiser is trained); where featureSpp <
+ * c <= 1024 an extra c-sample render combined with the feature samples by
+ * sample count; where c > 1024 (the predicted variance at 1024 samples is
+ * above the threshold) a plain 1024-sample render alone.  Extra samples come
+ * from Philox4x32-10 streams (seed, entry * 1024 + sample).  d_level: null,
+ * or count x N bytes receiving each entry's bucket (index k = 4 << k samples,
+ * 0x88 = 1024-sample fallback, 0xFF = feature render only).  raysTraced:
+ * null, or receives the rays of the call.  0 on success. */
+int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out, uint8_t* d_level,
+                                double* raysTraced);
+/* Test access: `spp` Philox samples per (pose, ommatidium) of host poses
+ * with one seed, recording every ray (records: count x N x spp, as
+ * crRenderFrameRecorded) and the per-entry means (sums: count x N x 3). */
+int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long long seed, void* records,
+                     float* sums);
 /* One forward/backward pass on host rows (x: rows x 112 bf16 bit patterns,
  * base/target: rows x 3): returns the loss (-1 on error) and writes the
  * gradients and the current parameters (crDenoiserParamCount floats each). */

@@ -1,0 +1,146 @@
+"""The learned sample allocator and the adaptive render: the Philox-sampled
+adaptive kernel against the oracle ray by ray; its estimates against the
+plain render; minimum-sample labels; a trained allocator's adaptive render
+against the 1024-sample plain render (error and rays); determinism and the
+checkpoint round trip."""
+import numpy as np
+import pytest
+import torch
+
+import eyeRendererHelperFunctions as eh
+import gltf_ref
+import oracle
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL, SKY_ATOL, DIR_ATOL = 1e-5, 1e-7, 1e-5, 2e-6
+
+
+def _terrain(lib, tmp_path):
+    info = scenes.terrain_scene(str(tmp_path), cells=128, extent=60.0, cones=300, n_omm=1500, poses=8)
+    eh.lastError(lib)
+    lib.loadGlTFscene(info["gltf"].encode())
+    assert eh.lastError(lib) == ""
+    eh.gotoFirstCompoundEye(lib)
+    return info
+
+
+def test_adaptive_kernel_matches_oracle(lib, small, small_ref):
+    ref, sc = small_ref
+    omm = ref.cameras[0]["omm"]
+    eh.lastError(lib)
+    lib.loadGlTFscene(small["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    N, spp = len(omm), 64
+    poses = np.stack([small["pose"], scenes.pose_rows(np.array([1.0, 0.7, -2.0]), 0.8)]).astype(np.float32)
+    rec = np.zeros((2 * N * spp,), eh.RAY_RECORD_DTYPE)
+    sums = np.zeros((2, N, 3), np.float32)
+    assert lib.crAdaptiveRecord(poses, 2, spp, 7, rec.ctypes.data, sums) == 0, eh.lastError(lib)
+    rec = rec.reshape(2, N * spp)
+    for p in range(2):
+        r = rec[p]
+        draws = np.stack([r["normalDraw"], r["uniformDraw"]], axis=1)
+        o2, d2 = oracle.gen_rays(omm, spp, poses[p], draws)
+        np.testing.assert_allclose(d2, r["direction"].reshape(-1, 3), rtol=0, atol=DIR_ATOL)
+        org, dirs = r["origin"].reshape(-1, 3), r["direction"].reshape(-1, 3)
+        hit, t, b1, b2 = sc.trace(org, dirs, np.repeat(omm[:, 7], spp))
+        assert np.array_equal(hit, r["hitId"])
+        want = sc.render_rays(omm, spp, org, dirs)[0]
+        sky = (hit < 0).reshape(N, spp).mean(axis=1)[:, None]
+        assert (np.abs(sums[p] - want) <= RTOL * np.abs(want) + ATOL + SKY_ATOL * sky).all()
+    # normal / uniform draws look like N(0,1) / U(0,1]
+    nd, ud = rec["normalDraw"].ravel(), rec["uniformDraw"].ravel()
+    assert abs(nd.mean()) < 0.02 and abs(nd.std() - 1) < 0.02
+    assert ud.min() > 0 and ud.max() <= 1 and abs(ud.mean() - 0.5) < 0.01
+
+
+def test_adaptive_estimate_matches_plain_render(lib, tmp_path):
+    info = _terrain(lib, tmp_path)
+    rng = np.random.default_rng(4)
+    poses = scenes.random_poses(info["height_fn"], 3, rng, 20.0)
+    n = lib.getCurrentEyeOmmatidialCount()
+    rec = np.zeros((3 * n * 256,), eh.RAY_RECORD_DTYPE)
+    a256 = np.zeros((3, n, 3), np.float32)
+    assert lib.crAdaptiveRecord(poses, 3, 256, 11, rec.ctypes.data, a256) == 0, eh.lastError(lib)
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+    p1024 = eh.renderPoses(lib, poses)
+    lib.setCurrentEyeSamplesPerOmmatidium(32)
+    p32 = eh.renderPoses(lib, poses)
+    rmse = lambda a: float(np.sqrt(((a - p1024) ** 2).mean()))
+    # 256 Philox samples sit between 32 and 1024 XORWOW samples
+    assert rmse(a256) < 0.6 * rmse(p32), (rmse(a256), rmse(p32))
+
+
+def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
+    info = _terrain(lib, tmp_path)
+    n = lib.getCurrentEyeOmmatidialCount()
+    rng = np.random.default_rng(9)
+    train = scenes.random_poses(info["height_fn"], 24, rng, 20.0)
+    held = scenes.random_poses(info["height_fn"], 4, rng, 20.0)
+    lib.crDenoiserRelease()  # no denoiser: entries the feature render covers keep its mean
+    assert lib.crAllocatorInit(2) == 0
+    thr = 1.0 / 512.0
+    labels = np.zeros((24, n), np.uint16)
+    for k in range(0, 24, 8):
+        lab = np.zeros((8, n), np.uint16)
+        assert lib.crAllocatorAddTrainingPoses(train[k:k + 8], 8, 8, thr, 8, lab.ctypes.data) == 0, eh.lastError(lib)
+        labels[k:k + 8] = lab
+    assert lib.crAllocatorTrainingRows() == 24 * n
+    vals = set(np.unique(labels).tolist())
+    assert vals <= {0, 4, 8, 16, 32, 64, 128, 256, 512, 1024}
+    assert len(vals) >= 4  # the scene needs different counts in different places
+    # labels follow the per-ommatidium sample spread: plain 8-sample std of
+    # ommatidia labelled 4 or 8 is below that of ommatidia labelled >= 256
+    lib.setCurrentEyeSamplesPerOmmatidium(8)
+    # the spread proxy: |8-sample render - 1024-sample render|
+    p8 = eh.renderPoses(lib, train[:8])
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+    p1k = eh.renderPoses(lib, train[:8])
+    err = np.abs(p8 - p1k).max(axis=2)
+    lo, hi = labels[:8] <= 8, (labels[:8] >= 256) | (labels[:8] == 0)
+    if lo.any() and hi.any():
+        assert err[lo].mean() < err[hi].mean()
+    loss = np.zeros(1500, np.float32)
+    assert lib.crAllocatorTrain(1500, 4096, 1e-3, 5, loss.ctypes.data) == 0, eh.lastError(lib)
+    assert loss[-50:].mean() < 0.5 * loss[:20].mean()
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    p16 = np.zeros((4, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
+    d_poses = torch.from_numpy(p16).to(dev)
+    out = torch.zeros((4, n, 3), dtype=torch.float32, device=dev)
+    lev = torch.zeros((4, n), dtype=torch.uint8, device=dev)
+    rays = eh.c_double(0.0)
+    assert lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), 4, 8, out.data_ptr(), lev.data_ptr(),
+                                           eh.ctypes.byref(rays)) == 0, eh.lastError(lib)
+    torch.cuda.synchronize()
+    adaptive = out.cpu().numpy()
+    levels = lev.cpu().numpy().astype(np.int64)
+    assert set(np.unique(levels).tolist()) <= set(range(9)) | {0x88, 0xFF}
+    spp_of = np.where(levels == 0xFF, 0, np.where(levels == 0x88, 1024, 4 << (levels & 0x7F)))
+    assert abs(rays.value - (4 * n * 8 + spp_of.sum())) < 0.5
+    assert rays.value < 0.5 * 4 * n * 1024  # far fewer rays than the plain 1024-sample render
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+    plain = eh.renderPoses(lib, held)
+    rmse = float(np.sqrt(((adaptive - plain) ** 2).mean()))
+    print("labels", {int(v): int((labels == v).sum()) for v in np.unique(labels)},
+          "levels", {int(v): int((levels == v).sum()) for v in np.unique(levels)},
+          "rays/plain1024 %.4f rmse %.6f" % (rays.value / (4 * n * 1024), rmse))
+    assert rmse <= 1.0 / 255.0, rmse
+
+    # determinism: reloading restarts the feature and adaptive streams
+    path = str(tmp_path / "alloc.bin")
+    assert lib.crAllocatorSave(path.encode()) == 0
+    assert lib.crAllocatorInit(77) == 0
+    assert lib.crAllocatorLoad(path.encode()) == 0
+    again = []
+    for _ in range(2):
+        lib.loadGlTFscene(info["gltf"].encode())
+        eh.gotoFirstCompoundEye(lib)
+        o2 = torch.zeros_like(out)
+        assert lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), 4, 8, o2.data_ptr(), None, None) == 0
+        torch.cuda.synchronize()
+        again.append(o2.cpu().numpy())
+    assert np.array_equal(again[0], again[1])
