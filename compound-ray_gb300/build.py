@@ -20,7 +20,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["render.cu", "lbvh.cu", "mlp.cu"]
+CU_SOURCES = ["render.cu", "lbvh.cu", "mlp.cu", "mlp_tc.cu"]
 CPP_SOURCES = ["gltf.cpp", "png.cpp", "bvh.cpp", "denoiser.cpp", "eye_renderer.cpp"]
 
 

@@ -78,6 +78,7 @@ static_assert(sizeof(RayRecord) == 64, "ray record is 64 bytes");
 enum : uint32_t {
   kErrStackOverflow = 1u,
   kErrRngDoubleFlag = 2u,
+  kErrMmaTimeout = 4u,  // a tensor-core wait ran out of its iteration limit
 };
 
 constexpr uint32_t kRngPlanes = 8;
@@ -163,6 +164,12 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
 // assembleFeatures + the layer-by-layer forward.
 cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
                           const MlpWeights& w, float* out, cudaStream_t stream, bool residual = true);
+// The same prediction on the tcgen05 tensor cores (mlp_tc.cu): accumulators
+// in TMEM, operands in shared memory; errFlag receives kErrMmaTimeout if a
+// bounded wait ran out.
+cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
+                            const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream,
+                            bool residual = true);
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
                        float* baseo, float* targeto, cudaStream_t stream);
 

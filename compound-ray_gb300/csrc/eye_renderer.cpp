@@ -294,7 +294,8 @@ struct Renderer {
     if (h != 0) {
       check(cudaMemsetAsync(errWord(), 0, sizeof(uint32_t), stream()), "cudaMemset");
       throw std::runtime_error("render kernel raised error flags " + std::to_string(h) +
-                               ((h & kErrStackOverflow) ? " (BVH traversal stack overflow)" : ""));
+                               ((h & kErrStackOverflow) ? " (BVH traversal stack overflow)" : "") +
+                               ((h & kErrMmaTimeout) ? " (tensor-core wait timed out)" : ""));
     }
   }
 
@@ -1234,6 +1235,7 @@ namespace {
 
 struct DenoiseState {
   Denoiser net;
+  int inferKernel = 1;  // 0: mma.sync fused kernel, 1: tcgen05 fused kernel (default)
   size_t cam = static_cast<size_t>(-1);
   uint64_t generation = ~0ull;
   DevBuf<int> nb;
@@ -1350,6 +1352,17 @@ size_t crDenoiserParamCount(void) { return Denoiser::kParams; }
 
 void crDenoiserRelease(void) { DS().net.release(); }
 
+int crSetDenoiserKernel(int kind) {
+  if (kind != 0 && kind != 1) {
+    setError("crSetDenoiserKernel: kind must be 0 (mma.sync) or 1 (tcgen05)");
+    return -1;
+  }
+  DS().inferKernel = kind;
+  return 0;
+}
+
+int crGetDenoiserKernel(void) { return DS().inferKernel; }
+
 int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSpp, int targetSpp) {
   return guarded(
       "crDenoiserAddTrainingPoses",
@@ -1405,8 +1418,12 @@ int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureS
                         false);
         for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
           const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
-          check(inferDenoiser(d.stats.ptr + first * e.N * kFeatureStats, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(),
-                              d_out + 3 * first * e.N, r.stream()),
+          const float* st = d.stats.ptr + first * e.N * kFeatureStats;
+          check(d.inferKernel == 1
+                    ? inferDenoiserTc(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
+                                      r.errWord(), r.stream())
+                    : inferDenoiser(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
+                                    r.stream()),
                 "denoiser inference");
         }
         return 0;
@@ -1663,13 +1680,16 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           denoiseFeatures(r, d, e, poses + 4 * first, P, fs, false);
           rays += static_cast<double>(rows) * fs;
           d.pred.ensure(rows * 3);
-          check(inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, d.alloc.weights(), d.pred.ptr, st, false),
-                "allocator inference");
+          auto infer = [&](const MlpWeights& w, float* o, bool residual) {
+            return d.inferKernel == 1
+                       ? inferDenoiserTc(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, r.errWord(), st, residual)
+                       : inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, st, residual);
+          };
+          check(infer(d.alloc.weights(), d.pred.ptr, false), "allocator inference");
           const float* learned = nullptr;
           if (d.net.ready()) {
             d.learned.ensure(rows * 3);
-            check(inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d.learned.ptr, st),
-                  "denoiser inference");
+            check(infer(d.net.weights(), d.learned.ptr, true), "denoiser inference");
             learned = d.learned.ptr;
           }
           d.level.ensure(rows);

@@ -141,6 +141,9 @@ def configureExtras(eyeRenderer):
                                         ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crDenoiserPredictRows.restype = c_int
     L.crDenoiserRelease.restype = None
+    L.crSetDenoiserKernel.argtypes = [c_int]
+    L.crSetDenoiserKernel.restype = c_int
+    L.crGetDenoiserKernel.restype = c_int
     L.crAllocatorInit.argtypes = [c_int]
     L.crAllocatorInit.restype = c_int
     L.crAllocatorAddTrainingPoses.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int, c_float,

@@ -164,6 +164,11 @@ int crGetRenderVariantCount(void);
 int crDenoiserInit(int seed);                 /* fresh He-initialised weights */
 size_t crDenoiserParamCount(void);
 void crDenoiserRelease(void);                 /* drops the network (the adaptive render then uses feature means) */
+/* Network pass of the learned and adaptive renders: 0 = fused mma.sync
+ * kernel (bit-identical to the layer-by-layer training path), 1 = fused
+ * tcgen05 kernel (accumulators in TMEM; the default).  -1 on a bad kind. */
+int crSetDenoiserKernel(int kind);
+int crGetDenoiserKernel(void);
 /* Renders `count` host poses (12 floats each) of the current eye twice --
  * a featureSpp-sample feature render and a targetSpp-sample plain render --
  * and appends count x N (features, target) rows to the training set. */

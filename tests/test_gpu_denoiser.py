@@ -59,11 +59,25 @@ def test_fused_inference_matches_layer_path(lib, tmp_path):
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     fused = np.zeros((3, n, 3), np.float32)
+    assert lib.crSetDenoiserKernel(0) == 0  # the mma.sync kernel repeats the training path bit for bit
     assert lib.crDenoiserRenderPoses(poses, 3, 8, fused) == 0, eh.lastError(lib)
     layered = np.zeros((rows, 3), np.float32)
     assert lib.crDenoiserPredictRows(X, base, rows, layered) == 0, eh.lastError(lib)
     assert np.array_equal(fused.reshape(-1, 3).view(np.uint32), layered.view(np.uint32))
     assert (X[:, 105:] == 0).all()
+    # the tcgen05 kernel: the same network on the 5th-generation tensor cores
+    # (fp32 sums in another order, so bf16 activations may round one step apart)
+    assert lib.crSetDenoiserKernel(1) == 0
+    try:
+        lib.loadGlTFscene(info["gltf"].encode())
+        eh.gotoFirstCompoundEye(lib)
+        tc = np.zeros((3, n, 3), np.float32)
+        assert lib.crDenoiserRenderPoses(poses, 3, 8, tc) == 0, eh.lastError(lib)
+    finally:
+        lib.crSetDenoiserKernel(1)
+    corr = np.abs(layered - base).max() + 1e-6
+    terr = np.abs(tc.reshape(-1, 3) - layered)
+    assert terr.max() <= 0.05 * corr and terr.mean() <= 0.005 * corr, (terr.max(), terr.mean(), corr)
     params = np.zeros(mlp_ref.N_PARAMS, np.float32)
     grads = np.zeros(mlp_ref.N_PARAMS, np.float32)
     assert lib.crDenoiserGradient(X[:64].copy(), base[:64].copy(), base[:64].copy(), 64, grads, params) >= 0
