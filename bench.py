@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--no-adaptive", action="store_true", help="skip the sample-allocator measurement")
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
+    ap.add_argument("--cut", type=float, default=1.0 / 64, help="near-field cut radius (fraction of the scene extent) for --profile")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
     return ap.parse_args()
 
@@ -62,10 +63,13 @@ def workload(poses):
     return info
 
 
-# From an ncu capture of renderKernel on one 256-pose launch of this workload
-# (variant 2): DRAM bytes read + written, and warp instructions per ray.
-RENDER_DRAM_BYTES_PER_LAUNCH = 54536704 + 187921408
-RENDER_WARP_INSTR_PER_RAY = 23060962816 / (256 * 6000 * 256)
+# From ncu captures of renderKernel on one 256-pose launch of this workload
+# (variant 2), keyed by the near-field cut fraction in use: DRAM bytes read
+# + written per launch, and warp instructions per ray.
+RENDER_LAUNCH_COUNTERS = {
+    0.0: (54536704 + 187921408, 23060962816 / (256 * 6000 * 256)),
+    1.0 / 128: (53614336 + 197225472, 14751017834 / (256 * 6000 * 256)),
+}
 SM_COUNT = 152
 
 
@@ -369,9 +373,10 @@ def run_ours(args):
     # Issue-rate roofline: warp instructions per ray from an ncu capture of
     # this kernel on this launch (smsp__inst_executed.sum / rays), against 4
     # schedulers x 1 instruction per cycle on every SM at the maximum clock.
-    issue_per_ray = RENDER_WARP_INSTR_PER_RAY
+    counters = RENDER_LAUNCH_COUNTERS.get(float(lib.crGetCutRadius()))
+    issue_per_ray = counters[1] if counters else None
     issue_peak = 4.0 * SM_COUNT * sm_max_mhz() * 1e6
-    issue_achieved = issue_per_ray * launch_n * N * spp / launch_s
+    issue_achieved = issue_per_ray * launch_n * N * spp / launch_s if counters else None
     clk = clocks.summary()
     line = {
         "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -380,18 +385,20 @@ def run_ours(args):
         "config": {"workload": "terrain %d tris, droplet eye 6000 omm x 256 spp, %d-pose trajectory" % (info["triangles"], P),
                    "rays_per_step": rays_step, "eye_frames_per_step": P, "l2": "flushed (512 MB write) between steps",
                    "poses_per_launch": POSES_PER_LAUNCH,
-                   "autotune": {"variant": best.value, "ms_64_poses": [round(float(x), 3) for x in tune_ms]}},
+                   "autotune": {"variant": best.value, "ms_64_poses": [round(float(x), 3) for x in tune_ms],
+                                "near_field_cut_fraction": float(lib.crGetCutRadius())}},
         "eye_frames_per_s": value / (N * spp),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},
         "gpu_launches": args.steps * len(chunks) * (2 if spp > 32 else 1),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": RENDER_DRAM_BYTES_PER_LAUNCH if launch_n == POSES_PER_LAUNCH else None,
+                     "traffic": counters[0] if counters and launch_n == POSES_PER_LAUNCH else None,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one 256-pose launch (ncu); "
                                      "the per-ray demand bytes above are served from L1/L2",
                      "peak_source": src,
                      "issue": {"achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
-                               "frac": issue_achieved / issue_peak, "instr_per_ray": issue_per_ray,
+                               "frac": issue_achieved / issue_peak if counters else None,
+                               "instr_per_ray": issue_per_ray,
                                "note": "the limiter: smsp__inst_executed.sum per ray from ncu x live rays/s"},
                      "bytes_per_ray": per_ray, "node_visits_per_ray": nodes.value, "tri_tests_per_ray": tris.value,
                      "hit_fraction": hit_frac, "launch_ms": statistics.mean(full),
@@ -711,7 +718,7 @@ def run_profile(args):
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])
-    if lib.crSetRenderVariant(args.variant) != 0:
+    if lib.crSetRenderVariant(args.variant) != 0 or lib.crSetCutRadius(args.cut) != 0:
         raise RuntimeError(eh.lastError(lib))
     P = min(args.poses, POSES_PER_LAUNCH)
     poses = info["poses"][:P]

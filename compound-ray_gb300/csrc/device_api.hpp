@@ -55,7 +55,16 @@ struct DevEye {
   //       of a launch, generated up front so that the poses of the launch can
   //       be spread over several warps (renderDrawBytes).
   float2* draws = nullptr;
+  // cuts: null, or P x kCutStride float4 receiving each pose's near-field
+  //       cut (render.cu, cutKernel) for a ball of radius cutRadius around
+  //       the pose position; maxRel bounds |ommatidium position - focal
+  //       offset along the axis| over the eye.  Results do not depend on it.
+  float4* cuts = nullptr;
+  float cutRadius = 0.f;
+  float maxRel = 0.f;
 };
+constexpr int kCutEntries = 8;
+constexpr int kCutStride = 1 + 2 * kCutEntries;
 
 // One pose = 4 x float4: position, local x axis, local y axis, local z axis
 // (w components unused).
@@ -166,10 +175,11 @@ cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, 
                           const MlpWeights& w, float* out, cudaStream_t stream, bool residual = true);
 // The same prediction on the tcgen05 tensor cores (mlp_tc.cu): accumulators
 // in TMEM, operands in shared memory; errFlag receives kErrMmaTimeout if a
-// bounded wait ran out.
+// bounded wait ran out.  order: null, or the eye's direction order (rows of
+// a tile are then neighbouring ommatidia; results do not depend on it).
 cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
                             const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream,
-                            bool residual = true);
+                            bool residual = true, const uint32_t* order = nullptr);
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
                        float* baseo, float* targeto, cudaStream_t stream);
 

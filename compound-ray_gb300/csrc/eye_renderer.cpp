@@ -63,6 +63,7 @@ struct EyeDev {
   DevBuf<uint32_t> rng;
   DevBuf<float> sums;  // N x 3 of the last frame
   uint32_t N = 0, spp = 0;
+  float maxRel = 0.f;  // largest |position - focal offset * unit axis| over the ommatidia
   bool configured = false;
   bool haveSums = false;
   void release() {
@@ -131,6 +132,8 @@ struct Renderer {
   DevBuf<float4> poses;
   DevBuf<float> scratch;
   DevBuf<float2> draws;  // pre-drawn random numbers of small-eye launches
+  DevBuf<float4> cuts;   // per-pose near-field cuts
+  float cutFactor = 0.f; // cut radius as a fraction of the scene extent (0: off)
   DevBuf<float> batchOut;
   DevBuf<uint32_t> err;
   cudaStream_t ownStream = nullptr;
@@ -327,6 +330,14 @@ struct Renderer {
         e.order.release();
         e.order.ensure(std::max<size_t>(1, N));
       }
+      float mr = 0.f;
+      for (const Ommatidium& o : c.omm) {
+        const double al = std::sqrt(double(o.dir.x) * o.dir.x + double(o.dir.y) * o.dir.y + double(o.dir.z) * o.dir.z);
+        const double s = al > 0 ? o.focalPointOffset / al : 0.0;
+        const double rx = o.pos.x - s * o.dir.x, ry = o.pos.y - s * o.dir.y, rz = o.pos.z - s * o.dir.z;
+        mr = std::max(mr, static_cast<float>(std::sqrt(rx * rx + ry * ry + rz * rz) * 1.001 + 1e-6));
+      }
+      e.maxRel = mr;
       if (N) {
         const std::vector<uint32_t> ord = directionOrder(c.omm);
         check(cudaMemcpyAsync(e.order.ptr, ord.data(), 4 * static_cast<size_t>(N), cudaMemcpyHostToDevice, stream()),
@@ -373,10 +384,23 @@ struct Renderer {
       if (need) scratch.ensure(need);
       DevEye de = devEye(e);
       withDraws(de, P, !rec && !stats);
+      withCuts(de, P, e.maxRel);
       check(launchRender(dev, de, d_poses + 4 * first, P, d_out + 3 * first * e.N, need ? scratch.ptr : nullptr,
                          errWord(), rec, stream(), stats),
             "render launch");
     }
+  }
+
+  // Near-field cuts for a P-pose launch when a cut radius is set and the
+  // traversal stack has room for the cut entries above the deepest leaf.
+  void withCuts(DevEye& de, uint32_t P, float maxRel) {
+    de.cuts = nullptr;
+    if (!(cutFactor > 0.f) || !(dev.extent > 0.f)) return;
+    if (bvhStats.maxDepth + kCutEntries + 2 > 64) return;
+    cuts.ensure(static_cast<size_t>(P) * kCutStride);
+    de.cuts = cuts.ptr;
+    de.cutRadius = cutFactor * dev.extent;
+    de.maxRel = maxRel;
   }
 
   // Gives a P-pose launch of a small eye a buffer for its pre-drawn random
@@ -1197,10 +1221,31 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
             best = v;
           }
         }
+        // Near-field cut radius (fraction of the scene extent), with the best variant.
+        setRenderVariant(best);
+        const float factors[] = {0.f, 1.f / 256, 1.f / 128, 1.f / 64, 1.f / 32, 1.f / 16};
+        float bestCut = 0.f, bestCutMs = INFINITY;
+        for (float f : factors) {
+          r.cutFactor = f;
+          float ms = INFINITY;
+          for (int rep = 0; rep < 2; ++rep) {
+            check(cudaEventRecord(a, st), "cudaEventRecord");
+            r.renderDevicePoses(e, reinterpret_cast<const float4*>(d_poses), count, out.ptr, nullptr);
+            check(cudaEventRecord(b, st), "cudaEventRecord");
+            check(cudaEventSynchronize(b), "cudaEventSynchronize");
+            check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+            check(cudaMemcpyAsync(e.rng.ptr, saved.ptr, words * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
+                  "cudaMemcpy");
+          }
+          if (ms < bestCutMs) {
+            bestCutMs = ms;
+            bestCut = f;
+          }
+        }
+        r.cutFactor = bestCut;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         r.checkErrWord();
-        setRenderVariant(best);
         (void)prev;
         if (bestVariant) *bestVariant = best;
         saved.release();
@@ -1209,6 +1254,17 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
       },
       -1);
 }
+
+int crSetCutRadius(float fractionOfExtent) {
+  if (!(fractionOfExtent >= 0.f) || fractionOfExtent > 1.f) {
+    setError("crSetCutRadius: the fraction must lie in [0, 1]");
+    return -1;
+  }
+  R().cutFactor = fractionOfExtent;
+  return 0;
+}
+
+float crGetCutRadius(void) { return R().cutFactor; }
 
 int crSetRenderVariant(int variant) {
   if (variant < 0 || variant >= renderVariantCount()) {
@@ -1421,7 +1477,7 @@ int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureS
           const float* st = d.stats.ptr + first * e.N * kFeatureStats;
           check(d.inferKernel == 1
                     ? inferDenoiserTc(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
-                                      r.errWord(), r.stream())
+                                      r.errWord(), r.stream(), true, e.order.ptr)
                     : inferDenoiser(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
                                     r.stream()),
                 "denoiser inference");
@@ -1682,7 +1738,8 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           d.pred.ensure(rows * 3);
           auto infer = [&](const MlpWeights& w, float* o, bool residual) {
             return d.inferKernel == 1
-                       ? inferDenoiserTc(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, r.errWord(), st, residual)
+                       ? inferDenoiserTc(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, r.errWord(), st, residual,
+                                         e.order.ptr)
                        : inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, st, residual);
           };
           check(infer(d.alloc.weights(), d.pred.ptr, false), "allocator inference");

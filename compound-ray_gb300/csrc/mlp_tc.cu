@@ -148,6 +148,15 @@ constexpr uint32_t kOffBias = kOffA1 + kActBytes;                    // 3 x 128 
 constexpr uint32_t kOffBar = kOffBias + (3 * kMlpHidden + 16) * 4;  // mbarrier (8 B) + TMEM address (4 B)
 constexpr uint32_t kTcSmem = kOffBar + 16 + 128;                    // + alignment slack
 
+// Row (pose * N + ommatidium) processed at position x: poses in order, the
+// ommatidia of a pose in the eye's direction order, so that a tile's rows
+// are neighbouring ommatidia whose neighbour statistics overlap in L1.
+__device__ __forceinline__ uint64_t rowAt(uint64_t x, uint32_t N, const uint32_t* __restrict__ order) {
+  const uint64_t p = x / N;
+  const uint32_t j = static_cast<uint32_t>(x - p * N);
+  return p * N + (order ? __ldg(order + j) : j);
+}
+
 // Stages W[in x out] (global, bf16, row-major) as a K-major operand of
 // `rows` output rows (zero beyond `out`) and `in` columns.
 __device__ void stageWeights(unsigned char* dst, const __nv_bfloat16* __restrict__ w, int in, int out, int rows) {
@@ -161,7 +170,7 @@ __device__ void stageWeights(unsigned char* dst, const __nv_bfloat16* __restrict
 __global__ void __launch_bounds__(kTcThreads, 1)
     inferTcKernel(const float* __restrict__ stats, const float4* __restrict__ omm, const int* __restrict__ nb,
                   uint32_t N, uint64_t rows, MlpWeights w, bool residual, float* __restrict__ out,
-                  uint32_t* errFlag) {
+                  uint32_t* errFlag, const uint32_t* __restrict__ order) {
   extern __shared__ __align__(128) unsigned char smemRaw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 127) & ~uintptr_t(127));
   float* bias = reinterpret_cast<float*>(sm + kOffBias);  // b1 | b2 | b3 | b4 (16)
@@ -209,13 +218,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // Features of row tid / 4 into A0 (K = 112 layout), a quarter per thread.
     {
       const uint32_t r = static_cast<uint32_t>(tid >> 2), q = static_cast<uint32_t>(tid & 3);
-      const uint64_t frow = tile * kTcRows + r;
+      const uint64_t fpos = tile * kTcRows + r;
+      const uint64_t frow = fpos < rows ? rowAt(fpos, N, order) : fpos;
       unsigned char* a0 = sm + kOffA0;
       auto put = [a0, r](int k, __nv_bfloat16 v) {
         *reinterpret_cast<__nv_bfloat16*>(a0 + coreOffset(r, static_cast<uint32_t>(k), kFeatureWidth)) = v;
       };
       static constexpr int kBegin[4] = {0, 1, 3, 5}, kEnd[4] = {1, 3, 5, kNeighbours};
-      if (frow < rows) {
+      if (fpos < rows) {
         feat::featureRowTo(stats, omm, nb, N, frow, q == 0, kBegin[q], kEnd[q], put, nullptr);
       } else {
         for (int k = static_cast<int>(q); k < kFeatureWidth; k += 4) put(k, __float2bfloat16(0.f));
@@ -268,8 +278,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       } else if (cb == 0) {
         float v[4];
         tmemLoad4(laneBase, v);
-        const uint64_t row = tile * kTcRows + static_cast<uint64_t>(myRow);
-        if (row < rows) {
+        const uint64_t pos = tile * kTcRows + static_cast<uint64_t>(myRow);
+        if (pos < rows) {
+          const uint64_t row = rowAt(pos, N, order);
           const float* b4 = bias + 3 * kMlpHidden;
           for (int c = 0; c < 3; ++c) {
             const float y = v[c] + b4[c];
@@ -290,7 +301,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }  // namespace
 
 cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
-                            const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream, bool residual) {
+                            const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream, bool residual,
+                            const uint32_t* order) {
   const uint64_t rows = static_cast<uint64_t>(N) * P;
   if (rows == 0) return cudaSuccess;
   static int smCount = 0;
@@ -307,7 +319,7 @@ cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb
   }
   const uint64_t tiles = (rows + kTcRows - 1) / kTcRows;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(tiles, static_cast<uint64_t>(smCount)));
-  inferTcKernel<<<grid, kTcThreads, kTcSmem, stream>>>(stats, omm, nb, N, rows, w, residual, out, errFlag);
+  inferTcKernel<<<grid, kTcThreads, kTcSmem, stream>>>(stats, omm, nb, N, rows, w, residual, out, errFlag, order);
   return cudaGetLastError();
 }
 

@@ -239,17 +239,11 @@ __device__ __forceinline__ void childSpan(const Ray& r, float cx, float cy, floa
   tf = min3(mx + hx, my + hy, fminf(mz + hz, tmax));
 }
 
-// Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
+// Traversal loop over the BVH2 from `node`, with `sp` deferred entries
+// already on the stack; updates the closest hit `h`.
 template <bool kCount>
-__device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
-                                             uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests) {
-  h.t = tmax;
-  h.id = 0xffffffffu;
-  h.pos = 0;
-  if (sc.triCount == 0) return;
-  int stack[kStackSize];
-  int sp = 0;
-  int node = 0;
+__device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack, int sp,
+                                             int node, uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests) {
   for (;;) {
     if (node >= 0) {
       if (kCount) ++nodeVisits;
@@ -297,6 +291,176 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
     }
     if (sp == 0) return;
     node = stack[--sp];
+  }
+}
+
+// Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
+// cut: null, or the pose's near-field cut (cutKernel): the subtrees whose
+// boxes meet a ball around the eye are searched first, and a hit found there
+// within the ball's guaranteed radius (in distance, hence t * dlen with dlen
+// = |direction|) is final: every triangle nearer than it lies in the ball and
+// so in one of those subtrees.  Otherwise the search continues from the root
+// with the hit found so far.  Either way the result is the closest hit.
+template <bool kCount>
+__device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
+                                             uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests,
+                                             const float4* __restrict__ cut = nullptr, float dlen = 0.f) {
+  h.t = tmax;
+  h.id = 0xffffffffu;
+  h.pos = 0;
+  if (sc.triCount == 0) return;
+  int stack[kStackSize];
+  if (cut) {
+    const float4 hdr = __ldg(cut);
+    const int count = __float_as_int(hdr.x);
+    if (count > 0) {
+      // Entries are stored far to near; the nearest hit box is entered first.
+      int sp = 0, node = 0;
+      bool any = false;
+      for (int k = 0; k < count; ++k) {
+        const float4 a = __ldg(cut + 1 + 2 * k), b = __ldg(cut + 2 + 2 * k);
+        float tn, tf;
+        childSpan(r, a.x, a.y, a.z, b.x, b.y, b.z, tmin, h.t, tn, tf);
+        if (tn <= tf) {
+          if (any) stack[sp++] = node;
+          node = __float_as_int(a.w);
+          any = true;
+        }
+      }
+      if (any) traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests);
+      if (h.id != 0xffffffffu && h.t * dlen <= hdr.y) return;
+    }
+  }
+  traverseFrom<kCount>(sc, r, tmin, h, stack, 0, 0, errFlag, nodeVisits, triTests);
+}
+
+// Near-field cut of one pose: at most kCutEntries BVH subtrees (box + ref)
+// covering every box that meets the ball of radius R around the pose
+// position, grown from the root's children by repeatedly splitting the
+// largest entry while the count allows; entries that miss the ball are
+// dropped.  Header: (count, guaranteed radius, 0, 0) where the guaranteed
+// radius R - rEye (rEye bounds how far ray origins lie from the pose
+// position: maxRel times the sum of the pose axes' lengths) is shrunk by
+// 1e-4 relative.  Entries sorted far to near by box distance.
+__device__ __forceinline__ float boxDist2(float px, float py, float pz, float cx, float cy, float cz, float ex,
+                                          float ey, float ez) {
+  const float dx = fmaxf(fabsf(px - cx) - ex, 0.f), dy = fmaxf(fabsf(py - cy) - ey, 0.f),
+              dz = fmaxf(fabsf(pz - cz) - ez, 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void cutKernel(DevScene sc, const float4* __restrict__ poses, uint32_t P, float R, float maxRel,
+                          float4* __restrict__ cuts) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  float4* out = cuts + static_cast<size_t>(p) * kCutStride;
+  const float4 P0 = poses[4 * p], X = poses[4 * p + 1], Y = poses[4 * p + 2], Z = poses[4 * p + 3];
+  const float rEye = maxRel * (sqrtf(X.x * X.x + X.y * X.y + X.z * X.z) + sqrtf(Y.x * Y.x + Y.y * Y.y + Y.z * Y.z) +
+                               sqrtf(Z.x * Z.x + Z.y * Z.y + Z.z * Z.z));
+  const float rGuard = R - rEye;
+  float c[kCutEntries][3], e[kCutEntries][3];
+  int ref[kCutEntries];
+  bool frozen[kCutEntries];
+  int count = 0;
+  const float R2 = R * R * 1.0002f;  // the ball test errs on the side of keeping a box
+  if (rGuard > 0.f && sc.triCount > 0) {
+    auto meets = [&](float cx, float cy, float cz, float ex, float ey, float ez) {
+      return boxDist2(P0.x, P0.y, P0.z, cx, cy, cz, ex, ey, ez) <= R2;
+    };
+    auto children = [&](int node, float (*cc)[3], float (*ce)[3], int* cr, int& nc) {
+      const float4* n = sc.nodes + 4 * node;
+      const float4 n0 = n[0], n1 = n[1], n2 = n[2];
+      const int4 n3 = reinterpret_cast<const int4*>(n)[3];
+      nc = 0;
+      if (meets(n0.x, n0.y, n0.z, n0.w, n1.x, n1.y)) {
+        cc[nc][0] = n0.x; cc[nc][1] = n0.y; cc[nc][2] = n0.z;
+        ce[nc][0] = n0.w; ce[nc][1] = n1.x; ce[nc][2] = n1.y;
+        cr[nc++] = n3.x;
+      }
+      if (meets(n1.z, n1.w, n2.x, n2.y, n2.z, n2.w)) {
+        cc[nc][0] = n1.z; cc[nc][1] = n1.w; cc[nc][2] = n2.x;
+        ce[nc][0] = n2.y; ce[nc][1] = n2.z; ce[nc][2] = n2.w;
+        cr[nc++] = n3.y;
+      }
+    };
+    float cc[2][3], ce[2][3];
+    int cr[2], nc;
+    children(0, cc, ce, cr, nc);
+    for (int k = 0; k < nc; ++k) {
+      for (int a = 0; a < 3; ++a) {
+        c[count][a] = cc[k][a];
+        e[count][a] = ce[k][a];
+      }
+      ref[count] = cr[k];
+      frozen[count] = false;
+      ++count;
+    }
+    for (int iter = 0; iter < 4 * kCutEntries; ++iter) {
+      int best = -1;
+      float size = -1.f;
+      for (int k = 0; k < count; ++k) {
+        if (ref[k] < 0 || frozen[k]) continue;
+        const float s = fmaxf(e[k][0], fmaxf(e[k][1], e[k][2]));
+        if (s > size) {
+          size = s;
+          best = k;
+        }
+      }
+      if (best < 0) break;
+      children(ref[best], cc, ce, cr, nc);
+      if (count - 1 + nc > kCutEntries) {
+        frozen[best] = true;
+        continue;
+      }
+      if (nc == 0) {  // the box meets the ball but neither child does
+        --count;
+        for (int a = 0; a < 3; ++a) {
+          c[best][a] = c[count][a];
+          e[best][a] = e[count][a];
+        }
+        ref[best] = ref[count];
+        frozen[best] = frozen[count];
+        continue;
+      }
+      for (int a = 0; a < 3; ++a) {
+        c[best][a] = cc[0][a];
+        e[best][a] = ce[0][a];
+      }
+      ref[best] = cr[0];
+      frozen[best] = false;
+      if (nc == 2) {
+        for (int a = 0; a < 3; ++a) {
+          c[count][a] = cc[1][a];
+          e[count][a] = ce[1][a];
+        }
+        ref[count] = cr[1];
+        frozen[count] = false;
+        ++count;
+      }
+    }
+    // far to near
+    for (int i = 1; i < count; ++i)
+      for (int j = i; j > 0; --j) {
+        const float dj = boxDist2(P0.x, P0.y, P0.z, c[j][0], c[j][1], c[j][2], e[j][0], e[j][1], e[j][2]);
+        const float dk =
+            boxDist2(P0.x, P0.y, P0.z, c[j - 1][0], c[j - 1][1], c[j - 1][2], e[j - 1][0], e[j - 1][1], e[j - 1][2]);
+        if (dj <= dk) break;
+        for (int a = 0; a < 3; ++a) {
+          const float tc = c[j][a], te = e[j][a];
+          c[j][a] = c[j - 1][a];
+          e[j][a] = e[j - 1][a];
+          c[j - 1][a] = tc;
+          e[j - 1][a] = te;
+        }
+        const int tr = ref[j];
+        ref[j] = ref[j - 1];
+        ref[j - 1] = tr;
+      }
+  }
+  out[0] = make_float4(__int_as_float(count), rGuard * (1.0f - 1e-4f), 0.f, 0.f);
+  for (int k = 0; k < count; ++k) {
+    out[1 + 2 * k] = make_float4(c[k][0], c[k][1], c[k][2], __int_as_float(ref[k]));
+    out[2 + 2 * k] = make_float4(e[k][0], e[k][1], e[k][2], 0.f);
   }
 }
 
@@ -531,7 +695,11 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
       const Ray ray = setupRay(org, dir, sc.extent);
       Hit h;
-      traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+      if (eye.cuts)
+        traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests,
+                             eye.cuts + static_cast<size_t>(p) * kCutStride, sqrtf(dot(dir, dir)));
+      else
+        traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
       v3 c;
       float b1 = 0.f, b2 = 0.f;
       if (h.id != 0xffffffffu) {
@@ -983,6 +1151,12 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
     if (e != cudaSuccess) return e;
     plan = splitPoses(plan, P);
   }
+  if (eye.cuts) {
+    if (!(eye.cutRadius > 0.f)) return cudaErrorInvalidValue;
+    cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, eye.cutRadius, eye.maxRel, eye.cuts);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   const uint64_t threads = plan.tasks * 32;
   const unsigned block = 128;
   const uint64_t blocks = (threads + block - 1) / block;
@@ -1023,6 +1197,12 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     plan = splitPoses(plan, P);
+  }
+  if (eye.cuts) {
+    if (!(eye.cutRadius > 0.f)) return cudaErrorInvalidValue;
+    cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, eye.cutRadius, eye.maxRel, eye.cuts);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
   const uint64_t blocks = (plan.tasks * 32 + 127) / 128;
   renderKernel<3, 5><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr,

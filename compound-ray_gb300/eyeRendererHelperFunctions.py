@@ -191,6 +191,9 @@ def configureExtras(eyeRenderer):
     L.crMeasureTraversal.restype = c_int
     L.crAutotune.argtypes = [c_void_p, c_size_t, POINTER(c_int), ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crAutotune.restype = c_int
+    L.crSetCutRadius.argtypes = [c_float]
+    L.crSetCutRadius.restype = c_int
+    L.crGetCutRadius.restype = c_float
     L.crSetRenderVariant.argtypes = [c_int]
     L.crSetRenderVariant.restype = c_int
     L.crGetRenderVariant.restype = c_int

@@ -149,6 +149,14 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
  * is not null, crGetRenderVariantCount() timings).  The eye's random streams
  * are restored after every trial, so tuning changes no result.  0 on success. */
 int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant);
+/* Near-field cut: the radius, as a fraction of the scene's largest vertex
+ * coordinate, of the ball around each pose position whose BVH subtrees every
+ * ray searches first (0 = off, the default).  A hit found there within the
+ * ball is final; other rays continue from the root, so results never depend
+ * on it.  crAutotune also picks this radius among 0 and 1/256 .. 1/16.
+ * No counterpart in the reference. */
+int crSetCutRadius(float fractionOfExtent);
+float crGetCutRadius(void);
 int crSetRenderVariant(int variant);
 int crGetRenderVariant(void);
 int crGetRenderVariantCount(void);

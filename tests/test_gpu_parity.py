@@ -352,3 +352,28 @@ def test_raw_samples_projection(lib, small):
     frame = eh.getFrame(lib, n, 12)
     assert (frame[:8, :, 3] == 255).all() and (frame[8:] == 0).all()
     assert frame[:8, :, :3].any()
+
+
+@pytest.mark.parametrize("fraction", [1.0 / 512, 1.0 / 64, 1.0 / 8])
+def test_near_field_cut_changes_no_result(lib, small, tmp_path, fraction):
+    """Rays that search the pose's near-field cut first give the same closest
+    hits, colours and random streams as rays that start at the root, on the
+    small scene (eye among boxes) and the terrain (eye just above ground)."""
+    info = scenes.terrain_scene(str(tmp_path), cells=128, extent=60.0, cones=300, n_omm=1500, poses=12)
+    for path, spp, poses in ((small["gltf"], 32, None), (info["gltf"], 16, info["poses"])):
+        if poses is None:
+            rng = np.random.default_rng(1)
+            poses = np.stack([scenes.pose_rows(np.array([rng.uniform(-6, 6), rng.uniform(0.2, 1.5), rng.uniform(-6, 6)]),
+                                               rng.uniform(0, 6.28)) for _ in range(12)])
+        outs, recs = [], []
+        for f in (0.0, fraction):
+            assert lib.crSetCutRadius(f) == 0
+            _load(lib, path, spp)
+            outs.append(eh.renderPoses(lib, poses))
+            lib.setCameraPosition(*[float(v) for v in poses[3][:3]])
+            lib.setCameraLocalSpace(*[float(v) for v in poses[3][3:]])
+            recs.append(eh.renderFrameRecorded(lib))
+        lib.crSetCutRadius(0.0)
+        assert np.array_equal(outs[0], outs[1])
+        assert np.array_equal(recs[0]["hitId"], recs[1]["hitId"])
+        assert np.array_equal(recs[0]["t"], recs[1]["t"])
