@@ -660,10 +660,17 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
             best = ms if best is None else min(best, ms)
         return best
 
+    # Kernel variant and near-field cut radius for this scene and eye, tuned
+    # on plain 1024-sample renders of four held-out poses (streams restored).
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+    best = ctypes.c_int(0)
+    tune_ms = np.zeros(lib.crGetRenderVariantCount(), np.float32)
+    if lib.crAutotune(d_poses.data_ptr(), 4, ctypes.byref(best), tune_ms) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    cut = float(lib.crGetCutRadius())
     ms_adaptive = timed(adaptive)
     img = d_out.cpu().numpy()
     lev = d_lev.cpu().numpy()
-    lib.setCurrentEyeSamplesPerOmmatidium(1024)
 
     def plain():
         if lib.crRenderPosesDevice(d_poses.data_ptr(), held_poses, d_out.data_ptr()) != 0:
@@ -678,6 +685,7 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
     return {"scene": "heightfield 2048^2 cells + 20000 cones (%d tris, GPU LBVH), %d-ommatidium panoramic eye, "
                      "acceptance 0.5-5 deg" % (info["triangles"], N),
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
+            "autotune": {"variant": best.value, "near_field_cut_fraction": cut},
             "label_histogram": lab_hist, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
             "train_s": t_train, "rmse_vs_plain_1024": rmse, "target_rmse": 1.0 / 255.0,
             "meets_target": rmse <= 1.0 / 255.0,

@@ -261,7 +261,10 @@ size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
 // null, or count x spp records of a single-bucket launch (tests).
 cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
-                           RayRecord* rec, cudaStream_t stream);
+                           RayRecord* rec, cudaStream_t stream, const float4* cuts = nullptr);
+// Near-field cuts of P poses (kCutStride float4 each; see DevEye::cuts).
+cudaError_t launchCuts(const DevScene& scene, const float4* poses, uint32_t P, float radius, float maxRel,
+                       float4* cuts, cudaStream_t stream);
 // Minimum-sample labels: entries with label 0 get `spp` when the standard
 // deviation across the k renders outs[k][rows][3] is below thr in every channel.
 cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, float thr, uint16_t* label,

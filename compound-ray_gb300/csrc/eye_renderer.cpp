@@ -1368,6 +1368,7 @@ void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dpos
     const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
     DevEye de = fe;
     r.withDraws(de, P, true);
+    r.withCuts(de, P, e.maxRel);
     check(launchFeatures(r.dev, de, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
                          r.stream()),
           "feature render");
@@ -1652,9 +1653,15 @@ int crAllocatorAddTrainingPoses(const float* poses12, size_t count, int featureS
           const uint32_t* ent = d.entries.ptr;
           float* part = d.partials.ptr;
           const AdaptiveLaunch L = planAdaptive(&ent, &rows, &c, &part, 1);
+          DevEye ce;
+          r.withCuts(ce, static_cast<uint32_t>(count), e.maxRel);
+          if (ce.cuts)
+            check(launchCuts(r.dev, d.poses.ptr, static_cast<uint32_t>(count), ce.cutRadius, ce.maxRel, ce.cuts, st),
+                  "cuts");
           for (int k = 0; k < seeds; ++k)
             check(launchAdaptive(r.dev, e.omm.ptr, e.N, d.poses.ptr, L, 0x5eed0000ull + static_cast<uint64_t>(k),
-                                 d.labelOuts.ptr + static_cast<size_t>(k) * rows * 3, r.errWord(), nullptr, st),
+                                 d.labelOuts.ptr + static_cast<size_t>(k) * rows * 3, r.errWord(), nullptr, st,
+                                 ce.cuts),
                   "label render");
           check(launchLabels(d.labelOuts.ptr, seeds, rows, c, threshold, d.labels.ptr, st), "labels");
         }
@@ -1786,8 +1793,11 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
               pf += adaptivePartialFloats(cnt[k], spp[k]);
             }
             const AdaptiveLaunch L = planAdaptive(ent, n, spp, part, kAdaptiveBuckets);
+            DevEye ce;
+            r.withCuts(ce, P, e.maxRel);
+            if (ce.cuts) check(launchCuts(r.dev, poses + 4 * first, P, ce.cutRadius, ce.maxRel, ce.cuts, st), "cuts");
             check(launchAdaptive(r.dev, e.omm.ptr, e.N, poses + 4 * first, L, 0xada90000ull + d.adaptiveFrame,
-                                 d.sums.ptr, r.errWord(), nullptr, st),
+                                 d.sums.ptr, r.errWord(), nullptr, st, ce.cuts),
                   "adaptive render");
           }
           check(launchAdaptiveFinish(d.level.ptr, rows, fs, d.stats.ptr, learned, d.sums.ptr, d_out + 3 * first * e.N,
@@ -1834,7 +1844,12 @@ int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long 
         float* pp = part.ptr;
         const uint32_t c = static_cast<uint32_t>(spp);
         const AdaptiveLaunch L = planAdaptive(&ep, &rows, &c, &pp, 1);
-        check(launchAdaptive(r.dev, e.omm.ptr, e.N, d.poses.ptr, L, seed, s.ptr, r.errWord(), rec.ptr, st),
+        DevEye ce;
+        r.withCuts(ce, static_cast<uint32_t>(count), e.maxRel);
+        if (ce.cuts)
+          check(launchCuts(r.dev, d.poses.ptr, static_cast<uint32_t>(count), ce.cutRadius, ce.maxRel, ce.cuts, st),
+                "cuts");
+        check(launchAdaptive(r.dev, e.omm.ptr, e.N, d.poses.ptr, L, seed, s.ptr, r.errWord(), rec.ptr, st, ce.cuts),
               "adaptive render");
         check(cudaMemcpyAsync(records, rec.ptr, rows * spp * sizeof(RayRecord), cudaMemcpyDeviceToHost, st),
               "cudaMemcpy");

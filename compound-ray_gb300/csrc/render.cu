@@ -1281,7 +1281,7 @@ namespace {
 __global__ void __launch_bounds__(128, 5)
     adaptiveKernel(DevScene sc, const float4* __restrict__ omm, uint32_t N, const float4* __restrict__ poses,
                    AdaptiveLaunch L, unsigned long long seed, float* __restrict__ sums, uint32_t* errFlag,
-                   RayRecord* __restrict__ rec) {
+                   RayRecord* __restrict__ rec, const float4* __restrict__ cuts) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // totalTasks < 2^31 (checked at launch)
   if (task >= L.totalTasks) return;
@@ -1326,7 +1326,11 @@ __global__ void __launch_bounds__(128, 5)
       const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
       const Ray ray = setupRay(org, dir, sc.extent);
       Hit h;
-      traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+      if (cuts)
+        traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests, cuts + static_cast<size_t>(p) * kCutStride,
+                            sqrtf(dot(dir, dir)));
+      else
+        traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
       v3 c;
       float b1 = 0.f, b2 = 0.f;
       if (h.id != 0xffffffffu) {
@@ -1553,9 +1557,17 @@ size_t adaptivePartialFloats(uint64_t count, uint32_t spp) {
   return adaptiveChunks(spp) > 1 ? count * adaptiveChunks(spp) * 3 : 0;
 }
 
+cudaError_t launchCuts(const DevScene& scene, const float4* poses, uint32_t P, float radius, float maxRel,
+                       float4* cuts, cudaStream_t stream) {
+  if (P == 0) return cudaSuccess;
+  if (!(radius > 0.f) || !cuts) return cudaErrorInvalidValue;
+  cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, radius, maxRel, cuts);
+  return cudaGetLastError();
+}
+
 cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
-                           RayRecord* rec, cudaStream_t stream) {
+                           RayRecord* rec, cudaStream_t stream, const float4* cuts) {
   if (L.totalTasks == 0) return cudaSuccess;
   if (rec && L.nBuckets != 1) return cudaErrorInvalidValue;
   for (uint32_t k = 0; k < L.nBuckets; ++k) {
@@ -1566,7 +1578,7 @@ cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N,
   if (L.totalTasks >= (1ull << 27)) return cudaErrorInvalidConfiguration;  // 32-bit thread ids
   const uint64_t blocks = (L.totalTasks * 32 + 127) / 128;
   adaptiveKernel<<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
-                                                                      rec);
+                                                                      rec, cuts);
   cudaError_t e = cudaGetLastError();
   for (uint32_t k = 0; k < L.nBuckets && e == cudaSuccess; ++k) {
     if (adaptiveChunks(L.b[k].spp) == 1) continue;

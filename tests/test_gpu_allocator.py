@@ -49,6 +49,16 @@ def test_adaptive_kernel_matches_oracle(lib, small, small_ref):
         want = sc.render_rays(omm, spp, org, dirs)[0]
         sky = (hit < 0).reshape(N, spp).mean(axis=1)[:, None]
         assert (np.abs(sums[p] - want) <= RTOL * np.abs(want) + ATOL + SKY_ATOL * sky).all()
+    # the near-field cut changes no hit and no sum
+    assert lib.crSetCutRadius(1.0 / 64) == 0
+    try:
+        rec2 = np.zeros_like(rec.reshape(-1))
+        sums2 = np.zeros_like(sums)
+        assert lib.crAdaptiveRecord(poses, 2, spp, 7, rec2.ctypes.data, sums2) == 0, eh.lastError(lib)
+    finally:
+        lib.crSetCutRadius(0.0)
+    assert np.array_equal(rec2["hitId"], rec.reshape(-1)["hitId"])
+    assert np.array_equal(sums2, sums)
     # normal / uniform draws look like N(0,1) / U(0,1]
     nd, ud = rec["normalDraw"].ravel(), rec["uniformDraw"].ravel()
     assert abs(nd.mean()) < 0.02 and abs(nd.std() - 1) < 0.02
