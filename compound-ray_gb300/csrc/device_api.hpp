@@ -23,6 +23,13 @@ struct DevScene {
   // and per texture (first texel, width, height, 0).
   const uint32_t* texels = nullptr;
   const int4* texTable = nullptr;
+  // Lighting-on shading (off by default, as the reference's params.lighting):
+  // per triangle in original order 5 float4 (scene.hpp's lighting layout),
+  // and four point lights (position xyz + intensity; colour).
+  const float4* light = nullptr;
+  int lighting = 0;
+  float4 lightPos[4] = {};
+  float4 lightCol[4] = {};
 };
 
 // Samples one width x height RGBA8 texture at n (u, v) coordinates twice:

@@ -123,6 +123,8 @@ struct Renderer {
   DevBuf<float4> nodes, tris, shade;
   DevBuf<uint32_t> texels;
   DevBuf<int4> texTable;
+  DevBuf<float4> light;  // lighting-on data, uploaded when lighting is first used
+  bool lighting = false;  // crSetLighting; off as in the reference (libEyeRenderer.cpp:98)
   DevScene dev;
   std::vector<EyeDev> eyes;  // parallel to scene.cameras
   size_t current = 0;
@@ -158,6 +160,7 @@ struct Renderer {
     shade.release();
     texels.release();
     texTable.release();
+    light.release();
     frame.release();
     poses.release();
     scratch.release();
@@ -260,9 +263,48 @@ struct Renderer {
     }
     dev.texels = texels.ptr;
     dev.texTable = texTable.ptr;
+    applyLighting();
     float ext = 0.f;
     for (float v : scene.triVerts) ext = std::max(ext, std::fabs(v));
     dev.extent = ext;
+  }
+
+  // Lighting-on state of the device scene: the per-triangle data (uploaded on
+  // first use) and the four point lights of libEyeRenderer.cpp:100-118, placed
+  // around the scene's bounding box (centre c, largest extent e):
+  //   c + (e, e, e), c + (-e, e/2, -e/2), c + (0, 4, -5), c + (1, -6, 0).
+  void applyLighting() {
+    dev.lighting = 0;
+    dev.light = nullptr;
+    if (!lighting || !loaded || scene.triangleCount() == 0) return;
+    if (!light.ptr) {
+      const size_t n = scene.triLight.size() / 4;
+      light.ensure(n);
+      check(cudaMemcpyAsync(light.ptr, scene.triLight.data(), n * sizeof(float4), cudaMemcpyHostToDevice, stream()),
+            "cudaMemcpy");
+      check(cudaStreamSynchronize(stream()), "lighting upload");
+    }
+    lightSetup(scene, dev.lightPos, dev.lightCol);
+    dev.light = light.ptr;
+    dev.lighting = 1;
+  }
+
+  static void lightSetup(const SceneData& sc, float4* pos, float4* col) {
+    const f3 lo = sc.sceneMin, hi = sc.sceneMax;
+    const float cx = (lo.x + hi.x) * 0.5f, cy = (lo.y + hi.y) * 0.5f, cz = (lo.z + hi.z) * 0.5f;
+    const float e = std::max(hi.x - lo.x, std::max(hi.y - lo.y, hi.z - lo.z));
+    pos[0] = make_float4(cx + e, cy + e, cz + e, 5.0f);
+    pos[1] = make_float4(cx - e, cy + 0.5f * e, cz - 0.5f * e, 3.0f);
+    pos[2] = make_float4(cx + 0.0f, cy + 4.0f, cz - 5.0f, 5.0f);
+    pos[3] = make_float4(cx + 1.0f, cy - 6.0f, cz + 0.0f, 0.5f);
+    col[0] = make_float4(1.0f, 1.0f, 0.8f, 0.f);
+    col[1] = make_float4(0.8f, 0.8f, 1.0f, 0.f);
+    col[2] = make_float4(1.0f, 1.0f, 0.8f, 0.f);
+    col[3] = make_float4(1.0f, 1.0f, 0.8f, 0.f);
+  }
+
+  void requireUnlit(const char* what) const {
+    if (lighting) throw std::runtime_error(std::string(what) + " renders with lighting off only (crSetLighting(0))");
   }
 
   Camera& cam() {
@@ -997,6 +1039,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
   return guarded(
       "crBatchCreate",
       [&]() -> int {
+        R().requireUnlit("crBatchCreate");
         Renderer& r = R();
         if (!r.loaded) throw std::runtime_error("no scene loaded");
         if (!cams || nCams == 0 || posesPerCam == 0 || !d_poses || !d_out)
@@ -1083,6 +1126,7 @@ int crBatchLaunch(int handle) {
   return guarded(
       "crBatchLaunch",
       [&]() -> int {
+        R().requireUnlit("crBatchLaunch");
         auto it = batches().find(handle);
         if (it == batches().end()) throw std::runtime_error("unknown batch handle");
         if (it->second.generation != R().generation)
@@ -1255,6 +1299,45 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
       -1);
 }
 
+int crSetLighting(int on) {
+  return guarded(
+      "crSetLighting",
+      [&]() -> int {
+        Renderer& r = R();
+        r.lighting = on != 0;
+        if (r.loaded && !r.pendingBvh && !r.pendingGpuBuild) r.applyLighting();
+        return 0;
+      },
+      -1);
+}
+
+int crGetLighting(void) { return R().lighting ? 1 : 0; }
+
+int crGetSceneLighting(float* light, float* lightPos, float* lightCol) {
+  Renderer& r = R();
+  if (!r.loaded) {
+    setError("crGetSceneLighting: no scene loaded");
+    return -1;
+  }
+  if (light) std::memcpy(light, r.scene.triLight.data(), r.scene.triLight.size() * sizeof(float));
+  float4 pos[4], col[4];
+  Renderer::lightSetup(r.scene, pos, col);
+  for (int i = 0; i < 4; ++i) {
+    if (lightPos) {
+      lightPos[4 * i] = pos[i].x;
+      lightPos[4 * i + 1] = pos[i].y;
+      lightPos[4 * i + 2] = pos[i].z;
+      lightPos[4 * i + 3] = pos[i].w;
+    }
+    if (lightCol) {
+      lightCol[3 * i] = col[i].x;
+      lightCol[3 * i + 1] = col[i].y;
+      lightCol[3 * i + 2] = col[i].z;
+    }
+  }
+  return 0;
+}
+
 int crSetCutRadius(float fractionOfExtent) {
   if (!(fractionOfExtent >= 0.f) || fractionOfExtent > 1.f) {
     setError("crSetCutRadius: the fraction must lie in [0, 1]");
@@ -1424,6 +1507,7 @@ int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSp
   return guarded(
       "crDenoiserAddTrainingPoses",
       [&]() -> int {
+        R().requireUnlit("crDenoiserAddTrainingPoses");
         Renderer& r = R();
         DenoiseState& d = DS();
         if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit first");
@@ -1465,6 +1549,7 @@ int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureS
   return guarded(
       "crDenoiserRenderPosesDevice",
       [&]() -> int {
+        R().requireUnlit("crDenoiserRenderPosesDevice");
         Renderer& r = R();
         DenoiseState& d = DS();
         if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit or crDenoiserLoad first");
@@ -1622,6 +1707,7 @@ int crAllocatorAddTrainingPoses(const float* poses12, size_t count, int featureS
   return guarded(
       "crAllocatorAddTrainingPoses",
       [&]() -> int {
+        R().requireUnlit("crAllocatorAddTrainingPoses");
         Renderer& r = R();
         DenoiseState& d = DS();
         if (!d.alloc.ready()) throw std::runtime_error("call crAllocatorInit first");
@@ -1727,6 +1813,7 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
   return guarded(
       "crAdaptiveRenderPosesDevice",
       [&]() -> int {
+        R().requireUnlit("crAdaptiveRenderPosesDevice");
         Renderer& r = R();
         DenoiseState& d = DS();
         if (!d.alloc.ready()) throw std::runtime_error("call crAllocatorInit (and train) or crAllocatorLoad first");
@@ -1820,6 +1907,7 @@ int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long 
   return guarded(
       "crAdaptiveRecord",
       [&]() -> int {
+        R().requireUnlit("crAdaptiveRecord");
         Renderer& r = R();
         DenoiseState& d = DS();
         if (!poses12 || !records || !sums) throw std::runtime_error("null pointer");

@@ -394,6 +394,27 @@ struct Loader {
     return m.textureImage[static_cast<size_t>(t)];
   }
 
+  // Lighting parameters of a material (MulticamScene.cpp:626-715,
+  // cuda/MaterialData.h:42-50): metallic and roughness factors (default 1),
+  // metallic-roughness and normal textures as scene texture indices.
+  void materialLighting(int matIdx, float& metallic, float& roughness, int& mrTex, int& nTex) const {
+    metallic = roughness = 1.0f;
+    mrTex = nTex = -1;
+    if (matIdx < 0) return;
+    const Json& mat = m.doc["materials"][static_cast<size_t>(matIdx)];
+    const Json& pbr = mat["pbrMetallicRoughness"];
+    if (pbr.has("metallicFactor")) metallic = static_cast<float>(pbr["metallicFactor"].asNumber());
+    if (pbr.has("roughnessFactor")) roughness = static_cast<float>(pbr["roughnessFactor"].asNumber());
+    auto texOf = [&](const Json& info) {
+      const int t = info.integer("index", -1);
+      if (t < 0 || static_cast<size_t>(t) >= m.textureImage.size())
+        throw std::runtime_error("material " + std::to_string(matIdx) + ": texture index out of range");
+      return m.textureImage[static_cast<size_t>(t)];
+    };
+    if (pbr.has("metallicRoughnessTexture")) mrTex = texOf(pbr["metallicRoughnessTexture"]);
+    if (mat.has("normalTexture")) nTex = texOf(mat["normalTexture"]);
+  }
+
   void addMesh(const Json& mesh, const double* xf) {
     for (const Json& prim : mesh["primitives"].items()) {
       if (prim.integer("mode", 4) != 4) {
@@ -442,12 +463,39 @@ struct Loader {
       const int tex = ctype == -1 ? matTex : -1;  // vertex colours take precedence
       Accessor ta;
       bool hasUv = false;
-      if (tex >= 0 && attrs.has("TEXCOORD_0")) {
+      if (attrs.has("TEXCOORD_0")) {
         ta = accessor(m, attrs.integer("TEXCOORD_0", -1));
         if (ta.compType == 5121) throw std::runtime_error("gltf accessor component type not supported");
-        if (ta.compType != 5126 || ta.comps != 2) throw std::runtime_error("TEXCOORD_0 must be float VEC2");
-        hasUv = true;
+        if (tex >= 0 && (ta.compType != 5126 || ta.comps != 2)) throw std::runtime_error("TEXCOORD_0 must be float VEC2");
+        hasUv = ta.compType == 5126 && ta.comps == 2;
       }
+      // Lighting data: vertex normals (float VEC3) through the normal matrix.
+      Accessor na;
+      bool hasN = false;
+      if (attrs.has("NORMAL")) {
+        na = accessor(m, attrs.integer("NORMAL", -1));
+        hasN = na.compType == 5126 && na.comps == 3;
+      }
+      double nm[9];  // inverse transpose of the upper 3x3 of xf
+      {
+        const double a = xf[0], b = xf[1], c = xf[2], d = xf[4], e = xf[5], f = xf[6], g = xf[8], h = xf[9],
+                     i = xf[10];
+        const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+        const double id = det != 0.0 ? 1.0 / det : 0.0;
+        // cofactor matrix / det = inverse transpose
+        nm[0] = (e * i - f * h) * id;
+        nm[1] = -(d * i - f * g) * id;
+        nm[2] = (d * h - e * g) * id;
+        nm[3] = -(b * i - c * h) * id;
+        nm[4] = (a * i - c * g) * id;
+        nm[5] = -(a * h - b * g) * id;
+        nm[6] = (b * f - c * e) * id;
+        nm[7] = -(a * f - c * d) * id;
+        nm[8] = (a * e - b * d) * id;
+      }
+      float metallic, roughness;
+      int mrTex, nTex;
+      materialLighting(prim.integer("material", -1), metallic, roughness, mrTex, nTex);
 
       // Indices (u8 / u16 / u32); a primitive without indices has no triangles,
       // as a build input with zero index triplets in the reference.
@@ -488,6 +536,24 @@ struct Loader {
         }
         s.triColours.insert(s.triColours.end(), cols, cols + 12);
         s.triShading.push_back(ctype != -1 ? kShadeVertexColour : tex >= 0 ? kShadeTexture : kShadeBaseColour);
+        float lt[kLightFloats];
+        static const float kDefaultUv[6] = {0.f, 0.f, 0.f, 1.f, 1.f, 0.f};
+        for (int k = 0; k < 3; ++k) {
+          const uint32_t vi = ia.getU(3 * t + static_cast<size_t>(k));
+          for (int q = 0; q < 3; ++q) lt[3 * k + q] = 0.f;
+          if (hasN && vi < na.count) {
+            const double n0 = na.getF(vi, 0), n1 = na.getF(vi, 1), n2 = na.getF(vi, 2);
+            for (int q = 0; q < 3; ++q) lt[3 * k + q] = static_cast<float>(nm[3 * q] * n0 + nm[3 * q + 1] * n1 + nm[3 * q + 2] * n2);
+          }
+          lt[9 + 2 * k] = hasUv && vi < ta.count ? ta.getF(vi, 0) : kDefaultUv[2 * k];
+          lt[10 + 2 * k] = hasUv && vi < ta.count ? ta.getF(vi, 1) : kDefaultUv[2 * k + 1];
+        }
+        lt[15] = metallic;
+        lt[16] = roughness;
+        lt[17] = static_cast<float>(mrTex);
+        lt[18] = static_cast<float>(nTex);
+        lt[19] = static_cast<float>((hasN ? 1 : 0) | (hasUv ? 2 : 0));
+        s.triLight.insert(s.triLight.end(), lt, lt + kLightFloats);
       }
       mp.triCount = static_cast<uint32_t>(triCount);
       s.meshes.push_back(mp);

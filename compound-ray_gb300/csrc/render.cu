@@ -241,7 +241,7 @@ __device__ __forceinline__ void childSpan(const Ray& r, float cx, float cy, floa
 
 // Traversal loop over the BVH2 from `node`, with `sp` deferred entries
 // already on the stack; updates the closest hit `h`.
-template <bool kCount>
+template <bool kCount, bool kAnyHit = false>
 __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack, int sp,
                                              int node, uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests) {
   for (;;) {
@@ -288,6 +288,7 @@ __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, f
         const float4* t = sc.tris + 3 * (first + k);
         testTriangle(r, __ldg(t), __ldg(t + 1), __ldg(t + 2), first + k, tmin, h);
       }
+      if (kAnyHit && h.id != 0xffffffffu) return;  // occlusion query: any hit will do
     }
     if (sp == 0) return;
     node = stack[--sp];
@@ -544,6 +545,101 @@ __device__ __forceinline__ v3 shadeHit(const DevScene& sc, uint32_t pos, float b
 
 #define CR_PI_F 3.14159265358979323846f
 
+// ---------------------------------------------------------------------------
+// Lighting-on closest hit (shaders.cu:812-880): GGX/Smith shading of four
+// point lights with shadow rays, from the base colour above.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ v3 vmul(v3 a, v3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+
+// shaders.cu:67-90
+__device__ __forceinline__ v3 schlick(v3 spec, float VdH) {
+  const float f = powf(1.0f - VdH, 5.0f);
+  return spec + vmul(mk(1.0f, 1.0f, 1.0f) - spec, mk(f, f, f));
+}
+__device__ __forceinline__ float smithVis(float NdL, float NdV, float alpha) {
+  const float a2 = alpha * alpha;
+  const float ggx0 = NdL * sqrtf(NdV * NdV * (1.0f - a2) + a2);
+  const float ggx1 = NdV * sqrtf(NdL * NdL * (1.0f - a2) + a2);
+  return 2.0f * NdL * NdV / (ggx0 + ggx1);
+}
+__device__ __forceinline__ float ggxNormal(float NdH, float alpha) {
+  const float a2 = alpha * alpha;
+  const float x = NdH * NdH * (a2 - 1.0f) + 1.0f;
+  return a2 / (CR_PI_F * x * x);
+}
+
+// Occlusion query (shaders.cu:140-163): any triangle in [tmin, tmax].
+__device__ __forceinline__ bool occluded(const DevScene& sc, v3 o, v3 d, float tmin, float tmax, uint32_t* errFlag) {
+  const Ray r = setupRay(o, d, sc.extent);
+  Hit h;
+  h.t = tmax;
+  h.id = 0xffffffffu;
+  h.pos = 0;
+  int stack[kStackSize];
+  uint32_t nv = 0, tt = 0;
+  traverseFrom<false, true>(sc, r, tmin, h, stack, 0, 0, errFlag, nv, tt);
+  return h.id != 0xffffffffu;
+}
+
+__device__ v3 shadeLit(const DevScene& sc, const Hit& h, float b1, float b2, v3 dir, v3 base, uint32_t* errFlag) {
+  const float4* L = sc.light + 5 * static_cast<size_t>(h.id);
+  const float4 l0 = __ldg(L), l1 = __ldg(L + 1), l2 = __ldg(L + 2), l3 = __ldg(L + 3), l4 = __ldg(L + 4);
+  const float4* t = sc.tris + 3 * h.pos;
+  const float4 q0 = __ldg(t), q1 = __ldg(t + 1), q2 = __ldg(t + 2);
+  const v3 P0 = mk(q0.x, q0.y, q0.z), P1 = mk(q1.x, q1.y, q1.z), P2 = mk(q2.x, q2.y, q2.z);
+  const float w0 = 1.0f - b1 - b2;
+  const v3 P = P0 * w0 + P1 * b1 + P2 * b2;
+  const int flags = static_cast<int>(l4.w);
+  const v3 Ng = normalize(cross(P1 - P0, P2 - P0));
+  v3 N = Ng;
+  if (flags & 1) N = normalize(mk(l0.x, l0.y, l0.z) * w0 + mk(l0.w, l1.x, l1.y) * b1 + mk(l1.z, l1.w, l2.x) * b2);
+  const float u0 = l2.y, v0 = l2.z, u1 = l2.w, v1 = l3.x, u2 = l3.y, v2 = l3.z;
+  float U = b1, Vt = b2;  // without TEXCOORD_0 the coordinates are the barycentrics (LocalGeometry.h:99-102)
+  if (flags & 2) {
+    U = w0 * u0 + b1 * u1 + b2 * u2;
+    Vt = w0 * v0 + b1 * v1 + b2 * v2;
+  }
+  float metallic = l3.w, roughness = l4.x;
+  const int mrTex = static_cast<int>(l4.y), nTex = static_cast<int>(l4.z);
+  if (mrTex >= 0) {  // (occlusion, roughness, metallic)
+    const float4 mr = sampleTexture(sc.texels, __ldg(sc.texTable + mrTex), U, Vt);
+    roughness *= mr.y;
+    metallic *= mr.z;
+  }
+  const float F0 = 0.04f;
+  const v3 diff = base * ((1.0f - F0) * (1.0f - metallic));
+  const v3 spec = mk(F0, F0, F0) + (base - mk(F0, F0, F0)) * metallic;
+  const float alpha = roughness * roughness;
+  if (nTex >= 0) {
+    const float4 T = sampleTexture(sc.texels, __ldg(sc.texTable + nTex), U, Vt);
+    const float du1 = u0 - u2, du2 = u1 - u2, dv1 = v0 - v2, dv2 = v1 - v2;
+    const v3 dp1 = P0 - P2, dp2 = P1 - P2;
+    const float invdet = 1.f / (du1 * dv2 - dv1 * du2);
+    const v3 dpdu = (dp1 * dv2 - dp2 * dv1) * invdet;
+    const v3 dpdv = (dp1 * -du2 + dp2 * du1) * invdet;
+    N = normalize(normalize(dpdu) * (2.0f * T.x - 1.0f) + normalize(dpdv) * (2.0f * T.y - 1.0f) + N * (2.0f * T.z - 1.0f));
+  }
+  const v3 V = normalize(dir) * -1.0f;
+  v3 result = mk(0.f, 0.f, 0.f);
+  for (int i = 0; i < 4; ++i) {
+    const float4 lp = sc.lightPos[i], lc = sc.lightCol[i];
+    const v3 Lv = mk(lp.x, lp.y, lp.z) - P;
+    const float Ldist = sqrtf(dot(Lv, Lv));
+    const v3 Ld = Lv * (1.0f / Ldist);
+    const v3 H = normalize(Ld + V);
+    const float NdL = dot(N, Ld), NdV = dot(N, V), NdH = dot(N, H), VdH = dot(V, H);
+    if (NdL > 0.0f && NdV > 0.0f && !occluded(sc, P, Ld, 0.001f, Ldist - 0.001f, errFlag)) {
+      const v3 F = schlick(spec, VdH);
+      const float G = smithVis(NdL, NdV, alpha);
+      const float D = ggxNormal(NdH, alpha);
+      const v3 d = vmul(mk(1.0f, 1.0f, 1.0f) - F, diff) * (1.0f / CR_PI_F);
+      const v3 s = F * (G * D);
+      result = result + vmul(mk(lc.x, lc.y, lc.z) * (lp.w * NdL), d + s);
+    }
+  }
+  return result;
+}
+
 __device__ __forceinline__ v3 shadeMiss(int miss, v3 dirIn) {
   const v3 dir = normalize(dirIn);
   if (miss == 1) {
@@ -629,9 +725,10 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
                                            uint32_t P, const WarpPlan& plan, uint64_t task, float* __restrict__ out,
                                            float* __restrict__ scratch, uint32_t* errFlag,
                                            RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests) {
-  constexpr bool kRecord = kMode == 1;
-  constexpr bool kCount = kMode == 2;
-  constexpr bool kFeat = kMode == 3;
+  constexpr bool kRecord = (kMode & 3) == 1;
+  constexpr bool kCount = (kMode & 3) == 2;
+  constexpr bool kFeat = (kMode & 3) == 3;
+  constexpr bool kLit = (kMode & 4) != 0;  // lighting-on shading (modes 4 render, 5 record)
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t p0 = 0, p1 = P;
   if (plan.poseSplits > 1) {
@@ -706,6 +803,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
         b1 = xdiv(h.V, h.det);
         b2 = xdiv(h.W, h.det);
         c = shadeHit(sc, h.pos, b1, b2);
+        if (kLit) c = shadeLit(sc, h, b1, b2, dir, c, errFlag);
       } else {
         c = shadeMiss(sc.miss, dir);
       }
@@ -1162,7 +1260,13 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
   const uint64_t blocks = (threads + block - 1) / block;
   if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
   const unsigned g = static_cast<unsigned>(blocks);
-  if (rec) {
+  if (scene.lighting && !stats) {
+    if (!scene.light) return cudaErrorInvalidValue;
+    if (rec)
+      renderKernel<5, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
+    else
+      renderKernel<4, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+  } else if (rec) {
     renderKernel<1, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
   } else if (stats) {
     renderKernel<2, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats);

@@ -73,6 +73,8 @@ struct HitboxMesh {
 
 enum class MissShader { DefaultBackground = 0, SimpleSky = 1 };
 
+constexpr int kLightFloats = 20;
+
 // How a triangle's hit colour is found (shaders.cu:788-811).
 enum : uint8_t {
   kShadeBaseColour = 0,    // material base colour factor as is
@@ -96,6 +98,17 @@ struct SceneData {
   //   kShadeTexture:      (u, v, texture index, 0) at each vertex.
   std::vector<float> triColours;
   std::vector<uint8_t> triShading;  // one kShade* per triangle
+  // Lighting-on shading data (kLightFloats per triangle, original order):
+  //   0-8   vertex normals n0, n1, n2 in world space (the object normals times
+  //         the inverse transpose of the node transform, not normalised;
+  //         zero without NORMAL)
+  //   9-14  texture coordinates uv0, uv1, uv2 (TEXCOORD_0, else (0,0) (0,1)
+  //         (1,0) as cuda/LocalGeometry.h:99-101)
+  //   15    metallic factor, 16 roughness factor (default 1, 1)
+  //   17    metallic-roughness texture (scene texture index, -1 none)
+  //   18    normal texture (-1 none)
+  //   19    flags: 1 = vertex normals, 2 = TEXCOORD_0 present
+  std::vector<float> triLight;
   std::vector<uint32_t> texels;     // RGBA8 (r in the low byte) of every texture
   std::vector<Texture> textures;
   std::vector<MeshPrim> meshes;

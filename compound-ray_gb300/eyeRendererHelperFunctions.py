@@ -191,6 +191,11 @@ def configureExtras(eyeRenderer):
     L.crMeasureTraversal.restype = c_int
     L.crAutotune.argtypes = [c_void_p, c_size_t, POINTER(c_int), ndpointer(np.float32, flags="C_CONTIGUOUS")]
     L.crAutotune.restype = c_int
+    L.crSetLighting.argtypes = [c_int]
+    L.crSetLighting.restype = c_int
+    L.crGetLighting.restype = c_int
+    L.crGetSceneLighting.argtypes = [c_void_p, c_void_p, c_void_p]
+    L.crGetSceneLighting.restype = c_int
     L.crSetCutRadius.argtypes = [c_float]
     L.crSetCutRadius.restype = c_int
     L.crGetCutRadius.restype = c_float
@@ -305,6 +310,16 @@ def compareTextureSampling(eyeRenderer, texels, width, height, uv):
     if eyeRenderer.crCompareTextureSampling(texels, int(width), int(height), uv.reshape(-1), len(uv), soft, hard) != 0:
         raise RuntimeError(lastError(eyeRenderer))
     return soft, hard
+
+
+def getSceneLighting(eyeRenderer):
+    """(T, 20) lighting-on records, (4, 4) light positions + intensities, (4, 3) colours."""
+    light = np.zeros((eyeRenderer.crGetTriangleCount(), 20), np.float32)
+    pos = np.zeros((4, 4), np.float32)
+    col = np.zeros((4, 3), np.float32)
+    if eyeRenderer.crGetSceneLighting(light.ctypes.data, pos.ctypes.data, col.ctypes.data) != 0:
+        raise RuntimeError(lastError(eyeRenderer))
+    return light, pos, col
 
 
 def getOmmatidia(eyeRenderer):

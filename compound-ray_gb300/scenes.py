@@ -208,14 +208,30 @@ class GltfBuilder:
         self.accessors.append(acc)
         return len(self.accessors) - 1
 
-    def material(self, rgba, name="mat"):
-        self.materials.append({"name": name, "pbrMetallicRoughness": {"baseColorFactor": [float(c) for c in rgba]}})
+    def material(self, rgba, name="mat", metallic=None, roughness=None, mr_texture=None, normal_texture=None,
+                 base_texture=None):
+        pbr = {"baseColorFactor": [float(c) for c in rgba]}
+        if metallic is not None:
+            pbr["metallicFactor"] = float(metallic)
+        if roughness is not None:
+            pbr["roughnessFactor"] = float(roughness)
+        if mr_texture is not None:
+            pbr["metallicRoughnessTexture"] = {"index": int(mr_texture)}
+        if base_texture is not None:
+            pbr["baseColorTexture"] = {"index": int(base_texture)}
+        mat = {"name": name, "pbrMetallicRoughness": pbr}
+        if normal_texture is not None:
+            mat["normalTexture"] = {"index": int(normal_texture)}
+        self.materials.append(mat)
         return len(self.materials) - 1
 
     def mesh(self, name, positions, indices, colours=None, material=None, translation=None, rotation=None,
-             scale=None, matrix=None, index_type=None, colour_type=5126, extras=None, texcoords=None):
+             scale=None, matrix=None, index_type=None, colour_type=5126, extras=None, texcoords=None,
+             normals=None):
         positions = np.asarray(positions, np.float32).reshape(-1, 3)
         attrs = {"POSITION": self.accessor(positions, 5126, "VEC3", minmax=True)}
+        if normals is not None:
+            attrs["NORMAL"] = self.accessor(np.asarray(normals, np.float32).reshape(-1, 3), 5126, "VEC3")
         if texcoords is not None:
             attrs["TEXCOORD_0"] = self.accessor(np.asarray(texcoords, np.float32).reshape(-1, 2), 5126, "VEC2")
         if colours is not None:
@@ -559,6 +575,62 @@ def fixture_scene(npz, variant, outdir):
                                      "compound-projection": str(z[key + "__projection"])}})
         g.nodes.append({"name": str(name), "camera": len(g.cameras) - 1, "matrix": matrix})
     return g.write(os.path.join(outdir, variant + ".gltf"), embed=True)
+
+
+def lit_scene(outdir, seed=SEED, n_omm=600, spp=16):
+    """A scene for the lighting-on path: a ground quad with vertex normals,
+    a base-colour texture and a normal texture; 24 boxes, half with smooth
+    vertex normals (corner directions) and half with flat normals, on
+    materials of random metallic / roughness factors, some with a
+    metallic-roughness texture and some with a normal texture, a few under a
+    rotated and uniformly scaled node; simple_sky.  Returns the small-scene
+    dict."""
+    os.makedirs(outdir, exist_ok=True)
+    rng = np.random.default_rng(seed + 13)
+    g = GltfBuilder()
+    g.scene_extras = {"background-shader": "simple_sky"}
+    rgb = rng.integers(0, 256, size=(16, 16, 3), dtype=np.uint8)
+    t_base = g.texture(g.image(png_bytes(rgb, colour_type=2)))
+    nrm = np.clip(np.stack([rng.normal(0.5, 0.08, (8, 8)), rng.normal(0.5, 0.08, (8, 8)),
+                            rng.uniform(0.85, 1.0, (8, 8))], axis=2) * 255, 0, 255).astype(np.uint8)
+    t_norm = g.texture(g.image(png_bytes(nrm, colour_type=2)))
+    mr = np.stack([np.full((8, 8), 255), rng.integers(60, 256, (8, 8)), rng.integers(0, 256, (8, 8))],
+                  axis=2).astype(np.uint8)
+    t_mr = g.texture(g.image(png_bytes(mr, colour_type=2)))
+    ground = np.array([[-10, 0, -10], [10, 0, -10], [10, 0, 10], [-10, 0, 10]], np.float64)
+    g.mesh("ground", ground, np.array([[0, 2, 1], [0, 3, 2]]),
+           material=g.material([1, 1, 1, 1], metallic=0.0, roughness=0.7, base_texture=t_base, normal_texture=t_norm),
+           texcoords=np.array([[0, 0], [4, 0], [4, 4], [0, 4]], np.float32), normals=np.tile([0, 1, 0], (4, 1)))
+    placed = 0
+    while placed < 24:
+        c = rng.uniform(-7.0, 7.0, size=2)
+        e = rng.uniform(0.3, 1.6, size=3)
+        if abs(c[0]) < e[0] / 2 + 0.4 and abs(c[1]) < e[2] / 2 + 0.4:
+            continue
+        v, f = box_mesh([c[0] - e[0] / 2, 0.0, c[1] - e[2] / 2], [c[0] + e[0] / 2, e[1], c[1] + e[2] / 2])
+        kw = {}
+        if placed % 2 == 0:
+            centre = v.mean(axis=0)
+            n = v - centre
+            kw["normals"] = n / np.linalg.norm(n, axis=1, keepdims=True)
+        if placed % 3 == 0:
+            kw["texcoords"] = rng.uniform(-1, 2, size=(8, 2)).astype(np.float32)
+        mat = g.material(np.concatenate([rng.uniform(0.1, 1.0, 3), [1.0]]), metallic=rng.uniform(0, 1),
+                         roughness=rng.uniform(0.2, 1.0), mr_texture=t_mr if placed % 4 == 1 else None,
+                         normal_texture=t_norm if placed % 4 == 2 else None)
+        if placed >= 20:  # rotated and uniformly scaled about the origin
+            g.mesh("rbox%d" % placed, v * 0.5, f, material=mat, rotation=[0.0, math.sin(0.3), 0.0, math.cos(0.3)],
+                   scale=[1.5, 1.5, 1.5], **kw)
+        else:
+            g.mesh("box%d" % placed, v, f, material=mat, **kw)
+        placed += 1
+    d = fibonacci_sphere(n_omm)
+    eye_path = os.path.join(outdir, "lit.eye")
+    write_eye(eye_path, d * 0.001, d, 3.0 * DEG, 0.0)
+    g.compound_camera("insect-eye", "lit.eye", translation=[0.0, 0.5, 0.0])
+    path = g.write(os.path.join(outdir, "lit.gltf"), embed=True)
+    pose = pose_rows(np.array([0.0, 0.5, 0.0]), 0.0)
+    return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm}
 
 
 def terrain_height_fn(heights, extent):

@@ -156,6 +156,21 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
  * on it.  crAutotune also picks this radius among 0 and 1/256 .. 1/16.
  * No counterpart in the reference. */
 int crSetCutRadius(float fractionOfExtent);
+/* Lighting-on shading (shaders.cu:812-880): 1 = the GGX/Smith path with four
+ * point lights around the scene's bounding box and shadow rays, from metallic
+ * / roughness factors, metallic-roughness and normal textures and vertex
+ * normals; 0 = off, the default (the reference's params.lighting is false,
+ * libEyeRenderer.cpp:98).  The plain render entry points honour it; batched,
+ * learned and adaptive renders refuse to run while it is on.  No counterpart
+ * in the reference's API. */
+int crSetLighting(int on);
+int crGetLighting(void);
+/* The loaded scene's lighting-on data: 20 floats per triangle (world vertex
+ * normals n0 n1 n2, texture coordinates uv0 uv1 uv2, metallic, roughness,
+ * metallic-roughness texture, normal texture, flags 1 = normals 2 = texture
+ * coordinates), the four lights' position + intensity (16 floats) and
+ * colours (12 floats).  Null pointers are skipped.  0 on success. */
+int crGetSceneLighting(float* light, float* lightPos, float* lightCol);
 float crGetCutRadius(void);
 int crSetRenderVariant(int variant);
 int crGetRenderVariant(void);

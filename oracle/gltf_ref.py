@@ -207,6 +207,8 @@ class RefScene:
         self.verts = []
         self.colours = []
         self.flags = []
+        self.light = []  # (T, 20) lighting-on records per primitive
+        self.world_boxes = []  # (lo, hi) float32 per primitive
         self.images = []  # (h, w, 4) uint8 per image
         self.meshes = []  # (name, tri offset, tri count)
         self.cameras = []
@@ -225,6 +227,22 @@ class RefScene:
         else:
             v, c, f = np.zeros((0, 3, 3), np.float32), np.zeros((0, 3, 4), np.float32), np.zeros(0, np.uint8)
         return v, c, f
+
+    def lighting(self):
+        """Lighting-on data: (T, 20) records, light positions + intensities
+        (4, 4) and colours (4, 3) around the scene box (libEyeRenderer.cpp:100-118)."""
+        light = np.concatenate(self.light).astype(np.float32) if self.light else np.zeros((0, 20), np.float32)
+        lo = np.min([b[0] for b in self.world_boxes], axis=0).astype(np.float32)
+        hi = np.max([b[1] for b in self.world_boxes], axis=0).astype(np.float32)
+        c = ((lo + hi) * np.float32(0.5)).astype(np.float32)
+        e = np.float32((hi - lo).max())
+        f = np.float32
+        pos = np.array([[c[0] + e, c[1] + e, c[2] + e, 5.0],
+                        [c[0] - e, c[1] + f(0.5) * e, c[2] - f(0.5) * e, 3.0],
+                        [c[0] + f(0.0), c[1] + f(4.0), c[2] - f(5.0), 5.0],
+                        [c[0] + f(1.0), c[1] - f(6.0), c[2] + f(0.0), 0.5]], np.float32)
+        col = np.array([[1.0, 1.0, 0.8], [0.8, 0.8, 1.0], [1.0, 1.0, 0.8], [1.0, 1.0, 0.8]], np.float32)
+        return light, pos, col
 
     def textures(self):
         """(table (K,3) of first texel / width / height, uint32 texels)."""
@@ -341,7 +359,7 @@ def load(path):
             for prim in mesh["primitives"]:
                 if prim.get("mode", 4) != 4:
                     continue
-                pos, _ = accessor(prim["attributes"]["POSITION"])
+                pos, pacc = accessor(prim["attributes"]["POSITION"])
                 off = sum(len(v) for v in sc.verts)
                 if "indices" not in prim:
                     sc.meshes.append((mesh.get("name", ""), off, 0))
@@ -390,6 +408,53 @@ def load(path):
                     sc.colours.append(vcol[tri])
                 sc.verts.append(world[tri])
                 sc.flags.append(np.full(len(tri), flag, np.uint8))
+                # lighting-on records
+                lo = np.array(pacc["min"], np.float32) if "min" in pacc else pos.min(axis=0)
+                hi = np.array(pacc["max"], np.float32) if "max" in pacc else pos.max(axis=0)
+                corners = np.array([[hi[0] if c & 1 else lo[0], hi[1] if c & 2 else lo[1], hi[2] if c & 4 else lo[2]]
+                                    for c in range(8)], np.float64)
+                cx, cy, cz = _apply(xf, corners[:, 0], corners[:, 1], corners[:, 2], 1.0)
+                cw = np.stack([cx, cy, cz], axis=1)
+                sc.world_boxes.append((cw.min(axis=0).astype(np.float32), cw.max(axis=0).astype(np.float32)))
+                a, b_, c_, d, e, f, g, h, i = xf[0], xf[1], xf[2], xf[4], xf[5], xf[6], xf[8], xf[9], xf[10]
+                det = a * (e * i - f * h) - b_ * (d * i - f * g) + c_ * (d * h - e * g)
+                idt = 1.0 / det if det != 0.0 else 0.0
+                nm = [(e * i - f * h) * idt, -(d * i - f * g) * idt, (d * h - e * g) * idt,
+                      -(b_ * i - c_ * h) * idt, (a * i - c_ * g) * idt, -(a * h - b_ * g) * idt,
+                      (b_ * f - c_ * e) * idt, -(a * f - c_ * d) * idt, (a * e - b_ * d) * idt]
+                rec = np.zeros((len(tri), 20), np.float32)
+                lflags = 0
+                if "NORMAL" in prim["attributes"]:
+                    nrm, nacc = accessor(prim["attributes"]["NORMAL"])
+                    if nacc["componentType"] == 5126 and nacc["type"] == "VEC3":
+                        lflags |= 1
+                        n64 = nrm.astype(np.float64)
+                        wn = np.stack([nm[3 * q] * n64[:, 0] + nm[3 * q + 1] * n64[:, 1] + nm[3 * q + 2] * n64[:, 2]
+                                       for q in range(3)], axis=1).astype(np.float32)
+                        rec[:, 0:9] = wn[tri].reshape(len(tri), 9)
+                uvs = np.tile(np.array([0, 0, 0, 1, 1, 0], np.float32), (len(tri), 1))
+                if "TEXCOORD_0" in prim["attributes"]:
+                    uv, uacc = accessor(prim["attributes"]["TEXCOORD_0"])
+                    if uacc["componentType"] == 5126 and uacc["type"] == "VEC2":
+                        lflags |= 2
+                        uvs = uv.astype(np.float32)[tri].reshape(len(tri), 6)
+                rec[:, 9:15] = uvs
+                met, rough, mrt, nt = 1.0, 1.0, -1, -1
+                if mat is not None and mat >= 0:
+                    m_ = doc["materials"][mat]
+                    pb = m_.get("pbrMetallicRoughness", {})
+                    met = pb.get("metallicFactor", 1.0)
+                    rough = pb.get("roughnessFactor", 1.0)
+                    if "metallicRoughnessTexture" in pb:
+                        mrt = tex_image[pb["metallicRoughnessTexture"]["index"]]
+                    if "normalTexture" in m_:
+                        nt = tex_image[m_["normalTexture"]["index"]]
+                rec[:, 15] = np.float32(met)
+                rec[:, 16] = np.float32(rough)
+                rec[:, 17] = mrt
+                rec[:, 18] = nt
+                rec[:, 19] = lflags
+                sc.light.append(rec)
                 sc.meshes.append((mesh.get("name", ""), off, len(tri)))
         else:
             for c in n.get("children", []):

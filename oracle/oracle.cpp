@@ -15,6 +15,10 @@
 //                           linear / normalised-coordinate sampler), filtered
 //                           by the texture unit's documented bilinear rule
 //                           with weights in 1/256 steps
+//   lighting-on hit ....... libEyeRenderer3/shaders.cu:60-90, 812-880 (GGX /
+//                           Smith, four point lights of
+//                           libEyeRenderer.cpp:100-118, shadow rays as the
+//                           closest-hit search limited to [0.001, d - 0.001])
 //   miss programs ......... libEyeRenderer3/shaders.cu:740-756
 //   sample scaling/sum .... libEyeRenderer3/shaders.cu:730, 341-347
 //   make_color ............ libEyeRenderer3/shaders.cu:180-189
@@ -68,6 +72,11 @@ struct Scene {
   std::vector<uint8_t> f; // shading kind: 0 base colour, 1 vertex colours, 2 texture
   std::vector<uint32_t> texels;  // RGBA8, red in the low byte
   std::vector<int32_t> texTable; // per texture: first texel, width, height
+  // lighting-on data: 20 floats per triangle (normals, uvs, metallic,
+  // roughness, mr texture, normal texture, flags) and four lights
+  std::vector<float> light;
+  int lighting = 0;
+  float lightPos[4][4] = {}, lightCol[4][3] = {};
   // BVH: nodes with a box and either two children or a triangle range.
   struct Node {
     double lo[3], hi[3];
@@ -377,7 +386,7 @@ void sampleTexture(const uint32_t* tx, int width, int height, float u, float v, 
   }
 }
 
-V3 shadeHit(const Scene& s, uint32_t t, float b1, float b2) {
+V3 baseColour(const Scene& s, uint32_t t, float b1, float b2) {
   const float* c = &s.c[12 * t];
   if (!s.f[t]) return mk(c[0], c[1], c[2]);
   const float w0 = 1.0f - b1 - b2;
@@ -393,6 +402,98 @@ V3 shadeHit(const Scene& s, uint32_t t, float b1, float b2) {
   }
   const V3 C = mk(w0 * c[0] + b1 * c[4] + b2 * c[8], w0 * c[1] + b1 * c[5] + b2 * c[9], w0 * c[2] + b1 * c[6] + b2 * c[10]);
   return mk(std::pow(C.x, 2.2f), std::pow(C.y, 2.2f), std::pow(C.z, 2.2f));
+}
+
+Hit32 trace32(const Scene& s, const float* o, const float* d, float tmin, float tmax);
+
+V3 vmul(V3 a, V3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+
+// shaders.cu:67-90
+V3 schlick(V3 spec, float VdH) {
+  const float f = std::pow(1.0f - VdH, 5.0f);
+  return add(spec, vmul(sub(mk(1, 1, 1), spec), mk(f, f, f)));
+}
+float smithVis(float NdL, float NdV, float alpha) {
+  const float a2 = alpha * alpha;
+  const float ggx0 = NdL * std::sqrt(NdV * NdV * (1.0f - a2) + a2);
+  const float ggx1 = NdV * std::sqrt(NdL * NdL * (1.0f - a2) + a2);
+  return 2.0f * NdL * NdV / (ggx0 + ggx1);
+}
+float ggxNormal(float NdH, float alpha) {
+  const float a2 = alpha * alpha;
+  const float x = NdH * NdH * (a2 - 1.0f) + 1.0f;
+  return a2 / (kPi * x * x);
+}
+
+// Lighting-on shading of a hit with base colour `base` (shaders.cu:812-880).
+V3 shadeLit(const Scene& s, uint32_t t, float b1, float b2, V3 dir, V3 base) {
+  const float* L = &s.light[20 * static_cast<size_t>(t)];
+  const float* v = &s.v[9 * static_cast<size_t>(t)];
+  const V3 P0 = mk(v[0], v[1], v[2]), P1 = mk(v[3], v[4], v[5]), P2 = mk(v[6], v[7], v[8]);
+  const float w0 = 1.0f - b1 - b2;
+  const V3 P = add(add(scl(w0, P0), scl(b1, P1)), scl(b2, P2));
+  const int flags = static_cast<int>(L[19]);
+  V3 N = normalize(cross(sub(P1, P0), sub(P2, P0)));
+  if (flags & 1)
+    N = normalize(add(add(scl(w0, mk(L[0], L[1], L[2])), scl(b1, mk(L[3], L[4], L[5]))), scl(b2, mk(L[6], L[7], L[8]))));
+  const float u0 = L[9], v0 = L[10], u1 = L[11], v1 = L[12], u2 = L[13], v2 = L[14];
+  float U = b1, Vt = b2;
+  if (flags & 2) {
+    U = w0 * u0 + b1 * u1 + b2 * u2;
+    Vt = w0 * v0 + b1 * v1 + b2 * v2;
+  }
+  float metallic = L[15], roughness = L[16];
+  const int mrTex = static_cast<int>(L[17]), nTex = static_cast<int>(L[18]);
+  auto sample = [&](int tex, float* rgba) {
+    const int32_t* e = &s.texTable[3 * static_cast<size_t>(tex)];
+    sampleTexture(&s.texels[static_cast<size_t>(e[0])], e[1], e[2], U, Vt, rgba);
+  };
+  if (mrTex >= 0) {
+    float mr[4];
+    sample(mrTex, mr);
+    roughness *= mr[1];
+    metallic *= mr[2];
+  }
+  const float F0 = 0.04f;
+  const V3 diff = scl((1.0f - F0) * (1.0f - metallic), base);
+  const V3 spec = add(mk(F0, F0, F0), scl(metallic, sub(base, mk(F0, F0, F0))));
+  const float alpha = roughness * roughness;
+  if (nTex >= 0) {
+    float T[4];
+    sample(nTex, T);
+    const float du1 = u0 - u2, du2 = u1 - u2, dv1 = v0 - v2, dv2 = v1 - v2;
+    const V3 dp1 = sub(P0, P2), dp2 = sub(P1, P2);
+    const float invdet = 1.f / (du1 * dv2 - dv1 * du2);
+    const V3 dpdu = scl(invdet, sub(scl(dv2, dp1), scl(dv1, dp2)));
+    const V3 dpdv = scl(invdet, add(scl(-du2, dp1), scl(du1, dp2)));
+    N = normalize(add(add(scl(2.0f * T[0] - 1.0f, normalize(dpdu)), scl(2.0f * T[1] - 1.0f, normalize(dpdv))),
+                      scl(2.0f * T[2] - 1.0f, N)));
+  }
+  const V3 V = scl(-1.0f, normalize(dir));
+  V3 result = mk(0, 0, 0);
+  for (int i = 0; i < 4; ++i) {
+    const V3 Lv = sub(mk(s.lightPos[i][0], s.lightPos[i][1], s.lightPos[i][2]), P);
+    const float Ldist = std::sqrt(dot(Lv, Lv));
+    const V3 Ld = scl(1.0f / Ldist, Lv);
+    const V3 H = normalize(add(Ld, V));
+    const float NdL = dot(N, Ld), NdV = dot(N, V), NdH = dot(N, H), VdH = dot(V, H);
+    if (NdL > 0.0f && NdV > 0.0f) {
+      const float o[3] = {P.x, P.y, P.z}, d[3] = {Ld.x, Ld.y, Ld.z};
+      if (trace32(s, o, d, 0.001f, Ldist - 0.001f).id != 0xffffffffu) continue;
+      const V3 F = schlick(spec, VdH);
+      const float G = smithVis(NdL, NdV, alpha), D = ggxNormal(NdH, alpha);
+      const V3 dterm = scl(1.0f / kPi, vmul(sub(mk(1, 1, 1), F), diff));
+      const V3 sterm = scl(G * D, F);
+      result = add(result, vmul(scl(s.lightPos[i][3] * NdL, mk(s.lightCol[i][0], s.lightCol[i][1], s.lightCol[i][2])),
+                                add(dterm, sterm)));
+    }
+  }
+  return result;
+}
+
+V3 shadeHit(const Scene& s, uint32_t t, float b1, float b2, V3 dir) {
+  const V3 base = baseColour(s, t, b1, b2);
+  return s.lighting ? shadeLit(s, t, b1, b2, dir, base) : base;
 }
 
 V3 shadeMiss(int miss, V3 dirIn) {
@@ -447,6 +548,19 @@ extern "C" {
 
 // Base colour textures of a scene: the texels of all textures and per
 // texture (first texel, width, height).
+// Lighting-on data: 20 floats per triangle (original order), four lights
+// as position xyz + intensity (16 floats) and colour (12 floats); on != 0
+// switches the lit shading on.
+void orc_scene_set_lighting(void* h, const float* light, const float* lightPos, const float* lightCol, int on) {
+  Scene* s = static_cast<Scene*>(h);
+  s->light.assign(light, light + 20 * static_cast<size_t>(s->T));
+  for (int i = 0; i < 4; ++i) {
+    for (int k = 0; k < 4; ++k) s->lightPos[i][k] = lightPos[4 * i + k];
+    for (int k = 0; k < 3; ++k) s->lightCol[i][k] = lightCol[3 * i + k];
+  }
+  s->lighting = on;
+}
+
 void orc_scene_set_textures(void* h, const uint32_t* texels, size_t nTexels, const int32_t* table, uint32_t nTex) {
   Scene* s = static_cast<Scene*>(h);
   s->texels.assign(texels, texels + nTexels);
@@ -526,8 +640,8 @@ void orc_shade(void* sc, int miss, const float* dir, const int32_t* hitId, const
                float* rgb) {
   const Scene& s = *static_cast<Scene*>(sc);
   for (size_t i = 0; i < n; ++i) {
-    const V3 c = hitId[i] >= 0 ? shadeHit(s, static_cast<uint32_t>(hitId[i]), b1[i], b2[i])
-                               : shadeMiss(miss, mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]));
+    const V3 d = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+    const V3 c = hitId[i] >= 0 ? shadeHit(s, static_cast<uint32_t>(hitId[i]), b1[i], b2[i], d) : shadeMiss(miss, d);
     rgb[3 * i] = c.x;
     rgb[3 * i + 1] = c.y;
     rgb[3 * i + 2] = c.z;
@@ -560,8 +674,8 @@ void orc_render_rays(void* sc, int miss, const float* omm, uint32_t N, uint32_t 
     for (uint32_t k = 0; k < spp; ++k) {
       const size_t i = static_cast<size_t>(po) * spp + k;
       const Hit32 h = trace32(s, org + 3 * i, dir + 3 * i, tmin, 1e16f);
-      const V3 c = h.id != 0xffffffffu ? shadeHit(s, h.id, h.V / h.det, h.W / h.det)
-                                       : shadeMiss(miss, mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]));
+      const V3 d = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+      const V3 c = h.id != 0xffffffffu ? shadeHit(s, h.id, h.V / h.det, h.W / h.det, d) : shadeMiss(miss, d);
       sum = add(sum, scl(scale, c));
     }
     out[3 * po] = sum.x;
@@ -588,7 +702,8 @@ size_t orc_render_draws(void* sc, int miss, const float* omm, uint32_t N, uint32
       float org[3], dir[3];
       genRay(omm + 8 * o, poses12 + 12 * p, draws[2 * i], draws[2 * i + 1], org, dir);
       const Hit32 h = trace32(s, org, dir, tmin, 1e16f);
-      const V3 c = h.id != 0xffffffffu ? shadeHit(s, h.id, h.V / h.det, h.W / h.det) : shadeMiss(miss, mk(dir[0], dir[1], dir[2]));
+      const V3 d = mk(dir[0], dir[1], dir[2]);
+      const V3 c = h.id != 0xffffffffu ? shadeHit(s, h.id, h.V / h.det, h.W / h.det, d) : shadeMiss(miss, d);
       sum = add(sum, scl(scale, c));
     }
     out[3 * po] = sum.x;

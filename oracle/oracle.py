@@ -58,6 +58,7 @@ def lib():
         L.orc_make_color.argtypes = [f32, c_size_t, u8]
         u32 = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
         L.orc_scene_set_textures.argtypes = [c_void_p, u32, c_size_t, i32, c_uint32]
+        L.orc_scene_set_lighting.argtypes = [c_void_p, f32, f32, f32, c_int]
         L.orc_sample_texture.argtypes = [u32, c_int, c_int, f32, c_size_t, f32]
         L.orc_max_threads.restype = c_int
         _lib = L
@@ -87,6 +88,14 @@ class OracleScene:
             texels = np.ascontiguousarray(textures[1], np.uint32).reshape(-1)
             self._tex = (table, texels)
             lib().orc_scene_set_textures(self._h, texels, texels.size, table, table.size // 3)
+
+    def set_lighting(self, light, light_pos, light_col, on=True):
+        """Lighting-on shading: (T, 20) per-triangle data, (4, 4) light
+        positions + intensities, (4, 3) colours."""
+        self._light = _f32(light).reshape(-1)
+        assert self._light.size == 20 * self.T
+        lib().orc_scene_set_lighting(self._h, self._light, _f32(light_pos).reshape(-1), _f32(light_col).reshape(-1),
+                                     1 if on else 0)
 
     def __del__(self):
         if getattr(self, "_h", None):
