@@ -269,6 +269,17 @@ size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
 cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
                            RayRecord* rec, cudaStream_t stream, const float4* cuts = nullptr);
+// isInsideHitGeometry for n points (xyz floats) against one hitbox mesh
+// (object-space triangles, 3 float3 each): the inverse of the mesh's node
+// transform (row-major 3x3 and translation, double) and the ray start
+// x = object box min.x - 1; out: one byte per point, 1 = inside.
+struct InsideQuery {
+  double inv[9];
+  double t[3];
+  double startX;
+};
+cudaError_t launchInside(const float3* tris, uint32_t nTris, const InsideQuery& q, const float* pts, size_t n,
+                         uint8_t* out, cudaStream_t stream);
 // Near-field cuts of P poses (kCutStride float4 each; see DevEye::cuts).
 cudaError_t launchCuts(const DevScene& scene, const float4* poses, uint32_t P, float radius, float maxRel,
                        float4* cuts, cudaStream_t stream);

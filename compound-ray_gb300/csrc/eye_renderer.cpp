@@ -906,6 +906,54 @@ bool isInsideHitGeometry(float x, float y, float z, char* name) {
       false);
 }
 
+int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, unsigned char* inside) {
+  return guarded(
+      "crInsideHitGeometryBatch",
+      [&]() -> int {
+        if (!name || (n && (!points || !inside))) throw std::runtime_error("null pointer");
+        const HitboxMesh* hm = nullptr;
+        for (const HitboxMesh& h : R().scene.hitboxes)
+          if (h.name == name) hm = &h;
+        if (!hm) throw std::runtime_error(std::string("no hitbox named '") + name + "'");
+        if (n == 0) return 0;
+        // Inverse transform exactly as pointInsideHitbox forms it.
+        const double* x = hm->xform;
+        const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
+        const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+        if (det == 0.0) {
+          std::memset(inside, 0, n);
+          return 0;
+        }
+        InsideQuery q;
+        const double inv[9] = {(e * i - f * h) / det, (c * h - b * i) / det, (b * f - c * e) / det,
+                               (f * g - d * i) / det, (a * i - c * g) / det, (c * d - a * f) / det,
+                               (d * h - e * g) / det, (b * g - a * h) / det, (a * e - b * d) / det};
+        std::memcpy(q.inv, inv, sizeof(inv));
+        q.t[0] = x[3];
+        q.t[1] = x[7];
+        q.t[2] = x[11];
+        q.startX = hm->objMin.x - 1.0;
+        Renderer& r = R();
+        cudaStream_t st = r.stream();
+        const uint32_t nt = static_cast<uint32_t>(hm->tris.size() / 3);
+        DevBuf<float3> tri;
+        DevBuf<float> pts;
+        DevBuf<uint8_t> res;
+        tri.ensure(std::max<size_t>(1, hm->tris.size()));
+        pts.ensure(3 * n);
+        res.ensure(n);
+        static_assert(sizeof(f3) == sizeof(float3), "f3 and float3 share a layout");
+        if (nt) check(cudaMemcpyAsync(tri.ptr, hm->tris.data(), nt * 3 * sizeof(float3), cudaMemcpyHostToDevice, st),
+                      "cudaMemcpy");
+        check(cudaMemcpyAsync(pts.ptr, points, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st), "cudaMemcpy");
+        check(launchInside(tri.ptr, nt, q, pts.ptr, n, res.ptr, st), "hitbox query");
+        check(cudaMemcpyAsync(inside, res.ptr, n, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+        check(cudaStreamSynchronize(st), "hitbox query");
+        return 0;
+      },
+      -1);
+}
+
 static float3 boundsByName(const char* name, bool wantMax) {
   if (!name) return make_float3(0.f, 0.f, 0.f);
   const SceneData& s = R().scene;

@@ -1661,6 +1661,75 @@ size_t adaptivePartialFloats(uint64_t count, uint32_t spp) {
   return adaptiveChunks(spp) > 1 ? count * adaptiveChunks(spp) * 3 : 0;
 }
 
+namespace {
+
+// Parity ray cast of sutil/hitscanprocessing.cpp:20-83 for many points, in
+// explicitly rounded double arithmetic in the host test's operation order
+// (gltf.cpp pointInsideHitbox), so both give the same answer bit for bit.
+__global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, InsideQuery q,
+                             const float* __restrict__ pts, size_t n, uint8_t* __restrict__ out) {
+  const size_t k = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double qx = __dsub_rn(static_cast<double>(pts[3 * k]), q.t[0]);
+  const double qy = __dsub_rn(static_cast<double>(pts[3 * k + 1]), q.t[1]);
+  const double qz = __dsub_rn(static_cast<double>(pts[3 * k + 2]), q.t[2]);
+  double o[3];
+  for (int r = 0; r < 3; ++r)
+    o[r] = __dadd_rn(__dadd_rn(__dmul_rn(q.inv[3 * r], qx), __dmul_rn(q.inv[3 * r + 1], qy)),
+                     __dmul_rn(q.inv[3 * r + 2], qz));
+  const double sx = q.startX, sy = o[1], sz = o[2];
+  double dx = __dsub_rn(o[0], sx);
+  const double dl = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), 0.0), 0.0));
+  if (dl == 0.0) {
+    out[k] = 0;
+    return;
+  }
+  dx = __ddiv_rn(dx, dl);
+  unsigned crossings = 0;
+  for (uint32_t t = 0; t < nTris; ++t) {
+    const float3 p0 = tris[3 * t], p1 = tris[3 * t + 1], p2 = tris[3 * t + 2];
+    // vertex differences in float, as the host test's float members give them
+    const double e1[3] = {__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z)};
+    const double e2[3] = {__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z)};
+    double nv[3] = {__dsub_rn(__dmul_rn(e1[1], e2[2]), __dmul_rn(e1[2], e2[1])),
+                    __dsub_rn(__dmul_rn(e1[2], e2[0]), __dmul_rn(e1[0], e2[2])),
+                    __dsub_rn(__dmul_rn(e1[0], e2[1]), __dmul_rn(e1[1], e2[0]))};
+    const double nl =
+        __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(nv[0], nv[0]), __dmul_rn(nv[1], nv[1])), __dmul_rn(nv[2], nv[2])));
+    if (nl == 0.0) continue;
+    for (int c = 0; c < 3; ++c) nv[c] = __ddiv_rn(nv[c], nl);
+    const double den = __dmul_rn(nv[0], dx);
+    if (den == 0.0) continue;
+    const double dist = __ddiv_rn(
+        __dadd_rn(__dadd_rn(__dmul_rn(__dsub_rn(p0.x, sx), nv[0]), __dmul_rn(__dsub_rn(p0.y, sy), nv[1])),
+                  __dmul_rn(__dsub_rn(p0.z, sz), nv[2])),
+        den);
+    if (dist == 0.0) continue;
+    const double hit[3] = {__dadd_rn(sx, __dmul_rn(dist, dx)), sy, sz};
+    if (dist < 0.0 || hit[0] > o[0]) continue;
+    auto edgeOk = [&](float3 s0, float3 s1) {
+      const double ed[3] = {__fsub_rn(s1.x, s0.x), __fsub_rn(s1.y, s0.y), __fsub_rn(s1.z, s0.z)};
+      const double fe[3] = {__dsub_rn(hit[0], s0.x), __dsub_rn(hit[1], s0.y), __dsub_rn(hit[2], s0.z)};
+      const double cx = __dsub_rn(__dmul_rn(ed[1], fe[2]), __dmul_rn(ed[2], fe[1]));
+      const double cy = __dsub_rn(__dmul_rn(ed[2], fe[0]), __dmul_rn(ed[0], fe[2]));
+      const double cz = __dsub_rn(__dmul_rn(ed[0], fe[1]), __dmul_rn(ed[1], fe[0]));
+      return __dadd_rn(__dadd_rn(__dmul_rn(nv[0], cx), __dmul_rn(nv[1], cy)), __dmul_rn(nv[2], cz)) >= 0.0;
+    };
+    if (!edgeOk(p0, p1) || !edgeOk(p1, p2) || !edgeOk(p2, p0)) continue;
+    ++crossings;
+  }
+  out[k] = (crossings & 1u) ? 1 : 0;
+}
+
+}  // namespace
+
+cudaError_t launchInside(const float3* tris, uint32_t nTris, const InsideQuery& q, const float* pts, size_t n,
+                         uint8_t* out, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  insideKernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, stream>>>(tris, nTris, q, pts, n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launchCuts(const DevScene& scene, const float4* poses, uint32_t P, float radius, float maxRel,
                        float4* cuts, cudaStream_t stream) {
   if (P == 0) return cudaSuccess;

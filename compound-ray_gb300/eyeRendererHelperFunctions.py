@@ -194,6 +194,9 @@ def configureExtras(eyeRenderer):
     L.crSetLighting.argtypes = [c_int]
     L.crSetLighting.restype = c_int
     L.crGetLighting.restype = c_int
+    L.crInsideHitGeometryBatch.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_char_p,
+                                           ndpointer(np.uint8, flags="C_CONTIGUOUS")]
+    L.crInsideHitGeometryBatch.restype = c_int
     L.crGetSceneLighting.argtypes = [c_void_p, c_void_p, c_void_p]
     L.crGetSceneLighting.restype = c_int
     L.crSetCutRadius.argtypes = [c_float]

@@ -77,6 +77,13 @@ float3 getGeometryMinBounds(char* name);                        /* :66 */
 
 /* ---- Additions (no counterpart in the reference) ----------------------- */
 
+/* isInsideHitGeometry for n points at once on the GPU: points n x 3 floats
+ * (world space), inside n bytes (1 = inside the hitbox mesh `name`), the
+ * same parity ray cast and answers as isInsideHitGeometry point by point
+ * (sutil/hitscanprocessing.cpp:20-83).  0 on success, -1 for an unknown
+ * hitbox or a CUDA error. */
+int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, unsigned char* inside);
+
 /* Copies the last error message (NUL-terminated, truncated to len) and
  * returns its full length; 0 when no error is pending.  Reading clears it. */
 int crGetLastError(char* buf, size_t len);

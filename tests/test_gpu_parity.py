@@ -377,3 +377,25 @@ def test_near_field_cut_changes_no_result(lib, small, tmp_path, fraction):
         assert np.array_equal(outs[0], outs[1])
         assert np.array_equal(recs[0]["hitId"], recs[1]["hitId"])
         assert np.array_equal(recs[0]["t"], recs[1]["t"])
+
+
+def test_hitbox_batch_matches_point_queries(lib, tmp_path):
+    """crInsideHitGeometryBatch (GPU) answers as isInsideHitGeometry does,
+    point by point, for a rotated, scaled, translated hitbox mesh."""
+    g = scenes.GltfBuilder()
+    v, f = scenes.box_mesh([-1, -1, -1], [1, 1, 1])
+    g.mesh("ground", np.array([[-5, 0, -5], [5, 0, -5], [5, 0, 5]], np.float64), np.array([[0, 2, 1]]))
+    g.mesh("arena", v, f, extras={"hitbox": True}, translation=[2.0, 0.5, -1.0],
+           rotation=[0.0, np.sin(0.35), 0.0, np.cos(0.35)], scale=[1.5, 0.8, 2.0])
+    g.perspective_camera("cam")
+    eh.lastError(lib)
+    lib.loadGlTFscene(g.write(str(tmp_path / "hb.gltf")).encode())
+    assert eh.lastError(lib) == ""
+    rng = np.random.default_rng(8)
+    pts = rng.uniform([-2, -1.5, -5], [6, 2.5, 3], size=(3000, 3)).astype(np.float32)
+    out = np.zeros(len(pts), np.uint8)
+    assert lib.crInsideHitGeometryBatch(pts, len(pts), b"arena", out) == 0, eh.lastError(lib)
+    want = np.array([lib.isInsideHitGeometry(float(x), float(y), float(z), b"arena") for x, y, z in pts], np.uint8)
+    assert np.array_equal(out, want)
+    assert 200 < want.sum() < 2800
+    assert lib.crInsideHitGeometryBatch(pts, len(pts), b"nothing", out) == -1
