@@ -297,6 +297,7 @@ def run_ours(args):
     best = ctypes.c_int(0)
     if lib.crAutotune(d_poses.data_ptr(), min(64, P), ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
+    cut_fraction = float(lib.crGetCutRadius())  # the autotuner's radius for this workload
 
     # Traversal statistics for the roofline's per-ray bytes (not timed).
     nodes = ctypes_double()
@@ -373,7 +374,7 @@ def run_ours(args):
     # Issue-rate roofline: warp instructions per ray from an ncu capture of
     # this kernel on this launch (smsp__inst_executed.sum / rays), against 4
     # schedulers x 1 instruction per cycle on every SM at the maximum clock.
-    counters = RENDER_LAUNCH_COUNTERS.get(float(lib.crGetCutRadius()))
+    counters = RENDER_LAUNCH_COUNTERS.get(cut_fraction)
     issue_per_ray = counters[1] if counters else None
     issue_peak = 4.0 * SM_COUNT * sm_max_mhz() * 1e6
     issue_achieved = issue_per_ray * launch_n * N * spp / launch_s if counters else None
@@ -386,7 +387,7 @@ def run_ours(args):
                    "rays_per_step": rays_step, "eye_frames_per_step": P, "l2": "flushed (512 MB write) between steps",
                    "poses_per_launch": POSES_PER_LAUNCH,
                    "autotune": {"variant": best.value, "ms_64_poses": [round(float(x), 3) for x in tune_ms],
-                                "near_field_cut_fraction": float(lib.crGetCutRadius())}},
+                                "near_field_cut_fraction": cut_fraction}},
         "eye_frames_per_s": value / (N * spp),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},

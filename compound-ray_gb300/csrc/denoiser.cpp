@@ -118,10 +118,21 @@ void Denoiser::forward(const void* X, int rows, cudaStream_t s) {
 
 float Denoiser::forwardBackward(const void* X, const float* base, const float* target, int rows, bool wantLoss,
                                 cudaStream_t s) {
+  if (wantLoss) ck(cudaMemsetAsync(lossSum_, 0, 4, s), "memset");
+  step(X, base, target, rows, wantLoss ? lossSum_ : nullptr, s);
+  if (!wantLoss) return 0.f;
+  float e2 = 0.f;
+  ck(cudaMemcpyAsync(&e2, lossSum_, 4, cudaMemcpyDeviceToHost, s), "loss readback");
+  ck(cudaStreamSynchronize(s), "step");
+  return e2 / (3.0f * static_cast<float>(rows));
+}
+
+// Forward, loss gradient and backward of one minibatch into grads_, with the
+// summed squared error added to *lossAcc (device) when given.  No host sync.
+void Denoiser::step(const void* X, const float* base, const float* target, int rows, float* lossAcc, cudaStream_t s) {
   const uint16_t* w = static_cast<const uint16_t*>(wbf_);
   forward(X, rows, s);
-  if (wantLoss) ck(cudaMemsetAsync(lossSum_, 0, 4, s), "memset");
-  ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, wantLoss ? lossSum_ : nullptr, s), "loss");
+  ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, lossAcc, s), "loss");
   // Output layer.
   ck(gemmBf16(0, kHidden, kOut, rows, h_[2], kHidden, true, dyb_, kOut, false, grads_ + offW4, nullptr, kOut, nullptr,
               nullptr, s),
@@ -145,11 +156,6 @@ float Denoiser::forwardBackward(const void* X, const float* base, const float* t
                   kHidden, nullptr, h_[l - 1], s),
          "dZ");
   }
-  if (!wantLoss) return 0.f;
-  float e2 = 0.f;
-  ck(cudaMemcpyAsync(&e2, lossSum_, 4, cudaMemcpyDeviceToHost, s), "loss readback");
-  ck(cudaStreamSynchronize(s), "step");
-  return e2 / (3.0f * static_cast<float>(rows));
 }
 
 void Denoiser::addRows(const void* X, const float* base, const float* target, size_t rows, cudaStream_t s) {
@@ -183,31 +189,51 @@ void Denoiser::addRows(const void* X, const float* base, const float* target, si
 void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s) {
   if (!ready()) throw std::runtime_error("denoiser not initialised");
   if (rows_ == 0) throw std::runtime_error("no training rows");
+  if (steps <= 0) return;
   batch = static_cast<int>(std::min<size_t>(static_cast<size_t>(batch), rows_));
   ensureBatch(batch);
+  // The shuffled order of an epoch lives on the device and the per-step
+  // losses accumulate there: the loop issues kernels only, no host waits.
   std::mt19937 rng(seed);
   std::vector<uint32_t> perm(rows_);
   std::iota(perm.begin(), perm.end(), 0u);
   std::shuffle(perm.begin(), perm.end(), rng);
+  uint32_t* permDev = dalloc<uint32_t>(rows_);
+  float* lossDev = dalloc<float>(static_cast<size_t>(steps));
+  ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
+  ck(cudaMemsetAsync(lossDev, 0, static_cast<size_t>(steps) * 4, s), "memset");
   size_t cursor = 0;
-  for (int st = 0; st < steps; ++st) {
-    if (cursor + static_cast<size_t>(batch) > rows_) {
-      std::shuffle(perm.begin(), perm.end(), rng);
-      cursor = 0;
+  try {
+    for (int st = 0; st < steps; ++st) {
+      if (cursor + static_cast<size_t>(batch) > rows_) {
+        ck(cudaStreamSynchronize(s), "epoch");  // the previous order is no longer read
+        std::shuffle(perm.begin(), perm.end(), rng);
+        ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
+        cursor = 0;
+      }
+      ck(gatherRows(X_, base_, target_, permDev + cursor, batch, Xb_, baseb_, targetb_, s), "gather");
+      cursor += static_cast<size_t>(batch);
+      step(Xb_, baseb_, targetb_, batch, loss ? lossDev + st : nullptr, s);
+      ++adamT_;
+      // half-cosine decay of the step size over this call, down to 5%
+      const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
+      ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr * decay, 0.9f, 0.999f, 1e-8f, adamT_, wbf_,
+                  s),
+         "adam");
     }
-    ck(cudaMemcpyAsync(idx_, perm.data() + cursor, static_cast<size_t>(batch) * 4, cudaMemcpyHostToDevice, s), "idx");
-    cursor += static_cast<size_t>(batch);
-    ck(gatherRows(X_, base_, target_, idx_, batch, Xb_, baseb_, targetb_, s), "gather");
-    const bool want = loss != nullptr;
-    const float l = forwardBackward(Xb_, baseb_, targetb_, batch, want, s);
-    if (loss) loss[st] = l;
-    ++adamT_;
-    // half-cosine decay of the step size over this call, down to 5%
-    const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
-    ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr * decay, 0.9f, 0.999f, 1e-8f, adamT_, wbf_, s),
-       "adam");
+    if (loss) {
+      ck(cudaMemcpyAsync(loss, lossDev, static_cast<size_t>(steps) * 4, cudaMemcpyDeviceToHost, s), "loss readback");
+    }
+    ck(cudaStreamSynchronize(s), "train");
+  } catch (...) {
+    dfree(permDev);
+    dfree(lossDev);
+    throw;
   }
-  ck(cudaStreamSynchronize(s), "train");
+  dfree(permDev);
+  dfree(lossDev);
+  if (loss)
+    for (int st = 0; st < steps; ++st) loss[st] /= 3.0f * static_cast<float>(batch);
 }
 
 void Denoiser::infer(const void* X, const float* base, size_t rows, float* out, cudaStream_t s) {

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __n
                                                   bool aTrans, const __nv_bfloat16* __restrict__ B, int ldb,
                                                   bool bTrans, float* __restrict__ Cf, __nv_bfloat16* __restrict__ Hb,
                                                   int ldc, const float* __restrict__ bias,
-                                                  const __nv_bfloat16* __restrict__ mask) {
+                                                  const __nv_bfloat16* __restrict__ mask, int kSlice = 0) {
   __shared__ __nv_bfloat16 As[BM][BK + kPad];
   __shared__ __nv_bfloat16 Bs[BN][BK + kPad];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -71,21 +71,26 @@ __global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __n
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  // Split K: block z covers [z * kSlice, (z + 1) * kSlice) and writes its
+  // partial tile to slice z of Cf (M x N each, ldc = N).
+  const int kBeg = kSlice ? static_cast<int>(blockIdx.z) * kSlice : 0;
+  const int kEnd = kSlice ? min(K, kBeg + kSlice) : K;
+  if (kSlice) Cf += static_cast<size_t>(blockIdx.z) * M * N;
+  for (int k0 = kBeg; k0 < kEnd; k0 += BK) {
     // Tile loads walk the operand's contiguous dimension with consecutive
     // threads (k for a row-major A / transposed B, m or n otherwise).
     for (int e = tid; e < BM * BK; e += 128) {
       const int r = aTrans ? e % BM : e / BK, c = aTrans ? e / BM : e % BK;
       const int m = m0 + r, k = k0 + c;
       __nv_bfloat16 v = zero;
-      if (m < M && k < K) v = aTrans ? A[static_cast<size_t>(k) * lda + m] : A[static_cast<size_t>(m) * lda + k];
+      if (m < M && k < kEnd) v = aTrans ? A[static_cast<size_t>(k) * lda + m] : A[static_cast<size_t>(m) * lda + k];
       As[r][c] = v;
     }
     for (int e = tid; e < BN * BK; e += 128) {
       const int r = bTrans ? e / BK : e % BN, c = bTrans ? e % BK : e / BN;
       const int n = n0 + r, k = k0 + c;
       __nv_bfloat16 v = zero;
-      if (n < N && k < K) v = bTrans ? B[static_cast<size_t>(n) * ldb + k] : B[static_cast<size_t>(k) * ldb + n];
+      if (n < N && k < kEnd) v = bTrans ? B[static_cast<size_t>(n) * ldb + k] : B[static_cast<size_t>(k) * ldb + n];
       Bs[r][c] = v;
     }
     __syncthreads();
@@ -396,10 +401,47 @@ __global__ void gatherRowsKernel(const __nv_bfloat16* __restrict__ X, const floa
 
 }  // namespace
 
+namespace {
+// Split-K partial sums: slices[s][m][n] summed in slice order into C.
+__global__ void splitKReduceKernel(const float* __restrict__ part, int slices, int M, int N, float* __restrict__ C,
+                                   int ldc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * N) return;
+  const int m = i / N, n = i % N;
+  float s = 0.f;
+  for (int k = 0; k < slices; ++k) s += part[static_cast<size_t>(k) * M * N + i];
+  C[static_cast<size_t>(m) * ldc + n] = s;
+}
+float* g_splitK = nullptr;
+size_t g_splitKFloats = 0;
+}  // namespace
+
 cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
                      bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
                      cudaStream_t stream) {
   if (M <= 0 || N <= 0) return cudaSuccess;
+  // Weight gradients (a long K over the minibatch, a small M x N) split K
+  // into slices of 256 so that enough blocks run; the partial tiles are then
+  // summed in slice order (deterministic).
+  const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  if (mode == 0 && K >= 1024 && tiles < 64 && !bTrans) {
+    const int slice = 256, slices = (K + slice - 1) / slice;
+    const size_t need = static_cast<size_t>(slices) * M * N;
+    if (need > g_splitKFloats) {
+      if (g_splitK) cudaFree(g_splitK);
+      g_splitK = nullptr;
+      g_splitKFloats = 0;
+      cudaError_t e = cudaMalloc(&g_splitK, need * sizeof(float));
+      if (e != cudaSuccess) return e;
+      g_splitKFloats = need;
+    }
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, slices);
+    gemmKernel<0><<<grid, 128, 0, stream>>>(M, N, K, static_cast<const __nv_bfloat16*>(A), lda, aTrans,
+                                            static_cast<const __nv_bfloat16*>(B), ldb, bTrans, g_splitK, nullptr, N,
+                                            nullptr, nullptr, slice);
+    splitKReduceKernel<<<(M * N + 255) / 256, 256, 0, stream>>>(g_splitK, slices, M, N, Cf, ldc);
+    return cudaGetLastError();
+  }
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
   auto a = static_cast<const __nv_bfloat16*>(A);
   auto b = static_cast<const __nv_bfloat16*>(B);

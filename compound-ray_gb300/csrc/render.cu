@@ -240,10 +240,14 @@ __device__ __forceinline__ void childSpan(const Ray& r, float cx, float cy, floa
 }
 
 // Traversal loop over the BVH2 from `node`, with `sp` deferred entries
-// already on the stack; updates the closest hit `h`.
+// already on the stack; updates the closest hit `h`.  restart: when the
+// stack runs empty and the hit is not within `guard` (distance, t * dlen),
+// go on once more from the root (the near-field cut's second phase, in the
+// same loop so the code is not inlined twice).
 template <bool kCount, bool kAnyHit = false>
 __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack, int sp,
-                                             int node, uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests) {
+                                             int node, uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests,
+                                             bool restart = false, float guard = 0.f, float dlen = 0.f) {
   for (;;) {
     if (node >= 0) {
       if (kCount) ++nodeVisits;
@@ -290,7 +294,16 @@ __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, f
       }
       if (kAnyHit && h.id != 0xffffffffu) return;  // occlusion query: any hit will do
     }
-    if (sp == 0) return;
+    if (sp == 0) {
+      if (restart) {
+        restart = false;
+        if (!(h.id != 0xffffffffu && h.t * dlen <= guard)) {
+          node = 0;
+          continue;
+        }
+      }
+      return;
+    }
     node = stack[--sp];
   }
 }
@@ -311,28 +324,27 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
   h.pos = 0;
   if (sc.triCount == 0) return;
   int stack[kStackSize];
+  int sp = 0, node = 0;
+  bool restart = false;
+  float guard = 0.f;
   if (cut) {
     const float4 hdr = __ldg(cut);
     const int count = __float_as_int(hdr.x);
-    if (count > 0) {
-      // Entries are stored far to near; the nearest hit box is entered first.
-      int sp = 0, node = 0;
-      bool any = false;
-      for (int k = 0; k < count; ++k) {
-        const float4 a = __ldg(cut + 1 + 2 * k), b = __ldg(cut + 2 + 2 * k);
-        float tn, tf;
-        childSpan(r, a.x, a.y, a.z, b.x, b.y, b.z, tmin, h.t, tn, tf);
-        if (tn <= tf) {
-          if (any) stack[sp++] = node;
-          node = __float_as_int(a.w);
-          any = true;
-        }
+    // Entries are stored far to near; the nearest hit box is entered first.
+    // When no cut box is hit the search starts at the root directly.
+    for (int k = 0; k < count; ++k) {
+      const float4 a = __ldg(cut + 1 + 2 * k), b = __ldg(cut + 2 + 2 * k);
+      float tn, tf;
+      childSpan(r, a.x, a.y, a.z, b.x, b.y, b.z, tmin, h.t, tn, tf);
+      if (tn <= tf) {
+        if (restart) stack[sp++] = node;
+        node = __float_as_int(a.w);
+        restart = true;
       }
-      if (any) traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests);
-      if (h.id != 0xffffffffu && h.t * dlen <= hdr.y) return;
     }
+    guard = hdr.y;
   }
-  traverseFrom<kCount>(sc, r, tmin, h, stack, 0, 0, errFlag, nodeVisits, triTests);
+  traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests, restart, guard, dlen);
 }
 
 // Near-field cut of one pose: at most kCutEntries BVH subtrees (box + ref)
