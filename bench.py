@@ -52,6 +52,10 @@ def parse_args():
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     ap.add_argument("--cut", type=float, default=1.0 / 64, help="near-field cut radius (fraction of the scene extent) for --profile")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
+    ap.add_argument("--profile-learned", action="store_true", help="profiling case: learned render of held-out poses")
+    ap.add_argument("--profile-adaptive", action="store_true", help="profiling case: adaptive learned render")
+    ap.add_argument("--denoiser-kernel", type=int, default=1, help="denoiser inference kernel for --profile-learned: "
+                    "0 mma.sync, 1 tcgen05")
     return ap.parse_args()
 
 
@@ -354,7 +358,11 @@ def run_ours(args):
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
     learned = None if args.no_learned else run_learned(lib, eh, args, stream)
+    learned_terrain = None if args.no_learned else run_learned(lib, eh, args, stream, scene="terrain",
+                                                                  train_poses=1000)
     adaptive = None if args.no_adaptive else run_adaptive(lib, eh, args, stream)
+    adaptive_small = None if args.no_adaptive else run_adaptive(lib, eh, args, stream, scene="small",
+                                                                 train_poses=256, held_poses=1000)
 
     if rank != 0:
         if world > 1:
@@ -413,8 +421,10 @@ def run_ours(args):
         line["batch_uneven"] = batch
     if learned:
         line["learned_denoiser"] = learned
+        line["learned_denoiser_terrain"] = learned_terrain
     if adaptive:
         line["learned_allocator"] = adaptive
+        line["learned_allocator_small"] = adaptive_small
     if not args.no_cpu_baseline:
         cb = cpu_baseline(info, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -456,55 +466,88 @@ def run_batch(lib, eh, args, stream):
     d_poses = torch.from_numpy(p16).to(dev)
     d_out = torch.empty(sum(3 * P * n for n in info["n"]), dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
-    h = lib.crBatchCreate(cams, n_eyes, P, d_poses.data_ptr(), d_out.data_ptr())
-    if h <= 0:
+    # Autotune (register variant, near-field cut radius) on the eye with the
+    # most rays per pose; the batch is recorded with the chosen settings.
+    big = int(np.argmax([n * s for n, s in zip(info["n"], info["spp"])]))
+    lib.gotoCamera(int(cams[big]))
+    prev_cut, prev_variant = float(lib.crGetCutRadius()), int(lib.crGetRenderVariant())
+    tune_ms = np.zeros(lib.crGetRenderVariantCount(), np.float32)
+    best = ctypes.c_int(0)
+    if lib.crAutotune(d_poses[big * P].data_ptr(), P, ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
-    for _ in range(max(1, args.warmup)):
-        if lib.crBatchLaunch(h) != 0:
+    cut = float(lib.crGetCutRadius())
+
+    def timed_batch(cut_fraction):
+        lib.crSetCutRadius(cut_fraction)
+        h = lib.crBatchCreate(cams, n_eyes, P, d_poses.data_ptr(), d_out.data_ptr())
+        if h <= 0:
             raise RuntimeError(eh.lastError(lib))
-    torch.cuda.synchronize()
-    ms = []
-    for _ in range(args.steps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        if lib.crBatchLaunch(h) != 0:
-            raise RuntimeError(eh.lastError(lib))
-        b.record(stream)
+        for _ in range(max(1, args.warmup)):
+            if lib.crBatchLaunch(h) != 0:
+                raise RuntimeError(eh.lastError(lib))
         torch.cuda.synchronize()
-        ms.append(a.elapsed_time(b))
-    lat = np.zeros(n_eyes, np.float32)
-    total = ctypes.c_float(0.0)
-    if lib.crBatchLatencies(h, lat, ctypes.byref(total)) != 0:
-        raise RuntimeError(eh.lastError(lib))
-    lib.crBatchDestroy(h)
+        ms = []
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            if lib.crBatchLaunch(h) != 0:
+                raise RuntimeError(eh.lastError(lib))
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        lat = np.zeros(n_eyes, np.float32)
+        total = ctypes.c_float(0.0)
+        if lib.crBatchLatencies(h, lat, ctypes.byref(total)) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        lib.crBatchDestroy(h)
+        return statistics.mean(ms), lat
+
+    ms_nocut = timed_batch(0.0)[0] if cut > 0 else None
+    ms, lat = timed_batch(cut)
+    lib.crSetCutRadius(prev_cut)  # the later sections keep the main workload's settings
+    lib.crSetRenderVariant(prev_variant)
     rays = int(sum(n * s for n, s in zip(info["n"], info["spp"])) * P)
-    return {"eyes": n_eyes, "poses_per_eye": P, "rays_per_launch": rays, "launch_ms": statistics.mean(ms),
-            "rays_per_s": rays / (statistics.mean(ms) / 1000.0),
+    return {"eyes": n_eyes, "poses_per_eye": P, "rays_per_launch": rays, "launch_ms": ms,
+            "rays_per_s": rays / (ms / 1000.0),
             "eye_latency_ms_p50": float(np.percentile(lat, 50)), "eye_latency_ms_p99": float(np.percentile(lat, 99)),
-            "graph": "one persistent work-queue kernel (+ chunk sums) replayed from a CUDA graph"}
+            "autotune": {"variant": int(best.value), "near_field_cut_fraction": cut,
+                         "launch_ms_without_cut": ms_nocut},
+            "graph": "near-field cuts + one persistent work-queue kernel (+ chunk sums) replayed from a CUDA graph"}
 
 
-def run_learned(lib, eh, args, stream, train_poses=1000, held_poses=1000, steps=8000, batch=8192):
-    """Learned denoiser on the terrain scene and its 6000-ommatidium droplet
-    eye (the workload above): trains on 8-sample features and 1024-sample
-    targets of `train_poses` random poses (seeded, x/z within +-60 m, eye
-    0.5 m above the ground, uniform yaw), then on `held_poses` held-out
-    random poses reports the RMSE against the 1024-sample plain render, the
-    plain sample count that matches it, and eye-frames/s of the learned form
-    against the plain form at that matched RMSE and at 1024 samples (all
-    timed with CUDA events on device-resident poses)."""
+def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_poses=1000, steps=8000, batch=8192):
+    """Learned denoiser.  scene "small": the ground + 64 boxes scene and its
+    1000-ommatidium Fibonacci-sphere eye (acceptance 3 deg), random poses
+    within +-8 m outside the boxes; "terrain": the terrain scene and its
+    6000-ommatidium droplet eye (the workload above), random poses within
+    +-60 m.  Eyes 0.5 m above the ground, uniform yaw, seeded.  Trains on
+    8-sample features and 1024-sample targets of `train_poses` poses, then on
+    `held_poses` held-out poses reports the RMSE against the 1024-sample
+    plain render, the plain sample count that matches it, and eye-frames/s
+    of the learned form against the plain form at that matched RMSE and at
+    1024 samples (all timed with CUDA events on device-resident poses)."""
     import torch
 
     import scenes
 
-    info = workload(1024)
+    rng = np.random.default_rng(scenes.SEED + 11)
+    if scene == "terrain":
+        info = workload(1024)
+        train = scenes.random_poses(info["height_fn"], train_poses, rng, 60.0)
+        held = scenes.random_poses(info["height_fn"], held_poses, rng, 60.0)
+        label = "terrain (%d tris), %%d-ommatidium droplet eye" % info["triangles"]
+    else:
+        info = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
+        train = scenes.open_poses(info["boxes"], train_poses, rng)
+        held = scenes.open_poses(info["boxes"], held_poses, rng)
+        label = "ground + 64 boxes (770 tris, simple_sky), %d-ommatidium Fibonacci-sphere eye, acceptance 3 deg"
     lib.crSetStream(stream.cuda_stream)
     lib.loadGlTFscene(info["gltf"].encode())
+    err = eh.lastError(lib)
+    if err:
+        raise RuntimeError(err)
     eh.gotoFirstCompoundEye(lib)
     N = lib.getCurrentEyeOmmatidialCount()
-    rng = np.random.default_rng(scenes.SEED + 11)
-    train = scenes.random_poses(info["height_fn"], train_poses, rng, 60.0)
-    held = scenes.random_poses(info["height_fn"], held_poses, rng, 60.0)
     t0 = time.perf_counter()
     if lib.crDenoiserInit(1) != 0 or lib.crDenoiserAddTrainingPoses(train, len(train), 8, 1024) != 0:
         raise RuntimeError(eh.lastError(lib))
@@ -566,7 +609,7 @@ def run_learned(lib, eh, args, stream, train_poses=1000, held_poses=1000, steps=
             break
     ms_matched = sweep[matched][1] if matched else None
     fps_learned = held_poses / (ms_learned / 1000.0)
-    return {"scene": "terrain (%d tris), %d-ommatidium droplet eye" % (info["triangles"], N),
+    return {"scene": label % N,
             "train_poses": train_poses, "train_ommatidium_frames": train_poses * N,
             "held_out_poses": held_poses, "steps": steps, "batch": batch, "final_loss": float(loss[-100:].mean()),
             "data_s": t_data, "train_s": t_train, "rmse_learned_8spp": r_learned, "rmse_plain_8spp": sweep[8][0],
@@ -579,30 +622,41 @@ def run_learned(lib, eh, args, stream, train_poses=1000, held_poses=1000, steps=
             "speedup_vs_plain_1024": ms_1024 / ms_learned}
 
 
-def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_steps=3000, den_steps=3000,
-                 batch=8192, threshold=1.0 / 512.0, seeds=8):
-    """Learned sample allocator plus denoiser at scale: a 2048 x 2048-cell
-    heightfield over 400 m with 20,000 cone plants (9.03 M triangles, GPU
-    linear BVH) and a 100,000-ommatidium panoramic eye (Fibonacci sphere,
-    acceptance U(0.5, 5) deg).  The allocator is trained on minimum-sample
-    labels (smallest count in 4..1024 whose colour standard deviation across
-    8 seeds is below 1/512) of `train_poses` random poses, the denoiser on the
-    same poses (8-sample features, 1024-sample targets); on `held_poses`
-    held-out random poses the adaptive learned render is compared with the
-    plain 1024-sample render: RMSE, rays and time (CUDA events)."""
+def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_poses=32, alloc_steps=3000,
+                 den_steps=3000, batch=8192, threshold=1.0 / 512.0, seeds=8, profile=False):
+    """Learned sample allocator plus denoiser.  scene "large": a 2048 x
+    2048-cell heightfield over 400 m with 20,000 cone plants (9.03 M
+    triangles, GPU linear BVH) and a 100,000-ommatidium panoramic eye
+    (Fibonacci sphere, acceptance U(0.5, 5) deg), random poses within
+    +-150 m; "small": the ground + 64 boxes scene and its 1000-ommatidium
+    eye, random poses within +-8 m outside the boxes.  The allocator is
+    trained on minimum-sample labels (smallest count in 4..1024 whose colour
+    standard deviation across 8 seeds is below 1/512) of `train_poses`
+    random poses, the denoiser on the same poses (8-sample features,
+    1024-sample targets); on `held_poses` held-out random poses the adaptive
+    learned render is compared with the plain 1024-sample render: RMSE, rays
+    and time (CUDA events).  profile: after training and tuning, render the
+    held-out poses adaptively twice (untimed; the case the kernel profiles
+    capture) and return None."""
     import ctypes
 
     import torch
 
     import scenes
 
-    d = os.path.join(tempfile.gettempdir(), "cr_bench_large_%d" % scenes.SEED)
     t0 = time.perf_counter()
-    info = scenes.terrain_scene(d, cells=2048, extent=400.0, cones=20000, n_omm=100000, poses=4,
-                                eye_kind="panoramic", aa_deg=(0.5, 5.0))
+    if scene == "large":
+        d = os.path.join(tempfile.gettempdir(), "cr_bench_large_%d" % scenes.SEED)
+        info = scenes.terrain_scene(d, cells=2048, extent=400.0, cones=20000, n_omm=100000, poses=4,
+                                    eye_kind="panoramic", aa_deg=(0.5, 5.0))
+        label = ("heightfield 2048^2 cells + 20000 cones (%d tris, GPU LBVH), %%d-ommatidium panoramic eye, "
+                 "acceptance 0.5-5 deg" % info["triangles"])
+    else:
+        info = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
+        label = "ground + 64 boxes (770 tris, simple_sky), %d-ommatidium Fibonacci-sphere eye, acceptance 3 deg"
     t_scene = time.perf_counter() - t0
     lib.crSetStream(stream.cuda_stream)
-    lib.crSetBvhBuilder(1)
+    lib.crSetBvhBuilder(1 if scene == "large" else 0)
     t0 = time.perf_counter()
     lib.loadGlTFscene(info["gltf"].encode())
     err = eh.lastError(lib)
@@ -612,8 +666,12 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
     N = lib.getCurrentEyeOmmatidialCount()
     t_load = time.perf_counter() - t0
     rng = np.random.default_rng(scenes.SEED + 21)
-    train = scenes.random_poses(info["height_fn"], train_poses, rng, 150.0)
-    held = scenes.random_poses(info["height_fn"], held_poses, rng, 150.0)
+    if scene == "large":
+        train = scenes.random_poses(info["height_fn"], train_poses, rng, 150.0)
+        held = scenes.random_poses(info["height_fn"], held_poses, rng, 150.0)
+    else:
+        train = scenes.open_poses(info["boxes"], train_poses, rng)
+        held = scenes.open_poses(info["boxes"], held_poses, rng)
     dev = torch.device("cuda", torch.cuda.current_device())
     p16 = np.zeros((held_poses, 16), np.float32)
     for k in range(4):
@@ -626,11 +684,13 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
     if lib.crAllocatorInit(3) != 0 or lib.crDenoiserInit(4) != 0:
         raise RuntimeError(eh.lastError(lib))
     labels = np.zeros((train_poses, N), np.uint16)
-    for k in range(0, train_poses, 4):
-        lab = np.zeros((4, N), np.uint16)
-        if lib.crAllocatorAddTrainingPoses(train[k:k + 4], 4, 8, threshold, seeds, lab.ctypes.data) != 0:
+    chunk = max(1, min(64, 400000 // N))  # poses per label search
+    for k in range(0, train_poses, chunk):
+        c = min(chunk, train_poses - k)
+        lab = np.zeros((c, N), np.uint16)
+        if lib.crAllocatorAddTrainingPoses(train[k:k + c], c, 8, threshold, seeds, lab.ctypes.data) != 0:
             raise RuntimeError(eh.lastError(lib))
-        labels[k:k + 4] = lab
+        labels[k:k + c] = lab
     if lib.crDenoiserAddTrainingPoses(train, train_poses, 8, 1024) != 0:
         raise RuntimeError(eh.lastError(lib))
     t_data = time.perf_counter() - t0
@@ -669,6 +729,13 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
     if lib.crAutotune(d_poses.data_ptr(), 4, ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
     cut = float(lib.crGetCutRadius())
+    if profile:
+        adaptive()
+        adaptive()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "adaptive learned render of %d held-out poses, twice" % held_poses,
+                          "rays": rays.value, "variant": best.value, "cut": cut}))
+        return None
     ms_adaptive = timed(adaptive)
     img = d_out.cpu().numpy()
     lev = d_lev.cpu().numpy()
@@ -683,8 +750,7 @@ def run_adaptive(lib, eh, args, stream, train_poses=16, held_poses=32, alloc_ste
     lib.crSetBvhBuilder(0)
     rays_plain = float(held_poses) * N * 1024
     lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
-    return {"scene": "heightfield 2048^2 cells + 20000 cones (%d tris, GPU LBVH), %d-ommatidium panoramic eye, "
-                     "acceptance 0.5-5 deg" % (info["triangles"], N),
+    return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
             "autotune": {"variant": best.value, "near_field_cut_fraction": cut},
             "label_histogram": lab_hist, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
@@ -709,6 +775,51 @@ def hit_fraction(lib, eh):
     camera's current pose (the 256-sample eye of the workload)."""
     rec = eh.renderFrameRecorded(lib)
     return float((rec["hitId"] >= 0).mean())
+
+
+def run_profile_learned(args):
+    """Profiling case of the learned sections (no timing): --profile-learned
+    trains the terrain denoiser briefly and renders min(--poses, 1000)
+    held-out poses through the learned form twice with denoiser kernel
+    --denoiser-kernel; --profile-adaptive runs the sample-allocator section's
+    set-up and renders its held-out poses adaptively twice."""
+    import torch
+
+    torch.cuda.set_device(0)
+    import eyeRendererHelperFunctions as eh
+
+    import scenes
+
+    lib = eh.loadRenderer()
+    lib.setVerbosity(False)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    lib.crSetStream(stream.cuda_stream)
+    if args.profile_adaptive:
+        run_adaptive(lib, eh, args, stream, held_poses=min(args.poses, 32), profile=True)
+        return
+    info = workload(1024)
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    N = lib.getCurrentEyeOmmatidialCount()
+    rng = np.random.default_rng(scenes.SEED + 11)
+    P = min(args.poses, 1000)
+    train = scenes.random_poses(info["height_fn"], 20, rng, 60.0)
+    held = scenes.random_poses(info["height_fn"], P, rng, 60.0)
+    if lib.crDenoiserInit(1) != 0 or lib.crDenoiserAddTrainingPoses(train, len(train), 8, 64) != 0 or \
+            lib.crDenoiserTrain(20, 4096, 1e-3, 3, None) != 0 or lib.crSetDenoiserKernel(args.denoiser_kernel) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    p16 = np.zeros((P, 16), np.float32)
+    for k in range(4):
+        p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
+    d_poses = torch.from_numpy(p16).cuda()
+    d_out = torch.empty((P, N, 3), dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        if lib.crDenoiserRenderPosesDevice(d_poses.data_ptr(), P, 8, d_out.data_ptr()) != 0:
+            raise RuntimeError(eh.lastError(lib))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "learned render of %d held-out terrain poses, twice" % P,
+                      "denoiser_kernel": args.denoiser_kernel, "checksum": float(d_out.sum())}))
 
 
 def run_profile(args):
@@ -740,6 +851,8 @@ def main():
     args = parse_args()
     if args.profile:
         run_profile(args)
+    elif args.profile_learned or args.profile_adaptive:
+        run_profile_learned(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -223,11 +223,13 @@ int batchBlocksPerSM(int variant);
 // Persistent launch over all eyes' warp tasks (taskBase: nEyes ascending
 // task offsets) followed by the chunk sums of the eyes with chunks > 1
 // (cellBase: nEyes ascending offsets into their P*N cells).  ctrl must hold
-// 2 + nEyes words, set to {0, ~0, 0...} before the launch.
+// 2 + nEyes words, set to {0, ~0, 0...} before the launch.  cutPoses > 0:
+// first build the near-field cuts of the eyes whose DevEye::cuts is set
+// (cutPoses poses per eye, each eye's cuts laid out like a plain launch's).
 cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsigned long long* taskBase,
                         const unsigned long long* cellBase, uint32_t nEyes, unsigned long long totalTasks,
                         unsigned long long totalCells, unsigned long long* ctrl, uint32_t* errFlag, int variant,
-                        int gridBlocks, cudaStream_t stream);
+                        int gridBlocks, uint32_t cutPoses, cudaStream_t stream);
 
 // Adaptive sampling (render.cu).  An entry e = pose * N + ommatidium is
 // rendered at its bucket's sample count; buckets hold counts 4 << index.

@@ -501,9 +501,11 @@ struct Batch {
   DevBuf<BatchEye> table;
   DevBuf<unsigned long long> taskBase, cellBase, ctrl;
   DevBuf<float> scratch;
+  DevBuf<float4> cuts;  // per eye P x kCutStride, when the near-field cut is on
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   unsigned long long totalTasks = 0, totalCells = 0;
+  uint32_t cutPoses = 0;
   int variant = 0, grid = 0;
   uint64_t generation = 0;
   void release() {
@@ -516,6 +518,7 @@ struct Batch {
     cellBase.release();
     ctrl.release();
     scratch.release();
+    cuts.release();
   }
 };
 
@@ -1098,6 +1101,14 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
         std::vector<BatchEye> table(nCams);
         std::vector<unsigned long long> tb(nCams), cb(nCams);
         size_t outOff = 0, scratchFloats = 0;
+        // The near-field cut radius in force now is recorded into the graph.
+        r.ensureUploaded();
+        const bool useCuts = r.cutFactor > 0.f && r.dev.extent > 0.f &&
+                             r.bvhStats.maxDepth + kCutEntries + 2 <= 64;
+        if (useCuts) {
+          b.cuts.ensure(nCams * posesPerCam * kCutStride);
+          b.cutPoses = static_cast<uint32_t>(posesPerCam);
+        }
         for (size_t i = 0; i < nCams; ++i) {
           const int ci = cams[i];
           if (ci < 0 || static_cast<size_t>(ci) >= r.scene.cameras.size() ||
@@ -1114,6 +1125,11 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
           be.plan = planWarps(e.N, e.spp);
           be.P = static_cast<uint32_t>(posesPerCam);
           be.scratch = nullptr;
+          if (useCuts) {
+            be.eye.cuts = b.cuts.ptr + i * posesPerCam * kCutStride;
+            be.eye.cutRadius = r.cutFactor * r.dev.extent;
+            be.eye.maxRel = e.maxRel;
+          }
           tb[i] = b.totalTasks;
           cb[i] = b.totalCells;
           b.outOffset.push_back(outOff);
@@ -1154,7 +1170,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
         if (ce == cudaSuccess) ce = cudaMemsetAsync(b.ctrl.ptr + 1, 0xff, sizeof(unsigned long long), st);
         if (ce == cudaSuccess)
           ce = launchBatch(r.dev, b.table.ptr, b.taskBase.ptr, b.cellBase.ptr, static_cast<uint32_t>(nCams),
-                           b.totalTasks, b.totalCells, b.ctrl.ptr, err, b.variant, b.grid, st);
+                           b.totalTasks, b.totalCells, b.ctrl.ptr, err, b.variant, b.grid, b.cutPoses, st);
         cudaGraph_t g = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(st, &g);
         check(ce, "batch capture");

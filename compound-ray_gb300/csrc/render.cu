@@ -315,18 +315,21 @@ __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, f
 // = |direction|) is final: every triangle nearer than it lies in the ball and
 // so in one of those subtrees.  Otherwise the search continues from the root
 // with the hit found so far.  Either way the result is the closest hit.
-template <bool kCount>
-__device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
-                                             uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests,
-                                             const float4* __restrict__ cut = nullptr, float dlen = 0.f) {
+//
+// beginTrace sets up that search (the hit, the stack with the cut entries,
+// the start node) for traverseFrom; it returns false when the scene is empty
+// (the ray misses).
+__device__ __forceinline__ bool beginTrace(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
+                                           int* stack, int& sp, int& node, bool& restart, float& guard,
+                                           const float4* __restrict__ cut) {
   h.t = tmax;
   h.id = 0xffffffffu;
   h.pos = 0;
-  if (sc.triCount == 0) return;
-  int stack[kStackSize];
-  int sp = 0, node = 0;
-  bool restart = false;
-  float guard = 0.f;
+  sp = 0;
+  node = 0;
+  restart = false;
+  guard = 0.f;
+  if (sc.triCount == 0) return false;
   if (cut) {
     const float4 hdr = __ldg(cut);
     const int count = __float_as_int(hdr.x);
@@ -344,6 +347,18 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
     }
     guard = hdr.y;
   }
+  return true;
+}
+
+template <bool kCount>
+__device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, float tmin, float tmax, Hit& h,
+                                             uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests,
+                                             const float4* __restrict__ cut = nullptr, float dlen = 0.f) {
+  int stack[kStackSize];
+  int sp, node;
+  bool restart;
+  float guard;
+  if (!beginTrace(sc, r, tmin, tmax, h, stack, sp, node, restart, guard, cut)) return;
   traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests, restart, guard, dlen);
 }
 
@@ -362,12 +377,9 @@ __device__ __forceinline__ float boxDist2(float px, float py, float pz, float cx
   return dx * dx + dy * dy + dz * dz;
 }
 
-__global__ void cutKernel(DevScene sc, const float4* __restrict__ poses, uint32_t P, float R, float maxRel,
-                          float4* __restrict__ cuts) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  float4* out = cuts + static_cast<size_t>(p) * kCutStride;
-  const float4 P0 = poses[4 * p], X = poses[4 * p + 1], Y = poses[4 * p + 2], Z = poses[4 * p + 3];
+__device__ __forceinline__ void buildCut(const DevScene& sc, const float4* __restrict__ pose, float R, float maxRel,
+                                         float4* __restrict__ out) {
+  const float4 P0 = pose[0], X = pose[1], Y = pose[2], Z = pose[3];
   const float rEye = maxRel * (sqrtf(X.x * X.x + X.y * X.y + X.z * X.z) + sqrtf(Y.x * Y.x + Y.y * Y.y + Y.z * Y.z) +
                                sqrtf(Z.x * Z.x + Z.y * Z.y + Z.z * Z.z));
   const float rGuard = R - rEye;
@@ -475,6 +487,13 @@ __global__ void cutKernel(DevScene sc, const float4* __restrict__ poses, uint32_
     out[1 + 2 * k] = make_float4(c[k][0], c[k][1], c[k][2], __int_as_float(ref[k]));
     out[2 + 2 * k] = make_float4(e[k][0], e[k][1], e[k][2], 0.f);
   }
+}
+
+__global__ void cutKernel(DevScene sc, const float4* __restrict__ poses, uint32_t P, float R, float maxRel,
+                          float4* __restrict__ cuts) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  buildCut(sc, poses + 4 * p, R, maxRel, cuts + static_cast<size_t>(p) * kCutStride);
 }
 
 // ---------------------------------------------------------------------------
@@ -1092,6 +1111,17 @@ __global__ void __launch_bounds__(128, kMinBlocks) batchKernel(DevScene sc, cons
   }
 }
 
+// Near-field cuts of every eye of a batch: thread i builds the cut of pose
+// i % P of eye i / P (each eye has P poses) when that eye has a cut buffer.
+__global__ void batchCutKernel(DevScene sc, const BatchEye* __restrict__ eyes, uint32_t nEyes, uint32_t P) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= static_cast<uint64_t>(nEyes) * P) return;
+  const uint32_t e = static_cast<uint32_t>(i / P), p = static_cast<uint32_t>(i % P);
+  const DevEye& de = eyes[e].eye;
+  if (!de.cuts || p >= eyes[e].P) return;
+  buildCut(sc, eyes[e].poses + 4 * p, de.cutRadius, de.maxRel, de.cuts + static_cast<size_t>(p) * kCutStride);
+}
+
 // Chunk sums of every eye with more than 32 samples: cell c belongs to the
 // last eye whose cellBase <= c.
 __global__ void batchCombineKernel(const BatchEye* __restrict__ eyes, const unsigned long long* __restrict__ cellBase,
@@ -1340,8 +1370,14 @@ int batchBlocksPerSM(int variant) {
 cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsigned long long* taskBase,
                         const unsigned long long* cellBase, uint32_t nEyes, unsigned long long totalTasks,
                         unsigned long long totalCells, unsigned long long* ctrl, uint32_t* errFlag, int variant,
-                        int gridBlocks, cudaStream_t stream) {
+                        int gridBlocks, uint32_t cutPoses, cudaStream_t stream) {
   if (nEyes == 0 || gridBlocks <= 0) return cudaSuccess;
+  if (cutPoses) {
+    const uint64_t n = static_cast<uint64_t>(nEyes) * cutPoses;
+    batchCutKernel<<<static_cast<unsigned>((n + 63) / 64), 64, 0, stream>>>(scene, eyes, nEyes, cutPoses);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   switch (variant) {
     case 1:
       batchKernel<6><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);

@@ -434,7 +434,7 @@ def small_scene(outdir, seed=SEED, n_omm=1000, spp=32):
     g.scene_extras = {"background-shader": "simple_sky"}
     ground = np.array([[-10, 0, -10], [10, 0, -10], [10, 0, 10], [-10, 0, 10]], np.float64)
     g.mesh("ground", ground, np.array([[0, 2, 1], [0, 3, 2]]), colours=np.tile([0.5, 0.5, 0.5, 1.0], (4, 1)))
-    verts, faces, cols = [], [], []
+    verts, faces, cols, boxes = [], [], [], []
     placed = 0
     while placed < 64:
         c = rng.uniform(-8.0, 8.0, size=2)
@@ -443,10 +443,12 @@ def small_scene(outdir, seed=SEED, n_omm=1000, spp=32):
         # Keep the eye (0, 0.5, 0) outside every box.
         if abs(c[0]) < e[0] / 2 + 0.3 and abs(c[1]) < e[2] / 2 + 0.3:
             continue
-        v, f = box_mesh([c[0] - e[0] / 2, 0.0, c[1] - e[2] / 2], [c[0] + e[0] / 2, e[1], c[1] + e[2] / 2])
+        lo, hi = [c[0] - e[0] / 2, 0.0, c[1] - e[2] / 2], [c[0] + e[0] / 2, e[1], c[1] + e[2] / 2]
+        v, f = box_mesh(lo, hi)
         faces.append(f + 8 * placed)
         verts.append(v)
         cols.append(col)
+        boxes.append((lo, hi))
         placed += 1
     g.mesh("boxes", np.concatenate(verts), np.concatenate(faces), colours=np.concatenate(cols))
     d = fibonacci_sphere(n_omm)
@@ -455,7 +457,26 @@ def small_scene(outdir, seed=SEED, n_omm=1000, spp=32):
     g.compound_camera("insect-eye", "small.eye", translation=[0.0, 0.5, 0.0])
     path = g.write(os.path.join(outdir, "small.gltf"), embed=True)
     pose = pose_rows(np.array([0.0, 0.5, 0.0]), 0.0)
-    return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm}
+    return {"gltf": path, "eye": eye_path, "pose": pose, "spp": spp, "n_omm": n_omm,
+            "boxes": np.asarray(boxes, np.float64)}
+
+
+def open_poses(boxes, count, rng, half_width=8.0, eye_height=0.5, margin=0.05):
+    """(count, 12) random poses of the small scene: x, z uniform in
+    +-half_width, `eye_height` above the ground, uniform yaw, outside every
+    box (boxes: (n, 2, 3) min/max corners) by at least `margin`."""
+    out = np.zeros((count, 12), np.float32)
+    i = 0
+    while i < count:
+        x, z = rng.uniform(-half_width, half_width, size=2)
+        yaw = rng.uniform(0, 2 * math.pi)
+        p = np.array([x, eye_height, z])
+        inside = ((boxes[:, 0] - margin <= p) & (p <= boxes[:, 1] + margin)).all(axis=1)
+        if inside.any():
+            continue
+        out[i] = pose_rows(p, yaw)
+        i += 1
+    return out
 
 
 def textured_scene(outdir, seed=SEED, n_omm=1000, spp=32):

@@ -19,9 +19,20 @@ def _p16(poses12):
     return out
 
 
-def test_batch_equals_per_eye_renders(lib, tmp_path):
+@pytest.mark.parametrize("cut", [0.0, 1.0 / 16])
+def test_batch_equals_per_eye_renders(lib, tmp_path, cut):
+    """cut: near-field cut radius (fraction of the scene extent) in force when
+    the batch is recorded; the per-eye references are rendered without one."""
+    try:
+        _batch_case(lib, tmp_path, cut)
+    finally:
+        lib.crSetCutRadius(0.0)
+
+
+def _batch_case(lib, tmp_path, cut):
     import torch
 
+    lib.crSetCutRadius(0.0)
     info = scenes.batch_scene(str(tmp_path), n_eyes=5, poses_per_eye=3, n_min=100, n_max=700,
                               spp_choices=(8, 32, 48, 100, 5))
     lib.loadGlTFscene(info["gltf"].encode())
@@ -47,6 +58,7 @@ def test_batch_equals_per_eye_renders(lib, tmp_path):
         lib.setCurrentEyeSamplesPerOmmatidium(info["spp"][i])
     d_out = torch.zeros(sum(sizes), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
+    assert lib.crSetCutRadius(cut) == 0
     h = lib.crBatchCreate(cams, len(cams), P, d_poses.data_ptr(), d_out.data_ptr())
     assert h > 0, eh.lastError(lib)
     lat = np.zeros(len(cams), np.float32)
