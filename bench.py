@@ -357,6 +357,7 @@ def run_ours(args):
     e2e_value = world * rays_step * args.steps / e2e_total
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
+    projection = run_projection(lib, eh, args, stream)
     learned = None if args.no_learned else run_learned(lib, eh, args, stream)
     learned_terrain = None if args.no_learned else run_learned(lib, eh, args, stream, scene="terrain",
                                                                   train_poses=1000)
@@ -419,6 +420,7 @@ def run_ours(args):
     }
     if batch:
         line["batch_uneven"] = batch
+    line["spherical_projection"] = projection
     if learned:
         line["learned_denoiser"] = learned
         line["learned_denoiser_terrain"] = learned_terrain
@@ -431,6 +433,45 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_projection(lib, eh, args, stream, n=100000, w=1024, h=512):
+    """spherical_orientationwise image of an n-ommatidium Fibonacci-sphere
+    eye (small scene, 1 sample) at w x h: renderFrame time with the
+    candidate-grid search and with the exhaustive search in index order
+    (the reference's loop); both give the same image (checked here too)."""
+    import ctypes
+
+    import scenes
+
+    info = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
+    lib.crSetStream(stream.cuda_stream)
+    lib.loadGlTFscene(info["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    d = scenes.fibonacci_sphere(n)
+    omm = np.zeros((n, 8), np.float32)
+    omm[:, 0:3], omm[:, 3:6], omm[:, 6] = d * 0.001, d, 0.01
+    lib.setOmmatidia.argtypes = [ctypes.c_void_p, ctypes.c_size_t]
+    lib.setOmmatidia(omm.ctypes.data, n)
+    lib.setCurrentEyeSamplesPerOmmatidium(1)
+    lib.setCurrentEyeShaderName(b"spherical_orientationwise")
+    eh.setRenderSize(lib, w, h)
+    res, frames = {}, []
+    for mode, key in ((1, "ms_exhaustive"), (0, "ms_grid")):
+        lib.crSetProjectionSearch(mode)
+        lib.setCurrentEyeSamplesPerOmmatidium(1)  # restarts the streams: both first frames see the same colours
+        lib.renderFrame()
+        frames.append(eh.getFrame(lib, w, h).copy())
+        ms = min(lib.renderFrame() for _ in range(3))
+        err = eh.lastError(lib)
+        if err:
+            raise RuntimeError(err)
+        res[key] = ms
+    lib.crSetProjectionSearch(0)
+    return {"eye_ommatidia": n, "image": [w, h], "shader": "spherical_orientationwise",
+            "ms_per_frame_grid": res["ms_grid"], "ms_per_frame_exhaustive": res["ms_exhaustive"],
+            "speedup": res["ms_exhaustive"] / res["ms_grid"], "identical_images": bool(np.array_equal(*frames)),
+            "timing": "renderFrame wall clock (1-sample render of the eye + projection), best of 3"}
 
 
 def run_batch(lib, eh, args, stream):

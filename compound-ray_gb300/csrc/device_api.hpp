@@ -315,11 +315,27 @@ cudaError_t noAllocScratch(float** ptr);
 //  mode 0: single_dimension_fast (row 0, x < N), mode 1: single_dimension.
 cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, int h, int mode,
                           cudaStream_t stream);
+// Candidates of the spherical projections binned by unit vector: a G^3 grid
+// over [-1, 1]^3, cell (cz * G + cy) * G + cx holding items[start[c] ..
+// start[c + 1]) (ommatidium indices >= 1, ascending).  G == 0: no candidate.
+struct SphereGridView {
+  const uint32_t* start = nullptr;  // G^3 + 1 offsets
+  const uint32_t* items = nullptr;
+  int G = 0;
+};
+// The four candidate sets: 0 positions, 1 directions, 2 directions of the
+// ommatidia with position.x < 0, 3 those with position.x > 0.
+struct SphereGridSet {
+  SphereGridView g[4];
+};
+
 // Spherical projections (kind: 0 positionwise, 1 orientationwise, 2 split
 // orientationwise, 3 orientationwise ids, 4 positionwise ids); lenScratch
-// holds 2 * N floats.
+// holds 2 * N floats.  grids: the candidate grids (searched around each
+// pixel's point), or null for the exhaustive search in index order; both
+// give the same image.
 cudaError_t launchSpherical(const float4* omm, float* lenScratch, uint32_t N, const float* sums, uchar4* frame, int w,
-                            int h, int kind, cudaStream_t stream);
+                            int h, int kind, const SphereGridSet* grids, cudaStream_t stream);
 // raw_ommatidial_samples from a recorded frame (N x spp records).
 cudaError_t launchRawSamples(const RayRecord* rec, uint32_t N, uint32_t spp, uchar4* frame, int w, int h,
                              cudaStream_t stream);

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -57,25 +58,92 @@ struct DevBuf {
   }
 };
 
+// One candidate grid of the spherical projections (SphereGridView).
+struct SphereGrid {
+  DevBuf<uint32_t> start, items;
+  int G = 0;
+};
+
 struct EyeDev {
   DevBuf<float4> omm;
   DevBuf<uint32_t> order;  // warp-segment order of the ommatidia (directionOrder)
   DevBuf<uint32_t> rng;
   DevBuf<float> sums;  // N x 3 of the last frame
+  SphereGrid grids[4];  // spherical-projection candidates, built on first use
+  bool gridsBuilt = false;
   uint32_t N = 0, spp = 0;
   float maxRel = 0.f;  // largest |position - focal offset * unit axis| over the ommatidia
   bool configured = false;
   bool haveSums = false;
+  void releaseGrids() {
+    for (SphereGrid& g : grids) {
+      g.start.release();
+      g.items.release();
+      g.G = 0;
+    }
+    gridsBuilt = false;
+  }
   void release() {
     omm.release();
     order.release();
     rng.release();
     sums.release();
+    releaseGrids();
     N = spp = 0;
     configured = false;
     haveSums = false;
   }
 };
+
+// Candidate grids of the spherical projections for an eye's ommatidia:
+// set 0 positions, 1 directions, 2 / 3 directions of the ommatidia with
+// position.x < 0 / > 0 (float comparisons, as the projection makes them).
+// Index 0 is left out (it is every pixel's starting candidate), and so are
+// vectors of zero or non-finite length (their angle is NaN and never wins).
+// Unit vectors in double pick the cell; G ~ sqrt(n) / 3 puts about two
+// candidates in a cell that the sphere crosses.
+void buildSphereGrids(EyeDev& e, const std::vector<Ommatidium>& omm, cudaStream_t st) {
+  const size_t N = omm.size();
+  for (int which = 0; which < 4; ++which) {
+    SphereGrid& g = e.grids[which];
+    std::vector<uint32_t> idx;
+    std::vector<std::array<double, 3>> unit;
+    for (size_t i = 1; i < N; ++i) {
+      const Ommatidium& o = omm[i];
+      if (which == 2 && !(o.pos.x < 0.f)) continue;
+      if (which == 3 && !(o.pos.x > 0.f)) continue;
+      const f3 v = which == 0 ? o.pos : o.dir;
+      const double x = v.x, y = v.y, z = v.z, l = std::sqrt(x * x + y * y + z * z);
+      if (!(l > 0.0) || !std::isfinite(l)) continue;
+      idx.push_back(static_cast<uint32_t>(i));
+      unit.push_back({x / l, y / l, z / l});
+    }
+    g.start.release();
+    g.items.release();
+    g.G = 0;
+    if (idx.empty()) continue;
+    const int G = std::max(1, std::min(128, static_cast<int>(std::lround(0.33 * std::sqrt(double(idx.size()))))));
+    const size_t cells = static_cast<size_t>(G) * G * G;
+    std::vector<uint32_t> cellOf(idx.size()), start(cells + 1, 0), items(idx.size());
+    for (size_t k = 0; k < idx.size(); ++k) {
+      int c[3];
+      for (int a = 0; a < 3; ++a)
+        c[a] = std::min(G - 1, std::max(0, static_cast<int>(std::floor((unit[k][a] + 1.0) * 0.5 * G))));
+      cellOf[k] = static_cast<uint32_t>((static_cast<size_t>(c[2]) * G + c[1]) * G + c[0]);
+      ++start[cellOf[k] + 1];
+    }
+    for (size_t c = 0; c < cells; ++c) start[c + 1] += start[c];
+    std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+    for (size_t k = 0; k < idx.size(); ++k) items[fill[cellOf[k]]++] = idx[k];
+    g.start.ensure(cells + 1);
+    g.items.ensure(items.size());
+    check(cudaMemcpyAsync(g.start.ptr, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    check(cudaMemcpyAsync(g.items.ptr, items.data(), items.size() * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+    check(cudaStreamSynchronize(st), "projection grid upload");
+    g.G = G;
+  }
+  e.gridsBuilt = true;
+}
 
 constexpr uint32_t kMaxPosesPerLaunch = 256;
 
@@ -136,6 +204,7 @@ struct Renderer {
   DevBuf<float2> draws;  // pre-drawn random numbers of small-eye launches
   DevBuf<float4> cuts;   // per-pose near-field cuts
   float cutFactor = 0.f; // cut radius as a fraction of the scene extent (0: off)
+  bool projectionGrid = true;  // spherical projections search candidate grids (false: every candidate)
   DevBuf<float> batchOut;
   DevBuf<uint32_t> err;
   cudaStream_t ownStream = nullptr;
@@ -366,6 +435,7 @@ struct Renderer {
       e.spp = spp;
       e.configured = false;
       e.haveSums = false;
+      e.releaseGrids();
       if (N) check(cudaMemcpyAsync(e.omm.ptr, c.omm.data(), sizeof(Ommatidium) * N, cudaMemcpyHostToDevice, stream()),
                    "cudaMemcpy");
       if (countChanged) {
@@ -470,15 +540,25 @@ struct Renderer {
     throw std::runtime_error("unknown compound projection '" + shader + "'");
   }
 
-  void project(EyeDev& e, const std::string& shader, const RayRecord* rec) {
+  void project(EyeDev& e, const std::vector<Ommatidium>& omm, const std::string& shader, const RayRecord* rec) {
     ensureFrame();
     const int kind = projectionKind(shader);
     if (kind < 10) {
       check(launchProject(e.sums.ptr, e.N, frame.ptr, width, height, kind, stream()), "projection launch");
     } else if (kind < 20) {
+      SphereGridSet set;
+      if (projectionGrid) {
+        if (!e.gridsBuilt) buildSphereGrids(e, omm, stream());
+        for (int k = 0; k < 4; ++k) {
+          set.g[k].start = e.grids[k].start.ptr;
+          set.g[k].items = e.grids[k].items.ptr;
+          set.g[k].G = e.grids[k].G;
+        }
+      }
       DevBuf<float> len;
       len.ensure(std::max<size_t>(1, 2 * static_cast<size_t>(e.N)));
-      check(launchSpherical(e.omm.ptr, len.ptr, e.N, e.sums.ptr, frame.ptr, width, height, kind - 10, stream()),
+      check(launchSpherical(e.omm.ptr, len.ptr, e.N, e.sums.ptr, frame.ptr, width, height, kind - 10,
+                            projectionGrid ? &set : nullptr, stream()),
             "projection launch");
       check(cudaStreamSynchronize(stream()), "projection");
       len.release();
@@ -647,7 +727,7 @@ double renderFrame(void) {
           if (raw) rec.ensure(std::max<size_t>(1, static_cast<size_t>(e.N) * e.spp));
           r.renderDevicePoses(e, r.poses.ptr, 1, e.sums.ptr, raw ? rec.ptr : nullptr);
           e.haveSums = true;
-          r.project(e, c.projection, rec.ptr);
+          r.project(e, c.omm, c.projection, rec.ptr);
           if (raw) {
             check(cudaStreamSynchronize(r.stream()), "projection");
             rec.release();
@@ -874,6 +954,7 @@ void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
       ++r.generation;
       e.release();
     } else if (e.omm.ptr && count) {
+      e.releaseGrids();
       check(cudaMemcpyAsync(e.omm.ptr, v.data(), sizeof(Ommatidium) * count, cudaMemcpyHostToDevice, r.stream()),
             "cudaMemcpy");
       const std::vector<uint32_t> ord = directionOrder(v);
@@ -1425,6 +1506,17 @@ int crSetRenderVariant(int variant) {
 int crGetRenderVariant(void) { return renderVariant(); }
 
 int crGetRenderVariantCount(void) { return renderVariantCount(); }
+
+int crSetProjectionSearch(int mode) {
+  if (mode != 0 && mode != 1) {
+    setError("crSetProjectionSearch: mode must be 0 (grid) or 1 (every candidate)");
+    return -1;
+  }
+  R().projectionGrid = mode == 0;
+  return 0;
+}
+
+int crGetProjectionSearch(void) { return R().projectionGrid ? 0 : 1; }
 
 // ---------------------------------------------------------------------------
 // Learned denoiser (denoiser.hpp): the network is process-wide; its feature

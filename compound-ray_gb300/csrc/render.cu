@@ -994,12 +994,11 @@ __global__ void projectKernel(const float* __restrict__ sums, uint32_t N, uchar4
 //  3 orientationwise ids, 4 positionwise ids (index in RGBA, base 256).
 // The candidate lengths are precomputed per ommatidium (len), identical to
 // recomputing them per pixel.
-__global__ void sphericalKernel(const float4* __restrict__ omm, const float* __restrict__ len, uint32_t N,
-                                const float* __restrict__ sums, uchar4* frame, int w, int h, int kind) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y;
-  if (x >= w || y >= h || N == 0) return;
-  const float ux = static_cast<float>(x) / static_cast<float>(w), uy = static_cast<float>(y) / static_cast<float>(h);
+
+// Point on the sphere of pixel (x, y) and its horizontal image coordinate.
+__device__ __forceinline__ v3 sphericalPixel(int x, int y, int w, int h, int kind, float& ux) {
+  ux = static_cast<float>(x) / static_cast<float>(w);
+  const float uy = static_cast<float>(y) / static_cast<float>(h);
   float dx, dy;
   if (kind == 2) {
     const float sx = ux * 2.0f;
@@ -1012,17 +1011,41 @@ __global__ void sphericalKernel(const float4* __restrict__ omm, const float* __r
   }
   const float ax = dx * -CR_PI_F + CR_PI_F / 2.0f, ay = dy * (CR_PI_F / 2.0f);
   const float cosY = cosf(ay);
-  const v3 p = mk(cosf(ax) * cosY, sinf(ay), sinf(ax) * cosY);
+  return mk(cosf(ax) * cosY, sinf(ay), sinf(ax) * cosY);
+}
+
+// The compared quantity: angle between candidate i's vector and the pixel's
+// point, as the reference computes it.
+__device__ __forceinline__ float sphericalAngle(const float4* __restrict__ omm, const float* __restrict__ len,
+                                                uint32_t N, bool byPos, uint32_t i, v3 p, float lp) {
+  const float4 a = __ldg(omm + 2 * i), b = __ldg(omm + 2 * i + 1);
+  const v3 v = byPos ? mk(a.x, a.y, a.z) : mk(a.w, b.x, b.y);
+  return acosf(dot(v, p) / (__ldg(len + (byPos ? i : N + i)) * lp));
+}
+
+__device__ __forceinline__ void sphericalWrite(uint32_t bi, int kind, const float* __restrict__ sums, uchar4* frame,
+                                               size_t px) {
+  uchar4 c;
+  if (kind >= 3) c = make_uchar4(static_cast<uint8_t>(bi >> 24), static_cast<uint8_t>((bi >> 16) & 0xff),
+                                 static_cast<uint8_t>((bi >> 8) & 0xff), static_cast<uint8_t>(bi & 0xff));
+  else c = makeColour(sums[3 * bi], sums[3 * bi + 1], sums[3 * bi + 2]);
+  frame[px] = c;
+}
+
+// Exhaustive form: every candidate in index order, as the reference does.
+__global__ void sphericalKernel(const float4* __restrict__ omm, const float* __restrict__ len, uint32_t N,
+                                const float* __restrict__ sums, uchar4* frame, int w, int h, int kind) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= w || y >= h || N == 0) return;
+  float ux;
+  const v3 p = sphericalPixel(x, y, w, h, kind, ux);
   const float lp = sqrtf(dot(p, p));
   const bool byPos = (kind == 0 || kind == 4);
-  auto vec = [&](uint32_t i) {
-    const float4 a = __ldg(omm + 2 * i), b = __ldg(omm + 2 * i + 1);
-    return byPos ? mk(a.x, a.y, a.z) : mk(a.w, b.x, b.y);
-  };
-  float best = acosf(dot(vec(0), p) / (len[byPos ? 0 : N] * lp));
+  float best = sphericalAngle(omm, len, N, byPos, 0, p, lp);
   uint32_t bi = 0;
   for (uint32_t i = 1; i < N; ++i) {
-    const float ang = acosf(dot(vec(i), p) / (len[byPos ? i : N + i] * lp));
+    const float ang = sphericalAngle(omm, len, N, byPos, i, p, lp);
     bool ok = ang < best;
     if (kind == 2) {
       const float px = __ldg(omm + 2 * i).x;
@@ -1033,11 +1056,81 @@ __global__ void sphericalKernel(const float4* __restrict__ omm, const float* __r
       bi = i;
     }
   }
-  uchar4 c;
-  if (kind >= 3) c = make_uchar4(static_cast<uint8_t>(bi >> 24), static_cast<uint8_t>((bi >> 16) & 0xff),
-                                 static_cast<uint8_t>((bi >> 8) & 0xff), static_cast<uint8_t>(bi & 0xff));
-  else c = makeColour(sums[3 * bi], sums[3 * bi + 1], sums[3 * bi + 2]);
-  frame[static_cast<size_t>(y) * w + x] = c;
+  sphericalWrite(bi, kind, sums, frame, static_cast<size_t>(y) * w + x);
+}
+
+// Grid form, same result.  The candidates i >= 1 of the pixel's set are
+// binned by their unit vector into a G^3 grid over [-1, 1]^3 (SphereGrid).
+// Candidate 0 starts, as in the exhaustive form; cells are searched in boxes
+// around the pixel's unit point q that grow (one cell, then doubling radii)
+// until the box holds every point within chord distance
+// 2 sin((best + margin) / 2) of q.  Candidates compare by (angle, index), so
+// the smallest index wins among equal angles.  margin (0.01 rad) bounds twice
+// the difference between a computed angle and the true one, so every
+// candidate left outside the box has a computed angle above the best.
+// A NaN angle never wins; a NaN angle of candidate 0 makes 0 the answer.
+__global__ void sphericalGridKernel(const float4* __restrict__ omm, const float* __restrict__ len, uint32_t N,
+                                    SphereGridSet grids, const float* __restrict__ sums, uchar4* frame, int w, int h,
+                                    int kind) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= w || y >= h || N == 0) return;
+  float ux;
+  const v3 p = sphericalPixel(x, y, w, h, kind, ux);
+  const float lp = sqrtf(dot(p, p));
+  const bool byPos = (kind == 0 || kind == 4);
+  float best = sphericalAngle(omm, len, N, byPos, 0, p, lp);
+  uint32_t bi = 0;
+  const SphereGridView* g = nullptr;
+  if (kind == 2) {
+    if (ux < 0.5f) g = &grids.g[2];
+    else if (ux > 0.5f) g = &grids.g[3];
+  } else {
+    g = &grids.g[byPos ? 0 : 1];
+  }
+  if (best == best && g && g->G > 0) {
+    const int G = g->G;
+    const float cell = 2.0f / static_cast<float>(G);
+    const float inv = 1.0f / lp;
+    const float q[3] = {p.x * inv, p.y * inv, p.z * inv};
+    auto cellOf = [&](float c) { return min(G - 1, max(0, static_cast<int>(floorf((c + 1.0f) / cell)))); };
+    int vlo[3] = {1, 1, 1}, vhi[3] = {0, 0, 0};  // visited box (empty)
+    float r = cell;
+    for (;;) {
+      int lo[3], hi[3];
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = cellOf(q[a] - r - 1e-5f);
+        hi[a] = cellOf(q[a] + r + 1e-5f);
+      }
+      for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy)
+          for (int cx = lo[0]; cx <= hi[0]; ++cx) {
+            if (cx >= vlo[0] && cx <= vhi[0] && cy >= vlo[1] && cy <= vhi[1] && cz >= vlo[2] && cz <= vhi[2]) continue;
+            const uint32_t c = (static_cast<uint32_t>(cz) * G + cy) * G + cx;
+            const uint32_t e = __ldg(g->start + c + 1);
+            for (uint32_t k = __ldg(g->start + c); k < e; ++k) {
+              const uint32_t i = __ldg(g->items + k);
+              const float ang = sphericalAngle(omm, len, N, byPos, i, p, lp);
+              if (ang < best || (ang == best && i < bi)) {
+                best = ang;
+                bi = i;
+              }
+            }
+          }
+      for (int a = 0; a < 3; ++a) {
+        vlo[a] = lo[a];
+        vhi[a] = hi[a];
+      }
+      const float reach = best + 0.01f;
+      const float need = reach >= CR_PI_F ? 2.0f : 2.0f * sinf(0.5f * reach);
+      if (r >= need) break;
+      bool whole = true;
+      for (int a = 0; a < 3; ++a) whole = whole && lo[a] == 0 && hi[a] == G - 1;
+      if (whole) break;
+      r = fminf(2.0f * r, need);
+    }
+  }
+  sphericalWrite(bi, kind, sums, frame, static_cast<size_t>(y) * w + x);
 }
 
 __global__ void lengthsKernel(const float4* __restrict__ omm, uint32_t N, float* len) {
@@ -1397,11 +1490,15 @@ cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsig
 }
 
 cudaError_t launchSpherical(const float4* omm, float* lenScratch, uint32_t N, const float* sums, uchar4* frame, int w,
-                            int h, int kind, cudaStream_t stream) {
+                            int h, int kind, const SphereGridSet* grids, cudaStream_t stream) {
   if (w <= 0 || h <= 0 || N == 0) return cudaSuccess;
+  if (kind < 0 || kind > 4) return cudaErrorInvalidValue;
   lengthsKernel<<<(N + 255) / 256, 256, 0, stream>>>(omm, N, lenScratch);
   dim3 grid((w + 127) / 128, h);
-  sphericalKernel<<<grid, 128, 0, stream>>>(omm, lenScratch, N, sums, frame, w, h, kind);
+  if (grids)
+    sphericalGridKernel<<<grid, 128, 0, stream>>>(omm, lenScratch, N, *grids, sums, frame, w, h, kind);
+  else
+    sphericalKernel<<<grid, 128, 0, stream>>>(omm, lenScratch, N, sums, frame, w, h, kind);
   return cudaGetLastError();
 }
 

@@ -204,6 +204,9 @@ def configureExtras(eyeRenderer):
     L.crGetCutRadius.restype = c_float
     L.crSetRenderVariant.argtypes = [c_int]
     L.crSetRenderVariant.restype = c_int
+    L.crSetProjectionSearch.argtypes = [c_int]
+    L.crSetProjectionSearch.restype = c_int
+    L.crGetProjectionSearch.restype = c_int
     L.crGetRenderVariant.restype = c_int
     L.crGetRenderVariantCount.restype = c_int
     L.crSetStream.argtypes = [c_void_p]

@@ -182,6 +182,14 @@ float crGetCutRadius(void);
 int crSetRenderVariant(int variant);
 int crGetRenderVariant(void);
 int crGetRenderVariantCount(void);
+/* Candidate search of the spherical projections (spherical_positionwise,
+ * _orientationwise, _split_orientationwise and the _ids forms): 0 (default)
+ * searches grids of the ommatidia binned by unit vector around each pixel's
+ * point, 1 tests every ommatidium as the reference's shaders do
+ * (shaders.cu:412-640).  Both give the same image.  No counterpart in the
+ * reference. */
+int crSetProjectionSearch(int mode);
+int crGetProjectionSearch(void);
 
 /* ---- Learned per-ommatidium denoiser ------------------------------------
  * A 4-layer MLP (feature row of 112 -> 128 -> 128 -> 128 -> 3, ReLU) that
