@@ -3,18 +3,20 @@
 // Builds, on the device, the same BVH2 layout the render kernel traverses
 // (bvh.hpp) from world-space triangles, replacing the reference's OptiX
 // acceleration-structure builds (libEyeRenderer3/MulticamScene.cpp:1052-1428):
-//   1. 30-bit Morton codes of the triangle centroids in the centroid bounds;
+//   1. 63-bit Morton codes (21 bits per axis) of the triangle centroids in
+//      the centroid bounds' cube;
 //   2. an LSD radix sort of (code, triangle) pairs, 8-bit digits, stable;
 //   3. the binary radix tree of Karras ("Maximizing Parallelism in the
 //      Construction of BVHs, Octrees, and k-d Trees", HPG 2012): internal
 //      node i covers a contiguous range of sorted triangles, equal codes are
 //      split by position;
-//   4. bottom-up boxes, one thread per leaf, the second thread to reach a
-//      node builds its box;
-//   5. subtrees of at most kLbvhLeaf triangles collapse into leaves (their
-//      triangles are contiguous in sorted order), and the node array and the
-//      leaf-ordered triangle and shading arrays are written out.
-// Internal node 0 is the root; node slots of collapsed subtrees stay unused.
+//   4. bottom-up boxes and surface-area costs, one thread per leaf, the
+//      second thread to reach a node builds its box and cost; a node of at
+//      most kLbvhLeaf triangles becomes a leaf when that is cheaper under
+//      the host builder's cost model (bvh.cpp: 1.2 per node, 1 per triangle);
+//   5. the node array and the leaf-ordered triangle and shading arrays are
+//      written out (a leaf's triangles are contiguous in sorted order).
+// Internal node 0 is the root; node slots inside leaves stay unused.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -24,22 +26,26 @@
 namespace cr {
 namespace {
 
-constexpr uint32_t kLbvhLeaf = 4;
+constexpr uint32_t kLbvhLeaf = 8;  // largest leaf (the render layout's 3-bit count)
+constexpr float kLbvhCostNode = 1.2f, kLbvhCostTri = 1.0f;
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 
-__device__ __forceinline__ uint32_t expandBits(uint32_t v) {
-  v = (v * 0x00010001u) & 0xFF0000FFu;
-  v = (v * 0x00000101u) & 0x0F00F00Fu;
-  v = (v * 0x00000011u) & 0xC30C30C3u;
-  v = (v * 0x00000005u) & 0x49249249u;
+// Spreads the low 21 bits of v to every third bit.
+__device__ __forceinline__ uint64_t expandBits(uint64_t v) {
+  v &= 0x1FFFFFull;
+  v = (v | (v << 32)) & 0x001F00000000FFFFull;
+  v = (v | (v << 16)) & 0x001F0000FF0000FFull;
+  v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+  v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
   return v;
 }
 
 __global__ void mortonKernel(const float* __restrict__ verts, uint32_t T, float3 lo, float3 scale,
-                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+                             uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   const float* v = verts + 9 * static_cast<size_t>(t);
@@ -50,15 +56,15 @@ __global__ void mortonKernel(const float* __restrict__ verts, uint32_t T, float3
     c[k] = 0.5f * a + 0.5f * b;
   }
   const float q[3] = {(c[0] - lo.x) * scale.x, (c[1] - lo.y) * scale.y, (c[2] - lo.z) * scale.z};
-  uint32_t m[3];
-  for (int k = 0; k < 3; ++k) m[k] = static_cast<uint32_t>(fminf(fmaxf(q[k], 0.0f), 1023.0f));
+  uint64_t m[3];
+  for (int k = 0; k < 3; ++k) m[k] = static_cast<uint64_t>(fminf(fmaxf(q[k], 0.0f), 2097151.0f));
   keys[t] = (expandBits(m[0]) << 2) | (expandBits(m[1]) << 1) | expandBits(m[2]);
   vals[t] = t;
 }
 
 // Radix sort pass 1: per-tile digit counts, stored digit-major
 // (hist[d * tiles + tile]) so one exclusive scan gives global offsets.
-__global__ void radixCountKernel(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t tiles,
+__global__ void radixCountKernel(const uint64_t* __restrict__ keys, uint32_t n, int shift, uint32_t tiles,
                                  uint32_t* __restrict__ hist) {
   __shared__ uint32_t cnt[kRadix];
   for (int d = threadIdx.x; d < kRadix; d += blockDim.x) cnt[d] = 0;
@@ -66,7 +72,7 @@ __global__ void radixCountKernel(const uint32_t* __restrict__ keys, uint32_t n, 
   const size_t base = static_cast<size_t>(blockIdx.x) * kSortTile;
   for (int r = 0; r < kSortItems; ++r) {
     const size_t i = base + static_cast<size_t>(r) * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & (kRadix - 1)], 1u);
+    if (i < n) atomicAdd(&cnt[static_cast<uint32_t>(keys[i] >> shift) & (kRadix - 1)], 1u);
   }
   __syncthreads();
   for (int d = threadIdx.x; d < kRadix; d += blockDim.x) hist[static_cast<size_t>(d) * tiles + blockIdx.x] = cnt[d];
@@ -99,9 +105,9 @@ __global__ void scanKernel(uint32_t* data, uint32_t count) {
 // Radix sort pass 2: stable scatter.  The tile is processed in kSortItems
 // rounds of one key per thread, in order; within a round a key's rank is the
 // number of equal digits before it (earlier warps, then earlier lanes).
-__global__ void radixScatterKernel(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+__global__ void radixScatterKernel(const uint64_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
                                    uint32_t n, int shift, uint32_t tiles, const uint32_t* __restrict__ offsets,
-                                   uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut) {
+                                   uint64_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut) {
   constexpr int kWarps = kSortThreads / 32;
   __shared__ uint32_t run[kRadix];            // keys of this digit already placed by this tile
   __shared__ uint32_t warpCnt[kWarps][kRadix];
@@ -114,8 +120,8 @@ __global__ void radixScatterKernel(const uint32_t* __restrict__ keysIn, const ui
     __syncthreads();
     const size_t i = base + static_cast<size_t>(r) * kSortThreads + threadIdx.x;
     const bool ok = i < n;
-    const uint32_t key = ok ? keysIn[i] : 0u;
-    const uint32_t d = ok ? ((key >> shift) & (kRadix - 1)) : kRadix;  // kRadix = no digit
+    const uint64_t key = ok ? keysIn[i] : 0ull;
+    const uint32_t d = ok ? static_cast<uint32_t>((key >> shift) & (kRadix - 1)) : kRadix;  // kRadix = no digit
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
     const uint32_t before = __popc(peers & ((1u << lane) - 1u));
     if (ok && before == 0) warpCnt[warp][d] = __popc(peers);
@@ -140,15 +146,15 @@ __global__ void radixScatterKernel(const uint32_t* __restrict__ keysIn, const ui
   }
 }
 
-__device__ __forceinline__ int delta(const uint32_t* __restrict__ k, int n, int i, int j) {
+__device__ __forceinline__ int delta(const uint64_t* __restrict__ k, int n, int i, int j) {
   if (j < 0 || j >= n) return -1;
-  const uint32_t a = k[i], b = k[j];
-  if (a != b) return __clz(a ^ b);
-  return 32 + __clz(static_cast<uint32_t>(i) ^ static_cast<uint32_t>(j));
+  const uint64_t a = k[i], b = k[j];
+  if (a != b) return __clzll(static_cast<long long>(a ^ b));
+  return 64 + __clz(static_cast<uint32_t>(i) ^ static_cast<uint32_t>(j));
 }
 
 // Karras hierarchy.  Node ids: internal 0..n-2, leaf g -> n-1+g.
-__global__ void hierarchyKernel(const uint32_t* __restrict__ keys, int n, int* __restrict__ left,
+__global__ void hierarchyKernel(const uint64_t* __restrict__ keys, int n, int* __restrict__ left,
                                 int* __restrict__ right, int* __restrict__ parent, int* __restrict__ first,
                                 int* __restrict__ last) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,12 +186,26 @@ __global__ void hierarchyKernel(const uint32_t* __restrict__ keys, int n, int* _
   last[i] = hi;
 }
 
-// Bottom-up boxes.  boxes: 6 floats per node id (lo xyz, hi xyz).  Each
+__device__ __forceinline__ float halfArea(const volatile float* b) {
+  const float dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ int count(int node, int n, const int* first, const int* last) {
+  return node >= n - 1 ? 1 : last[node] - first[node] + 1;
+}
+
+// Bottom-up boxes and costs.  boxes: 6 floats per node id (lo xyz, hi xyz);
+// cost: surface-area cost of the node's subtree (half area times the
+// expected work); leafy[i] = 1 when inner node i is cheaper as a leaf.  Each
 // leaf thread climbs; the first thread to reach a node stops there, the
-// second (which sees both children finished) builds the box and continues.
+// second (which sees both children finished) builds the box and cost and
+// continues.
 __global__ void boxesKernel(const float* __restrict__ verts, const uint32_t* __restrict__ order, int n,
                             const int* __restrict__ left, const int* __restrict__ right,
-                            const int* __restrict__ parent, float* boxes, unsigned* visits) {
+                            const int* __restrict__ parent, const int* __restrict__ first,
+                            const int* __restrict__ last, float* boxes, float* cost, uint8_t* leafy,
+                            unsigned* visits) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const float* v = verts + 9 * static_cast<size_t>(order[g]);
@@ -194,21 +214,40 @@ __global__ void boxesKernel(const float* __restrict__ verts, const uint32_t* __r
     b[k] = fminf(fminf(v[k], v[3 + k]), v[6 + k]);
     b[3 + k] = fmaxf(fmaxf(v[k], v[3 + k]), v[6 + k]);
   }
+  cost[n - 1 + g] = kLbvhCostTri * halfArea(b);
   int node = parent[n - 1 + g];
   while (node >= 0) {
     __threadfence();
     if (atomicAdd(&visits[node], 1u) == 0u) return;
     __threadfence();
-    const volatile float* a = boxes + 6 * static_cast<size_t>(left[node]);
-    const volatile float* c = boxes + 6 * static_cast<size_t>(right[node]);
+    const int l = left[node], r = right[node];
+    const volatile float* a = boxes + 6 * static_cast<size_t>(l);
+    const volatile float* c = boxes + 6 * static_cast<size_t>(r);
     float* o = boxes + 6 * static_cast<size_t>(node);
     for (int k = 0; k < 3; ++k) {
       o[k] = fminf(a[k], c[k]);
       o[3 + k] = fmaxf(a[3 + k], c[3 + k]);
     }
+    const float area = halfArea(o);
+    const volatile float* cv = cost;
+    const float split = kLbvhCostNode * area + cv[l] + cv[r];
+    const int cnt = count(node, n, first, last);
+    const float asLeaf = kLbvhCostTri * static_cast<float>(cnt) * area;
+    const bool leaf = node != 0 && cnt <= static_cast<int>(kLbvhLeaf) && asLeaf <= split;
+    leafy[node] = leaf ? 1 : 0;
+    cost[node] = leaf ? asLeaf : split;
     if (node == 0) return;
     node = parent[node];
   }
+}
+
+// True when inner node i lies inside a leaf: it or an ancestor of at most
+// kLbvhLeaf triangles was made a leaf.
+__device__ __forceinline__ bool insideLeaf(int i, int n, const int* parent, const int* first, const int* last,
+                                          const uint8_t* leafy) {
+  for (int a = i; a > 0 && count(a, n, first, last) <= static_cast<int>(kLbvhLeaf); a = parent[a])
+    if (leafy[a]) return true;
+  return false;
 }
 
 __device__ __forceinline__ void centreExtent(const float* b, float* c, float* e) {
@@ -219,30 +258,28 @@ __device__ __forceinline__ void centreExtent(const float* b, float* c, float* e)
   }
 }
 
-__device__ __forceinline__ int count(int node, int n, const int* first, const int* last) {
-  return node >= n - 1 ? 1 : last[node] - first[node] + 1;
-}
-
 // Child reference in the render layout: inner node index, or leaf code.
-__device__ __forceinline__ int childRef(int c, int n, const int* first, const int* last) {
+// Called for the children of emitted nodes only, so a child made a leaf is
+// the top of its leaf.
+__device__ __forceinline__ int childRef(int c, int n, const int* first, const int* last, const uint8_t* leafy) {
   if (c >= n - 1) return ~static_cast<int>((static_cast<uint32_t>(c - (n - 1)) << 3) | 0u);
   const int cnt = last[c] - first[c] + 1;
-  if (cnt <= static_cast<int>(kLbvhLeaf))
-    return ~static_cast<int>((static_cast<uint32_t>(first[c]) << 3) | static_cast<uint32_t>(cnt - 1));
+  if (leafy[c]) return ~static_cast<int>((static_cast<uint32_t>(first[c]) << 3) | static_cast<uint32_t>(cnt - 1));
   return c;
 }
 
 __global__ void emitNodesKernel(int n, const int* __restrict__ left, const int* __restrict__ right,
-                                const int* __restrict__ first, const int* __restrict__ last,
+                                const int* __restrict__ parent, const int* __restrict__ first,
+                                const int* __restrict__ last, const uint8_t* __restrict__ leafy,
                                 const float* __restrict__ boxes, float4* __restrict__ nodes, unsigned* stats) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
-  if (i != 0 && count(i, n, first, last) <= static_cast<int>(kLbvhLeaf)) return;
+  if (insideLeaf(i, n, parent, first, last, leafy)) return;
   const int l = left[i], r = right[i];
   float ca[3], ea[3], cb[3], eb[3];
   centreExtent(boxes + 6 * static_cast<size_t>(l), ca, ea);
   centreExtent(boxes + 6 * static_cast<size_t>(r), cb, eb);
-  const int rl = childRef(l, n, first, last), rr = childRef(r, n, first, last);
+  const int rl = childRef(l, n, first, last, leafy), rr = childRef(r, n, first, last, leafy);
   float4* o = nodes + 4 * static_cast<size_t>(i);
   o[0] = make_float4(ca[0], ca[1], ca[2], ea[0]);
   o[1] = make_float4(ea[1], ea[2], cb[0], cb[1]);
@@ -252,22 +289,19 @@ __global__ void emitNodesKernel(int n, const int* __restrict__ left, const int* 
   atomicAdd(&stats[1], (rl < 0 ? 1u : 0u) + (rr < 0 ? 1u : 0u));
 }
 
-// Depth (in inner nodes above it) of every emitted leaf reference.
+// Depth (in inner nodes above it) of every emitted leaf reference: from
+// Karras leaf g, skip the nodes inside the leaf that holds it (below its
+// topmost ancestor made a leaf), then count the emitted ancestors.
 __global__ void depthKernel(int n, const int* __restrict__ parent, const int* __restrict__ first,
-                            const int* __restrict__ last, unsigned* stats) {
+                            const int* __restrict__ last, const uint8_t* __restrict__ leafy, unsigned* stats) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
-  // Only the deepest collapsed node above leaf g is referenced; walking from
-  // the Karras leaf counts at most the levels collapsed into that leaf too.
-  int node = parent[n - 1 + g];
+  int top = -1;
+  for (int a = parent[n - 1 + g]; a > 0 && count(a, n, first, last) <= static_cast<int>(kLbvhLeaf); a = parent[a])
+    if (leafy[a]) top = a;
+  int node = top >= 0 ? parent[top] : parent[n - 1 + g];
   unsigned depth = 0;
-  bool collapsed = true;
   while (node >= 0) {
-    if (collapsed && node != 0 && count(node, n, first, last) <= static_cast<int>(kLbvhLeaf)) {
-      node = parent[node];
-      continue;
-    }
-    collapsed = false;
     ++depth;
     node = node == 0 ? -1 : parent[node];
   }
@@ -298,10 +332,13 @@ size_t lbvhTempBytes(uint32_t T) {
   const size_t n = T;
   const size_t tiles = (n + kSortTile - 1) / kSortTile;
   size_t b = 0;
-  b += 4 * align256(n * 4);                    // keys, vals, keysAlt, valsAlt
+  b += 2 * align256(n * 8);                    // keys, keysAlt
+  b += 2 * align256(n * 4);                    // vals, valsAlt
   b += align256(tiles * kRadix * 4);           // histogram
   b += 5 * align256(2 * n * 4);                // left, right, parent, first, last (over-sized)
   b += align256(2 * n * 6 * 4);                // boxes of all node ids
+  b += align256(2 * n * 4);                    // costs of all node ids
+  b += align256(n);                            // leaf flags of the inner nodes
   b += align256(n * 4);                        // visit counters
   b += align256(16);                           // stats
   return b;
@@ -310,7 +347,7 @@ size_t lbvhTempBytes(uint32_t T) {
 cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_t* d_flags, uint32_t T,
                       const float* centroidLo, const float* centroidHi, float4* d_nodes, float4* d_tris,
                       float4* d_shade, void* d_temp, uint32_t* statsOut, cudaStream_t stream) {
-  if (T < 2 * kLbvhLeaf + 1) return cudaErrorInvalidValue;  // tiny scenes use the host builder
+  if (T < 9) return cudaErrorInvalidValue;  // tiny scenes use the host builder
   const size_t n = T;
   const uint32_t tiles = static_cast<uint32_t>((n + kSortTile - 1) / kSortTile);
   char* p = static_cast<char*>(d_temp);
@@ -319,9 +356,9 @@ cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_
     p += align256(bytes);
     return q;
   };
-  uint32_t* keys = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint64_t* keys = reinterpret_cast<uint64_t*>(take(n * 8));
   uint32_t* vals = reinterpret_cast<uint32_t*>(take(n * 4));
-  uint32_t* keys2 = reinterpret_cast<uint32_t*>(take(n * 4));
+  uint64_t* keys2 = reinterpret_cast<uint64_t*>(take(n * 8));
   uint32_t* vals2 = reinterpret_cast<uint32_t*>(take(n * 4));
   uint32_t* hist = reinterpret_cast<uint32_t*>(take(static_cast<size_t>(tiles) * kRadix * 4));
   int* left = reinterpret_cast<int*>(take(2 * n * 4));
@@ -330,6 +367,8 @@ cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_
   int* first = reinterpret_cast<int*>(take(2 * n * 4));
   int* last = reinterpret_cast<int*>(take(2 * n * 4));
   float* boxes = reinterpret_cast<float*>(take(2 * n * 6 * 4));
+  float* cost = reinterpret_cast<float*>(take(2 * n * 4));
+  uint8_t* leafy = reinterpret_cast<uint8_t*>(take(n));
   unsigned* visits = reinterpret_cast<unsigned*>(take(n * 4));
   unsigned* stats = reinterpret_cast<unsigned*>(take(16));
 
@@ -340,25 +379,26 @@ cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_
   // top-level splits on its long axes instead of cutting its thin axis as
   // often as the others, which would make sibling boxes overlap.
   const float big = fmaxf(fmaxf(ext[0], ext[1]), ext[2]);
-  const float s = big > 0.f ? 1023.0f / big : 0.f;
+  const float s = big > 0.f ? 2097151.0f / big : 0.f;
   sc.x = sc.y = sc.z = s;
   const unsigned g = static_cast<unsigned>((n + 255) / 256);
   mortonKernel<<<g, 256, 0, stream>>>(d_verts, T, lo, sc, keys, vals);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
-  for (int shift = 0; shift < 30; shift += 8) {
+  uint64_t *kin = keys, *kout = keys2;
+  uint32_t *vin = vals, *vout = vals2;
+  for (int shift = 0; shift < 63; shift += 8) {
     radixCountKernel<<<tiles, kSortThreads, 0, stream>>>(kin, T, shift, tiles, hist);
     scanKernel<<<1, 1024, 0, stream>>>(hist, tiles * kRadix);
     radixScatterKernel<<<tiles, kSortThreads, 0, stream>>>(kin, vin, T, shift, tiles, hist, kout, vout);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    uint32_t* t = kin;
+    uint64_t* tk = kin;
     kin = kout;
-    kout = t;
-    t = vin;
+    kout = tk;
+    uint32_t* tv = vin;
     vin = vout;
-    vout = t;
+    vout = tv;
   }
   e = cudaMemsetAsync(parent, 0xff, 2 * n * 4, stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(visits, 0, n * 4, stream);
@@ -366,9 +406,11 @@ cudaError_t buildLbvh(const float* d_verts, const float* d_colours, const uint8_
   if (e != cudaSuccess) return e;
   const unsigned gi = static_cast<unsigned>((n - 1 + 255) / 256);
   hierarchyKernel<<<gi, 256, 0, stream>>>(kin, static_cast<int>(n), left, right, parent, first, last);
-  boxesKernel<<<g, 256, 0, stream>>>(d_verts, vin, static_cast<int>(n), left, right, parent, boxes, visits);
-  emitNodesKernel<<<gi, 256, 0, stream>>>(static_cast<int>(n), left, right, first, last, boxes, d_nodes, stats);
-  depthKernel<<<g, 256, 0, stream>>>(static_cast<int>(n), parent, first, last, stats);
+  boxesKernel<<<g, 256, 0, stream>>>(d_verts, vin, static_cast<int>(n), left, right, parent, first, last, boxes, cost,
+                                     leafy, visits);
+  emitNodesKernel<<<gi, 256, 0, stream>>>(static_cast<int>(n), left, right, parent, first, last, leafy, boxes, d_nodes,
+                                          stats);
+  depthKernel<<<g, 256, 0, stream>>>(static_cast<int>(n), parent, first, last, leafy, stats);
   gatherKernel<<<g, 256, 0, stream>>>(d_verts, d_colours, d_flags, vin, T, d_tris, d_shade);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
