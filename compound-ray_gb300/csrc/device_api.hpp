@@ -279,6 +279,14 @@ struct InsideQuery {
   double inv[9];
   double t[3];
   double startX;
+  // Grid over the object-space (y, z) plane: cell (cz * G + cy) lists, in
+  // cellItems[cellStart[c] .. cellStart[c + 1]), every triangle whose (y, z)
+  // box, widened by a margin, meets the cell; cell of y is
+  // floor((y - y0) * inv) clamped to [0, G).  G == 0: test every triangle.
+  const uint32_t* cellStart = nullptr;
+  const uint32_t* cellItems = nullptr;
+  double y0 = 0.0, z0 = 0.0, cellInv = 0.0;
+  int G = 0;
 };
 cudaError_t launchInside(const float3* tris, uint32_t nTris, const InsideQuery& q, const float* pts, size_t n,
                          uint8_t* out, cudaStream_t stream);

@@ -990,6 +990,70 @@ bool isInsideHitGeometry(float x, float y, float z, char* name) {
       false);
 }
 
+// (y, z) grid of a hitbox mesh's object-space triangles for the batched
+// inside query (InsideQuery).  A triangle is listed in every cell that its
+// (y, z) box meets after widening by 1e-5 of (mesh extent + largest
+// coordinate): the parity cast counts a triangle only where its point lies
+// in the triangle's (y, z) projection up to double rounding, far inside that
+// margin, so the cell of any point holds every triangle the full loop could
+// count for it.  About two triangles per cell, at most 256 x 256 cells.
+struct HitGrid {
+  std::vector<uint32_t> start, items;
+  double y0 = 0.0, z0 = 0.0, inv = 0.0;
+  int G = 0;
+};
+
+HitGrid buildHitGrid(const HitboxMesh& m) {
+  HitGrid g;
+  const size_t nt = m.tris.size() / 3;
+  if (nt == 0) return g;
+  double ylo = INFINITY, yhi = -INFINITY, zlo = INFINITY, zhi = -INFINITY, big = 0.0;
+  for (const f3& v : m.tris) {
+    ylo = std::min(ylo, double(v.y));
+    yhi = std::max(yhi, double(v.y));
+    zlo = std::min(zlo, double(v.z));
+    zhi = std::max(zhi, double(v.z));
+    big = std::max({big, std::fabs(double(v.x)), std::fabs(double(v.y)), std::fabs(double(v.z))});
+  }
+  if (!std::isfinite(ylo + yhi + zlo + zhi + big)) return g;  // non-finite vertices: test every triangle
+  const double ext = std::max(yhi - ylo, zhi - zlo);
+  const double eps = 1e-5 * (ext + big) + 1e-30;
+  g.G = std::max(1, std::min(256, static_cast<int>(std::sqrt(double(nt) / 2.0))));
+  g.y0 = ylo - eps;
+  g.z0 = zlo - eps;
+  const double size = ext + 2.0 * eps;
+  g.inv = double(g.G) / size;
+  auto cellOf = [&](double v, double v0) {
+    const double c = std::floor((v - v0) * g.inv);
+    return c < 0.0 ? 0 : (c >= double(g.G) ? g.G - 1 : static_cast<int>(c));
+  };
+  std::vector<int> box(4 * nt);
+  g.start.assign(static_cast<size_t>(g.G) * g.G + 1, 0);
+  for (size_t t = 0; t < nt; ++t) {
+    const f3 &a = m.tris[3 * t], &b = m.tris[3 * t + 1], &c = m.tris[3 * t + 2];
+    const double y0 = std::min({double(a.y), double(b.y), double(c.y)}) - eps;
+    const double y1 = std::max({double(a.y), double(b.y), double(c.y)}) + eps;
+    const double z0 = std::min({double(a.z), double(b.z), double(c.z)}) - eps;
+    const double z1 = std::max({double(a.z), double(b.z), double(c.z)}) + eps;
+    int* bx = &box[4 * t];
+    bx[0] = cellOf(y0, g.y0);
+    bx[1] = cellOf(y1, g.y0);
+    bx[2] = cellOf(z0, g.z0);
+    bx[3] = cellOf(z1, g.z0);
+    for (int cz = bx[2]; cz <= bx[3]; ++cz)
+      for (int cy = bx[0]; cy <= bx[1]; ++cy) ++g.start[static_cast<size_t>(cz) * g.G + cy + 1];
+  }
+  for (size_t c = 0; c + 1 < g.start.size(); ++c) g.start[c + 1] += g.start[c];
+  g.items.resize(g.start.back());
+  std::vector<uint32_t> fill(g.start.begin(), g.start.end() - 1);
+  for (size_t t = 0; t < nt; ++t) {
+    const int* bx = &box[4 * t];
+    for (int cz = bx[2]; cz <= bx[3]; ++cz)
+      for (int cy = bx[0]; cy <= bx[1]; ++cy) g.items[fill[static_cast<size_t>(cz) * g.G + cy]++] = static_cast<uint32_t>(t);
+  }
+  return g;
+}
+
 int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, unsigned char* inside) {
   return guarded(
       "crInsideHitGeometryBatch",
@@ -1029,6 +1093,23 @@ int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, un
         static_assert(sizeof(f3) == sizeof(float3), "f3 and float3 share a layout");
         if (nt) check(cudaMemcpyAsync(tri.ptr, hm->tris.data(), nt * 3 * sizeof(float3), cudaMemcpyHostToDevice, st),
                       "cudaMemcpy");
+        const HitGrid grid = buildHitGrid(*hm);
+        DevBuf<uint32_t> cellStart, cellItems;
+        if (grid.G > 0) {
+          cellStart.ensure(grid.start.size());
+          cellItems.ensure(std::max<size_t>(1, grid.items.size()));
+          check(cudaMemcpyAsync(cellStart.ptr, grid.start.data(), grid.start.size() * 4, cudaMemcpyHostToDevice, st),
+                "cudaMemcpy");
+          if (!grid.items.empty())
+            check(cudaMemcpyAsync(cellItems.ptr, grid.items.data(), grid.items.size() * 4, cudaMemcpyHostToDevice, st),
+                  "cudaMemcpy");
+          q.cellStart = cellStart.ptr;
+          q.cellItems = cellItems.ptr;
+          q.y0 = grid.y0;
+          q.z0 = grid.z0;
+          q.cellInv = grid.inv;
+          q.G = grid.G;
+        }
         check(cudaMemcpyAsync(pts.ptr, points, 3 * n * sizeof(float), cudaMemcpyHostToDevice, st), "cudaMemcpy");
         check(launchInside(tri.ptr, nt, q, pts.ptr, n, res.ptr, st), "hitbox query");
         check(cudaMemcpyAsync(inside, res.ptr, n, cudaMemcpyDeviceToHost, st), "cudaMemcpy");

@@ -1811,6 +1811,8 @@ namespace {
 // Parity ray cast of sutil/hitscanprocessing.cpp:20-83 for many points, in
 // explicitly rounded double arithmetic in the host test's operation order
 // (gltf.cpp pointInsideHitbox), so both give the same answer bit for bit.
+// With a (y, z) grid only the triangles of the point's cell are tested; the
+// grid lists every triangle the full loop could count there.
 __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, InsideQuery q,
                              const float* __restrict__ pts, size_t n, uint8_t* __restrict__ out) {
   const size_t k = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1831,7 +1833,20 @@ __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, In
   }
   dx = __ddiv_rn(dx, dl);
   unsigned crossings = 0;
-  for (uint32_t t = 0; t < nTris; ++t) {
+  // The ray runs along x at the point's (y, z): only triangles listed in the
+  // grid cell of (y, z) can be crossed.
+  uint32_t first = 0, end = nTris;
+  if (q.G > 0) {
+    auto cellOf = [&](double v, double v0) {
+      const double c = floor(__dmul_rn(__dsub_rn(v, v0), q.cellInv));
+      return c < 0.0 ? 0 : (c >= static_cast<double>(q.G) ? q.G - 1 : static_cast<int>(c));
+    };
+    const uint32_t c = static_cast<uint32_t>(cellOf(sz, q.z0) * q.G + cellOf(sy, q.y0));
+    first = q.cellStart[c];
+    end = q.cellStart[c + 1];
+  }
+  for (uint32_t j = first; j < end; ++j) {
+    const uint32_t t = q.G > 0 ? q.cellItems[j] : j;
     const float3 p0 = tris[3 * t], p1 = tris[3 * t + 1], p2 = tris[3 * t + 2];
     // vertex differences in float, as the host test's float members give them
     const double e1[3] = {__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z)};
