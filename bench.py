@@ -842,6 +842,8 @@ def run_profile_learned(args):
     info = workload(1024)
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
+    if lib.crSetRenderVariant(args.variant) != 0 or lib.crSetCutRadius(args.cut) != 0:
+        raise RuntimeError(eh.lastError(lib))
     N = lib.getCurrentEyeOmmatidialCount()
     rng = np.random.default_rng(scenes.SEED + 11)
     P = min(args.poses, 1000)

@@ -180,11 +180,17 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
 // assembleFeatures + the layer-by-layer forward.
 cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
                           const MlpWeights& w, float* out, cudaStream_t stream, bool residual = true);
-// The same prediction on the tcgen05 tensor cores (mlp_tc.cu): accumulators
-// in TMEM, operands in shared memory; errFlag receives kErrMmaTimeout if a
-// bounded wait ran out.  order: null, or the eye's direction order (rows of
-// a tile are then neighbouring ommatidia; results do not depend on it).
-cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
+// Inputs of the tcgen05 prediction (mlp_tc.cu): per row of the P x N
+// statistics three float4 of derived values (derived: 3 N P float4), per
+// ommatidium its unit axis and acceptance angle (axes: N float4).
+cudaError_t deriveFeatureStats(const float* stats, const float4* omm, uint32_t N, uint32_t P, float4* derived,
+                               float4* axes, cudaStream_t stream);
+// The same prediction on the tcgen05 tensor cores (mlp_tc.cu) from
+// deriveFeatureStats' output: accumulators in TMEM, operands in shared
+// memory; errFlag receives kErrMmaTimeout if a bounded wait ran out.  order:
+// null, or the eye's direction order (rows of a tile are then neighbouring
+// ommatidia; results do not depend on it).
+cudaError_t inferDenoiserTc(const float4* derived, const float4* axes, const int* nb, uint32_t N, uint32_t P,
                             const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream,
                             bool residual = true, const uint32_t* order = nullptr);
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,

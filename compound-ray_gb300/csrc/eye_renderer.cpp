@@ -1619,6 +1619,7 @@ struct DenoiseState {
   uint32_t featSpp = 0, targetSpp = 0;
   bool featReady = false, targetReady = false;
   DevBuf<float> stats, base, out, scratch;
+  DevBuf<float4> derived, axes;  // inputs of the tcgen05 inference (deriveFeatureStats)
   DevBuf<uint16_t> X;
   DevBuf<float4> poses;
   // Sample-count allocator: a second network of the same shape, trained on
@@ -1798,9 +1799,14 @@ int crDenoiserRenderPosesDevice(const float* d_poses, size_t count, int featureS
         for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
           const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
           const float* st = d.stats.ptr + first * e.N * kFeatureStats;
+          if (d.inferKernel == 1) {
+            d.derived.ensure(static_cast<size_t>(3) * P * e.N);
+            d.axes.ensure(std::max<size_t>(1, e.N));
+            check(deriveFeatureStats(st, e.omm.ptr, e.N, P, d.derived.ptr, d.axes.ptr, r.stream()), "feature statistics");
+          }
           check(d.inferKernel == 1
-                    ? inferDenoiserTc(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
-                                      r.errWord(), r.stream(), true, e.order.ptr)
+                    ? inferDenoiserTc(d.derived.ptr, d.axes.ptr, d.nb.ptr, e.N, P, d.net.weights(),
+                                      d_out + 3 * first * e.N, r.errWord(), r.stream(), true, e.order.ptr)
                     : inferDenoiser(st, e.omm.ptr, d.nb.ptr, e.N, P, d.net.weights(), d_out + 3 * first * e.N,
                                     r.stream()),
                 "denoiser inference");
@@ -2067,9 +2073,15 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           denoiseFeatures(r, d, e, poses + 4 * first, P, fs, false);
           rays += static_cast<double>(rows) * fs;
           d.pred.ensure(rows * 3);
+          if (d.inferKernel == 1) {
+            d.derived.ensure(3 * rows);
+            d.axes.ensure(std::max<size_t>(1, e.N));
+            check(deriveFeatureStats(d.stats.ptr, e.omm.ptr, e.N, P, d.derived.ptr, d.axes.ptr, st),
+                  "feature statistics");
+          }
           auto infer = [&](const MlpWeights& w, float* o, bool residual) {
             return d.inferKernel == 1
-                       ? inferDenoiserTc(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, r.errWord(), st, residual,
+                       ? inferDenoiserTc(d.derived.ptr, d.axes.ptr, d.nb.ptr, e.N, P, w, o, r.errWord(), st, residual,
                                          e.order.ptr)
                        : inferDenoiser(d.stats.ptr, e.omm.ptr, d.nb.ptr, e.N, P, w, o, st, residual);
           };

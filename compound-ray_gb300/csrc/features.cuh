@@ -112,6 +112,57 @@ __device__ __forceinline__ void featureRowTo(const float* __restrict__ stats, co
     for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) put(k, __float2bfloat16(0.f));
 }
 
+// The per-(pose, ommatidium) values a feature row reads, derived once:
+// three float4 (m0, m1, m2, 4 sd0), (4 sd1, 4 sd2, hit, logDepth),
+// (n0, n1, n2, 0), the same float operations as ommStats.
+__device__ __forceinline__ void deriveStats(const float* __restrict__ s, float4* __restrict__ out) {
+  const OmmStats r = ommStats(s);
+  out[0] = make_float4(r.m[0], r.m[1], r.m[2], r.sd[0] * 4.0f);
+  out[1] = make_float4(r.sd[1] * 4.0f, r.sd[2] * 4.0f, r.hit, r.logDepth);
+  out[2] = make_float4(r.n[0], r.n[1], r.n[2], 0.f);
+}
+
+// featureRowTo from derived statistics (deriveStats, three float4 per row)
+// and unit axes ((axis, acceptance angle) per ommatidium, as ommAxis gives
+// them): the same feature values with vector loads and no transcendental
+// functions per gathered ommatidium.
+template <typename Put>
+__device__ __forceinline__ void featureRowDerived(const float4* __restrict__ derived, const float4* __restrict__ axes,
+                                                  const int* __restrict__ nb, uint32_t N, size_t row, bool withSelf,
+                                                  int jBegin, int jEnd, Put put) {
+  const uint32_t p = static_cast<uint32_t>(row / N), o = static_cast<uint32_t>(row % N);
+  const float4* dp = derived + static_cast<size_t>(p) * N * 3;
+  const float4 a0 = __ldg(dp + 3 * o), a1 = __ldg(dp + 3 * o + 1);
+  const float4 ax = __ldg(axes + o);
+  const float aa = ax.w;
+  const float3 d = make_float3(ax.x, ax.y, ax.z);
+  if (withSelf) {
+    const float4 a2 = __ldg(dp + 3 * o + 2);
+    const float f[kFeatBlock] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z,
+                                 d.x,  d.y,  d.z,  aa * 10.0f};
+    for (int k = 0; k < kFeatBlock; ++k) put(k, __float2bfloat16(f[k]));
+  }
+  if (jBegin >= jEnd) return;
+  const float inva = 1.0f / fmaxf(aa, 1e-6f);
+  float3 t1 = fabsf(d.y) < 0.9f ? make_float3(d.z, 0.f, -d.x) : make_float3(0.f, -d.z, d.y);
+  const float il = rsqrtf(fmaxf(t1.x * t1.x + t1.y * t1.y + t1.z * t1.z, 1e-30f));
+  t1 = make_float3(t1.x * il, t1.y * il, t1.z * il);
+  const float3 t2 = make_float3(d.y * t1.z - d.z * t1.y, d.z * t1.x - d.x * t1.z, d.x * t1.y - d.y * t1.x);
+  for (int j = jBegin; j < jEnd; ++j) {
+    const uint32_t q = static_cast<uint32_t>(__ldg(nb + kNeighbours * o + j));
+    const float4 b0 = __ldg(dp + 3 * q), b1 = __ldg(dp + 3 * q + 1), b2 = __ldg(dp + 3 * q + 2);
+    const float4 e = __ldg(axes + q);
+    const float3 g = make_float3(e.x - d.x, e.y - d.y, e.z - d.z);
+    const float u = (g.x * t1.x + g.y * t1.y + g.z * t1.z) * inva, v = (g.x * t2.x + g.y * t2.y + g.z * t2.z) * inva;
+    const float f[kFeatBlock] = {(b0.x - a0.x) * 4.0f, (b0.y - a0.y) * 4.0f, (b0.z - a0.z) * 4.0f,
+                                 b0.w, b1.x, b1.y, b1.z - a1.z, b1.w - a1.w, b2.x, b2.y, b2.z,
+                                 u, v, sqrtf(u * u + v * v), e.w * inva};
+    for (int k = 0; k < kFeatBlock; ++k) put(kFeatBlock * (j + 1) + k, __float2bfloat16(f[k]));
+  }
+  if (jEnd == kNeighbours)
+    for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) put(k, __float2bfloat16(0.f));
+}
+
 // The row into a linear bf16 array x[kFeatureWidth].
 __device__ __forceinline__ void featureRow(const float* __restrict__ stats, const float4* __restrict__ omm,
                                            const int* __restrict__ nb, uint32_t N, size_t row, bool withSelf,

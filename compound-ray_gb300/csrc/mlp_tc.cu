@@ -3,25 +3,30 @@
 // Same function as inferKernel in mlp.cu (feature rows from the feature-render
 // statistics, 112 -> 128 -> 128 -> 128 -> 8 network with bf16 operands and
 // fp32 accumulation, bias + ReLU between layers, residual add), laid out for
-// sm_103a's MMA unit:
-//   * one persistent block of 512 threads per SM; all weights staged once in
-//     shared memory as K-major UMMA operands (transposed to [out][in]) in the
-//     canonical no-swizzle layout: 8-row x 16-byte core matrices, core
-//     matrices along K 128 bytes apart (leading byte offset) and 8-row groups
-//     K*16 bytes apart (stride byte offset);
-//   * per tile of 128 rows, four threads assemble each row's 112 features
-//     (own block + neighbour 0 / neighbours 1-2 / 3-4 / 5 + padding) into the
-//     activation buffer in the same layout; one elected thread issues the
-//     layer's tcgen05.mma instructions (M = 128, N = 128, K = 16 each) into a
-//     128-column TMEM accumulator and commits them to an mbarrier;
-//   * warp w reads accumulator lanes 32 (w % 4) .. +31, columns 32 (w / 4)
-//     .. +31 back with tcgen05.ld, adds the bias, applies ReLU, rounds to
-//     bf16 and writes the next layer's operand; the last layer (N padded to
-//     16) adds the residual base.
-// The accumulators live in TMEM, so the epilogue needs 32 registers per
-// chunk instead of 64 per thread for a whole layer.  Every wait on the
-// mbarrier is bounded: on timeout the block records an error bit, waits
-// (bounded) for its last commit, frees its TMEM and returns.
+// sm_103a's MMA unit as a two-role pipeline in one persistent block of 768
+// threads per SM:
+//   * all weights are staged once in shared memory as K-major UMMA operands
+//     (transposed to [out][in]) in the canonical no-swizzle layout: 8-row x
+//     16-byte core matrices, core matrices along K 128 bytes apart (leading
+//     byte offset) and 8-row groups K*16 bytes apart (stride byte offset);
+//   * feature warps 0-15 build the 112 features of each row of a 128-row
+//     tile (four threads per row: own block + neighbour 0 / neighbours 1-2 /
+//     3-4 / 5 + padding) from statistics derived once per row (deriveKernel:
+//     three float4) and unit axes (axesKernel), into one of two tile
+//     buffers, and signal it full on an mbarrier;
+//   * network warps 16-23 take the full buffer: one elected thread issues
+//     each layer's tcgen05.mma instructions (M = 128, N = 128, K = 16 each)
+//     into a 128-column TMEM accumulator and commits them to an mbarrier.
+//     Warps 16 + q and 20 + q read accumulator lanes 32 q .. +31, columns
+//     0-63 and 64-127, with tcgen05.ld, add the bias, apply ReLU, round to
+//     bf16 and write the next layer's operand into the same tile buffer (the
+//     MMAs that read it are done);
+//     the last layer (N padded to 16) adds the residual base and writes the
+//     output, and its commit hands the buffer back to the feature warps.
+// So the feature warps gather tile i + 1 (and i + 2) while the network warps
+// run tile i.  Every mbarrier wait is bounded: on timeout the waiting side
+// records an error bit and stops; the other side then times out too, the
+// network warps wait (bounded) for their last commit, and the TMEM is freed.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -35,7 +40,9 @@ namespace cr {
 namespace {
 
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 512;  // 4 threads per row for the features; 16 warps share the epilogue
+constexpr int kFeatThreads = 512;  // feature warps 0-15: four threads per row
+constexpr int kNetThreads = 256;   // network warps 16-23: two per accumulator lane quarter
+constexpr int kTcThreads = kFeatThreads + kNetThreads;
 constexpr int kTmemCols = 128;
 constexpr uint32_t kSpinLimit = 1u << 26;  // bounded waits (far longer than one layer's MMAs)
 
@@ -142,11 +149,15 @@ constexpr uint32_t kOffW1 = 0;
 constexpr uint32_t kOffW2 = kOffW1 + kW1Bytes;
 constexpr uint32_t kOffW3 = kOffW2 + kWBytes;
 constexpr uint32_t kOffW4 = kOffW3 + kWBytes;
-constexpr uint32_t kOffA0 = kOffW4 + kW4Bytes;
-constexpr uint32_t kOffA1 = kOffA0 + kActBytes;
-constexpr uint32_t kOffBias = kOffA1 + kActBytes;                    // 3 x 128 + 16 floats
-constexpr uint32_t kOffBar = kOffBias + (3 * kMlpHidden + 16) * 4;  // mbarrier (8 B) + TMEM address (4 B)
-constexpr uint32_t kTcSmem = kOffBar + 16 + 128;                    // + alignment slack
+// Two tile buffers: features (K = 112 layout), then in place the hidden
+// activations of layers 1-3 (K = 128 layout).  Small enough that the rest of
+// the SM's 256 KB stays L1 cache for the feature gathers.
+constexpr uint32_t kOffB0 = kOffW4 + kW4Bytes;
+constexpr uint32_t kOffB1 = kOffB0 + kActBytes;
+constexpr uint32_t kOffBias = kOffB1 + kActBytes;                   // 3 x 128 + 16 floats
+constexpr uint32_t kOffBar = kOffBias + (3 * kMlpHidden + 16) * 4;  // 5 mbarriers (8 B each) + TMEM address
+constexpr uint32_t kTcSmem = kOffBar + 48 + 128;                    // + alignment slack
+static_assert(kTcSmem <= 227 * 1024, "shared memory plan exceeds a block's limit");
 
 // Row (pose * N + ommatidium) processed at position x: poses in order, the
 // ommatidia of a pose in the eye's direction order, so that a tile's rows
@@ -167,15 +178,55 @@ __device__ void stageWeights(unsigned char* dst, const __nv_bfloat16* __restrict
   }
 }
 
+// Derived statistics of every row and unit axes of every ommatidium for
+// featureRowDerived.
+__global__ void deriveKernel(const float* __restrict__ stats, uint64_t rows, float4* __restrict__ derived) {
+  const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  feat::deriveStats(stats + r * kFeatureStats, derived + 3 * r);
+}
+
+__global__ void axesKernel(const float4* __restrict__ omm, uint32_t N, float4* __restrict__ axes) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= N) return;
+  float aa;
+  const float3 d = feat::ommAxis(omm, o, aa);
+  axes[o] = make_float4(d.x, d.y, d.z, aa);
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbarArrive(uint32_t mbar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar) : "memory");
+}
+
+// AND of `v` over the network threads (named barrier 1).
+__device__ __forceinline__ bool netAll(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"(v ? 1u : 0u), "n"(kNetThreads)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void netSync() { asm volatile("bar.sync 1, %0;" ::"n"(kNetThreads) : "memory"); }
+
 __global__ void __launch_bounds__(kTcThreads, 1)
-    inferTcKernel(const float* __restrict__ stats, const float4* __restrict__ omm, const int* __restrict__ nb,
+    inferTcKernel(const float4* __restrict__ derived, const float4* __restrict__ axes, const int* __restrict__ nb,
                   uint32_t N, uint64_t rows, MlpWeights w, bool residual, float* __restrict__ out,
                   uint32_t* errFlag, const uint32_t* __restrict__ order) {
   extern __shared__ __align__(128) unsigned char smemRaw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 127) & ~uintptr_t(127));
   float* bias = reinterpret_cast<float*>(sm + kOffBias);  // b1 | b2 | b3 | b4 (16)
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(sm + kOffBar + 8);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kOffBar);  // full0, full1, empty0, empty1, mma
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(sm + kOffBar + 40);
   const int tid = threadIdx.x, warp = tid >> 5;
 
   stageWeights(sm + kOffW1, w.w1, kFeatureWidth, kMlpHidden, kMlpHidden);
@@ -188,12 +239,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     bias[2 * kMlpHidden + e] = w.b3[e];
   }
   if (tid < 16) bias[3 * kMlpHidden + tid] = tid < kMlpOut ? w.b4[tid] : 0.f;
-  const uint32_t mbar = smemAddr(bar);
+  const uint32_t fullBar[2] = {smemAddr(bars), smemAddr(bars + 1)};
+  const uint32_t emptyBar[2] = {smemAddr(bars + 2), smemAddr(bars + 3)};
+  const uint32_t mmaBar = smemAddr(bars + 4);
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    mbarInit(fullBar[0], kFeatThreads);
+    mbarInit(fullBar[1], kFeatThreads);
+    mbarInit(emptyBar[0], 1);
+    mbarInit(emptyBar[1], 1);
+    mbarInit(mmaBar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == kFeatThreads / 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tmemSlot)),
                  "r"(kTmemCols)
                  : "memory");
@@ -203,104 +260,141 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
-  const uint32_t tmem = *tmemSlot;
-  const int lq = warp & 3, cb = warp >> 2;  // TMEM lane quarter and 32-column block of this warp
-  const uint32_t laneBase = tmem + (static_cast<uint32_t>(lq * 32) << 16);
-  const int myRow = lq * 32 + (tid & 31);   // tile row whose accumulators this thread reads
-
-  uint32_t phase = 0;
-  bool ok = true;
   const uint64_t tiles = (rows + kTcRows - 1) / kTcRows;
-  const uint32_t sW[4] = {smemAddr(sm + kOffW1), smemAddr(sm + kOffW2), smemAddr(sm + kOffW3), smemAddr(sm + kOffW4)};
-  const uint32_t sA[2] = {smemAddr(sm + kOffA0), smemAddr(sm + kOffA1)};
 
-  for (uint64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    // Features of row tid / 4 into A0 (K = 112 layout), a quarter per thread.
-    {
-      const uint32_t r = static_cast<uint32_t>(tid >> 2), q = static_cast<uint32_t>(tid & 3);
-      const uint64_t fpos = tile * kTcRows + r;
-      const uint64_t frow = fpos < rows ? rowAt(fpos, N, order) : fpos;
-      unsigned char* a0 = sm + kOffA0;
-      auto put = [a0, r](int k, __nv_bfloat16 v) {
-        *reinterpret_cast<__nv_bfloat16*>(a0 + coreOffset(r, static_cast<uint32_t>(k), kFeatureWidth)) = v;
+  if (tid < kFeatThreads) {
+    // Feature warps: tile i of this block into buffer i & 1.
+    const uint32_t r = static_cast<uint32_t>(tid >> 2), q = static_cast<uint32_t>(tid & 3);
+    static constexpr int kBegin[4] = {0, 1, 3, 5}, kEnd[4] = {1, 3, 5, kNeighbours};
+    uint32_t i = 0;
+    for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++i) {
+      const uint32_t b = i & 1u;
+      if (i >= 2 && !waitParity(emptyBar[b], ((i >> 1) - 1u) & 1u)) {
+        atomicOr(errFlag, kErrMmaTimeout);
+        break;
+      }
+      unsigned char* fb = sm + (b ? kOffB1 : kOffB0);
+      auto put = [fb, r](int k, __nv_bfloat16 v) {
+        *reinterpret_cast<__nv_bfloat16*>(fb + coreOffset(r, static_cast<uint32_t>(k), kFeatureWidth)) = v;
       };
-      static constexpr int kBegin[4] = {0, 1, 3, 5}, kEnd[4] = {1, 3, 5, kNeighbours};
+      const uint64_t fpos = tile * kTcRows + r;
       if (fpos < rows) {
-        feat::featureRowTo(stats, omm, nb, N, frow, q == 0, kBegin[q], kEnd[q], put, nullptr);
+        feat::featureRowDerived(derived, axes, nb, N, rowAt(fpos, N, order), q == 0, kBegin[q], kEnd[q], put);
       } else {
         for (int k = static_cast<int>(q); k < kFeatureWidth; k += 4) put(k, __float2bfloat16(0.f));
       }
+      fenceAsyncShared();  // the tensor cores read the buffer through the async proxy
+      mbarArrive(fullBar[b]);
     }
-    // Four layers: A (buffer cur) x W -> TMEM -> bias/ReLU -> A (buffer 1-cur).
-    int cur = 0;
-    for (int layer = 0; layer < 4 && ok; ++layer) {
-      const uint32_t K = layer == 0 ? kFeatureWidth : kMlpHidden;
-      const uint32_t Nn = layer == 3 ? kW4Rows : kMlpHidden;
-      fenceAsyncShared();
-      tcFenceBefore();
-      __syncthreads();
-      tcFenceAfter();
-      if (tid == 0) {
-        const uint32_t idesc = instrDesc(kTcRows, Nn);
-        for (uint32_t ks = 0; ks < K / 16; ++ks) {
-          const uint64_t a = smemDesc(sA[cur] + ks * 256u, 128u, K * 16u);
-          const uint64_t b = smemDesc(sW[layer] + ks * 256u, 128u, K * 16u);
-          mmaBf16(tmem, a, b, idesc, ks > 0 ? 1u : 0u);
-        }
-        commitTo(mbar);
-      }
-      const bool landed = waitParity(mbar, phase);
-      if (!__syncthreads_and(landed)) {  // one decision for the whole block
+  } else {
+    // Network warps: the four layers of tile i from buffer i & 1.
+    const uint32_t tmem = *tmemSlot;
+    const int lq = warp & 3;                               // TMEM lane quarter this warp may read
+    const int half = (warp - kFeatThreads / 32) >> 2;      // columns 64 half .. +63
+    const int m = lq * 32 + (tid & 31);                    // accumulator lane = tile row
+    const uint32_t laneBase = tmem + (static_cast<uint32_t>(lq * 32) << 16);
+    const bool issuer = tid == kFeatThreads;
+    const uint32_t sW[4] = {smemAddr(sm + kOffW1), smemAddr(sm + kOffW2), smemAddr(sm + kOffW3),
+                            smemAddr(sm + kOffW4)};
+    const uint32_t sB[2] = {smemAddr(sm + kOffB0), smemAddr(sm + kOffB1)};
+    uint32_t phase = 0;
+    bool ok = true, pending = false;  // pending: a commit to mmaBar not yet waited for
+    uint32_t i = 0;
+    for (uint64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++i) {
+      const uint32_t b = i & 1u;
+      if (!netAll(waitParity(fullBar[b], (i >> 1) & 1u))) {
         ok = false;
-        if (tid == 0) atomicOr(errFlag, kErrMmaTimeout);
+        if (issuer) atomicOr(errFlag, kErrMmaTimeout);
         break;
       }
-      phase ^= 1u;
       tcFenceAfter();
-      if (layer < 3) {
-        const float* b = bias + layer * kMlpHidden;
-        unsigned char* dst = sm + (cur == 0 ? kOffA1 : kOffA0);
-        const int c0 = cb * 32;
-        float v[32];
-        tmemLoad32(laneBase + static_cast<uint32_t>(c0), v);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          uint4 q;
-          const int c = c0 + 8 * j;
-          q.x = packBf16(fmaxf(v[8 * j] + b[c], 0.f), fmaxf(v[8 * j + 1] + b[c + 1], 0.f));
-          q.y = packBf16(fmaxf(v[8 * j + 2] + b[c + 2], 0.f), fmaxf(v[8 * j + 3] + b[c + 3], 0.f));
-          q.z = packBf16(fmaxf(v[8 * j + 4] + b[c + 4], 0.f), fmaxf(v[8 * j + 5] + b[c + 5], 0.f));
-          q.w = packBf16(fmaxf(v[8 * j + 6] + b[c + 6], 0.f), fmaxf(v[8 * j + 7] + b[c + 7], 0.f));
-          *reinterpret_cast<uint4*>(dst + coreOffset(static_cast<uint32_t>(myRow), static_cast<uint32_t>(c),
-                                                     kMlpHidden)) = q;
+      unsigned char* h = sm + (b ? kOffB1 : kOffB0);
+      for (int layer = 0; layer < 4; ++layer) {
+        const uint32_t K = layer == 0 ? kFeatureWidth : kMlpHidden;
+        const uint32_t Nn = layer == 3 ? kW4Rows : kMlpHidden;
+        if (issuer) {
+          const uint32_t idesc = instrDesc(kTcRows, Nn);
+          for (uint32_t ks = 0; ks < K / 16; ++ks) {
+            const uint64_t a = smemDesc(sB[b] + ks * 256u, 128u, K * 16u);
+            const uint64_t bd = smemDesc(sW[layer] + ks * 256u, 128u, K * 16u);
+            mmaBf16(tmem, a, bd, idesc, ks > 0 ? 1u : 0u);
+          }
+          if (layer == 3) commitTo(emptyBar[b]);  // the tile buffer is free once these MMAs are done
+          commitTo(mmaBar);
         }
-        cur ^= 1;
-      } else if (cb == 0) {
-        float v[4];
-        tmemLoad4(laneBase, v);
-        const uint64_t pos = tile * kTcRows + static_cast<uint64_t>(myRow);
-        if (pos < rows) {
-          const uint64_t row = rowAt(pos, N, order);
-          const float* b4 = bias + 3 * kMlpHidden;
-          for (int c = 0; c < 3; ++c) {
-            const float y = v[c] + b4[c];
-            out[3 * row + c] = residual ? stats[row * kFeatureStats + c] + y : y;
+        pending = true;
+        if (!netAll(waitParity(mmaBar, phase))) {
+          ok = false;
+          if (issuer) atomicOr(errFlag, kErrMmaTimeout);
+          break;
+        }
+        pending = false;
+        phase ^= 1u;
+        tcFenceAfter();
+        if (layer < 3) {
+          const float* bl = bias + layer * kMlpHidden;
+#pragma unroll 1
+          for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
+            float v[32];
+            tmemLoad32(laneBase + static_cast<uint32_t>(c0), v);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              uint4 qv;
+              const int c = c0 + 8 * j;
+              qv.x = packBf16(fmaxf(v[8 * j] + bl[c], 0.f), fmaxf(v[8 * j + 1] + bl[c + 1], 0.f));
+              qv.y = packBf16(fmaxf(v[8 * j + 2] + bl[c + 2], 0.f), fmaxf(v[8 * j + 3] + bl[c + 3], 0.f));
+              qv.z = packBf16(fmaxf(v[8 * j + 4] + bl[c + 4], 0.f), fmaxf(v[8 * j + 5] + bl[c + 5], 0.f));
+              qv.w = packBf16(fmaxf(v[8 * j + 6] + bl[c + 6], 0.f), fmaxf(v[8 * j + 7] + bl[c + 7], 0.f));
+              *reinterpret_cast<uint4*>(h + coreOffset(static_cast<uint32_t>(m), static_cast<uint32_t>(c),
+                                                       kMlpHidden)) = qv;
+            }
+          }
+        } else if (half == 0) {
+          float v[4];
+          tmemLoad4(laneBase, v);
+          const uint64_t pos = tile * kTcRows + static_cast<uint64_t>(m);
+          if (pos < rows) {
+            const uint64_t row = rowAt(pos, N, order);
+            const float* b4 = bias + 3 * kMlpHidden;
+            const float4 mc = __ldg(derived + 3 * row);  // the mean colour, as the statistics hold it
+            const float mean[3] = {mc.x, mc.y, mc.z};
+            for (int c = 0; c < 3; ++c) {
+              const float y = v[c] + b4[c];
+              out[3 * row + c] = residual ? mean[c] + y : y;
+            }
           }
         }
+        // The next MMA reads h (async proxy) and overwrites the accumulator
+        // that every network thread has just read.
+        fenceAsyncShared();
+        tcFenceBefore();
+        netSync();
+        tcFenceAfter();
       }
     }
+    if (!ok && pending && issuer) waitParity(mmaBar, phase);  // let a late commit land before the TMEM is freed
   }
-  if (!ok && tid == 0) waitParity(mbar, phase);  // let a late commit land before the TMEM is freed
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
-  if (warp == 0)
+  if (warp == kFeatThreads / 32) {
+    const uint32_t tmem = *tmemSlot;
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
 }
 
 }  // namespace
 
-cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
+cudaError_t deriveFeatureStats(const float* stats, const float4* omm, uint32_t N, uint32_t P, float4* derived,
+                               float4* axes, cudaStream_t stream) {
+  const uint64_t rows = static_cast<uint64_t>(N) * P;
+  if (rows == 0) return cudaSuccess;
+  deriveKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(stats, rows, derived);
+  axesKernel<<<(N + 255) / 256, 256, 0, stream>>>(omm, N, axes);
+  return cudaGetLastError();
+}
+
+cudaError_t inferDenoiserTc(const float4* derived, const float4* axes, const int* nb, uint32_t N, uint32_t P,
                             const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream, bool residual,
                             const uint32_t* order) {
   const uint64_t rows = static_cast<uint64_t>(N) * P;
@@ -319,7 +413,7 @@ cudaError_t inferDenoiserTc(const float* stats, const float4* omm, const int* nb
   }
   const uint64_t tiles = (rows + kTcRows - 1) / kTcRows;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(tiles, static_cast<uint64_t>(smCount)));
-  inferTcKernel<<<grid, kTcThreads, kTcSmem, stream>>>(stats, omm, nb, N, rows, w, residual, out, errFlag, order);
+  inferTcKernel<<<grid, kTcThreads, kTcSmem, stream>>>(derived, axes, nb, N, rows, w, residual, out, errFlag, order);
   return cudaGetLastError();
 }
 

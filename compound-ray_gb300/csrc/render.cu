@@ -1443,9 +1443,18 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const uint64_t blocks = (plan.tasks * 32 + 127) / 128;
-  renderKernel<3, 5><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr,
-                                                                         errFlag, nullptr, nullptr);
+  const unsigned g = static_cast<unsigned>((plan.tasks * 32 + 127) / 128);
+  switch (g_renderVariant) {
+    case 1:
+      renderKernel<3, 6><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
+      break;
+    case 2:
+      renderKernel<3, 8><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
+      break;
+    default:
+      renderKernel<3, 5><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
+      break;
+  }
   return cudaGetLastError();
 }
 
