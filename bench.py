@@ -195,6 +195,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_throughput(units_per_rank, seconds, world, device=None):
+    """Whole-job throughput of `world` replicas that each processed
+    `units_per_rank` units in `seconds` of their own time: every rank's
+    units over the slowest rank's time (a max all-reduce across the process
+    group when world > 1).  Returns (units/s, slowest seconds)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return world * units_per_rank / seconds, seconds
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -327,14 +342,10 @@ def run_ours(args):
         torch.cuda.synchronize()
     if lib.crSynchronize() != 0:
         raise RuntimeError(eh.lastError(lib))
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-        torch.distributed.barrier()
     rays_step = P * N * spp
-    value = world * rays_step * args.steps / total_s
+    value, total_s = replica_throughput(rays_step * args.steps, sum(step_ms) / 1000.0, world, dev)
+    if world > 1:
+        torch.distributed.barrier()
 
     # End to end through the C ABI with host (pinned) buffers.
     h_poses = torch.from_numpy(poses12.copy()).pin_memory()
@@ -349,12 +360,7 @@ def run_ours(args):
         if lib.crRenderPoses(pose_np, P, out_np) != 0:
             raise RuntimeError(eh.lastError(lib))
         e2e_s.append(time.perf_counter() - t0)
-    e2e_total = sum(e2e_s)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * rays_step * args.steps / e2e_total
+    e2e_value, e2e_total = replica_throughput(rays_step * args.steps, sum(e2e_s), world, dev)
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
     projection = run_projection(lib, eh, args, stream)
