@@ -95,9 +95,11 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """nvidia-smi clock/throttle samples every 50 ms; summary() keeps the
+    samples stamped between start() and stop() (the timed region), so the
+    sampler is started a little ahead of it."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -105,6 +107,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
@@ -112,11 +115,22 @@ class ClockSampler:
             os.close(fd)
             self.out = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # nvidia-smi is sampling before the timed region starts
         except Exception:
             self.proc = None
         return self
+
+    def start(self):
+        import datetime
+
+        self.t0 = datetime.datetime.now()
+
+    def stop(self):
+        import datetime
+
+        self.t1 = datetime.datetime.now()
 
     def __exit__(self, *a):
         if self.proc:
@@ -130,24 +144,33 @@ class ClockSampler:
     def summary(self):
         if not self.proc or not self.path:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm, smax, reasons = [], [], set()
+        import datetime
+
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         with open(self.path) as f:
             for line in f:
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) < 9:
+                if len(parts) < 10:
                     continue
+                stamp = None
+                for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+                    try:
+                        stamp = datetime.datetime.strptime(parts[0], fmt)
+                        break
+                    except ValueError:
+                        pass
                 try:
-                    sm.append(float(parts[1]))
-                    smax.append(float(parts[2]))
+                    rows.append((stamp, float(parts[2]), float(parts[3]), parts[6:10]))
                 except ValueError:
                     continue
-                for n, v in zip(names, parts[5:9]):
-                    if v.lower().startswith("active"):
-                        reasons.add(n)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        inside = [r for r in rows if self.t0 and self.t1 and r[0] and self.t0 <= r[0] <= self.t1]
+        use = inside or rows
+        reasons = {n for r in use for n, v in zip(names, r[3]) if v.lower().startswith("active")}
+        return {"sm_mhz": statistics.median(r[1] for r in use) if use else None,
+                "sm_max_mhz": max(r[2] for r in use) if use else None, "reasons": sorted(reasons),
+                "samples": len(use), "window": "timed region" if inside else "around the timed region"}
 
 
 def cpu_baseline(info, target_s, rank_threads=0):
@@ -331,6 +354,7 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        clocks.start()
         for _ in range(args.steps):
             flush.fill_(1.0)
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chunks]
@@ -340,6 +364,7 @@ def run_ours(args):
             launch_ms.extend(zip([n for _, n in chunks], ms))
             step_ms.append(sum(ms))
         torch.cuda.synchronize()
+        clocks.stop()
     if lib.crSynchronize() != 0:
         raise RuntimeError(eh.lastError(lib))
     rays_step = P * N * spp
