@@ -1532,8 +1532,32 @@ cudaError_t launchProject(const float* sums, uint32_t N, uchar4* frame, int w, i
 // ---------------------------------------------------------------------------
 namespace {
 
+// Sort key of a sample by where its ray leaves the acceptance cone: the
+// splay (in standard deviations) and the turn about the axis, as a point of
+// the cone's cross-section, in a 2D Morton order of 16-bit cells over
+// [-4, 4]^2.  Samples with neighbouring keys leave in neighbouring directions.
+__device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
+  float sn, cs;
+  __sincosf(ud * CR_PI_F, &sn, &cs);
+  auto cell = [](float v) {
+    const float q = fminf(fmaxf((v + 4.0f) * (65535.0f / 8.0f), 0.0f), 65535.0f);
+    uint32_t x = static_cast<uint32_t>(q);
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+  };
+  return (cell(nd * cs) << 1) | cell(nd * sn);
+}
+
 // One warp task of a bucket: up to 32 samples of one entry, or several whole
 // entries when the bucket's count is below 32 (the render kernel's plan).
+// With more than 32 samples per task (a whole warp on one entry, spl rounds
+// of 32), the task's samples are first sorted by coneKey, so that each round
+// traces 32 rays in neighbouring directions, whose traversals are alike.
+// Every sample is still traced once with its own random numbers; only the
+// order of the per-lane sums changes.
 // Random numbers: Philox4x32-10 stream (seed, e * 1024 + s), one normal then
 // one uniform per sample (O(1) set-up per entry, unlike XORWOW's skip-ahead).
 __global__ void __launch_bounds__(128, 5)
@@ -1558,6 +1582,39 @@ __global__ void __launch_bounds__(128, 5)
   const bool valid = i < B.count;
   v3 col = mk(0.f, 0.f, 0.f);
   uint32_t nodeVisits = 0, triTests = 0;
+  __shared__ uint32_t sortKey[4][256], sortIdx[4][256];  // per warp of the block (128 threads)
+  uint32_t* key = sortKey[threadIdx.x >> 5];
+  uint32_t* idx = sortIdx[threadIdx.x >> 5];
+  if (valid && spl > 1) {  // the warp is one entry (segWidth 32): `valid` is warp-uniform
+    const uint32_t e = B.entries[i];
+    const uint32_t n = 32u * spl;  // 64, 128 or 256
+    for (uint32_t k = lane; k < n; k += 32u) {
+      curandStatePhilox4_32_10_t st;
+      curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + chunk * n + k, 0ull, &st);
+      const float nd = curand_normal(&st);
+      const float ud = curand_uniform(&st);
+      key[k] = coneKey(nd, ud);
+      idx[k] = k;
+    }
+    __syncwarp();
+    // bitonic sort of (key, idx) pairs, ascending
+    for (uint32_t size = 2; size <= n; size <<= 1)
+      for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+        for (uint32_t m = lane; m < n / 2; m += 32u) {
+          const uint32_t lo = 2u * stride * (m / stride) + (m % stride), hi = lo + stride;
+          const bool up = (lo & size) == 0u;
+          const uint32_t ka = key[lo], kb = key[hi];
+          if ((ka > kb) == up) {
+            key[lo] = kb;
+            key[hi] = ka;
+            const uint32_t t2 = idx[lo];
+            idx[lo] = idx[hi];
+            idx[hi] = t2;
+          }
+        }
+        __syncwarp();
+      }
+  }
   if (valid) {
     const uint32_t e = B.entries[i];
     const uint32_t p = e / N, o = e - p * N;
@@ -1574,7 +1631,7 @@ __global__ void __launch_bounds__(128, 5)
                    mk(Z.x, Z.y, Z.z) * relPos.z;
     const float invSpp = 1.0f / static_cast<float>(spp);
     for (uint32_t j = 0; j < spl; ++j) {
-      const uint32_t s = chunk * 32u * spl + j * segWidth + lane % segWidth;
+      const uint32_t s = chunk * 32u * spl + (spl > 1 ? idx[j * 32u + lane] : j * segWidth + lane % segWidth);
       curandStatePhilox4_32_10_t st;
       curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + s, 0ull, &st);
       const float nd = curand_normal(&st);
