@@ -954,6 +954,7 @@ void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
       ++r.generation;
       e.release();
     } else if (e.omm.ptr && count) {
+      ++r.generation;  // tables built from the old ommatidia (neighbours, batches) are stale
       e.releaseGrids();
       check(cudaMemcpyAsync(e.omm.ptr, v.data(), sizeof(Ommatidium) * count, cudaMemcpyHostToDevice, r.stream()),
             "cudaMemcpy");
