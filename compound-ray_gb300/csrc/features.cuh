@@ -122,6 +122,19 @@ __device__ __forceinline__ void deriveStats(const float* __restrict__ s, float4*
   out[2] = make_float4(r.n[0], r.n[1], r.n[2], 0.f);
 }
 
+// Stores a block of kFeatBlock features from k0 on, converting them to bf16
+// in pairs (the same round-to-nearest-even values as one at a time).
+template <typename Put>
+__device__ __forceinline__ void putBlock(int k0, const float* f, Put put) {
+#pragma unroll
+  for (int k = 0; k + 1 < kFeatBlock; k += 2) {
+    const __nv_bfloat162 p = __floats2bfloat162_rn(f[k], f[k + 1]);
+    put(k0 + k, p.x);
+    put(k0 + k + 1, p.y);
+  }
+  if (kFeatBlock & 1) put(k0 + kFeatBlock - 1, __float2bfloat16(f[kFeatBlock - 1]));
+}
+
 // featureRowTo from derived statistics (deriveStats, three float4 per row)
 // and unit axes ((axis, acceptance angle) per ommatidium, as ommAxis gives
 // them): the same feature values with vector loads and no transcendental
@@ -140,7 +153,7 @@ __device__ __forceinline__ void featureRowDerived(const float4* __restrict__ der
     const float4 a2 = __ldg(dp + 3 * o + 2);
     const float f[kFeatBlock] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z,
                                  d.x,  d.y,  d.z,  aa * 10.0f};
-    for (int k = 0; k < kFeatBlock; ++k) put(k, __float2bfloat16(f[k]));
+    putBlock(0, f, put);
   }
   if (jBegin >= jEnd) return;
   const float inva = 1.0f / fmaxf(aa, 1e-6f);
@@ -157,7 +170,7 @@ __device__ __forceinline__ void featureRowDerived(const float4* __restrict__ der
     const float f[kFeatBlock] = {(b0.x - a0.x) * 4.0f, (b0.y - a0.y) * 4.0f, (b0.z - a0.z) * 4.0f,
                                  b0.w, b1.x, b1.y, b1.z - a1.z, b1.w - a1.w, b2.x, b2.y, b2.z,
                                  u, v, sqrtf(u * u + v * v), e.w * inva};
-    for (int k = 0; k < kFeatBlock; ++k) put(kFeatBlock * (j + 1) + k, __float2bfloat16(f[k]));
+    putBlock(kFeatBlock * (j + 1), f, put);
   }
   if (jEnd == kNeighbours)
     for (int k = kFeatBlock * (kNeighbours + 1); k < kFeatureWidth; ++k) put(k, __float2bfloat16(0.f));

@@ -134,9 +134,12 @@ __device__ __forceinline__ void tmemLoad4(uint32_t taddr, float* v) {
   for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Two floats to a bf16 pair, round to nearest even: one paired conversion
+// (the conversion pipe's throughput limited the epilogue with two single
+// ones).
 __device__ __forceinline__ uint32_t packBf16(float lo, float hi) {
-  return static_cast<uint32_t>(__bfloat16_as_ushort(__float2bfloat16(lo))) |
-         (static_cast<uint32_t>(__bfloat16_as_ushort(__float2bfloat16(hi))) << 16);
+  const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&p);
 }
 
 // Shared memory plan (bytes).
@@ -337,17 +340,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
             float v[32];
             tmemLoad32(laneBase + static_cast<uint32_t>(c0), v);
+            // the chunk's 32 biases first, then the values, then the stores
+            float bb[32];
+            const uint32_t bs = smemAddr(bl + c0);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              uint4 qv;
-              const int c = c0 + 8 * j;
-              qv.x = packBf16(fmaxf(v[8 * j] + bl[c], 0.f), fmaxf(v[8 * j + 1] + bl[c + 1], 0.f));
-              qv.y = packBf16(fmaxf(v[8 * j + 2] + bl[c + 2], 0.f), fmaxf(v[8 * j + 3] + bl[c + 3], 0.f));
-              qv.z = packBf16(fmaxf(v[8 * j + 4] + bl[c + 4], 0.f), fmaxf(v[8 * j + 5] + bl[c + 5], 0.f));
-              qv.w = packBf16(fmaxf(v[8 * j + 6] + bl[c + 6], 0.f), fmaxf(v[8 * j + 7] + bl[c + 7], 0.f));
-              *reinterpret_cast<uint4*>(h + coreOffset(static_cast<uint32_t>(m), static_cast<uint32_t>(c),
-                                                       kMlpHidden)) = qv;
-            }
+            for (int k = 0; k < 8; ++k)
+              asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                           : "=f"(bb[4 * k]), "=f"(bb[4 * k + 1]), "=f"(bb[4 * k + 2]), "=f"(bb[4 * k + 3])
+                           : "r"(bs + 16u * k));
+            uint32_t qs[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              qs[k] = packBf16(fmaxf(v[2 * k] + bb[2 * k], 0.f), fmaxf(v[2 * k + 1] + bb[2 * k + 1], 0.f));
+            const uint32_t hs = smemAddr(h);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
+                               hs + coreOffset(static_cast<uint32_t>(m), static_cast<uint32_t>(c0 + 8 * j), kMlpHidden)),
+                           "r"(qs[4 * j]), "r"(qs[4 * j + 1]), "r"(qs[4 * j + 2]), "r"(qs[4 * j + 3])
+                           : "memory");
           }
         } else if (half == 0) {
           float v[4];
