@@ -133,9 +133,11 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
 // mean over the samples: colour (3), squared colour (3), hit flag, hit
 // distance (0 on a miss), hit-triangle normal facing the ray in the eye's
 // frame (3, 0 on a miss).  stats: P x N x kFeatureStats floats.
+// cutsReady: eye.cuts already holds these poses' near-field cuts (else they
+// are built first when eye.cuts is set).
 constexpr int kFeatureStats = 11;
 cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
-                           uint32_t* errFlag, cudaStream_t stream);
+                           uint32_t* errFlag, cudaStream_t stream, bool cutsReady = false);
 
 // Denoiser network (mlp.cu).  Feature rows are kFeatureWidth bf16 values:
 // kFeatBlock values of the ommatidium itself then of its kNeighbours nearest

@@ -1686,13 +1686,23 @@ void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dpos
   if (featSpp < 1 || featSpp > 32) throw std::runtime_error("feature renders use 1 to 32 samples per ommatidium");
   const DevEye fe = streamsFor(r, e, d.featRng, d.featSpp, d.featReady, featSpp);
   d.stats.ensure(std::max<size_t>(1, count * e.N * kFeatureStats));
+  // The near-field cuts of all poses in one launch (one thread per pose).
+  DevEye all = fe;
+  r.withCuts(all, static_cast<uint32_t>(count), e.maxRel);
+  if (all.cuts)
+    check(launchCuts(r.dev, dposes, static_cast<uint32_t>(count), all.cutRadius, all.maxRel, all.cuts, r.stream()),
+          "cuts");
   for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
     const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
     DevEye de = fe;
     r.withDraws(de, P, true);
-    r.withCuts(de, P, e.maxRel);
+    if (all.cuts) {
+      de.cuts = all.cuts + first * kCutStride;
+      de.cutRadius = all.cutRadius;
+      de.maxRel = all.maxRel;
+    }
     check(launchFeatures(r.dev, de, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
-                         r.stream()),
+                         r.stream(), true),
           "feature render");
   }
   if (!rows) return;

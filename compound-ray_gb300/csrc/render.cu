@@ -1426,7 +1426,7 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
 }
 
 cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
-                           uint32_t* errFlag, cudaStream_t stream) {
+                           uint32_t* errFlag, cudaStream_t stream, bool cutsReady) {
   if (P == 0 || eye.N == 0) return cudaSuccess;
   WarpPlan plan = planWarps(eye.N, eye.spp);
   if (plan.chunks != 1) return cudaErrorInvalidValue;  // feature renders use at most 32 samples
@@ -1437,7 +1437,7 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
     if (e != cudaSuccess) return e;
     plan = splitPoses(plan, P);
   }
-  if (eye.cuts) {
+  if (eye.cuts && !cutsReady) {
     if (!(eye.cutRadius > 0.f)) return cudaErrorInvalidValue;
     cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, eye.cutRadius, eye.maxRel, eye.cuts);
     const cudaError_t e = cudaGetLastError();
