@@ -431,7 +431,9 @@ def run_ours(args):
         "eye_frames_per_s": value / (N * spp),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},
-        "gpu_launches": args.steps * len(chunks) * (2 if spp > 32 else 1),
+        # per 256-pose launch: the pose's near-field cuts (when a radius is set),
+        # the render kernel and, above 32 samples, the chunk sums
+        "gpu_launches": args.steps * len(chunks) * ((2 if spp > 32 else 1) + (1 if cut_fraction > 0 else 0)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": counters[0] if counters and launch_n == POSES_PER_LAUNCH else None,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one 256-pose launch (ncu); "
