@@ -182,6 +182,10 @@ cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* n
 // assembleFeatures + the layer-by-layer forward.
 cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P,
                           const MlpWeights& w, float* out, cudaStream_t stream, bool residual = true);
+// The bounded-wait path of the tcgen05 kernels, on its own (mlp_tc.cu): one
+// block waits on an mbarrier that nothing arrives on, for `polls` polls, then
+// sets kErrMmaTimeout in errFlag and returns.
+cudaError_t launchWaitProbe(uint32_t polls, uint32_t* errFlag, cudaStream_t stream);
 // Inputs of the tcgen05 prediction (mlp_tc.cu): per row of the P x N
 // statistics three float4 of derived values (derived: 3 N P float4), per
 // ommatidium its unit axis and acceptance angle (axes: N float4).

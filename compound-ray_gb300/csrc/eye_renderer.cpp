@@ -40,12 +40,27 @@ void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Device bytes held by the library's buffers, and an optional cap on them
+// (0: none) under which an allocation fails as an out-of-memory cudaMalloc
+// would: the allocator's fault-injection knob (crSetDeviceMemoryCap).
+size_t& devHeld() {
+  static size_t held = 0;
+  return held;
+}
+size_t& devCap() {
+  static size_t cap = 0;
+  return cap;
+}
+
 template <typename T>
 struct DevBuf {
   T* ptr = nullptr;
   size_t count = 0;
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      cudaFree(ptr);
+      devHeld() -= count * sizeof(T);
+    }
     ptr = nullptr;
     count = 0;
   }
@@ -53,7 +68,12 @@ struct DevBuf {
     if (n <= count && ptr) return;
     release();
     if (n == 0) return;
-    check(cudaMalloc(reinterpret_cast<void**>(&ptr), n * sizeof(T)), "cudaMalloc");
+    const size_t bytes = n * sizeof(T);
+    if (devCap() && devHeld() + bytes > devCap())
+      throw std::runtime_error("device memory cap reached: " + std::to_string(devHeld()) + " bytes held, " +
+                               std::to_string(bytes) + " more requested, cap " + std::to_string(devCap()));
+    check(cudaMalloc(reinterpret_cast<void**>(&ptr), bytes), "cudaMalloc");
+    devHeld() += bytes;
     count = n;
   }
 };
@@ -1588,6 +1608,32 @@ int crSetRenderVariant(int variant) {
 int crGetRenderVariant(void) { return renderVariant(); }
 
 int crGetRenderVariantCount(void) { return renderVariantCount(); }
+
+int crSetDeviceMemoryCap(size_t bytes) {
+  devCap() = bytes;
+  return 0;
+}
+
+size_t crGetDeviceMemoryHeld(void) { return devHeld(); }
+
+int crSelfTestBoundedWait(unsigned int polls) {
+  return guarded(
+      "crSelfTestBoundedWait",
+      [&]() -> int {
+        Renderer& r = R();
+        uint32_t* err = r.errWord();
+        cudaStream_t st = r.stream();
+        check(cudaMemsetAsync(err, 0, sizeof(uint32_t), st), "cudaMemset");
+        check(launchWaitProbe(polls, err, st), "wait probe");
+        uint32_t word = 0;
+        check(cudaMemcpyAsync(&word, err, sizeof(word), cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+        check(cudaStreamSynchronize(st), "wait probe");
+        check(cudaMemsetAsync(err, 0, sizeof(uint32_t), st), "cudaMemset");
+        check(cudaStreamSynchronize(st), "wait probe");
+        return (word & kErrMmaTimeout) ? 1 : 0;
+      },
+      -1);
+}
 
 int crSetProjectionSearch(int mode) {
   if (mode != 0 && mode != 1) {

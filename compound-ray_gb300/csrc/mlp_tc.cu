@@ -394,7 +394,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// The bounded wait, on an mbarrier that nothing arrives on.
+__global__ void waitProbeKernel(uint32_t polls, uint32_t* errFlag) {
+  __shared__ uint64_t bar;
+  const uint32_t mbar = smemAddr(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  bool landed = false;
+  for (uint32_t i = 0; i < polls && !landed; ++i) landed = tryWait(mbar, 0);
+  if (!landed && threadIdx.x == 0) atomicOr(errFlag, kErrMmaTimeout);
+}
+
 }  // namespace
+
+cudaError_t launchWaitProbe(uint32_t polls, uint32_t* errFlag, cudaStream_t stream) {
+  waitProbeKernel<<<1, 32, 0, stream>>>(polls, errFlag);
+  return cudaGetLastError();
+}
 
 cudaError_t deriveFeatureStats(const float* stats, const float4* omm, uint32_t N, uint32_t P, float4* derived,
                                float4* axes, cudaStream_t stream) {

@@ -13,7 +13,7 @@ import ctypes
 import math
 import os
 from ctypes import (CDLL, POINTER, Structure, c_bool, c_char_p, c_double, c_float, c_int, c_size_t, c_ubyte,
-                    c_uint32, c_ulonglong, c_void_p)
+                    c_uint, c_uint32, c_ulonglong, c_void_p)
 
 import numpy as np
 from numpy.ctypeslib import ndpointer
@@ -204,6 +204,11 @@ def configureExtras(eyeRenderer):
     L.crGetCutRadius.restype = c_float
     L.crSetRenderVariant.argtypes = [c_int]
     L.crSetRenderVariant.restype = c_int
+    L.crSetDeviceMemoryCap.argtypes = [c_size_t]
+    L.crSetDeviceMemoryCap.restype = c_int
+    L.crGetDeviceMemoryHeld.restype = c_size_t
+    L.crSelfTestBoundedWait.argtypes = [c_uint]
+    L.crSelfTestBoundedWait.restype = c_int
     L.crSetProjectionSearch.argtypes = [c_int]
     L.crSetProjectionSearch.restype = c_int
     L.crGetProjectionSearch.restype = c_int

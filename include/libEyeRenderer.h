@@ -190,6 +190,18 @@ int crGetRenderVariantCount(void);
  * reference. */
 int crSetProjectionSearch(int mode);
 int crGetProjectionSearch(void);
+/* Failure-path knobs, no counterpart in the reference.
+ * crSetDeviceMemoryCap: device bytes the library's buffers may hold in
+ * total (0: no cap, the default); an allocation past it fails like an
+ * out-of-memory cudaMalloc: the call returns its error sentinel and the
+ * library stays usable.  crGetDeviceMemoryHeld: the bytes they hold now.
+ * crSelfTestBoundedWait: runs the tcgen05 kernels' bounded mbarrier wait on
+ * a barrier that nothing arrives on, for `polls` polls; 1 when the wait ran
+ * out and reported it through the error word (then cleared), 0 when it did
+ * not, -1 on a CUDA error. */
+int crSetDeviceMemoryCap(size_t bytes);
+size_t crGetDeviceMemoryHeld(void);
+int crSelfTestBoundedWait(unsigned int polls);
 
 /* ---- Learned per-ommatidium denoiser ------------------------------------
  * A 4-layer MLP (feature row of 112 -> 128 -> 128 -> 128 -> 3, ReLU) that
