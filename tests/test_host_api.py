@@ -184,6 +184,15 @@ def test_error_contract(lib, tmp_path):
     (tmp_path / "bad.eye").write_text("0 0 0 0 1 0 0.1\n")
     lib.loadGlTFscene(g.write(str(tmp_path / "e.gltf")).encode())
     assert "expected 8 values" in eh.lastError(lib)
+    # an eye file with no ommatidia: reported on stderr and the camera is not a
+    # compound eye (MulticamScene.cpp:301-306), no crash
+    g3 = scenes.GltfBuilder()
+    g3.mesh("box", v, fc)
+    g3.compound_camera("eye", "empty.eye")
+    (tmp_path / "empty.eye").write_text("")
+    lib.loadGlTFscene(g3.write(str(tmp_path / "z.gltf")).encode())
+    assert lib.getCameraCount() >= 1
+    assert not any((lib.gotoCamera(i), lib.isCompoundEyeActive())[1] for i in range(lib.getCameraCount()))
     # unknown background shader
     g2 = scenes.GltfBuilder()
     g2.mesh("box", v, fc)
