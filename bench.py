@@ -389,6 +389,7 @@ def run_ours(args):
 
     batch = None if args.no_batch else run_batch(lib, eh, args, stream)
     projection = run_projection(lib, eh, args, stream)
+    small = run_small(lib, eh, args, stream)
     learned = None if args.no_learned else run_learned(lib, eh, args, stream)
     learned_terrain = None if args.no_learned else run_learned(lib, eh, args, stream, scene="terrain",
                                                                   train_poses=1000)
@@ -460,12 +461,64 @@ def run_ours(args):
     if adaptive:
         line["learned_allocator"] = adaptive
         line["learned_allocator_small"] = adaptive_small
+    line["small_scene"] = small
     if not args.no_cpu_baseline:
         cb = cpu_baseline(info, args.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        one = cpu_baseline(info, 2.0, rank_threads=1)
+        line["cpu_baseline"]["single_thread_rays_per_s"] = one["value"]
+        import scenes
+
+        sm = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
+        c1 = cpu_baseline({"gltf": sm["gltf"], "poses": np.stack([sm["pose"]] * 256), "spp": sm["spp"]}, 2.0)
+        line["cpu_baseline"]["small_scene_rays_per_s"] = c1["value"]
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_small(lib, eh, args, stream, frames=200, poses=1024):
+    """The small scene (ground + 64 boxes, simple_sky) and its 1000-ommatidium
+    eye at 32 samples, one pose at the origin: renderFrame wall time per
+    frame (launch, sync and readback of the 1000 x 1 image, the reference's
+    speed-test measure) and device throughput over `poses` poses."""
+    import torch
+
+    import scenes
+
+    sm = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
+    lib.crSetStream(stream.cuda_stream)
+    lib.loadGlTFscene(sm["gltf"].encode())
+    eh.gotoFirstCompoundEye(lib)
+    lib.setCurrentEyeSamplesPerOmmatidium(sm["spp"])
+    N = lib.getCurrentEyeOmmatidialCount()
+    eh.setRenderSize(lib, N, 1)
+    for _ in range(20):
+        lib.renderFrame()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        lib.renderFrame()
+    frame_ms = 1000.0 * (time.perf_counter() - t0) / frames
+    err = eh.lastError(lib)
+    if err:
+        raise RuntimeError(err)
+    p16 = np.zeros((poses, 16), np.float32)
+    p16[:, 0:3] = sm["pose"][0:3]
+    p16[:, 4:7], p16[:, 8:11], p16[:, 12:15] = sm["pose"][3:6], sm["pose"][6:9], sm["pose"][9:12]
+    d_poses = torch.from_numpy(p16).cuda()
+    d_out = torch.empty((poses, N, 3), dtype=torch.float32, device="cuda")
+    lib.crRenderPosesDevice(d_poses.data_ptr(), poses, d_out.data_ptr())
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    if lib.crRenderPosesDevice(d_poses.data_ptr(), poses, d_out.data_ptr()) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    return {"eye": "%d ommatidia x %d samples" % (N, sm["spp"]), "render_frame_ms": frame_ms,
+            "render_frame_note": "renderFrame wall clock per frame, %d frames after 20 warm-up" % frames,
+            "rays_per_s_%d_poses" % poses: poses * N * sm["spp"] / (ms / 1000.0)}
 
 
 def run_projection(lib, eh, args, stream, n=100000, w=1024, h=512):
