@@ -102,16 +102,16 @@ void Denoiser::ensureBatch(int rows) {
 
 void Denoiser::forward(const void* X, int rows, cudaStream_t s) {
   const uint16_t* w = static_cast<const uint16_t*>(wbf_);
-  ck(gemmBf16(1, rows, kHidden, kFeatureWidth, X, kFeatureWidth, false, w + offW1, kHidden, false, zs_, h_[0], kHidden,
+  ck(gemm(1, rows, kHidden, kFeatureWidth, X, kFeatureWidth, false, w + offW1, kHidden, false, zs_, h_[0], kHidden,
               params_ + offB1, nullptr, s),
      "layer 1");
-  ck(gemmBf16(1, rows, kHidden, kHidden, h_[0], kHidden, false, w + offW2, kHidden, false, zs_, h_[1], kHidden,
+  ck(gemm(1, rows, kHidden, kHidden, h_[0], kHidden, false, w + offW2, kHidden, false, zs_, h_[1], kHidden,
               params_ + offB2, nullptr, s),
      "layer 2");
-  ck(gemmBf16(1, rows, kHidden, kHidden, h_[1], kHidden, false, w + offW3, kHidden, false, zs_, h_[2], kHidden,
+  ck(gemm(1, rows, kHidden, kHidden, h_[1], kHidden, false, w + offW3, kHidden, false, zs_, h_[2], kHidden,
               params_ + offB3, nullptr, s),
      "layer 3");
-  ck(gemmBf16(3, rows, kOut, kHidden, h_[2], kHidden, false, w + offW4, kOut, false, y_, nullptr, kOut,
+  ck(gemm(3, rows, kOut, kHidden, h_[2], kHidden, false, w + offW4, kOut, false, y_, nullptr, kOut,
               params_ + offB4, nullptr, s),
      "layer 4");
 }
@@ -134,11 +134,11 @@ void Denoiser::step(const void* X, const float* base, const float* target, int r
   forward(X, rows, s);
   ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, lossAcc, s), "loss");
   // Output layer.
-  ck(gemmBf16(0, kHidden, kOut, rows, h_[2], kHidden, true, dyb_, kOut, false, grads_ + offW4, nullptr, kOut, nullptr,
+  ck(gemm(0, kHidden, kOut, rows, h_[2], kHidden, true, dyb_, kOut, false, grads_ + offW4, nullptr, kOut, nullptr,
               nullptr, s),
      "dW4");
   ck(colSumF32(dyf_, rows, kOut, kOut, grads_ + offB4, s), "db4");
-  ck(gemmBf16(2, rows, kHidden, kOut, dyb_, kOut, false, w + offW4, kOut, true, nullptr, dz_[2], kHidden, nullptr, h_[2],
+  ck(gemm(2, rows, kHidden, kOut, dyb_, kOut, false, w + offW4, kOut, true, nullptr, dz_[2], kHidden, nullptr, h_[2],
               s),
      "dZ3");
   // Hidden layers 3, 2, 1.
@@ -147,12 +147,12 @@ void Denoiser::step(const void* X, const float* base, const float* target, int r
   for (int l = 2; l >= 0; --l) {
     const void* in = l == 0 ? X : h_[l - 1];
     const int kin = l == 0 ? kFeatureWidth : kHidden;
-    ck(gemmBf16(0, kin, kHidden, rows, in, kin, true, dz_[l], kHidden, false, grads_ + offW[l], nullptr, kHidden,
+    ck(gemm(0, kin, kHidden, rows, in, kin, true, dz_[l], kHidden, false, grads_ + offW[l], nullptr, kHidden,
                 nullptr, nullptr, s),
        "dW");
     ck(colSumBf16(dz_[l], rows, kHidden, kHidden, grads_ + offB[l], s), "db");
     if (l > 0)
-      ck(gemmBf16(2, rows, kHidden, kHidden, dz_[l], kHidden, false, w + offW[l], kHidden, true, nullptr, dz_[l - 1],
+      ck(gemm(2, rows, kHidden, kHidden, dz_[l], kHidden, false, w + offW[l], kHidden, true, nullptr, dz_[l - 1],
                   kHidden, nullptr, h_[l - 1], s),
          "dZ");
   }
@@ -186,7 +186,7 @@ void Denoiser::addRows(const void* X, const float* base, const float* target, si
   rows_ += rows;
 }
 
-void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s) {
+void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s, bool tc) {
   if (!ready()) throw std::runtime_error("denoiser not initialised");
   if (rows_ == 0) throw std::runtime_error("no training rows");
   if (steps <= 0) return;
@@ -203,6 +203,7 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
   ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
   ck(cudaMemsetAsync(lossDev, 0, static_cast<size_t>(steps) * 4, s), "memset");
   size_t cursor = 0;
+  tc_ = tc;
   try {
     for (int st = 0; st < steps; ++st) {
       if (cursor + static_cast<size_t>(batch) > rows_) {
@@ -225,7 +226,14 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
       ck(cudaMemcpyAsync(loss, lossDev, static_cast<size_t>(steps) * 4, cudaMemcpyDeviceToHost, s), "loss readback");
     }
     ck(cudaStreamSynchronize(s), "train");
+    tc_ = false;
+    if (tc) {
+      uint32_t flags = 0;
+      ck(takeTcGemmError(&flags), "tcgen05 GEMM status");
+      if (flags) throw std::runtime_error("a tcgen05 GEMM wait timed out during training");
+    }
   } catch (...) {
+    tc_ = false;
     dfree(permDev);
     dfree(lossDev);
     throw;
@@ -255,10 +263,23 @@ MlpWeights Denoiser::weights() const {
 }
 
 float Denoiser::gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost,
-                         float* paramsHost, cudaStream_t s) {
+                         float* paramsHost, cudaStream_t s, bool tc) {
   if (!ready()) throw std::runtime_error("denoiser not initialised");
   ensureBatch(rows);
-  const float l = forwardBackward(X, base, target, rows, true, s);
+  tc_ = tc;
+  float l;
+  try {
+    l = forwardBackward(X, base, target, rows, true, s);
+  } catch (...) {
+    tc_ = false;
+    throw;
+  }
+  tc_ = false;
+  if (tc) {
+    uint32_t flags = 0;
+    ck(takeTcGemmError(&flags), "tcgen05 GEMM status");
+    if (flags) throw std::runtime_error("a tcgen05 GEMM wait timed out");
+  }
   if (gradsHost) ck(cudaMemcpyAsync(gradsHost, grads_, kParams * 4, cudaMemcpyDeviceToHost, s), "grads");
   if (paramsHost) ck(cudaMemcpyAsync(paramsHost, params_, kParams * 4, cudaMemcpyDeviceToHost, s), "params");
   ck(cudaStreamSynchronize(s), "gradient");

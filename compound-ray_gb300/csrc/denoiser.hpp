@@ -48,7 +48,9 @@ class Denoiser {
   // `steps` Adam steps on minibatches of `batch` rows drawn by a seeded
   // shuffle of the training set; returns the mean squared error of each step
   // in `loss` (host, `steps` floats) if given.
-  void train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s);
+  // tc: the GEMMs run on the tcgen05 tensor cores (gemmBf16Tc), else on
+  // mma.sync (gemmBf16, the path the layer-by-layer prediction repeats).
+  void train(int steps, int batch, float lr, uint32_t seed, float* loss, cudaStream_t s, bool tc = true);
 
   // Prediction for `rows` feature rows (device): out = base + net(X)[:, :3],
   // layer by layer.
@@ -61,7 +63,7 @@ class Denoiser {
   // One forward/backward on the given rows with the current weights:
   // returns the loss and copies gradients and parameters to the host.
   float gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost, float* paramsHost,
-                 cudaStream_t s);
+                 cudaStream_t s, bool tc = false);
 
   void save(const std::string& path, cudaStream_t s);
   void load(const std::string& path, cudaStream_t s);
@@ -79,6 +81,12 @@ class Denoiser {
   float* v_ = nullptr;
   void* wbf_ = nullptr;  // bf16 copy of params_
   int adamT_ = 0;
+  bool tc_ = false;  // GEMMs of the running train() on tcgen05
+  cudaError_t gemm(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
+                   bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask, cudaStream_t s) {
+    return tc_ ? gemmBf16Tc(mode, M, N, K, A, lda, aTrans, B, ldb, bTrans, Cf, Hb, ldc, bias, mask, s)
+               : gemmBf16(mode, M, N, K, A, lda, aTrans, B, ldb, bTrans, Cf, Hb, ldc, bias, mask, s);
+  }
   // batch work buffers
   int cap_ = 0;
   void* Xb_ = nullptr;

@@ -166,6 +166,14 @@ static_assert(kFeatBlock * (kNeighbours + 1) <= kFeatureWidth, "feature row too 
 cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
                      bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
                      cudaStream_t stream);
+// The same GEMMs on the tcgen05 tensor cores (mlp_tc.cu): 128 x 128 output
+// tiles, K in chunks of 64, accumulators in TMEM.  A timed-out wait is
+// recorded in a device word that takeTcGemmError reads and clears
+// (kErrMmaTimeout).
+cudaError_t gemmBf16Tc(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
+                       bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
+                       cudaStream_t stream);
+cudaError_t takeTcGemmError(uint32_t* flags);
 cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream);
 cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream);
 cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,

@@ -1832,7 +1832,8 @@ int crDenoiserTrain(int steps, int batch, float lr, int seed, float* lossHistory
   return guarded(
       "crDenoiserTrain",
       [&]() -> int {
-        DS().net.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream());
+        DS().net.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream(),
+                       DS().inferKernel == 1);
         return 0;
       },
       -1);
@@ -1959,7 +1960,7 @@ float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* 
               "cudaMemcpy");
         check(cudaMemcpyAsync(b.ptr, base, static_cast<size_t>(rows) * 12, cudaMemcpyHostToDevice, s), "cudaMemcpy");
         check(cudaMemcpyAsync(t.ptr, target, static_cast<size_t>(rows) * 12, cudaMemcpyHostToDevice, s), "cudaMemcpy");
-        const float l = d.net.gradient(X.ptr, b.ptr, t.ptr, rows, grads, params, s);
+        const float l = d.net.gradient(X.ptr, b.ptr, t.ptr, rows, grads, params, s, d.inferKernel == 1);
         X.release();
         b.release();
         t.release();
@@ -2078,7 +2079,8 @@ int crAllocatorTrain(int steps, int batch, float lr, int seed, float* lossHistor
   return guarded(
       "crAllocatorTrain",
       [&]() -> int {
-        DS().alloc.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream());
+        DS().alloc.train(steps, batch, lr, static_cast<uint32_t>(seed), lossHistory, R().stream(),
+                         DS().inferKernel == 1);
         return 0;
       },
       -1);

@@ -14,8 +14,9 @@
 //   adamKernel       Adam on fp32 master weights, refreshing the bf16 copy;
 //   knnKernel        six nearest ommatidia by axis direction;
 //   featureKernel    assembles the 112-wide bf16 feature rows.
-// The GEMMs are 128 wide: the network is launch- and latency-bound, not
-// tensor-throughput-bound, so the warp-level mma.sync instruction is used.
+// These mma.sync GEMMs are the path the layer-by-layer prediction uses and
+// the training path of crSetDenoiserKernel(0); training runs on the tcgen05
+// GEMMs of mlp_tc.cu by default.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 

@@ -408,7 +408,268 @@ __global__ void waitProbeKernel(uint32_t polls, uint32_t* errFlag) {
   if (!landed && threadIdx.x == 0) atomicOr(errFlag, kErrMmaTimeout);
 }
 
+// ---------------------------------------------------------------------------
+// Training GEMMs on the tcgen05 tensor cores: C[M x N] = sum_k a(m, k) b(n, k)
+// with the operand conventions of gemmBf16 (mlp.cu):
+//   a(m, k) = aTrans ? A[k * lda + m] : A[m * lda + k],
+//   b(n, k) = bTrans ? B[n * ldb + k] : B[k * ldb + n],
+// and its epilogues (0 fp32 store, 1 bias + ReLU to bf16 and the fp32
+// pre-activation, 2 ReLU-derivative mask to bf16, 3 bias to fp32).
+// One 256-thread block per 128 x 128 output tile (N padded to a multiple of
+// 16 for the MMA), K in chunks of 64 staged by the threads into shared
+// memory in the canonical K-major no-swizzle layout, 16 bytes per load; one
+// thread issues the chunk's four tcgen05.mma (K 16 each) into the TMEM
+// accumulator and commits them; warps w and w + 4 read accumulator lanes
+// 32 w .. +31, columns 0-63 and 64-127.  grid.z > 1 splits
+// K into slices that write partial tiles (ldc = N) for a reduction in slice
+// order.  Waits are bounded; a timeout sets g_tcGemmErr.
+// ---------------------------------------------------------------------------
+constexpr int kGemmTile = 128;
+constexpr int kGemmChunk = 64;
+constexpr uint32_t kGemmStage = kGemmTile * kGemmChunk * 2;  // bytes per operand stage
+// Dynamic shared memory per block, sized so that at most four blocks share
+// an SM: their four 128-column accumulators fill its 512 TMEM columns, and
+// no block ever waits in tcgen05.alloc.
+constexpr uint32_t kGemmSmem = 56 * 1024;
+static_assert(2 * kGemmStage + 128 <= kGemmSmem, "staging exceeds the block's shared memory");
+static_assert(8 * 32 * 33 * 4 + 128 <= kGemmSmem, "epilogue tiles exceed the block's shared memory");
+__device__ uint32_t g_tcGemmErr;
+
+constexpr int kGemmThreads = 256;  // eight warps: two per accumulator lane quarter
+
+// Stages rows [0, rowsValid) x chunk columns of an operand whose element
+// (r, c) is at P[(row0 + r) * ld + k0 + c] (K contiguous: 8 elements per
+// 16-byte load) or, when `kMajorInMemory` is false, at
+// P[(k0 + c) * ld + row0 + r] (rows contiguous: 8 rows per 16-byte load,
+// scattered to their core-matrix rows); zero outside rowsValid and kEnd.
+__device__ __forceinline__ void stageOperand(unsigned char* dst, const __nv_bfloat16* __restrict__ P, int ld,
+                                             bool kMajorInMemory, int row0, int rowsValid, int rowsPadded, int k0,
+                                             int kEnd, int tid) {
+  const bool vec = (reinterpret_cast<uintptr_t>(P) & 15) == 0 && (ld & 7) == 0;
+  if (kMajorInMemory) {
+    // groups of 8 consecutive k of one row
+    for (int e = tid; e < rowsPadded * (kGemmChunk / 8); e += kGemmThreads) {
+      const int r = e / (kGemmChunk / 8), c = (e % (kGemmChunk / 8)) * 8;
+      const int k = k0 + c;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (r < rowsValid) {
+        const __nv_bfloat16* src = P + static_cast<size_t>(row0 + r) * ld + k;
+        if (vec && k + 8 <= kEnd) {
+          v = *reinterpret_cast<const uint4*>(src);
+        } else {
+          uint16_t t[8];
+          for (int j = 0; j < 8; ++j) t[j] = k + j < kEnd ? __bfloat16_as_ushort(src[j]) : 0;
+          v = make_uint4(t[0] | (uint32_t(t[1]) << 16), t[2] | (uint32_t(t[3]) << 16), t[4] | (uint32_t(t[5]) << 16),
+                         t[6] | (uint32_t(t[7]) << 16));
+        }
+      }
+      *reinterpret_cast<uint4*>(dst + coreOffset(static_cast<uint32_t>(r), static_cast<uint32_t>(c), kGemmChunk)) = v;
+    }
+  } else {
+    // groups of 8 consecutive rows of one k
+    for (int e = tid; e < (rowsPadded / 8) * kGemmChunk; e += kGemmThreads) {
+      const int c = e / (rowsPadded / 8), r = (e % (rowsPadded / 8)) * 8;
+      const int k = k0 + c;
+      uint16_t t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (k < kEnd) {
+        const __nv_bfloat16* src = P + static_cast<size_t>(k) * ld + row0 + r;
+        if (vec && r + 8 <= rowsValid) {
+          const uint4 v = *reinterpret_cast<const uint4*>(src);
+          t[0] = v.x & 0xffff; t[1] = v.x >> 16; t[2] = v.y & 0xffff; t[3] = v.y >> 16;
+          t[4] = v.z & 0xffff; t[5] = v.z >> 16; t[6] = v.w & 0xffff; t[7] = v.w >> 16;
+        } else {
+          for (int j = 0; j < 8; ++j) t[j] = r + j < rowsValid ? __bfloat16_as_ushort(src[j]) : 0;
+        }
+      }
+      for (int j = 0; j < 8; ++j)
+        *reinterpret_cast<uint16_t*>(dst + coreOffset(static_cast<uint32_t>(r + j), static_cast<uint32_t>(c),
+                                                      kGemmChunk)) = t[j];
+    }
+  }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    gemmTcKernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda, bool aTrans,
+                 const __nv_bfloat16* __restrict__ B, int ldb, bool bTrans, float* __restrict__ Cf,
+                 __nv_bfloat16* __restrict__ Hb, int ldc, const float* __restrict__ bias,
+                 const __nv_bfloat16* __restrict__ mask, int kSlice) {
+  extern __shared__ __align__(128) unsigned char gemmSmem[];
+  unsigned char* stage =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(gemmSmem) + 127) & ~uintptr_t(127));
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tmemSlot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kGemmTile, n0 = blockIdx.x * kGemmTile;
+  const int Mt = min(kGemmTile, M - m0);
+  const int Nt = min(kGemmTile, N - n0);
+  const uint32_t Nn = static_cast<uint32_t>((Nt + 15) & ~15);  // MMA N: a multiple of 16
+  const int kBeg = kSlice ? static_cast<int>(blockIdx.z) * kSlice : 0;
+  const int kEnd = kSlice ? min(K, kBeg + kSlice) : K;
+  if (kSlice) Cf += static_cast<size_t>(blockIdx.z) * M * N;
+  unsigned char* sA = stage;
+  unsigned char* sB = stage + kGemmStage;
+  const uint32_t mbar = smemAddr(&bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmemSlot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = tmemSlot;
+  uint32_t phase = 0;
+  bool ok = true, pending = false;
+  for (int k0 = kBeg; k0 < kEnd && ok; k0 += kGemmChunk) {
+    // a(m, k): K contiguous unless aTrans; b(n, k): K contiguous when bTrans.
+    stageOperand(sA, A, lda, !aTrans, m0, Mt, kGemmTile, k0, kEnd, tid);
+    stageOperand(sB, B, ldb, bTrans, n0, Nt, static_cast<int>(Nn), k0, kEnd, tid);
+    fenceAsyncShared();
+    tcFenceBefore();
+    __syncthreads();
+    tcFenceAfter();
+    if (tid == 0) {
+      const uint32_t idesc = instrDesc(kGemmTile, Nn);
+      for (uint32_t ks = 0; ks < kGemmChunk / 16; ++ks) {
+        const uint64_t a = smemDesc(smemAddr(sA) + ks * 256u, 128u, kGemmChunk * 16u);
+        const uint64_t b = smemDesc(smemAddr(sB) + ks * 256u, 128u, kGemmChunk * 16u);
+        mmaBf16(tmem, a, b, idesc, (k0 > kBeg || ks > 0) ? 1u : 0u);
+      }
+      commitTo(mbar);
+    }
+    pending = true;
+    if (!__syncthreads_and(waitParity(mbar, phase))) {
+      ok = false;
+      if (tid == 0) atomicOr(&g_tcGemmErr, kErrMmaTimeout);
+      break;
+    }
+    pending = false;
+    phase ^= 1u;
+    tcFenceAfter();
+  }
+  if (ok) {
+    // Each warp turns its 32 rows x 32 columns through shared memory (the
+    // staging area is free once the MMAs are done), so that a store writes
+    // 32 consecutive columns of one row.
+    const int lq = warp & 3, half = warp >> 2;  // lane quarter, and columns 64 half .. +63
+    const uint32_t laneBase = tmem + (static_cast<uint32_t>(lq * 32) << 16);
+    const bool empty = kEnd <= kBeg;  // no chunk ran: the accumulator holds nothing
+    float* t = reinterpret_cast<float*>(stage) + warp * (32 * 33);
+    for (int c0 = 64 * half; c0 < min(Nt, 64 * half + 64); c0 += 32) {
+      float v[32];
+      if (!empty) tmemLoad32(laneBase + static_cast<uint32_t>(c0), v);
+      else
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) t[lane * 33 + j] = v[j];  // row `lane`, column j
+      __syncwarp();
+      const int n = n0 + c0 + lane;
+      const bool colOk = c0 + lane < Nt;
+      const float bn = (kMode == 1 || kMode == 3) && colOk ? bias[n] : 0.f;
+      for (int r = 0; r < 32; ++r) {
+        const int m = m0 + lq * 32 + r;
+        if (m >= M || !colOk) continue;
+        const size_t o = static_cast<size_t>(m) * ldc + n;
+        const float acc = t[r * 33 + lane];
+        if (kMode == 0) {
+          Cf[o] = acc;
+        } else if (kMode == 1) {
+          const float z = acc + bn;
+          Cf[o] = z;
+          Hb[o] = __float2bfloat16(fmaxf(z, 0.f));
+        } else if (kMode == 2) {
+          Hb[o] = __float2bfloat16(__bfloat162float(mask[o]) > 0.f ? acc : 0.f);
+        } else {
+          Cf[o] = acc + bn;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (!ok && pending && tid == 0) waitParity(mbar, phase);  // let a late commit land before the TMEM is freed
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+__global__ void tcSplitReduceKernel(const float* __restrict__ part, int slices, int M, int N, float* __restrict__ C,
+                                    int ldc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * N) return;
+  const int m = i / N, n = i % N;
+  float s = 0.f;
+  for (int k = 0; k < slices; ++k) s += part[static_cast<size_t>(k) * M * N + i];
+  C[static_cast<size_t>(m) * ldc + n] = s;
+}
+
+float* g_tcSplit = nullptr;
+size_t g_tcSplitFloats = 0;
+
 }  // namespace
+
+cudaError_t gemmBf16Tc(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,
+                       bool bTrans, float* Cf, void* Hb, int ldc, const float* bias, const void* mask,
+                       cudaStream_t stream) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  if (mode < 0 || mode > 3) return cudaErrorInvalidValue;
+  const unsigned gx = static_cast<unsigned>((N + kGemmTile - 1) / kGemmTile);
+  const unsigned gy = static_cast<unsigned>((M + kGemmTile - 1) / kGemmTile);
+  auto a = static_cast<const __nv_bfloat16*>(A);
+  auto b = static_cast<const __nv_bfloat16*>(B);
+  auto h = static_cast<__nv_bfloat16*>(Hb);
+  auto mk = static_cast<const __nv_bfloat16*>(mask);
+  // Weight gradients: a long K over the minibatch and one or two output
+  // tiles; K is split into slices of 128 summed afterwards in slice order.
+  static bool attrSet = false;
+  if (!attrSet) {
+    const void* fns[4] = {reinterpret_cast<const void*>(gemmTcKernel<0>), reinterpret_cast<const void*>(gemmTcKernel<1>),
+                          reinterpret_cast<const void*>(gemmTcKernel<2>), reinterpret_cast<const void*>(gemmTcKernel<3>)};
+    for (const void* f : fns) {
+      const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+      if (e != cudaSuccess) return e;
+    }
+    attrSet = true;
+  }
+  if (mode == 0 && K >= 1024 && gx * gy < 64) {
+    const int slice = 128, slices = (K + slice - 1) / slice;
+    const size_t need = static_cast<size_t>(slices) * M * N;
+    if (need > g_tcSplitFloats) {
+      if (g_tcSplit) cudaFree(g_tcSplit);
+      g_tcSplit = nullptr;
+      g_tcSplitFloats = 0;
+      const cudaError_t e = cudaMalloc(&g_tcSplit, need * sizeof(float));
+      if (e != cudaSuccess) return e;
+      g_tcSplitFloats = need;
+    }
+    gemmTcKernel<0><<<dim3(gx, gy, slices), kGemmThreads, kGemmSmem, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans,
+                                                                       g_tcSplit, nullptr, N, nullptr, nullptr, slice);
+    tcSplitReduceKernel<<<(M * N + 255) / 256, 256, 0, stream>>>(g_tcSplit, slices, M, N, Cf, ldc);
+    return cudaGetLastError();
+  }
+  const dim3 grid(gx, gy);
+  switch (mode) {
+    case 0: gemmTcKernel<0><<<grid, kGemmThreads, kGemmSmem, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk, 0); break;
+    case 1: gemmTcKernel<1><<<grid, kGemmThreads, kGemmSmem, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk, 0); break;
+    case 2: gemmTcKernel<2><<<grid, kGemmThreads, kGemmSmem, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk, 0); break;
+    default: gemmTcKernel<3><<<grid, kGemmThreads, kGemmSmem, stream>>>(M, N, K, a, lda, aTrans, b, ldb, bTrans, Cf, h, ldc, bias, mk, 0); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t takeTcGemmError(uint32_t* flags) {
+  cudaError_t e = cudaMemcpyFromSymbol(flags, g_tcGemmErr, sizeof(uint32_t));
+  if (e != cudaSuccess) return e;
+  const uint32_t zero = 0;
+  return cudaMemcpyToSymbol(g_tcGemmErr, &zero, sizeof(uint32_t));
+}
 
 cudaError_t launchWaitProbe(uint32_t polls, uint32_t* errFlag, cudaStream_t stream) {
   waitProbeKernel<<<1, 32, 0, stream>>>(polls, errFlag);

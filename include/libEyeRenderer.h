@@ -214,9 +214,12 @@ int crSelfTestBoundedWait(unsigned int polls);
 int crDenoiserInit(int seed);                 /* fresh He-initialised weights */
 size_t crDenoiserParamCount(void);
 void crDenoiserRelease(void);                 /* drops the network (the adaptive render then uses feature means) */
-/* Network pass of the learned and adaptive renders: 0 = fused mma.sync
- * kernel (bit-identical to the layer-by-layer training path), 1 = fused
- * tcgen05 kernel (accumulators in TMEM; the default).  -1 on a bad kind. */
+/* Tensor-core path of the networks: 0 = mma.sync (the fused inference
+ * kernel is then bit-identical to the layer-by-layer path, and training runs
+ * its GEMMs on mma.sync), 1 = tcgen05 with accumulators in TMEM for the
+ * fused inference kernel and the training GEMMs (the default).  Set it
+ * before crDenoiserTrain / crAllocatorTrain to train on that path.  -1 on a
+ * bad kind. */
 int crSetDenoiserKernel(int kind);
 int crGetDenoiserKernel(void);
 /* Renders `count` host poses (12 floats each) of the current eye twice --

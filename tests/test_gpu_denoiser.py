@@ -11,8 +11,19 @@ import scenes
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("rows", [64, 500])
-def test_gradients_match_reference(lib, rows):
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("rows", [64, 500, 2000])
+def test_gradients_match_reference(lib, rows, kernel):
+    """kernel 0: the mma.sync GEMMs; 1: the tcgen05 GEMMs (2000 rows also
+    take the split-K weight-gradient path)."""
+    assert lib.crSetDenoiserKernel(kernel) == 0
+    try:
+        _gradients_case(lib, rows)
+    finally:
+        lib.crSetDenoiserKernel(1)
+
+
+def _gradients_case(lib, rows):
     assert lib.crDenoiserInit(7) == 0, eh.lastError(lib)
     n = lib.crDenoiserParamCount()
     assert n == mlp_ref.N_PARAMS
