@@ -148,22 +148,38 @@ __global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __n
 
 // out[n] = sum over m of in[m*ld + n], for bf16 or fp32 input.
 template <typename T>
-__global__ void colSumKernel(const T* __restrict__ in, int M, int N, int ld, float* __restrict__ out) {
-  const int n = blockIdx.x;
-  float s = 0.f;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-    if constexpr (sizeof(T) == 2) s += __bfloat162float(in[static_cast<size_t>(m) * ld + n]);
-    else s += in[static_cast<size_t>(m) * ld + n];
+__global__ void __launch_bounds__(1024) colSumKernel(const T* __restrict__ in, int M, int N, int ld,
+                                                     float* __restrict__ out) {
+  // 32 columns per block, one per lane, so that a warp reads 32 consecutive
+  // columns of a row; warp w sums rows w, w + 32, ... in four interleaved
+  // running sums, and the 32 warp sums are added in warp order.
+  __shared__ float part[32][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n = blockIdx.x * 32 + lane;
+  auto val = [&](int m) {
+    if constexpr (sizeof(T) == 2) return __bfloat162float(in[static_cast<size_t>(m) * ld + n]);
+    else return static_cast<float>(in[static_cast<size_t>(m) * ld + n]);
+  };
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  if (n < N) {
+    int m = w;
+    for (; m + 96 < M; m += 128) {
+      s0 += val(m);
+      s1 += val(m + 32);
+      s2 += val(m + 64);
+      s3 += val(m + 96);
+    }
+    for (; m < M; m += 32) s0 += val(m);
   }
-  __shared__ float red[256];
-  red[threadIdx.x] = s;
+  part[w][lane] = (s0 + s1) + (s2 + s3);
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
+  if (w == 0 && n < N) {
+    float t = 0.f;
+    for (int k = 0; k < 32; ++k) t += part[k][lane];
+    out[n] = t;
   }
-  if (threadIdx.x == 0) out[n] = red[0];
 }
+
 
 // Prediction = base + y[:, :3]; squared error against target; gradient of
 // the mean squared error w.r.t. y (fp32 and bf16 copies, padded columns 0).
@@ -458,12 +474,13 @@ cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool
 }
 
 cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream) {
-  colSumKernel<__nv_bfloat16><<<N, 256, 0, stream>>>(static_cast<const __nv_bfloat16*>(in), M, N, ld, out);
+  colSumKernel<__nv_bfloat16><<<(N + 31) / 32, 1024, 0, stream>>>(static_cast<const __nv_bfloat16*>(in), M, N, ld,
+                                                                   out);
   return cudaGetLastError();
 }
 
 cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream) {
-  colSumKernel<float><<<N, 256, 0, stream>>>(in, M, N, ld, out);
+  colSumKernel<float><<<(N + 31) / 32, 1024, 0, stream>>>(in, M, N, ld, out);
   return cudaGetLastError();
 }
 
