@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
     ap.add_argument("--profile-learned", action="store_true", help="profiling case: learned render of held-out poses")
     ap.add_argument("--profile-adaptive", action="store_true", help="profiling case: adaptive learned render")
+    ap.add_argument("--profile-train", type=int, default=0, metavar="STEPS",
+                    help="profiling case: STEPS denoiser training steps of 8192 rows on the terrain eye")
     ap.add_argument("--denoiser-kernel", type=int, default=1, help="denoiser inference kernel for --profile-learned: "
                     "0 mma.sync, 1 tcgen05")
     return ap.parse_args()
@@ -926,6 +928,23 @@ def run_profile_learned(args):
         run_adaptive(lib, eh, args, stream, held_poses=min(args.poses, 32), profile=True)
         return
     info = workload(1024)
+    if args.profile_train:
+        lib.loadGlTFscene(info["gltf"].encode())
+        eh.gotoFirstCompoundEye(lib)
+        rng = np.random.default_rng(scenes.SEED + 11)
+        train = scenes.random_poses(info["height_fn"], 40, rng, 60.0)
+        if lib.crDenoiserInit(1) != 0 or lib.crDenoiserAddTrainingPoses(train, len(train), 8, 64) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        for rep in range(2):  # the second call is the one timed
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if lib.crDenoiserTrain(args.profile_train, 8192, 1e-3, 3, None) != 0:
+                raise RuntimeError(eh.lastError(lib))
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+        print(json.dumps({"profile_case": "%d denoiser training steps of 8192 rows, twice" % args.profile_train,
+                          "ms_per_step_wall": 1e3 * dt / args.profile_train}))
+        return
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     if lib.crSetRenderVariant(args.variant) != 0 or lib.crSetCutRadius(args.cut) != 0:
@@ -980,7 +999,7 @@ def main():
     args = parse_args()
     if args.profile:
         run_profile(args)
-    elif args.profile_learned or args.profile_adaptive:
+    elif args.profile_learned or args.profile_adaptive or args.profile_train:
         run_profile_learned(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -34,13 +34,13 @@ constexpr uint32_t kVersion = 1;
 
 void Denoiser::release() {
   for (void* p : {static_cast<void*>(params_), static_cast<void*>(grads_), static_cast<void*>(m_), static_cast<void*>(v_),
-                  wbf_, Xb_, static_cast<void*>(baseb_), static_cast<void*>(targetb_), static_cast<void*>(zs_), h_[0],
+                  wbf_, wbfT_, Xb_, static_cast<void*>(baseb_), static_cast<void*>(targetb_), static_cast<void*>(zs_), h_[0],
                   h_[1], h_[2], dz_[0], dz_[1], dz_[2], static_cast<void*>(y_), static_cast<void*>(dyf_), dyb_,
                   static_cast<void*>(lossSum_), static_cast<void*>(idx_), X_, static_cast<void*>(base_),
                   static_cast<void*>(target_)})
     dfree(p);
   params_ = grads_ = m_ = v_ = nullptr;
-  wbf_ = Xb_ = nullptr;
+  wbf_ = wbfT_ = Xb_ = nullptr;
   baseb_ = targetb_ = zs_ = y_ = dyf_ = lossSum_ = nullptr;
   for (int i = 0; i < 3; ++i) h_[i] = dz_[i] = nullptr;
   dyb_ = nullptr;
@@ -59,6 +59,8 @@ void Denoiser::init(uint32_t seed, cudaStream_t s) {
   m_ = dalloc<float>(kParams);
   v_ = dalloc<float>(kParams);
   wbf_ = dalloc<uint16_t>(kParams);
+  wbfT_ = dalloc<uint16_t>(kParams);
+  ck(cudaMemsetAsync(wbfT_, 0, kParams * 2, s), "memset");
   std::vector<float> h(kParams, 0.f);
   std::mt19937 rng(seed);
   auto fill = [&](size_t off, int fanIn, int fanOut, float scale) {
@@ -73,6 +75,7 @@ void Denoiser::init(uint32_t seed, cudaStream_t s) {
   ck(cudaMemsetAsync(m_, 0, kParams * 4, s), "memset");
   ck(cudaMemsetAsync(v_, 0, kParams * 4, s), "memset");
   ck(toBf16(params_, wbf_, kParams, s), "bf16 copy");
+  ck(transposeWeightsBf16(params_, kParams, wbfT_, weightBlocks(), s), "bf16 transposes");
   ck(cudaStreamSynchronize(s), "init");
   adamT_ = 0;
 }
@@ -101,18 +104,21 @@ void Denoiser::ensureBatch(int rows) {
 }
 
 void Denoiser::forward(const void* X, int rows, cudaStream_t s) {
-  const uint16_t* w = static_cast<const uint16_t*>(wbf_);
-  ck(gemm(1, rows, kHidden, kFeatureWidth, X, kFeatureWidth, false, w + offW1, kHidden, false, zs_, h_[0], kHidden,
-              params_ + offB1, nullptr, s),
+  // B operand of each layer: the tcgen05 GEMMs read the transposed weights
+  // (K contiguous), the mma.sync GEMMs the row-major ones.
+  const uint16_t* w = static_cast<const uint16_t*>(tc_ ? wbfT_ : wbf_);
+  auto ldw = [&](int kin, int nout) { return tc_ ? kin : nout; };
+  ck(gemm(1, rows, kHidden, kFeatureWidth, X, kFeatureWidth, false, w + offW1, ldw(kFeatureWidth, kHidden), tc_,
+          zs_, h_[0], kHidden, params_ + offB1, nullptr, s),
      "layer 1");
-  ck(gemm(1, rows, kHidden, kHidden, h_[0], kHidden, false, w + offW2, kHidden, false, zs_, h_[1], kHidden,
-              params_ + offB2, nullptr, s),
+  ck(gemm(1, rows, kHidden, kHidden, h_[0], kHidden, false, w + offW2, ldw(kHidden, kHidden), tc_, zs_, h_[1],
+          kHidden, params_ + offB2, nullptr, s),
      "layer 2");
-  ck(gemm(1, rows, kHidden, kHidden, h_[1], kHidden, false, w + offW3, kHidden, false, zs_, h_[2], kHidden,
-              params_ + offB3, nullptr, s),
+  ck(gemm(1, rows, kHidden, kHidden, h_[1], kHidden, false, w + offW3, ldw(kHidden, kHidden), tc_, zs_, h_[2],
+          kHidden, params_ + offB3, nullptr, s),
      "layer 3");
-  ck(gemm(3, rows, kOut, kHidden, h_[2], kHidden, false, w + offW4, kOut, false, y_, nullptr, kOut,
-              params_ + offB4, nullptr, s),
+  ck(gemm(3, rows, kOut, kHidden, h_[2], kHidden, false, w + offW4, ldw(kHidden, kOut), tc_, y_, nullptr, kOut,
+          params_ + offB4, nullptr, s),
      "layer 4");
 }
 
@@ -218,8 +224,9 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
       ++adamT_;
       // half-cosine decay of the step size over this call, down to 5%
       const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
+      const WeightBlocks blocks = weightBlocks();
       ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr * decay, 0.9f, 0.999f, 1e-8f, adamT_, wbf_,
-                  s),
+                  s, wbfT_, &blocks),
          "adam");
     }
     if (loss) {
@@ -322,6 +329,7 @@ void Denoiser::load(const std::string& path, cudaStream_t s) {
   ck(cudaMemcpyAsync(m_, m.data(), kParams * 4, cudaMemcpyHostToDevice, s), "load");
   ck(cudaMemcpyAsync(v_, v.data(), kParams * 4, cudaMemcpyHostToDevice, s), "load");
   ck(toBf16(params_, wbf_, kParams, s), "bf16 copy");
+  ck(transposeWeightsBf16(params_, kParams, wbfT_, weightBlocks(), s), "bf16 transposes");
   ck(cudaStreamSynchronize(s), "load");
   adamT_ = static_cast<int>(hdr[3]);
 }

@@ -80,6 +80,13 @@ class Denoiser {
   float* m_ = nullptr;
   float* v_ = nullptr;
   void* wbf_ = nullptr;  // bf16 copy of params_
+  void* wbfT_ = nullptr;  // bf16 transposes of the weight matrices, at the same offsets
+  static WeightBlocks weightBlocks() {
+    return WeightBlocks{4,
+                        {int(offW1), int(offW2), int(offW3), int(offW4)},
+                        {kFeatureWidth, kHidden, kHidden, kHidden},
+                        {kHidden, kHidden, kHidden, kOut}};
+  }
   int adamT_ = 0;
   bool tc_ = false;  // GEMMs of the running train() on tcgen05
   cudaError_t gemm(int mode, int M, int N, int K, const void* A, int lda, bool aTrans, const void* B, int ldb,

@@ -178,8 +178,19 @@ cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStr
 cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream);
 cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
                     void* dyb, float* lossSum, cudaStream_t stream);
+// Row-major weight matrices inside a flat parameter vector.  Their
+// transposes (same offsets) are the K-contiguous operands of the tcgen05
+// forward GEMMs.
+struct WeightBlocks {
+  int count;
+  int off[4], rows[4], cols[4];
+};
+// Adam on the fp32 master weights; refreshes the bf16 copy wb and, when
+// wbT is given, the bf16 transposes of `blocks` in wbT.
 cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
-                     int t, void* wb, cudaStream_t stream);
+                     int t, void* wb, cudaStream_t stream, void* wbT = nullptr, const WeightBlocks* blocks = nullptr);
+// wbT = bf16 transposes of `blocks` of the n fp32 parameters w.
+cudaError_t transposeWeightsBf16(const float* w, size_t n, void* wbT, const WeightBlocks& blocks, cudaStream_t stream);
 cudaError_t toBf16(const float* in, void* out, size_t n, cudaStream_t stream);
 cudaError_t nearestOmmatidia(const float4* omm, uint32_t N, int* nb, cudaStream_t stream);
 cudaError_t assembleFeatures(const float* stats, const float4* omm, const int* nb, uint32_t N, uint32_t P, void* X,

@@ -11,7 +11,8 @@
 //                    derivative mask, plain fp32 store);
 //   colSumKernel     bias gradients;
 //   lossKernel       residual prediction, squared error and its gradient;
-//   adamKernel       Adam on fp32 master weights, refreshing the bf16 copy;
+//   adamKernel       Adam on fp32 master weights, refreshing the bf16 copy
+//                    and the transposed bf16 weight matrices;
 //   knnKernel        six nearest ommatidia by axis direction;
 //   featureKernel    assembles the 112-wide bf16 feature rows.
 // These mma.sync GEMMs are the path the layer-by-layer prediction uses and
@@ -146,40 +147,73 @@ __global__ void __launch_bounds__(128) gemmKernel(int M, int N, int K, const __n
       }
 }
 
-// out[n] = sum over m of in[m*ld + n], for bf16 or fp32 input.
+// out[n] = sum over m of in[m*ld + n], for bf16 or fp32 input.  Block
+// (g, slab) sums columns 32g .. 32g + 31 (one per lane, so a warp reads 32
+// consecutive columns of a row) over one slab of rows, its 8 warps taking
+// every 8th row; the slab's sum goes to a scratch row, and the block that
+// finishes a column group last adds the slabs' sums in slab order.  The
+// result does not depend on which block finishes when.  Launches share the
+// scratch and the counters, so they must not run concurrently (the denoiser
+// issues them on one stream).
+constexpr int kColSumMaxSlabs = 64;
+constexpr int kColSumMaxGroups = 128;  // N <= 4096
+__device__ float g_colSumPart[kColSumMaxSlabs * kColSumMaxGroups * 32];
+__device__ unsigned int g_colSumDone[kColSumMaxGroups];
+
 template <typename T>
-__global__ void __launch_bounds__(1024) colSumKernel(const T* __restrict__ in, int M, int N, int ld,
-                                                     float* __restrict__ out) {
-  // 32 columns per block, one per lane, so that a warp reads 32 consecutive
-  // columns of a row; warp w sums rows w, w + 32, ... in four interleaved
-  // running sums, and the 32 warp sums are added in warp order.
-  __shared__ float part[32][33];
+__global__ void __launch_bounds__(256) colSumKernel(const T* __restrict__ in, int M, int N, int ld, int rowsPerSlab,
+                                                    float* __restrict__ out) {
+  __shared__ float part[8][32];
+  __shared__ bool last;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int n = blockIdx.x * 32 + lane;
+  const int g = blockIdx.x, slab = blockIdx.y;
+  const int n = g * 32 + lane;
+  const int m0 = slab * rowsPerSlab, m1 = min(M, m0 + rowsPerSlab);
   auto val = [&](int m) {
     if constexpr (sizeof(T) == 2) return __bfloat162float(in[static_cast<size_t>(m) * ld + n]);
     else return static_cast<float>(in[static_cast<size_t>(m) * ld + n]);
   };
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+  float s0 = 0.f, s1 = 0.f;
   if (n < N) {
-    int m = w;
-    for (; m + 96 < M; m += 128) {
+    int m = m0 + w;
+    for (; m + 8 < m1; m += 16) {
       s0 += val(m);
-      s1 += val(m + 32);
-      s2 += val(m + 64);
-      s3 += val(m + 96);
+      s1 += val(m + 8);
     }
-    for (; m < M; m += 32) s0 += val(m);
+    for (; m < m1; m += 8) s0 += val(m);
   }
-  part[w][lane] = (s0 + s1) + (s2 + s3);
+  part[w][lane] = s0 + s1;
   __syncthreads();
-  if (w == 0 && n < N) {
+  if (w == 0) {
     float t = 0.f;
-    for (int k = 0; k < 32; ++k) t += part[k][lane];
-    out[n] = t;
+    for (int k = 0; k < 8; ++k) t += part[k][lane];
+    g_colSumPart[(slab * kColSumMaxGroups + g) * 32 + lane] = t;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&g_colSumDone[g], 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (last && w == 0) {
+    __threadfence();
+    float t = 0.f;
+    for (int sl = 0; sl < static_cast<int>(gridDim.y); ++sl)
+      t += __ldcg(&g_colSumPart[(sl * kColSumMaxGroups + g) * 32 + lane]);
+    if (n < N) out[n] = t;
+    if (lane == 0) g_colSumDone[g] = 0u;
   }
 }
 
+template <typename T>
+cudaError_t colSum(const T* in, int M, int N, int ld, float* out, cudaStream_t stream) {
+  if (N <= 0) return cudaSuccess;
+  const int groups = (N + 31) / 32;
+  if (groups > kColSumMaxGroups) return cudaErrorInvalidValue;
+  if (M <= 0) return cudaMemsetAsync(out, 0, static_cast<size_t>(N) * sizeof(float), stream);
+  const int rowsPerSlab = std::max(64, (M + kColSumMaxSlabs - 1) / kColSumMaxSlabs);
+  const int slabs = (M + rowsPerSlab - 1) / rowsPerSlab;  // <= kColSumMaxSlabs
+  colSumKernel<T><<<dim3(groups, slabs), 256, 0, stream>>>(in, M, N, ld, rowsPerSlab, out);
+  return cudaGetLastError();
+}
 
 // Prediction = base + y[:, :3]; squared error against target; gradient of
 // the mean squared error w.r.t. y (fp32 and bf16 copies, padded columns 0).
@@ -211,9 +245,21 @@ __global__ void lossKernel(const float* __restrict__ y, int ldy, const float* __
   }
 }
 
+// The transposed bf16 copy of parameter i, if it lies in one of `blocks`.
+__device__ __forceinline__ void putTransposed(int i, float wi, __nv_bfloat16* __restrict__ wbT, const WeightBlocks& b) {
+  for (int k = 0; k < b.count; ++k) {
+    const int j = i - b.off[k];
+    if (j >= 0 && j < b.rows[k] * b.cols[k]) {
+      const int r = j / b.cols[k], c = j - r * b.cols[k];
+      wbT[b.off[k] + c * b.rows[k] + r] = __float2bfloat16(wi);
+      return;
+    }
+  }
+}
+
 __global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                            float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2,
-                           __nv_bfloat16* __restrict__ wb) {
+                           __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbT, WeightBlocks blocks) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
@@ -224,6 +270,13 @@ __global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, f
   const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   w[i] = wi;
   if (wb) wb[i] = __float2bfloat16(wi);
+  if (wbT) putTransposed(i, wi, wbT, blocks);
+}
+
+__global__ void transposeWeightsKernel(const float* __restrict__ w, int n, __nv_bfloat16* __restrict__ wbT,
+                                       WeightBlocks blocks) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) putTransposed(i, w[i], wbT, blocks);
 }
 
 __global__ void toBf16Kernel(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, size_t n) {
@@ -474,14 +527,11 @@ cudaError_t gemmBf16(int mode, int M, int N, int K, const void* A, int lda, bool
 }
 
 cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream) {
-  colSumKernel<__nv_bfloat16><<<(N + 31) / 32, 1024, 0, stream>>>(static_cast<const __nv_bfloat16*>(in), M, N, ld,
-                                                                   out);
-  return cudaGetLastError();
+  return colSum(static_cast<const __nv_bfloat16*>(in), M, N, ld, out, stream);
 }
 
 cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream) {
-  colSumKernel<float><<<(N + 31) / 32, 1024, 0, stream>>>(in, M, N, ld, out);
-  return cudaGetLastError();
+  return colSum(in, M, N, ld, out, stream);
 }
 
 cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
@@ -493,11 +543,20 @@ cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* tar
 }
 
 cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
-                     int t, void* wb, cudaStream_t stream) {
+                     int t, void* wb, cudaStream_t stream, void* wbT, const WeightBlocks* blocks) {
   const float c1 = 1.f / (1.f - powf(b1, static_cast<float>(t)));
   const float c2 = 1.f / (1.f - powf(b2, static_cast<float>(t)));
+  WeightBlocks none{};
   adamKernel<<<(n + 255) / 256, 256, 0, stream>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2,
-                                                   static_cast<__nv_bfloat16*>(wb));
+                                                   static_cast<__nv_bfloat16*>(wb), static_cast<__nv_bfloat16*>(wbT),
+                                                   wbT && blocks ? *blocks : none);
+  return cudaGetLastError();
+}
+
+cudaError_t transposeWeightsBf16(const float* w, size_t n, void* wbT, const WeightBlocks& blocks, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  transposeWeightsKernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(
+      w, static_cast<int>(n), static_cast<__nv_bfloat16*>(wbT), blocks);
   return cudaGetLastError();
 }
 

@@ -432,7 +432,11 @@ constexpr uint32_t kGemmStage = kGemmTile * kGemmChunk * 2;  // bytes per operan
 // no block ever waits in tcgen05.alloc.
 constexpr uint32_t kGemmSmem = 56 * 1024;
 static_assert(2 * kGemmStage + 128 <= kGemmSmem, "staging exceeds the block's shared memory");
-static_assert(8 * 32 * 33 * 4 + 128 <= kGemmSmem, "epilogue tiles exceed the block's shared memory");
+constexpr uint32_t kGemmMaskOff = 8 * 32 * 33 * 4;  // after the eight warps' fp32 epilogue tiles
+constexpr int kGemmMaskLd = 40;                     // bf16 per mask row: 80 bytes, 16-byte aligned rows
+static_assert(kGemmMaskOff % 16 == 0, "mask tiles must start 16-byte aligned");
+static_assert(kGemmMaskOff + 8 * 32 * kGemmMaskLd * 2 + 128 <= kGemmSmem,
+              "epilogue tiles exceed the block's shared memory");
 __device__ uint32_t g_tcGemmErr;
 
 constexpr int kGemmThreads = 256;  // eight warps: two per accumulator lane quarter
@@ -466,24 +470,61 @@ __device__ __forceinline__ void stageOperand(unsigned char* dst, const __nv_bflo
       *reinterpret_cast<uint4*>(dst + coreOffset(static_cast<uint32_t>(r), static_cast<uint32_t>(c), kGemmChunk)) = v;
     }
   } else {
-    // groups of 8 consecutive rows of one k
-    for (int e = tid; e < (rowsPadded / 8) * kGemmChunk; e += kGemmThreads) {
-      const int c = e / (rowsPadded / 8), r = (e % (rowsPadded / 8)) * 8;
-      const int k = k0 + c;
-      uint16_t t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // 8 x 8 blocks (8 rows x 8 k), one per group of eight lanes: lane l8
+    // loads the block's 8 rows at k = 8 kg + l8 (16 bytes, rows contiguous in
+    // memory), the group transposes the block in three exchange rounds, and
+    // lane l8 stores row l8's 8 k as one 16-byte row of a core matrix, so the
+    // eight lanes of a store phase fill 128 contiguous bytes.
+    const int lane = tid & 31, q = lane >> 3, l8 = lane & 7;
+    const int groups = rowsPadded / 8, nBlocks = groups * (kGemmChunk / 8);  // nBlocks: a multiple of 4
+    for (int base = (tid >> 5) * 4; base < nBlocks; base += kGemmThreads / 8) {
+      const int b = base + q;  // < nBlocks for every lane: the warp runs each round whole
+      const int g = b % groups, kg = b / groups;
+      const int r = g * 8, k = k0 + kg * 8 + l8;
+      uint32_t w0 = 0u, w1 = 0u, w2 = 0u, w3 = 0u;
       if (k < kEnd) {
         const __nv_bfloat16* src = P + static_cast<size_t>(k) * ld + row0 + r;
         if (vec && r + 8 <= rowsValid) {
           const uint4 v = *reinterpret_cast<const uint4*>(src);
-          t[0] = v.x & 0xffff; t[1] = v.x >> 16; t[2] = v.y & 0xffff; t[3] = v.y >> 16;
-          t[4] = v.z & 0xffff; t[5] = v.z >> 16; t[6] = v.w & 0xffff; t[7] = v.w >> 16;
+          w0 = v.x; w1 = v.y; w2 = v.z; w3 = v.w;
         } else {
-          for (int j = 0; j < 8; ++j) t[j] = r + j < rowsValid ? __bfloat16_as_ushort(src[j]) : 0;
+          uint32_t t[8];
+          for (int j = 0; j < 8; ++j) t[j] = r + j < rowsValid ? __bfloat16_as_ushort(src[j]) : 0u;
+          w0 = t[0] | (t[1] << 16); w1 = t[2] | (t[3] << 16); w2 = t[4] | (t[5] << 16); w3 = t[6] | (t[7] << 16);
         }
       }
-      for (int j = 0; j < 8; ++j)
-        *reinterpret_cast<uint16_t*>(dst + coreOffset(static_cast<uint32_t>(r + j), static_cast<uint32_t>(c),
-                                                      kGemmChunk)) = t[j];
+      // Round 1, lanes l8 ^ 4: elements 4-7 of the low lanes for 0-3 of the high ones.
+      {
+        const bool hi = l8 & 4;
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, hi ? w0 : w2, 4);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, hi ? w1 : w3, 4);
+        if (hi) { w0 = r0; w1 = r1; } else { w2 = r0; w3 = r1; }
+      }
+      // Round 2, lanes l8 ^ 2: element pairs {2,3}, {6,7} against {0,1}, {4,5}.
+      {
+        const bool hi = l8 & 2;
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, hi ? w0 : w1, 2);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, hi ? w2 : w3, 2);
+        if (hi) { w0 = r0; w2 = r1; } else { w1 = r0; w3 = r1; }
+      }
+      // Round 3, lanes l8 ^ 1: odd elements of the even lane for even
+      // elements of the odd lane, two per exchanged word.
+      {
+        const bool hi = l8 & 1;
+        const uint32_t s0 = hi ? __byte_perm(w0, w1, 0x5410) : __byte_perm(w0, w1, 0x7632);
+        const uint32_t s1 = hi ? __byte_perm(w2, w3, 0x5410) : __byte_perm(w2, w3, 0x7632);
+        const uint32_t r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+        const uint32_t r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+        if (hi) {
+          w0 = __byte_perm(r0, w0, 0x7610); w1 = __byte_perm(r0, w1, 0x7632);
+          w2 = __byte_perm(r1, w2, 0x7610); w3 = __byte_perm(r1, w3, 0x7632);
+        } else {
+          w0 = __byte_perm(w0, r0, 0x5410); w1 = __byte_perm(w1, r0, 0x7610);
+          w2 = __byte_perm(w2, r1, 0x5410); w3 = __byte_perm(w3, r1, 0x7610);
+        }
+      }
+      *reinterpret_cast<uint4*>(dst + coreOffset(static_cast<uint32_t>(r + l8), static_cast<uint32_t>(kg * 8),
+                                                 kGemmChunk)) = make_uint4(w0, w1, w2, w3);
     }
   }
 }
@@ -561,17 +602,46 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     const uint32_t laneBase = tmem + (static_cast<uint32_t>(lq * 32) << 16);
     const bool empty = kEnd <= kBeg;  // no chunk ran: the accumulator holds nothing
     float* t = reinterpret_cast<float*>(stage) + warp * (32 * 33);
+    // kMode 2: the warp's 32 x 32 block of the mask, read in 16-byte pieces
+    // while the accumulators load, then turned through shared memory too.
+    __nv_bfloat16* mt = reinterpret_cast<__nv_bfloat16*>(stage + kGemmMaskOff) + warp * (32 * kGemmMaskLd);
+    const bool maskVec = kMode == 2 && (reinterpret_cast<uintptr_t>(mask) & 15) == 0 && (ldc & 7) == 0;
     for (int c0 = 64 * half; c0 < min(Nt, 64 * half + 64); c0 += 32) {
+      uint4 mq[4];
+      if (kMode == 2) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int m = m0 + lq * 32 + (lane >> 2) + 8 * i, cc = c0 + (lane & 3) * 8;
+          mq[i] = make_uint4(0u, 0u, 0u, 0u);
+          if (m < M) {
+            const __nv_bfloat16* src = mask + static_cast<size_t>(m) * ldc + n0 + cc;
+            if (maskVec && cc + 8 <= Nt) {
+              mq[i] = __ldg(reinterpret_cast<const uint4*>(src));
+            } else {
+              uint16_t e[8];
+              for (int j = 0; j < 8; ++j) e[j] = cc + j < Nt ? __bfloat16_as_ushort(src[j]) : 0;
+              mq[i] = make_uint4(e[0] | (uint32_t(e[1]) << 16), e[2] | (uint32_t(e[3]) << 16),
+                                 e[4] | (uint32_t(e[5]) << 16), e[6] | (uint32_t(e[7]) << 16));
+            }
+          }
+        }
+      }
       float v[32];
       if (!empty) tmemLoad32(laneBase + static_cast<uint32_t>(c0), v);
       else
         for (int j = 0; j < 32; ++j) v[j] = 0.f;
 #pragma unroll
       for (int j = 0; j < 32; ++j) t[lane * 33 + j] = v[j];  // row `lane`, column j
+      if (kMode == 2) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          *reinterpret_cast<uint4*>(mt + ((lane >> 2) + 8 * i) * kGemmMaskLd + (lane & 3) * 8) = mq[i];
+      }
       __syncwarp();
       const int n = n0 + c0 + lane;
       const bool colOk = c0 + lane < Nt;
       const float bn = (kMode == 1 || kMode == 3) && colOk ? bias[n] : 0.f;
+#pragma unroll
       for (int r = 0; r < 32; ++r) {
         const int m = m0 + lq * 32 + r;
         if (m >= M || !colOk) continue;
@@ -584,7 +654,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           Cf[o] = z;
           Hb[o] = __float2bfloat16(fmaxf(z, 0.f));
         } else if (kMode == 2) {
-          Hb[o] = __float2bfloat16(__bfloat162float(mask[o]) > 0.f ? acc : 0.f);
+          Hb[o] = __float2bfloat16(__bfloat162float(mt[r * kGemmMaskLd + lane]) > 0.f ? acc : 0.f);
         } else {
           Cf[o] = acc + bn;
         }
