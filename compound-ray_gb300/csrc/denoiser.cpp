@@ -134,11 +134,13 @@ float Denoiser::forwardBackward(const void* X, const float* base, const float* t
 }
 
 // Forward, loss gradient and backward of one minibatch into grads_, with the
-// summed squared error added to *lossAcc (device) when given.  No host sync.
-void Denoiser::step(const void* X, const float* base, const float* target, int rows, float* lossAcc, cudaStream_t s) {
+// summed squared error added to lossAcc[*lossIndex] (device; index 0 when
+// lossIndex is null) when lossAcc is given.  No host sync.
+void Denoiser::step(const void* X, const float* base, const float* target, int rows, float* lossAcc, cudaStream_t s,
+                    const int* lossIndex) {
   const uint16_t* w = static_cast<const uint16_t*>(wbf_);
   forward(X, rows, s);
-  ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, lossAcc, s), "loss");
+  ck(mlpLoss(y_, kOut, base, target, rows, nullptr, dyf_, dyb_, lossAcc, s, lossIndex), "loss");
   // Output layer.
   ck(gemm(0, kHidden, kOut, rows, h_[2], kHidden, true, dyb_, kOut, false, grads_ + offW4, nullptr, kOut, nullptr,
               nullptr, s),
@@ -198,37 +200,90 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
   if (steps <= 0) return;
   batch = static_cast<int>(std::min<size_t>(static_cast<size_t>(batch), rows_));
   ensureBatch(batch);
-  // The shuffled order of an epoch lives on the device and the per-step
-  // losses accumulate there: the loop issues kernels only, no host waits.
+  // The shuffled order of an epoch, the step sizes and Adam's bias
+  // corrections of every step, the per-step losses and the loop's position
+  // (TrainState) live on the device.  The first step runs as plain launches
+  // (it sets up what the kernels need), the next is captured as a CUDA graph
+  // and replayed for the rest; the host only reshuffles between epochs.
   std::mt19937 rng(seed);
   std::vector<uint32_t> perm(rows_);
   std::iota(perm.begin(), perm.end(), 0u);
   std::shuffle(perm.begin(), perm.end(), rng);
+  std::vector<float> sched(3 * static_cast<size_t>(steps));
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int st = 0; st < steps; ++st) {
+    // half-cosine decay of the step size over this call, down to 5%
+    const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
+    const float t = static_cast<float>(adamT_ + st + 1);
+    sched[3 * st] = lr * decay;
+    sched[3 * st + 1] = 1.f / (1.f - powf(b1, t));
+    sched[3 * st + 2] = 1.f / (1.f - powf(b2, t));
+  }
   uint32_t* permDev = dalloc<uint32_t>(rows_);
   float* lossDev = dalloc<float>(static_cast<size_t>(steps));
-  ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
-  ck(cudaMemsetAsync(lossDev, 0, static_cast<size_t>(steps) * 4, s), "memset");
-  size_t cursor = 0;
+  float* schedDev = dalloc<float>(sched.size());
+  TrainState* state = dalloc<TrainState>(1);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto cleanup = [&]() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    dfree(permDev);
+    dfree(lossDev);
+    dfree(schedDev);
+    dfree(state);
+  };
   tc_ = tc;
   try {
-    for (int st = 0; st < steps; ++st) {
+    ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
+    ck(cudaMemcpyAsync(schedDev, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice, s), "schedule");
+    ck(cudaMemsetAsync(lossDev, 0, static_cast<size_t>(steps) * 4, s), "memset");
+    ck(cudaMemsetAsync(state, 0, sizeof(TrainState), s), "memset");
+    const WeightBlocks blocks = weightBlocks();
+    auto oneStep = [&]() {
+      ck(gatherRows(X_, base_, target_, permDev, batch, Xb_, baseb_, targetb_, s, &state->offset), "gather");
+      step(Xb_, baseb_, targetb_, batch, loss ? lossDev : nullptr, s, &state->step);
+      ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), 0.f, b1, b2, 1e-8f, 1, wbf_, s, wbfT_, &blocks,
+                  schedDev, &state->step),
+         "adam");
+      ck(advanceTrainState(state, static_cast<uint32_t>(batch), s), "advance");
+    };
+    size_t cursor = 0;
+    for (int st = 0; st < steps;) {
       if (cursor + static_cast<size_t>(batch) > rows_) {
         ck(cudaStreamSynchronize(s), "epoch");  // the previous order is no longer read
         std::shuffle(perm.begin(), perm.end(), rng);
         ck(cudaMemcpyAsync(permDev, perm.data(), rows_ * 4, cudaMemcpyHostToDevice, s), "perm");
+        const TrainState at{st, 0u};
+        ck(cudaMemcpyAsync(state, &at, sizeof(at), cudaMemcpyHostToDevice, s), "state");
+        ck(cudaStreamSynchronize(s), "epoch");
         cursor = 0;
       }
-      ck(gatherRows(X_, base_, target_, permDev + cursor, batch, Xb_, baseb_, targetb_, s), "gather");
-      cursor += static_cast<size_t>(batch);
-      step(Xb_, baseb_, targetb_, batch, loss ? lossDev + st : nullptr, s);
-      ++adamT_;
-      // half-cosine decay of the step size over this call, down to 5%
-      const float decay = 0.05f + 0.95f * 0.5f * (1.0f + std::cos(3.14159265f * static_cast<float>(st) / steps));
-      const WeightBlocks blocks = weightBlocks();
-      ck(adamStep(params_, grads_, m_, v_, static_cast<int>(kParams), lr * decay, 0.9f, 0.999f, 1e-8f, adamT_, wbf_,
-                  s, wbfT_, &blocks),
-         "adam");
+      const int run = static_cast<int>(std::min<size_t>(static_cast<size_t>(steps - st),
+                                                        (rows_ - cursor) / static_cast<size_t>(batch)));
+      int done = 0;
+      if (!exec) {
+        oneStep();
+        done = 1;
+        if (run > 1) {
+          ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+          try {
+            oneStep();
+          } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+          }
+          ck(cudaStreamEndCapture(s, &graph), "capture");
+          ck(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+        }
+      }
+      for (; done < run; ++done) ck(cudaGraphLaunch(exec, s), "graph launch");
+      st += run;
+      cursor += static_cast<size_t>(run) * static_cast<size_t>(batch);
     }
+    adamT_ += steps;
     if (loss) {
       ck(cudaMemcpyAsync(loss, lossDev, static_cast<size_t>(steps) * 4, cudaMemcpyDeviceToHost, s), "loss readback");
     }
@@ -241,12 +296,10 @@ void Denoiser::train(int steps, int batch, float lr, uint32_t seed, float* loss,
     }
   } catch (...) {
     tc_ = false;
-    dfree(permDev);
-    dfree(lossDev);
+    cleanup();
     throw;
   }
-  dfree(permDev);
-  dfree(lossDev);
+  cleanup();
   if (loss)
     for (int st = 0; st < steps; ++st) loss[st] /= 3.0f * static_cast<float>(batch);
 }

@@ -72,7 +72,8 @@ class Denoiser {
   void ensureBatch(int rows);
   float forwardBackward(const void* X, const float* base, const float* target, int rows, bool wantLoss,
                         cudaStream_t s);
-  void step(const void* X, const float* base, const float* target, int rows, float* lossAcc, cudaStream_t s);
+  void step(const void* X, const float* base, const float* target, int rows, float* lossAcc, cudaStream_t s,
+            const int* lossIndex = nullptr);
   void forward(const void* X, int rows, cudaStream_t s);
 
   float* params_ = nullptr;

@@ -176,8 +176,17 @@ cudaError_t gemmBf16Tc(int mode, int M, int N, int K, const void* A, int lda, bo
 cudaError_t takeTcGemmError(uint32_t* flags);
 cudaError_t colSumBf16(const void* in, int M, int N, int ld, float* out, cudaStream_t stream);
 cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStream_t stream);
+// Position of a training loop on the device.  The kernels of one step read
+// it, so that one captured step can be replayed as a CUDA graph.
+struct TrainState {
+  int step;         // index into the step-size schedule and the loss array
+  uint32_t offset;  // first entry of this step's rows in the shuffled order
+};
+// lossIndex: null, or the device index added to lossSum.
 cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
-                    void* dyb, float* lossSum, cudaStream_t stream);
+                    void* dyb, float* lossSum, cudaStream_t stream, const int* lossIndex = nullptr);
+// state->step += 1, state->offset += rows.
+cudaError_t advanceTrainState(TrainState* state, uint32_t rows, cudaStream_t stream);
 // Row-major weight matrices inside a flat parameter vector.  Their
 // transposes (same offsets) are the K-contiguous operands of the tcgen05
 // forward GEMMs.
@@ -186,9 +195,12 @@ struct WeightBlocks {
   int off[4], rows[4], cols[4];
 };
 // Adam on the fp32 master weights; refreshes the bf16 copy wb and, when
-// wbT is given, the bf16 transposes of `blocks` in wbT.
+// wbT is given, the bf16 transposes of `blocks` in wbT.  sched: null, or
+// per step (step size, 1 / (1 - b1^t), 1 / (1 - b2^t)) on the device, read
+// at the device index *stepIdx in place of lr and t.
 cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
-                     int t, void* wb, cudaStream_t stream, void* wbT = nullptr, const WeightBlocks* blocks = nullptr);
+                     int t, void* wb, cudaStream_t stream, void* wbT = nullptr, const WeightBlocks* blocks = nullptr,
+                     const float* sched = nullptr, const int* stepIdx = nullptr);
 // wbT = bf16 transposes of `blocks` of the n fp32 parameters w.
 cudaError_t transposeWeightsBf16(const float* w, size_t n, void* wbT, const WeightBlocks& blocks, cudaStream_t stream);
 cudaError_t toBf16(const float* in, void* out, size_t n, cudaStream_t stream);
@@ -218,8 +230,10 @@ cudaError_t deriveFeatureStats(const float* stats, const float4* omm, uint32_t N
 cudaError_t inferDenoiserTc(const float4* derived, const float4* axes, const int* nb, uint32_t N, uint32_t P,
                             const MlpWeights& w, float* out, uint32_t* errFlag, cudaStream_t stream,
                             bool residual = true, const uint32_t* order = nullptr);
+// Rows idx[offset .. offset + rows) of the training set, offset = *offset
+// on the device when given, else 0.
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
-                       float* baseo, float* targeto, cudaStream_t stream);
+                       float* baseo, float* targeto, cudaStream_t stream, const uint32_t* offset = nullptr);
 
 // Tuning variants of the plain render kernel (see render.cu); the variant
 // is process-wide and picked by the autotuner in eye_renderer.cpp.

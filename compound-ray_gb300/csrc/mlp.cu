@@ -219,8 +219,10 @@ cudaError_t colSum(const T* in, int M, int N, int ld, float* out, cudaStream_t s
 // the mean squared error w.r.t. y (fp32 and bf16 copies, padded columns 0).
 __global__ void lossKernel(const float* __restrict__ y, int ldy, const float* __restrict__ base,
                            const float* __restrict__ target, int rows, float* __restrict__ pred,
-                           float* __restrict__ dyf, __nv_bfloat16* __restrict__ dyb, float* __restrict__ lossSum) {
+                           float* __restrict__ dyf, __nv_bfloat16* __restrict__ dyb, float* __restrict__ lossSum,
+                           const int* __restrict__ lossIndex) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (lossSum && lossIndex) lossSum += *lossIndex;
   float e2 = 0.f;
   if (r < rows) {
     const float scale = 2.0f / (3.0f * static_cast<float>(rows));
@@ -259,9 +261,16 @@ __device__ __forceinline__ void putTransposed(int i, float wi, __nv_bfloat16* __
 
 __global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                            float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2,
-                           __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbT, WeightBlocks blocks) {
+                           __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbT, WeightBlocks blocks,
+                           const float* __restrict__ sched, const int* __restrict__ stepIdx) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (sched) {
+    const float* e = sched + 3 * static_cast<size_t>(*stepIdx);
+    lr = e[0];
+    c1 = e[1];
+    c2 = e[2];
+  }
   const float gi = g[i];
   const float mi = b1 * m[i] + (1.f - b1) * gi;
   const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
@@ -457,10 +466,11 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 
 __global__ void gatherRowsKernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ base,
                                  const float* __restrict__ target, const uint32_t* __restrict__ idx, int rows,
-                                 __nv_bfloat16* __restrict__ Xo, float* __restrict__ baseo, float* __restrict__ targeto) {
+                                 __nv_bfloat16* __restrict__ Xo, float* __restrict__ baseo, float* __restrict__ targeto,
+                                 const uint32_t* __restrict__ offset) {
   const int r = blockIdx.x;
   if (r >= rows) return;
-  const size_t src = idx[r];
+  const size_t src = idx[(offset ? *offset : 0u) + r];
   for (int k = threadIdx.x; k < kFeatureWidth; k += blockDim.x)
     Xo[static_cast<size_t>(r) * kFeatureWidth + k] = X[src * kFeatureWidth + k];
   if (threadIdx.x < 3) {
@@ -535,21 +545,23 @@ cudaError_t colSumF32(const float* in, int M, int N, int ld, float* out, cudaStr
 }
 
 cudaError_t mlpLoss(const float* y, int ldy, const float* base, const float* target, int rows, float* pred, float* dyf,
-                    void* dyb, float* lossSum, cudaStream_t stream) {
+                    void* dyb, float* lossSum, cudaStream_t stream, const int* lossIndex) {
   if (rows <= 0) return cudaSuccess;
   lossKernel<<<(rows + 255) / 256, 256, 0, stream>>>(y, ldy, base, target, rows, pred, dyf,
-                                                      static_cast<__nv_bfloat16*>(dyb), lossSum);
+                                                      static_cast<__nv_bfloat16*>(dyb), lossSum, lossIndex);
   return cudaGetLastError();
 }
 
 cudaError_t adamStep(float* w, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
-                     int t, void* wb, cudaStream_t stream, void* wbT, const WeightBlocks* blocks) {
+                     int t, void* wb, cudaStream_t stream, void* wbT, const WeightBlocks* blocks, const float* sched,
+                     const int* stepIdx) {
   const float c1 = 1.f / (1.f - powf(b1, static_cast<float>(t)));
   const float c2 = 1.f / (1.f - powf(b2, static_cast<float>(t)));
   WeightBlocks none{};
   adamKernel<<<(n + 255) / 256, 256, 0, stream>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2,
                                                    static_cast<__nv_bfloat16*>(wb), static_cast<__nv_bfloat16*>(wbT),
-                                                   wbT && blocks ? *blocks : none);
+                                                   wbT && blocks ? *blocks : none, sched && stepIdx ? sched : nullptr,
+                                                   stepIdx);
   return cudaGetLastError();
 }
 
@@ -604,10 +616,20 @@ cudaError_t inferDenoiser(const float* stats, const float4* omm, const int* nb, 
 }
 
 cudaError_t gatherRows(const void* X, const float* base, const float* target, const uint32_t* idx, int rows, void* Xo,
-                       float* baseo, float* targeto, cudaStream_t stream) {
+                       float* baseo, float* targeto, cudaStream_t stream, const uint32_t* offset) {
   if (rows <= 0) return cudaSuccess;
   gatherRowsKernel<<<rows, 128, 0, stream>>>(static_cast<const __nv_bfloat16*>(X), base, target, idx, rows,
-                                             static_cast<__nv_bfloat16*>(Xo), baseo, targeto);
+                                             static_cast<__nv_bfloat16*>(Xo), baseo, targeto, offset);
+  return cudaGetLastError();
+}
+
+__global__ void advanceTrainKernel(TrainState* state, uint32_t rows) {
+  state->step += 1;
+  state->offset += rows;
+}
+
+cudaError_t advanceTrainState(TrainState* state, uint32_t rows, cudaStream_t stream) {
+  advanceTrainKernel<<<1, 1, 0, stream>>>(state, rows);
   return cudaGetLastError();
 }
 
