@@ -1424,6 +1424,23 @@ int crBatchDestroy(int handle) {
   return 0;
 }
 
+int renderBatch(const int* cams, size_t nCams, size_t posesPerCam, const float* d_poses, float* d_out) {
+  const int h = crBatchCreate(cams, nCams, posesPerCam, d_poses, d_out);
+  if (h < 0) return -1;
+  int rc = crBatchLaunch(h);
+  if (rc == 0) {
+    rc = guarded(
+        "renderBatch",
+        [&]() -> int {
+          check(cudaStreamSynchronize(R().stream()), "renderBatch");
+          return 0;
+        },
+        -1);
+  }
+  crBatchDestroy(h);
+  return rc;
+}
+
 // Same work as crRenderPosesDevice for callers that cannot allocate device
 // memory when they render: the chunk partials go to the library's fixed
 // device array instead of a library-allocated buffer, and the call makes no

@@ -185,6 +185,8 @@ def configureExtras(eyeRenderer):
     L.crBatchOutputOffset.restype = c_size_t
     L.crBatchDestroy.argtypes = [c_int]
     L.crBatchDestroy.restype = c_int
+    L.renderBatch.argtypes = [ndpointer(np.int32, flags="C_CONTIGUOUS"), c_size_t, c_size_t, c_void_p, c_void_p]
+    L.renderBatch.restype = c_int
     L.crRenderPosesDeviceNoAlloc.argtypes = [c_void_p, c_size_t, c_void_p]
     L.crRenderPosesDeviceNoAlloc.restype = c_int
     L.crMeasureTraversal.argtypes = [c_void_p, c_size_t, POINTER(c_double), POINTER(c_double)]

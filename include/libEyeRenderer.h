@@ -144,6 +144,10 @@ int crBatchLaunch(int handle);
 int crBatchLatencies(int handle, float* msPerCam, float* totalMs);
 size_t crBatchOutputOffset(int handle, size_t camIndex);
 int crBatchDestroy(int handle);
+/* One-shot batch: crBatchCreate, one launch, a wait for it, crBatchDestroy.
+ * Camera i's frames start at float offset 3 * posesPerCam * (the ommatidium
+ * counts of cams[0 .. i-1] summed) of d_out.  0 on success, -1 on error. */
+int renderBatch(const int* cams, size_t nCams, size_t posesPerCam, const float* d_poses, float* d_out);
 
 /* Diagnostic: renders `count` device poses (layout of crRenderPosesDevice)
  * of the current eye and reports the mean BVH node visits and triangle tests

@@ -80,3 +80,15 @@ def _batch_case(lib, tmp_path, cut):
     assert lib.crBatchDestroy(h) == 0
     assert lib.crBatchLaunch(h) == -1
     assert "unknown batch handle" in eh.lastError(lib)
+    # The one-shot form (create, launch, wait, destroy) gives the same frames.
+    for i, c in enumerate(cams):
+        lib.gotoCamera(int(c))
+        lib.setCurrentEyeSamplesPerOmmatidium(info["spp"][i])
+    d_out.zero_()
+    assert lib.renderBatch(cams, len(cams), P, d_poses.data_ptr(), d_out.data_ptr()) == 0, eh.lastError(lib)
+    got = d_out.cpu().numpy()
+    for i in range(len(cams)):
+        off = sum(sizes[:i])
+        assert np.array_equal(got[off:off + sizes[i]], refs[0][i]), "one-shot batch, eye %d" % i
+    assert lib.renderBatch(cams, 0, P, d_poses.data_ptr(), d_out.data_ptr()) == -1
+    assert "empty batch" in eh.lastError(lib)
