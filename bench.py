@@ -858,6 +858,35 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     if lib.crAutotune(d_poses.data_ptr(), 4, ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
     cut = float(lib.crGetCutRadius())
+    # Error budget: the largest number of halvings of the predicted counts
+    # (0, 0.5, .., 4) whose adaptive render of validation poses (neither
+    # trained on nor evaluated) stays within 90% of 1/255 RMSE against their
+    # plain 1024-sample render.
+    val_poses = 8 if scene == "large" else 200
+    if scene == "large":
+        val = scenes.random_poses(info["height_fn"], val_poses, rng, 150.0)
+    else:
+        val = scenes.open_poses(info["boxes"], val_poses, rng)
+    v16 = np.zeros((val_poses, 16), np.float32)
+    for k in range(4):
+        v16[:, 4 * k:4 * k + 3] = val[:, 3 * k:3 * k + 3]
+    d_vposes = torch.from_numpy(v16).to(dev)
+    d_vref = torch.empty((val_poses, N, 3), dtype=torch.float32, device=dev)
+    d_vout = torch.empty_like(d_vref)
+    if lib.crRenderPosesDevice(d_vposes.data_ptr(), val_poses, d_vref.data_ptr()) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    val_rmse, halvings = {}, 0.0
+    for h in np.arange(0.0, 4.01, 0.5):
+        if lib.crSetAllocatorHalvings(float(h)) != 0 or \
+                lib.crAdaptiveRenderPosesDevice(d_vposes.data_ptr(), val_poses, 8, d_vout.data_ptr(), None, None) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        val_rmse[str(float(h))] = float(torch.sqrt(((d_vout - d_vref) ** 2).mean()))
+        if val_rmse[str(float(h))] > 0.9 / 255.0:
+            break
+        halvings = float(h)
+    if lib.crSetAllocatorHalvings(halvings) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    del d_vref, d_vout
     if profile:
         adaptive()
         adaptive()
@@ -877,12 +906,14 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     ref = d_out.cpu().numpy()
     rmse = float(np.sqrt(((img - ref) ** 2).mean()))
     lib.crSetBvhBuilder(0)
+    lib.crSetAllocatorHalvings(0)
     rays_plain = float(held_poses) * N * 1024
     lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
     return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
             "autotune": {"variant": best.value, "near_field_cut_fraction": cut},
-            "label_histogram": lab_hist, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
+            "label_histogram": lab_hist, "halvings": halvings, "validation_poses": val_poses,
+            "validation_rmse_by_halvings": val_rmse, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
             "train_s": t_train, "rmse_vs_plain_1024": rmse, "target_rmse": 1.0 / 255.0,
             "meets_target": rmse <= 1.0 / 255.0,
             "rays_adaptive": rays.value, "rays_plain_1024": rays_plain, "ray_fraction": rays.value / rays_plain,

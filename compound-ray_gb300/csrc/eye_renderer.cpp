@@ -1697,6 +1697,7 @@ struct DenoiseState {
   DevBuf<unsigned long long> counts, tileScratch;
   std::vector<uint16_t> lastLabels;
   double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
+  float allocHalvings = 0.f;  // predicted counts are divided by 2^allocHalvings (crSetAllocatorHalvings)
 };
 
 DenoiseState& DS() {
@@ -2116,6 +2117,17 @@ int crAllocatorSave(const char* path) {
       -1);
 }
 
+int crSetAllocatorHalvings(float halvings) {
+  if (!(halvings >= 0.f) || halvings > 6.f) {
+    setError("crSetAllocatorHalvings: the value must lie in [0, 6]");
+    return -1;
+  }
+  DS().allocHalvings = halvings;
+  return 0;
+}
+
+float crGetAllocatorHalvings(void) { return DS().allocHalvings; }
+
 int crAllocatorLoad(const char* path) {
   return guarded(
       "crAllocatorLoad",
@@ -2171,7 +2183,7 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           d.level.ensure(rows);
           d.counts.ensure(kAdaptiveBuckets);
           check(cudaMemsetAsync(d.counts.ptr, 0, kAdaptiveBuckets * 8, st), "cudaMemset");
-          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st), "allocation");
+          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st, d.allocHalvings), "allocation");
           unsigned long long cnt[kAdaptiveBuckets];
           check(cudaMemcpyAsync(cnt, d.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st), "cudaMemcpy");
           check(cudaStreamSynchronize(st), "allocation");

@@ -1583,8 +1583,10 @@ __global__ void __launch_bounds__(128, 5)
   v3 col = mk(0.f, 0.f, 0.f);
   uint32_t nodeVisits = 0, triTests = 0;
   __shared__ uint32_t sortKey[4][256], sortIdx[4][256];  // per warp of the block (128 threads)
+  __shared__ float2 sortDraw[4][256];  // the task's random numbers, by sample, drawn once for key and trace
   uint32_t* key = sortKey[threadIdx.x >> 5];
   uint32_t* idx = sortIdx[threadIdx.x >> 5];
+  float2* draw = sortDraw[threadIdx.x >> 5];
   if (valid && spl > 1) {  // the warp is one entry (segWidth 32): `valid` is warp-uniform
     const uint32_t e = B.entries[i];
     const uint32_t n = 32u * spl;  // 64, 128 or 256
@@ -1595,6 +1597,7 @@ __global__ void __launch_bounds__(128, 5)
       const float ud = curand_uniform(&st);
       key[k] = coneKey(nd, ud);
       idx[k] = k;
+      draw[k] = make_float2(nd, ud);
     }
     __syncwarp();
     // bitonic sort of (key, idx) pairs, ascending
@@ -1631,11 +1634,21 @@ __global__ void __launch_bounds__(128, 5)
                    mk(Z.x, Z.y, Z.z) * relPos.z;
     const float invSpp = 1.0f / static_cast<float>(spp);
     for (uint32_t j = 0; j < spl; ++j) {
-      const uint32_t s = chunk * 32u * spl + (spl > 1 ? idx[j * 32u + lane] : j * segWidth + lane % segWidth);
-      curandStatePhilox4_32_10_t st;
-      curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + s, 0ull, &st);
-      const float nd = curand_normal(&st);
-      const float ud = curand_uniform(&st);
+      uint32_t s;
+      float nd, ud;
+      if (spl > 1) {
+        const uint32_t k = idx[j * 32u + lane];
+        s = chunk * 32u * spl + k;
+        const float2 d = draw[k];
+        nd = d.x;
+        ud = d.y;
+      } else {
+        s = chunk * 32u * spl + j * segWidth + lane % segWidth;
+        curandStatePhilox4_32_10_t st;
+        curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + s, 0ull, &st);
+        nd = curand_normal(&st);
+        ud = curand_uniform(&st);
+      }
       const v3 splayed = rotatePoint(axis, nd * sd, perp);
       const v3 rel = rotatePoint(splayed, ud * CR_PI_F, axis);
       const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
@@ -1735,13 +1748,17 @@ __global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows
 // outputs; the predicted count is 2^(10 l)): level = bucket index 0..8 of
 // 4 << index samples, 0x80 | 8 for a fallback entry (more than 1024 needed),
 // or kNoRender (at most featureSpp samples needed: the feature render suffices).
+// halvings: the predicted count (capped at 2048) is divided by 2^halvings
+// first, halvings >= 0 and possibly fractional (the per-entry error budget
+// traded for rays; a halving of 1 or more leaves no fallback).
 __global__ void allocateKernel(const float* __restrict__ pred, uint64_t rows, uint32_t featureSpp,
-                               uint8_t* __restrict__ level, unsigned long long* __restrict__ counts) {
+                               uint8_t* __restrict__ level, unsigned long long* __restrict__ counts, float halvings) {
   const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= rows) return;
   const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
-  float kf = ceilf(l * 10.0f - 1e-3f);
-  if (!(kf >= 2.0f)) kf = 2.0f;  // also NaN
+  const float l10 = l * 10.0f;
+  float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) - halvings - 1e-3f) : 2.0f;  // NaN: the least count
+  if (!(kf >= 2.0f)) kf = 2.0f;
   if (kf > 11.0f) kf = 11.0f;
   const int k = static_cast<int>(kf);
   uint8_t lv;
@@ -1995,10 +2012,10 @@ cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, 
 }
 
 cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
-                           unsigned long long* counts, cudaStream_t stream) {
+                           unsigned long long* counts, cudaStream_t stream, float halvings) {
   if (rows == 0) return cudaSuccess;
   allocateKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(pred, rows, featureSpp, level,
-                                                                                  counts);
+                                                                                  counts, halvings);
   return cudaGetLastError();
 }
 

@@ -277,6 +277,16 @@ int crAllocatorLoad(const char* path);
  * null, or receives the rays of the call.  0 on success. */
 int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureSpp, float* d_out, uint8_t* d_level,
                                 double* raysTraced);
+/* Error budget of the adaptive render: every predicted count (capped at
+ * 2048) is divided by 2^halvings before it is rounded up to a bucket
+ * (0 <= halvings <= 6, fractions allowed; 0, the default, renders each entry
+ * to the 1/512 standard deviation of its label).  Each halving raises an
+ * extra-sampled entry's expected error by about sqrt(2); from 1 on no entry
+ * falls back to the plain 1024-sample render.  Callers pick the largest
+ * value that keeps their aggregate error target on validation poses.  No
+ * counterpart in the reference. */
+int crSetAllocatorHalvings(float halvings);
+float crGetAllocatorHalvings(void);
 /* Test access: `spp` Philox samples per (pose, ommatidium) of host poses
  * with one seed, recording every ray (records: count x N x spp, as
  * crRenderFrameRecorded) and the per-entry means (sums: count x N x 3). */

@@ -154,3 +154,28 @@ def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
         torch.cuda.synchronize()
         again.append(o2.cpu().numpy())
     assert np.array_equal(again[0], again[1])
+
+    # the error budget: one halving moves every entry down one bucket (from
+    # the same restarted streams); a fallback entry joins the 1024 bucket
+    lv, rs = [], []
+    try:
+        for h in (0, 1):
+            lib.loadGlTFscene(info["gltf"].encode())
+            eh.gotoFirstCompoundEye(lib)
+            assert lib.crSetAllocatorHalvings(h) == 0 and lib.crGetAllocatorHalvings() == h
+            o2 = torch.zeros_like(out)
+            l2 = torch.zeros_like(lev)
+            r2 = eh.c_double(0.0)
+            assert lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), 4, 8, o2.data_ptr(), l2.data_ptr(),
+                                                   eh.ctypes.byref(r2)) == 0, eh.lastError(lib)
+            torch.cuda.synchronize()
+            lv.append(l2.cpu().numpy().astype(np.int64))
+            rs.append(r2.value)
+    finally:
+        lib.crSetAllocatorHalvings(0)
+    k0 = np.where(lv[0] == 0xFF, 3, np.where(lv[0] == 0x88, 11, (lv[0] & 0x7F) + 2))
+    k1 = np.maximum(k0 - 1, 2)
+    assert np.array_equal(lv[1], np.where(k1 <= 3, 0xFF, k1 - 2))
+    assert rs[1] < rs[0]
+    assert lib.crSetAllocatorHalvings(6.5) == -1
+    assert "[0, 6]" in eh.lastError(lib)
