@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
     ap.add_argument("--profile-learned", action="store_true", help="profiling case: learned render of held-out poses")
     ap.add_argument("--profile-adaptive", action="store_true", help="profiling case: adaptive learned render")
+    ap.add_argument("--adaptive-scene", choices=["large", "small"], default="large",
+                    help="scene of the --profile-adaptive case")
     ap.add_argument("--profile-train", type=int, default=0, metavar="STEPS",
                     help="profiling case: STEPS denoiser training steps of 8192 rows on the terrain eye")
     ap.add_argument("--denoiser-kernel", type=int, default=1, help="denoiser inference kernel for --profile-learned: "
@@ -889,8 +891,11 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     del d_vref, d_vout
     if profile:
         adaptive()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("adaptive_render")  # ncu --nvtx --nvtx-include adaptive_render/
         adaptive()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         print(json.dumps({"profile_case": "adaptive learned render of %d held-out poses, twice" % held_poses,
                           "rays": rays.value, "variant": best.value, "cut": cut}))
         return None
@@ -956,7 +961,11 @@ def run_profile_learned(args):
     torch.cuda.set_stream(stream)
     lib.crSetStream(stream.cuda_stream)
     if args.profile_adaptive:
-        run_adaptive(lib, eh, args, stream, held_poses=min(args.poses, 32), profile=True)
+        if args.adaptive_scene == "small":
+            run_adaptive(lib, eh, args, stream, scene="small", train_poses=256, held_poses=min(args.poses, 1000),
+                         profile=True)
+        else:
+            run_adaptive(lib, eh, args, stream, held_poses=min(args.poses, 32), profile=True)
         return
     info = workload(1024)
     if args.profile_train:

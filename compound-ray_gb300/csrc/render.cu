@@ -1557,7 +1557,12 @@ __device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
 // of 32), the task's samples are first sorted by coneKey, so that each round
 // traces 32 rays in neighbouring directions, whose traversals are alike.
 // Every sample is still traced once with its own random numbers; only the
-// order of the per-lane sums changes.
+// order of the per-lane sums changes.  The sort pays on scenes whose
+// traversals are long and vary from ray to ray; on small scenes (fewer than
+// kAdaptiveSortMinTris triangles) it costs more than it saves, and the
+// samples are traced in index order.
+constexpr uint32_t kAdaptiveSortMinTris = 16384;
+
 // Random numbers: Philox4x32-10 stream (seed, e * 1024 + s), one normal then
 // one uniform per sample (O(1) set-up per entry, unlike XORWOW's skip-ahead).
 __global__ void __launch_bounds__(128, 5)
@@ -1587,7 +1592,8 @@ __global__ void __launch_bounds__(128, 5)
   uint32_t* key = sortKey[threadIdx.x >> 5];
   uint32_t* idx = sortIdx[threadIdx.x >> 5];
   float2* draw = sortDraw[threadIdx.x >> 5];
-  if (valid && spl > 1) {  // the warp is one entry (segWidth 32): `valid` is warp-uniform
+  const bool sorted = spl > 1 && sc.triCount >= kAdaptiveSortMinTris;
+  if (valid && sorted) {  // the warp is one entry (segWidth 32): `valid` is warp-uniform
     const uint32_t e = B.entries[i];
     const uint32_t n = 32u * spl;  // 64, 128 or 256
     for (uint32_t k = lane; k < n; k += 32u) {
@@ -1636,7 +1642,7 @@ __global__ void __launch_bounds__(128, 5)
     for (uint32_t j = 0; j < spl; ++j) {
       uint32_t s;
       float nd, ud;
-      if (spl > 1) {
+      if (sorted) {
         const uint32_t k = idx[j * 32u + lane];
         s = chunk * 32u * spl + k;
         const float2 d = draw[k];
