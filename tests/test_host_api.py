@@ -201,6 +201,21 @@ def test_error_contract(lib, tmp_path):
     assert "unknown background shader" in eh.lastError(lib)
 
 
+def test_setter_ranges(lib):
+    """Host-side argument checks of the tuning setters (no GPU work)."""
+    eh.lastError(lib)
+    assert lib.crSetAllocatorHalvings(-0.5) == -1
+    assert "[0, 6]" in eh.lastError(lib)
+    assert lib.crSetAllocatorHalvings(float("nan")) == -1
+    assert "[0, 6]" in eh.lastError(lib)
+    assert lib.crSetAllocatorHalvings(2.5) == 0 and lib.crGetAllocatorHalvings() == 2.5
+    assert lib.crSetAllocatorHalvings(0) == 0 and lib.crGetAllocatorHalvings() == 0.0
+    assert lib.crSetCutRadius(1.5) == -1
+    assert "[0, 1]" in eh.lastError(lib)
+    assert lib.crSetRenderVariant(lib.crGetRenderVariantCount()) == -1
+    assert "out of range" in eh.lastError(lib)
+
+
 def test_eye_files_match_reference_reader(lib, tmp_path):
     """Pins .eye parsing against the reference's own Python reader
     (tests/golden/reference_eyes.npz, made by tests/golden/make_golden.py)."""
