@@ -2155,8 +2155,12 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
         const float4* poses = reinterpret_cast<const float4*>(d_poses);
         const uint32_t fs = static_cast<uint32_t>(featureSpp);
         double rays = 0;
-        for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
-          const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
+        // Poses per pass: at least 256, and up to 2^21 entries, so that a small
+        // eye's trajectory allocates once (one host wait for the bucket sizes)
+        // while the adaptive launch stays below 2^26 warp tasks.
+        const size_t perPass = std::max<size_t>(kMaxPosesPerLaunch, (size_t(1) << 21) / std::max<uint32_t>(1u, e.N));
+        for (size_t first = 0; first < count; first += perPass) {
+          const uint32_t P = static_cast<uint32_t>(std::min<size_t>(perPass, count - first));
           const uint64_t rows = static_cast<uint64_t>(P) * e.N;
           denoiseFeatures(r, d, e, poses + 4 * first, P, fs, false);
           rays += static_cast<double>(rows) * fs;
