@@ -233,7 +233,9 @@ int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSp
 size_t crDenoiserTrainingRows(void);
 /* `steps` Adam steps on shuffled minibatches, the step size decaying from
  * lr by a half cosine to 5% of it over the call; lossHistory: steps floats
- * (mean squared error per step) or null. */
+ * (mean squared error per step) or null.  The first step runs as plain
+ * launches; the rest replay it from a CUDA graph, with the loop's position
+ * kept on the device (the host waits only to reshuffle between epochs). */
 int crDenoiserTrain(int steps, int batch, float lr, int seed, float* lossHistory);
 /* The learned form: featureSpp-sample render + network, count x N x 3
  * (one fused feature + network kernel after the feature render). */
