@@ -757,7 +757,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
                  den_steps=3000, batch=8192, threshold=1.0 / 512.0, seeds=8, profile=False):
     """Learned sample allocator plus denoiser.  scene "large": a 2048 x
     2048-cell heightfield over 400 m with 20,000 cone plants (9.03 M
-    triangles, GPU linear BVH) and a 100,000-ommatidium panoramic eye
+    triangles, host SAH BVH) and a 100,000-ommatidium panoramic eye
     (Fibonacci sphere, acceptance U(0.5, 5) deg), random poses within
     +-150 m; "small": the ground + 64 boxes scene and its 1000-ommatidium
     eye, random poses within +-8 m outside the boxes.  The allocator is
@@ -780,14 +780,17 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
         d = os.path.join(tempfile.gettempdir(), "cr_bench_large_%d" % scenes.SEED)
         info = scenes.terrain_scene(d, cells=2048, extent=400.0, cones=20000, n_omm=100000, poses=4,
                                     eye_kind="panoramic", aa_deg=(0.5, 5.0))
-        label = ("heightfield 2048^2 cells + 20000 cones (%d tris, GPU LBVH), %%d-ommatidium panoramic eye, "
+        label = ("heightfield 2048^2 cells + 20000 cones (%d tris, host SAH BVH), %%d-ommatidium panoramic eye, "
                  "acceptance 0.5-5 deg" % info["triangles"])
     else:
         info = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
         label = "ground + 64 boxes (770 tris, simple_sky), %d-ommatidium Fibonacci-sphere eye, acceptance 3 deg"
     t_scene = time.perf_counter() - t0
     lib.crSetStream(stream.cuda_stream)
-    lib.crSetBvhBuilder(1 if scene == "large" else 0)
+    # The host SAH tree: on this scene both renders trace it faster than the
+    # GPU linear BVH (plain 1024 samples: 357 against 399 ms for 32 poses;
+    # adaptive: 44 against 53 ms); it takes ~10 s to build against ~1 s.
+    lib.crSetBvhBuilder(0)
     t0 = time.perf_counter()
     lib.loadGlTFscene(info["gltf"].encode())
     err = eh.lastError(lib)
