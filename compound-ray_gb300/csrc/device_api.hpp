@@ -317,12 +317,14 @@ cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
                            RayRecord* rec, cudaStream_t stream, const float4* cuts = nullptr);
 // isInsideHitGeometry for n points (xyz floats) against one hitbox mesh
-// (object-space triangles, 3 float3 each): the inverse of the mesh's node
-// transform (row-major 3x3 and translation, double) and the ray start
-// x = object box min.x - 1; out: one byte per point, 1 = inside.
+// (object-space triangles, 3 float3 each): the inverse of the 3x3 part of
+// the mesh's node transform (row-major, double; the object-space point is
+// rounded once to float; as in the reference, the node's translation does
+// not enter) and the ray start x = object box min.x - 1
+// (a float value); the cast itself runs in float as the reference's
+// (sutil/hitscanprocessing.cpp:20-83).  out: one byte per point, 1 = inside.
 struct InsideQuery {
   double inv[9];
-  double t[3];
   double startX;
   // Grid over the object-space (y, z) plane: cell (cz * G + cy) lists, in
   // cellItems[cellStart[c] .. cellStart[c + 1]), every triangle whose (y, z)

@@ -197,6 +197,21 @@ std::vector<uint32_t> directionOrder(const std::vector<Ommatidium>& omm) {
   return out;
 }
 
+// Bound on |position - focal offset * unit axis| over an eye's ommatidia
+// (how far a ray origin can lie from the pose position, in eye units),
+// widened by 0.1% + 1e-6 so the near-field cut's guaranteed radius stays
+// conservative after float rounding.
+float maxRelOf(const std::vector<Ommatidium>& omm) {
+  float mr = 0.f;
+  for (const Ommatidium& o : omm) {
+    const double al = std::sqrt(double(o.dir.x) * o.dir.x + double(o.dir.y) * o.dir.y + double(o.dir.z) * o.dir.z);
+    const double s = al > 0 ? o.focalPointOffset / al : 0.0;
+    const double rx = o.pos.x - s * o.dir.x, ry = o.pos.y - s * o.dir.y, rz = o.pos.z - s * o.dir.z;
+    mr = std::max(mr, static_cast<float>(std::sqrt(rx * rx + ry * ry + rz * rz) * 1.001 + 1e-6));
+  }
+  return mr;
+}
+
 void releaseBatches();
 
 struct Renderer {
@@ -462,14 +477,7 @@ struct Renderer {
         e.order.release();
         e.order.ensure(std::max<size_t>(1, N));
       }
-      float mr = 0.f;
-      for (const Ommatidium& o : c.omm) {
-        const double al = std::sqrt(double(o.dir.x) * o.dir.x + double(o.dir.y) * o.dir.y + double(o.dir.z) * o.dir.z);
-        const double s = al > 0 ? o.focalPointOffset / al : 0.0;
-        const double rx = o.pos.x - s * o.dir.x, ry = o.pos.y - s * o.dir.y, rz = o.pos.z - s * o.dir.z;
-        mr = std::max(mr, static_cast<float>(std::sqrt(rx * rx + ry * ry + rz * rz) * 1.001 + 1e-6));
-      }
-      e.maxRel = mr;
+      e.maxRel = maxRelOf(c.omm);
       if (N) {
         const std::vector<uint32_t> ord = directionOrder(c.omm);
         check(cudaMemcpyAsync(e.order.ptr, ord.data(), 4 * static_cast<size_t>(N), cudaMemcpyHostToDevice, stream()),
@@ -981,6 +989,9 @@ void setOmmatidia(OmmatidiumPacket* omms, size_t count) {
       const std::vector<uint32_t> ord = directionOrder(v);
       check(cudaMemcpyAsync(e.order.ptr, ord.data(), 4 * count, cudaMemcpyHostToDevice, r.stream()), "cudaMemcpy");
       check(cudaStreamSynchronize(r.stream()), "ommatidia upload");
+      // The near-field cut's guaranteed radius depends on how far the ray
+      // origins lie from the pose position: recompute it for the new records.
+      e.maxRel = maxRelOf(v);
     }
     c.omm = std::move(v);
   });
@@ -1098,10 +1109,7 @@ int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, un
                                (f * g - d * i) / det, (a * i - c * g) / det, (c * d - a * f) / det,
                                (d * h - e * g) / det, (b * g - a * h) / det, (a * e - b * d) / det};
         std::memcpy(q.inv, inv, sizeof(inv));
-        q.t[0] = x[3];
-        q.t[1] = x[7];
-        q.t[2] = x[11];
-        q.startX = hm->objMin.x - 1.0;
+        q.startX = hm->objMin.x - 1.0f;  // in float, as the reference's ray start
         Renderer& r = R();
         cudaStream_t st = r.stream();
         const uint32_t nt = static_cast<uint32_t>(hm->tris.size() / 3);

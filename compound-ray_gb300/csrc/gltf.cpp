@@ -735,8 +735,14 @@ f3 rotateAboutAxis(f3 p, float angle, f3 axis) {
   return f3{c * p.x + sn * cr.x + k * a.x, c * p.y + sn * cr.y + k * a.y, c * p.z + sn * cr.z + k * a.z};
 }
 
-bool pointInsideHitbox(const HitboxMesh& m, f3 wp) {
-  // Inverse of the affine transform (3x3 part inverted by cofactors).
+// The object-space point of a hitbox query, as the reference forms it
+// (hitscanprocessing.cpp:22): the inverse node transform times
+// make_float4(worldPoint), whose w is 0 (sutil/vec_math.h make_float4 of a
+// float3), so only the 3x3 part of the inverse applies and the node's
+// translation is ignored.  Here the 3x3 part is inverted by cofactors in
+// double and the product rounded once to float.  false when the transform
+// is singular.
+bool hitboxObjectPoint(const HitboxMesh& m, f3 wp, f3& out) {
   const double* x = m.xform;
   const double a = x[0], b = x[1], c = x[2], d = x[4], e = x[5], f = x[6], g = x[8], h = x[9], i = x[10];
   const double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
@@ -744,41 +750,57 @@ bool pointInsideHitbox(const HitboxMesh& m, f3 wp) {
   const double inv[9] = {(e * i - f * h) / det, (c * h - b * i) / det, (b * f - c * e) / det,
                          (f * g - d * i) / det, (a * i - c * g) / det, (c * d - a * f) / det,
                          (d * h - e * g) / det, (b * g - a * h) / det, (a * e - b * d) / det};
-  const double q[3] = {wp.x - x[3], wp.y - x[7], wp.z - x[11]};
+  const double q[3] = {wp.x, wp.y, wp.z};
   double o[3];
   for (int r = 0; r < 3; ++r) o[r] = inv[r * 3 + 0] * q[0] + inv[r * 3 + 1] * q[1] + inv[r * 3 + 2] * q[2];
-  // Ray from just outside the object box along +x to the point; count the
-  // triangle crossings before the point.
-  const double sx = m.objMin.x - 1.0, sy = o[1], sz = o[2];
-  double dx = o[0] - sx, dy = 0.0, dz = 0.0;
-  const double dl = std::sqrt(dx * dx + dy * dy + dz * dz);
-  if (dl == 0.0) return false;
-  dx /= dl;
+  out = f3{static_cast<float>(o[0]), static_cast<float>(o[1]), static_cast<float>(o[2])};
+  return true;
+}
+
+namespace {
+// float3 algebra in the operation order of the reference's vector helpers
+// (sutil/vec_math.h: dot left to right, cross by components, normalize as
+// v * (1 / sqrt(dot(v, v)))); this file is built without contraction.
+f3 sub(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+f3 cross(f3 a, f3 b) { return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+f3 normalize(f3 v) {
+  const float inv = 1.0f / std::sqrt(dot(v, v));
+  return f3{v.x * inv, v.y * inv, v.z * inv};
+}
+}  // namespace
+
+bool pointInsideObject(const HitboxMesh& m, f3 obj, const uint32_t* items, size_t nItems) {
+  // The reference's parity cast (sutil/hitscanprocessing.cpp:20-83), in float
+  // in its operation order: a ray from x = object box min.x - 1 along +x to
+  // the point, counting the triangle crossings before the point.  No special
+  // case is added: a point at the ray start gives a NaN direction, as there.
+  const f3 start{m.objMin.x - 1.0f, obj.y, obj.z};
+  const f3 dir = normalize(sub(obj, start));
   unsigned crossings = 0;
-  for (size_t t = 0; t + 3 <= m.tris.size(); t += 3) {
+  const size_t nt = items ? nItems : m.tris.size() / 3;
+  for (size_t j = 0; j < nt; ++j) {
+    const size_t t = 3 * (items ? items[j] : j);
     const f3 p0 = m.tris[t], p1 = m.tris[t + 1], p2 = m.tris[t + 2];
-    const double e1[3] = {p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
-    const double e2[3] = {p2.x - p0.x, p2.y - p0.y, p2.z - p0.z};
-    double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-    const double nl = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    if (nl == 0.0) continue;
-    for (double& v : n) v /= nl;
-    const double den = n[0] * dx;
-    if (den == 0.0) continue;
-    const double dist = ((p0.x - sx) * n[0] + (p0.y - sy) * n[1] + (p0.z - sz) * n[2]) / den;
-    if (dist == 0.0) continue;
-    const double hit[3] = {sx + dist * dx, sy, sz};
-    if (dist < 0.0 || hit[0] > o[0]) continue;
-    auto edgeOk = [&](f3 s0, f3 s1) {
-      const double ed[3] = {s1.x - s0.x, s1.y - s0.y, s1.z - s0.z};
-      const double fe[3] = {hit[0] - s0.x, hit[1] - s0.y, hit[2] - s0.z};
-      const double cx = ed[1] * fe[2] - ed[2] * fe[1], cy = ed[2] * fe[0] - ed[0] * fe[2], cz = ed[0] * fe[1] - ed[1] * fe[0];
-      return n[0] * cx + n[1] * cy + n[2] * cz >= 0.0;
-    };
-    if (!edgeOk(p0, p1) || !edgeOk(p1, p2) || !edgeOk(p2, p0)) continue;
+    const f3 n = normalize(cross(sub(p1, p0), sub(p2, p0)));
+    const float den = dot(n, dir);
+    if (den == 0) continue;
+    const float dist = dot(sub(p0, start), n) / den;
+    if (dist == 0) continue;
+    const f3 hit{start.x + dist * dir.x, start.y + dist * dir.y, start.z + dist * dir.z};
+    if (dist < 0 || hit.x > obj.x) continue;
+    if (dot(n, cross(sub(p1, p0), sub(hit, p0))) < 0) continue;
+    if (dot(n, cross(sub(p2, p1), sub(hit, p1))) < 0) continue;
+    if (dot(n, cross(sub(p0, p2), sub(hit, p2))) < 0) continue;
     ++crossings;
   }
   return crossings % 2 == 1;
+}
+
+bool pointInsideHitbox(const HitboxMesh& m, f3 wp) {
+  f3 obj;
+  if (!hitboxObjectPoint(m, wp, obj)) return false;
+  return pointInsideObject(m, obj, nullptr, 0);
 }
 
 }  // namespace cr

@@ -1897,30 +1897,59 @@ size_t adaptivePartialFloats(uint64_t count, uint32_t spp) {
 
 namespace {
 
-// Parity ray cast of sutil/hitscanprocessing.cpp:20-83 for many points, in
-// explicitly rounded double arithmetic in the host test's operation order
-// (gltf.cpp pointInsideHitbox), so both give the same answer bit for bit.
+// Parity ray cast of sutil/hitscanprocessing.cpp:20-83 for many points, as
+// the host query (gltf.cpp pointInsideHitbox) runs it, bit for bit: the
+// object-space point from the 3x3 part of the inverse transform (the
+// reference's product has w = 0) in explicitly rounded double arithmetic,
+// rounded once to float, then the reference's float cast in its
+// operation order on explicitly rounded single-precision PTX (no FTZ, no
+// contraction, so the --use_fast_math build of this file does not change it).
 // With a (y, z) grid only the triangles of the point's cell are tested; the
 // grid lists every triangle the full loop could count there.
+__device__ __forceinline__ float xsqrt(float a) {
+  float r;
+  asm("sqrt.rn.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ float fdot(float ax, float ay, float az, float bx, float by, float bz) {
+  return xadd(xadd(xmul(ax, bx), xmul(ay, by)), xmul(az, bz));
+}
+__device__ __forceinline__ void fcross(float ax, float ay, float az, float bx, float by, float bz, float& cx, float& cy,
+                                       float& cz) {
+  cx = xsub(xmul(ay, bz), xmul(az, by));
+  cy = xsub(xmul(az, bx), xmul(ax, bz));
+  cz = xsub(xmul(ax, by), xmul(ay, bx));
+}
+__device__ __forceinline__ void fnormalize(float& x, float& y, float& z) {
+  const float inv = xdiv(1.0f, xsqrt(fdot(x, y, z, x, y, z)));
+  x = xmul(x, inv);
+  y = xmul(y, inv);
+  z = xmul(z, inv);
+}
+// dot(n, cross(s1 - s0, hit - s0)) < 0: the hit lies outside edge s0 -> s1.
+__device__ __forceinline__ bool outsideEdge(float nx, float ny, float nz, float3 s0, float3 s1, float hx, float hy,
+                                            float hz) {
+  float cx, cy, cz;
+  fcross(xsub(s1.x, s0.x), xsub(s1.y, s0.y), xsub(s1.z, s0.z), xsub(hx, s0.x), xsub(hy, s0.y), xsub(hz, s0.z), cx, cy,
+         cz);
+  return fdot(nx, ny, nz, cx, cy, cz) < 0.0f;
+}
+
 __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, InsideQuery q,
                              const float* __restrict__ pts, size_t n, uint8_t* __restrict__ out) {
   const size_t k = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const double qx = __dsub_rn(static_cast<double>(pts[3 * k]), q.t[0]);
-  const double qy = __dsub_rn(static_cast<double>(pts[3 * k + 1]), q.t[1]);
-  const double qz = __dsub_rn(static_cast<double>(pts[3 * k + 2]), q.t[2]);
-  double o[3];
+  // w = 0 in the reference's product: no translation (gltf.cpp hitboxObjectPoint)
+  const double qx = static_cast<double>(pts[3 * k]);
+  const double qy = static_cast<double>(pts[3 * k + 1]);
+  const double qz = static_cast<double>(pts[3 * k + 2]);
+  float o[3];
   for (int r = 0; r < 3; ++r)
-    o[r] = __dadd_rn(__dadd_rn(__dmul_rn(q.inv[3 * r], qx), __dmul_rn(q.inv[3 * r + 1], qy)),
-                     __dmul_rn(q.inv[3 * r + 2], qz));
-  const double sx = q.startX, sy = o[1], sz = o[2];
-  double dx = __dsub_rn(o[0], sx);
-  const double dl = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), 0.0), 0.0));
-  if (dl == 0.0) {
-    out[k] = 0;
-    return;
-  }
-  dx = __ddiv_rn(dx, dl);
+    o[r] = __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(q.inv[3 * r], qx), __dmul_rn(q.inv[3 * r + 1], qy)),
+                                       __dmul_rn(q.inv[3 * r + 2], qz)));
+  const float sx = static_cast<float>(q.startX), sy = o[1], sz = o[2];
+  float dx = xsub(o[0], sx), dy = xsub(o[1], sy), dz = xsub(o[2], sz);
+  fnormalize(dx, dy, dz);
   unsigned crossings = 0;
   // The ray runs along x at the point's (y, z): only triangles listed in the
   // grid cell of (y, z) can be crossed.
@@ -1937,34 +1966,19 @@ __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, In
   for (uint32_t j = first; j < end; ++j) {
     const uint32_t t = q.G > 0 ? q.cellItems[j] : j;
     const float3 p0 = tris[3 * t], p1 = tris[3 * t + 1], p2 = tris[3 * t + 2];
-    // vertex differences in float, as the host test's float members give them
-    const double e1[3] = {__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z)};
-    const double e2[3] = {__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z)};
-    double nv[3] = {__dsub_rn(__dmul_rn(e1[1], e2[2]), __dmul_rn(e1[2], e2[1])),
-                    __dsub_rn(__dmul_rn(e1[2], e2[0]), __dmul_rn(e1[0], e2[2])),
-                    __dsub_rn(__dmul_rn(e1[0], e2[1]), __dmul_rn(e1[1], e2[0]))};
-    const double nl =
-        __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(nv[0], nv[0]), __dmul_rn(nv[1], nv[1])), __dmul_rn(nv[2], nv[2])));
-    if (nl == 0.0) continue;
-    for (int c = 0; c < 3; ++c) nv[c] = __ddiv_rn(nv[c], nl);
-    const double den = __dmul_rn(nv[0], dx);
-    if (den == 0.0) continue;
-    const double dist = __ddiv_rn(
-        __dadd_rn(__dadd_rn(__dmul_rn(__dsub_rn(p0.x, sx), nv[0]), __dmul_rn(__dsub_rn(p0.y, sy), nv[1])),
-                  __dmul_rn(__dsub_rn(p0.z, sz), nv[2])),
-        den);
-    if (dist == 0.0) continue;
-    const double hit[3] = {__dadd_rn(sx, __dmul_rn(dist, dx)), sy, sz};
-    if (dist < 0.0 || hit[0] > o[0]) continue;
-    auto edgeOk = [&](float3 s0, float3 s1) {
-      const double ed[3] = {__fsub_rn(s1.x, s0.x), __fsub_rn(s1.y, s0.y), __fsub_rn(s1.z, s0.z)};
-      const double fe[3] = {__dsub_rn(hit[0], s0.x), __dsub_rn(hit[1], s0.y), __dsub_rn(hit[2], s0.z)};
-      const double cx = __dsub_rn(__dmul_rn(ed[1], fe[2]), __dmul_rn(ed[2], fe[1]));
-      const double cy = __dsub_rn(__dmul_rn(ed[2], fe[0]), __dmul_rn(ed[0], fe[2]));
-      const double cz = __dsub_rn(__dmul_rn(ed[0], fe[1]), __dmul_rn(ed[1], fe[0]));
-      return __dadd_rn(__dadd_rn(__dmul_rn(nv[0], cx), __dmul_rn(nv[1], cy)), __dmul_rn(nv[2], cz)) >= 0.0;
-    };
-    if (!edgeOk(p0, p1) || !edgeOk(p1, p2) || !edgeOk(p2, p0)) continue;
+    float nx, ny, nz;
+    fcross(xsub(p1.x, p0.x), xsub(p1.y, p0.y), xsub(p1.z, p0.z), xsub(p2.x, p0.x), xsub(p2.y, p0.y), xsub(p2.z, p0.z),
+           nx, ny, nz);
+    fnormalize(nx, ny, nz);
+    const float den = fdot(nx, ny, nz, dx, dy, dz);
+    if (den == 0.0f) continue;
+    const float dist = xdiv(fdot(xsub(p0.x, sx), xsub(p0.y, sy), xsub(p0.z, sz), nx, ny, nz), den);
+    if (dist == 0.0f) continue;
+    const float hx = xadd(sx, xmul(dist, dx)), hy = xadd(sy, xmul(dist, dy)), hz = xadd(sz, xmul(dist, dz));
+    if (dist < 0.0f || hx > o[0]) continue;
+    if (outsideEdge(nx, ny, nz, p0, p1, hx, hy, hz) || outsideEdge(nx, ny, nz, p1, p2, hx, hy, hz) ||
+        outsideEdge(nx, ny, nz, p2, p0, hx, hy, hz))
+      continue;
     ++crossings;
   }
   out[k] = (crossings & 1u) ? 1 : 0;
@@ -2073,6 +2087,9 @@ static __device__ __align__(256) float g_noAllocScratch[kNoAllocScratchFloats];
 
 namespace {
 constexpr int kNoAllocMaxDevices = 64;
+// Per-device address cache.  It is filled without a lock: the library's
+// entry points are not thread-safe (one host thread at a time, as the
+// reference's global singletons), and this cache relies on that contract.
 float* s_noAllocScratch[kNoAllocMaxDevices] = {};
 }  // namespace
 

@@ -131,6 +131,11 @@ std::vector<Ommatidium> parseEyeFile(const std::string& path);
 
 // Parity ray cast of sutil/hitscanprocessing.cpp:20-83 for a hitbox mesh.
 bool pointInsideHitbox(const HitboxMesh& m, f3 worldPoint);
+// The two halves of pointInsideHitbox: the object-space point (double
+// inverse, rounded once to float; false for a singular transform), and the
+// float parity cast over the listed triangles (items, or all when null).
+bool hitboxObjectPoint(const HitboxMesh& m, f3 worldPoint, f3& objectPoint);
+bool pointInsideObject(const HitboxMesh& m, f3 objectPoint, const uint32_t* items, size_t nItems);
 
 // Rotates `point` by `angle` about `axis` (normalised first), the host pose
 // arithmetic of libEyeRenderer3/cameras/DataRecordCamera.h:83-87.

@@ -334,6 +334,52 @@ def box_mesh(lo, hi):
     return v, f
 
 
+def uv_sphere(nu, nv):
+    """Unit sphere of nu latitude bands x nv longitude steps: (nu + 1) * nv
+    vertices (the poles repeated per step) and 2 * nu * nv triangles."""
+    th = np.pi * np.arange(nu + 1) / nu
+    ph = 2 * np.pi * np.arange(nv) / nv
+    v = np.stack([np.outer(np.sin(th), np.cos(ph)), np.outer(np.cos(th), np.ones(nv)),
+                  np.outer(np.sin(th), np.sin(ph))], axis=-1).reshape(-1, 3)
+    f = []
+    for i in range(nu):
+        for j in range(nv):
+            a, b = i * nv + j, i * nv + (j + 1) % nv
+            c, d = a + nv, b + nv
+            f += [[a, c, b], [b, c, d]]
+    return v, np.array(f)
+
+
+# Hitbox fixture of the point-in-mesh tests: a 9216-triangle sphere as
+# "ball" (untransformed) and as "egg" (translated, rotated, scaled).
+HITBOX_EGG = {"translation": [0.3, -0.2, 0.1], "rotation": [0.2, float(np.sin(0.5)), 0.1, float(np.cos(0.5))],
+              "scale": [1.2, 0.7, 1.6]}
+
+
+def hitbox_scene(path):
+    """Writes the hitbox fixture scene (a ground triangle, the two hitboxes,
+    a perspective camera) to `path`; returns the path."""
+    v, f = uv_sphere(48, 96)
+    g = GltfBuilder()
+    g.mesh("ground", np.array([[-5, 0, -5], [5, 0, -5], [5, 0, 5]], np.float64), np.array([[0, 2, 1]]))
+    g.mesh("ball", v, f, extras={"hitbox": True})
+    g.mesh("egg", v, f, extras={"hitbox": True}, **HITBOX_EGG)
+    g.perspective_camera("cam")
+    return g.write(path)
+
+
+def hitbox_points(seed=12, n_random=2400, n_vertex=600):
+    """Query points of the hitbox tests: uniform points around the sphere,
+    then points whose (y, z) is a vertex's (rays along x through vertices
+    and edges), the first half with both y and z from one vertex."""
+    rng = np.random.default_rng(seed)
+    vf = uv_sphere(48, 96)[0].astype(np.float32)
+    on_vertex = np.stack([rng.uniform(-1.1, 1.1, n_vertex).astype(np.float32),
+                          vf[rng.integers(0, len(vf), n_vertex), 1], vf[rng.integers(0, len(vf), n_vertex), 2]], axis=1)
+    on_vertex[:n_vertex // 2, 1:] = vf[rng.integers(0, len(vf), n_vertex // 2)][:, 1:]
+    return np.concatenate([rng.uniform(-1.4, 1.4, size=(n_random, 3)).astype(np.float32), on_vertex])
+
+
 def value_noise(nx, nz, octaves, rng):
     """Sum of `octaves` bilinearly interpolated lattice-noise layers on an
     (nx, nz) vertex grid, frequency doubling and amplitude halving per octave;

@@ -121,8 +121,12 @@ int crRenderPosesDevice(const float* d_poses, size_t count, float* d_out);
  *    so that its device state exists;
  *  - the first call on each device looks up the array's device address; make
  *    that first call before any stream capture;
- *  - every call shares the array: calls that overlap on the GPU race.
- * Results are identical to crRenderPosesDevice's.  0 on success. */
+ *  - every call shares the array: calls that overlap on the GPU race;
+ *  - it does not spread the poses of a small eye over extra warps (that
+ *    needs a buffer of pre-drawn random numbers) and ignores the near-field
+ *    cut radius (the cuts need a buffer too), so small eyes and near-field
+ *    scenes render more slowly through it.
+ * Results are bit-identical to crRenderPosesDevice's.  0 on success. */
 int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out);
 
 /* Batched rendering of several compound cameras of the scene in ONE

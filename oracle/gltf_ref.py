@@ -213,6 +213,7 @@ class RefScene:
         self.meshes = []  # (name, tri offset, tri count)
         self.cameras = []
         self.hitboxes = []
+        self.hitbox_meshes = []  # {"name", "xform" (4x4 double), "tris" (T, 9) float32 object space}
         self.miss_name = "default_background"
 
     @property
@@ -353,7 +354,20 @@ def load(path):
                 c["kind"] = "perspective"
             sc.cameras.append(c)
         elif n.get("mesh", -1) >= 0 and _extra_true(doc["meshes"][n["mesh"]].get("extras"), "hitbox"):
-            sc.hitboxes.append(doc["meshes"][n["mesh"]].get("name", ""))
+            mesh = doc["meshes"][n["mesh"]]
+            sc.hitboxes.append(mesh.get("name", ""))
+            # object-space triangles and the node transform, as the reference
+            # keeps them per hitbox (MulticamScene.cpp:329-344)
+            tris = []
+            for prim in mesh["primitives"]:
+                if prim.get("mode", 4) != 4 or "indices" not in prim:
+                    continue
+                pos, _ = accessor(prim["attributes"]["POSITION"])
+                idx, _ = accessor(prim["indices"])
+                idx = idx.reshape(-1).astype(np.int64)
+                tris.append(pos.astype(np.float32)[idx[: len(idx) // 3 * 3].reshape(-1, 3)].reshape(-1, 9))
+            sc.hitbox_meshes.append({"name": mesh.get("name", ""), "xform": np.array(xf, np.float64).reshape(4, 4),
+                                     "tris": np.concatenate(tris) if tris else np.zeros((0, 9), np.float32)})
         elif n.get("mesh", -1) >= 0:
             mesh = doc["meshes"][n["mesh"]]
             for prim in mesh["primitives"]:

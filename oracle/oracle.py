@@ -183,3 +183,59 @@ def make_color(sums):
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+# ---------------------------------------------------------------------------
+# The reference's own code where it compiles here (oracle/build_ref.py).
+# ---------------------------------------------------------------------------
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def reference_root():
+    """The reference checkout used to build oracle/_ref ($CR_REFERENCE_ROOT,
+    else the path the build recorded), or None."""
+    root = os.environ.get("CR_REFERENCE_ROOT")
+    if not root:
+        try:
+            with open(os.path.join(REF_DIR, "reference_root.txt")) as f:
+                root = f.read().strip()
+        except OSError:
+            return None
+    return root if root and os.path.isdir(root) else None
+
+
+_ref_hitscan = None
+
+
+def ref_hitscan():
+    """ctypes handle of oracle/_ref/libref_hitscan.so (the reference's
+    sutil::hitscan::isPointWithinMesh), or None when it is not built."""
+    global _ref_hitscan
+    if _ref_hitscan is None:
+        path = os.path.join(REF_DIR, "libref_hitscan.so")
+        if not os.path.exists(path):
+            return None
+        try:
+            L = ctypes.CDLL(path)
+        except OSError:  # a library built for another machine
+            return None
+        f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        u8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+        L.ref_points_in_mesh.argtypes = [f32, c_size_t, f32, f32, c_size_t, u8]
+        L.ref_points_in_mesh.restype = c_int
+        _ref_hitscan = L
+    return _ref_hitscan
+
+
+def ref_points_in_mesh(tris, xform, pts):
+    """The reference's isPointWithinMesh for every point: tris (T, 9) object
+    space, xform a 4x4 node transform (rounded to float, as the reference
+    stores it), pts (n, 3) world points.  Returns n uint8 (1 = inside)."""
+    L = ref_hitscan()
+    if L is None:
+        raise RuntimeError("oracle/_ref/libref_hitscan.so is not built (oracle/build_ref.py)")
+    pts = _f32(pts).reshape(-1, 3)
+    out = np.zeros(len(pts), np.uint8)
+    if L.ref_points_in_mesh(_f32(tris).reshape(-1), len(tris), _f32(xform).reshape(-1), pts, len(pts), out) != 0:
+        raise RuntimeError("empty hitbox mesh")
+    return out

@@ -48,4 +48,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2 and not os.environ.get("CR_REFERENCE_ROOT"):
+        sys.exit("usage: %s <reference checkout> (or set CR_REFERENCE_ROOT)" % sys.argv[0])
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ["CR_REFERENCE_ROOT"])

@@ -15,6 +15,7 @@ Bars (from the renderer's correctness contract):
   * 8-bit frame: within one step of the oracle's make_color of the same sums.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -381,7 +382,8 @@ def test_near_field_cut_changes_no_result(lib, small, tmp_path, fraction):
 
 def test_hitbox_batch_matches_point_queries(lib, tmp_path):
     """crInsideHitGeometryBatch (GPU) answers as isInsideHitGeometry does,
-    point by point, for a rotated, scaled, translated hitbox mesh."""
+    point by point, for a rotated, scaled, translated hitbox mesh (whose
+    translation the query ignores, as the reference's does)."""
     g = scenes.GltfBuilder()
     v, f = scenes.box_mesh([-1, -1, -1], [1, 1, 1])
     g.mesh("ground", np.array([[-5, 0, -5], [5, 0, -5], [5, 0, 5]], np.float64), np.array([[0, 2, 1]]))
@@ -392,7 +394,7 @@ def test_hitbox_batch_matches_point_queries(lib, tmp_path):
     lib.loadGlTFscene(g.write(str(tmp_path / "hb.gltf")).encode())
     assert eh.lastError(lib) == ""
     rng = np.random.default_rng(8)
-    pts = rng.uniform([-2, -1.5, -5], [6, 2.5, 3], size=(3000, 3)).astype(np.float32)
+    pts = rng.uniform([-3, -1.5, -3], [3, 1.5, 3], size=(3000, 3)).astype(np.float32)
     out = np.zeros(len(pts), np.uint8)
     assert lib.crInsideHitGeometryBatch(pts, len(pts), b"arena", out) == 0, eh.lastError(lib)
     want = np.array([lib.isInsideHitGeometry(float(x), float(y), float(z), b"arena") for x, y, z in pts], np.uint8)
@@ -401,44 +403,24 @@ def test_hitbox_batch_matches_point_queries(lib, tmp_path):
     assert lib.crInsideHitGeometryBatch(pts, len(pts), b"nothing", out) == -1
 
 
-def _uv_sphere(nu, nv):
-    th = np.pi * np.arange(nu + 1) / nu
-    ph = 2 * np.pi * np.arange(nv) / nv
-    v = np.stack([np.outer(np.sin(th), np.cos(ph)), np.outer(np.cos(th), np.ones(nv)),
-                  np.outer(np.sin(th), np.sin(ph))], axis=-1).reshape(-1, 3)
-    f = []
-    for i in range(nu):
-        for j in range(nv):
-            a, b = i * nv + j, i * nv + (j + 1) % nv
-            c, d = a + nv, b + nv
-            f += [[a, c, b], [b, c, d]]
-    return v, np.array(f)
-
-
 def test_hitbox_batch_grid_on_a_large_mesh(lib, tmp_path):
     """The batched query searches a (y, z) grid of the hitbox's triangles:
     same answers as the full loop of isInsideHitGeometry on a 9216-triangle
     sphere, for random points and for points whose (y, z) is a vertex's
     (rays through vertices and along edges), untransformed and transformed."""
-    v, f = _uv_sphere(48, 96)
-    g = scenes.GltfBuilder()
-    g.mesh("ground", np.array([[-5, 0, -5], [5, 0, -5], [5, 0, 5]], np.float64), np.array([[0, 2, 1]]))
-    g.mesh("ball", v, f, extras={"hitbox": True})
-    g.mesh("egg", v, f, extras={"hitbox": True}, translation=[0.3, -0.2, 0.1],
-           rotation=[0.2, np.sin(0.5), 0.1, np.cos(0.5)], scale=[1.2, 0.7, 1.6])
-    g.perspective_camera("cam")
     eh.lastError(lib)
-    lib.loadGlTFscene(g.write(str(tmp_path / "ball.gltf")).encode())
+    lib.loadGlTFscene(scenes.hitbox_scene(str(tmp_path / "ball.gltf")).encode())
     assert eh.lastError(lib) == ""
-    rng = np.random.default_rng(12)
-    vf = v.astype(np.float32)
-    on_vertex = np.stack([rng.uniform(-1.1, 1.1, 600).astype(np.float32),
-                          vf[rng.integers(0, len(vf), 600), 1], vf[rng.integers(0, len(vf), 600), 2]], axis=1)
-    on_vertex[:300, 1:] = vf[rng.integers(0, len(vf), 300)][:, 1:]
-    pts = np.concatenate([rng.uniform(-1.4, 1.4, size=(2400, 3)).astype(np.float32), on_vertex])
+    pts = scenes.hitbox_points()
     for name in (b"ball", b"egg"):
         out = np.zeros(len(pts), np.uint8)
         assert lib.crInsideHitGeometryBatch(pts, len(pts), name, out) == 0, eh.lastError(lib)
         want = np.array([lib.isInsideHitGeometry(float(x), float(y), float(z), name) for x, y, z in pts], np.uint8)
         assert np.array_equal(out, want), (name, np.flatnonzero(out != want)[:10])
         assert 300 < want.sum() < 2700
+        # and as the reference's own code (sutil/hitscanprocessing.cpp,
+        # compiled here into tests/golden/reference_hitscan.npz): the same
+        # float cast on the same object-space floats
+        ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_hitscan.npz"))
+        assert np.array_equal(ref["points"], pts)
+        assert np.array_equal(out, ref[name.decode() + "__inside"]), np.flatnonzero(out != ref[name.decode() + "__inside"])

@@ -18,10 +18,6 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-5
-ATOL = 1e-7
-
-
 def _scene(tmp_path):
     g = scenes.GltfBuilder()
     g.scene_extras = {"background-shader": "simple_sky"}
@@ -89,10 +85,13 @@ def test_no_alloc_matches_allocating_entry_point(lib, tmp_path):
     assert lib.crSynchronize() == 0, eh.lastError(lib)
     assert torch.cuda.mem_get_info()[0] == free_before
 
+    # Same draws, rays, hits and chunk sums in the same order: the bits agree,
+    # although the allocating call pre-draws the random numbers and spreads
+    # the poses over more warps while the allocation-free one does not.
     a = [o.cpu().numpy() for o in outs]
-    np.testing.assert_allclose(a[3], a[0], rtol=RTOL, atol=ATOL)
-    np.testing.assert_allclose(a[4], a[1], rtol=RTOL, atol=ATOL)
-    np.testing.assert_allclose(a[5], a[2], rtol=RTOL, atol=ATOL)
+    assert np.array_equal(a[3], a[0])
+    assert np.array_equal(a[4], a[1])
+    assert np.array_equal(a[5], a[2])
     assert not np.array_equal(a[4], a[5])  # the streams advanced between the two calls
 
 
