@@ -27,71 +27,7 @@ import scenes
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-5
-ATOL = 1e-7
-SKY_ATOL = 1e-5
-DIR_ATOL = 2e-6
-
-
-def _load(lib, path, spp):
-    eh.lastError(lib)  # drop any message a previous test left behind
-    lib.loadGlTFscene(path.encode())
-    assert eh.lastError(lib) == ""
-    eh.gotoFirstCompoundEye(lib)
-    lib.setCurrentEyeSamplesPerOmmatidium(spp)
-
-
-def _oracle(path):
-    ref = gltf_ref.load(path)
-    v, c, f = ref.arrays()
-    cams = [c for c in ref.cameras if c["kind"] == "compound"]
-    return ref, oracle.OracleScene(v, c, f, ref.miss), cams[0]["omm"]
-
-
-def _check_frame(lib, sc, omm, spp, pose12):
-    rec = eh.renderFrameRecorded(lib)
-    N = len(omm)
-    assert rec.shape == (N, spp)
-    org = rec["origin"].reshape(-1, 3)
-    dirs = rec["direction"].reshape(-1, 3)
-    tmin = np.repeat(omm[:, 7], spp)
-
-    # Ray generation from the GPU's own draws.
-    draws = np.stack([rec["normalDraw"].reshape(-1), rec["uniformDraw"].reshape(-1)], axis=1)
-    o2, d2 = oracle.gen_rays(omm, spp, pose12, draws)
-    np.testing.assert_allclose(d2, dirs, rtol=0, atol=DIR_ATOL)
-    np.testing.assert_allclose(o2, org, rtol=1e-6, atol=1e-7)
-
-    # Closest hits on identical rays: bit-exact.
-    hit, t, b1, b2 = sc.trace(org, dirs, tmin)
-    gh = rec["hitId"].reshape(-1)
-    assert np.array_equal(hit, gh), "hit ids differ on %d of %d rays" % ((hit != gh).sum(), len(gh))
-    m = hit >= 0
-    assert np.array_equal(t[m].view(np.uint32), rec["t"].reshape(-1)[m].view(np.uint32))
-    assert np.array_equal(b1[m].view(np.uint32), rec["b1"].reshape(-1)[m].view(np.uint32))
-    assert np.array_equal(b2[m].view(np.uint32), rec["b2"].reshape(-1)[m].view(np.uint32))
-
-    # Independent double-precision search: only near-edge rays may differ.
-    h64, t64, e32, e64 = sc.trace_f64(org, dirs, tmin, hit32=hit)
-    diff = hit != h64
-    near = (e32 < 1e-6) | (e64 < 1e-6)
-    assert not (diff & ~near).any(), "fp32/fp64 disagree away from edges on %d rays" % (diff & ~near).sum()
-
-    # Shading of the same hits.
-    rgb = sc.shade(dirs, hit, b1, b2)
-    miss = (hit < 0)[:, None]
-    err = np.abs(rec["rgb"].reshape(-1, 3) - rgb)
-    assert (err <= RTOL * np.abs(rgb) + np.where(miss, SKY_ATOL, ATOL)).all(), "per-ray colour max err %.3g" % err.max()
-
-    # Per-ommatidium sums.
-    got = eh.getOmmatidialColours(lib)
-    want = sc.render_rays(omm, spp, org, dirs)[0]
-    sky_frac = miss.reshape(N, spp).mean(axis=1)[:, None]
-    err = np.abs(got - want)
-    tol = RTOL * np.abs(want) + ATOL + SKY_ATOL * sky_frac
-    assert (err <= tol).all(), "per-ommatidium colour: %d channels out of tolerance, max err %.3g" % (
-        (err > tol).sum(), err.max())
-    return rec, got
+from parity_checks import ATOL, DIR_ATOL, RTOL, SKY_ATOL, _check_frame, _load, _oracle  # noqa: F401
 
 
 def test_small_scene_spp32(lib, small, small_ref):
@@ -378,6 +314,30 @@ def test_near_field_cut_changes_no_result(lib, small, tmp_path, fraction):
         assert np.array_equal(outs[0], outs[1])
         assert np.array_equal(recs[0]["hitId"], recs[1]["hitId"])
         assert np.array_equal(recs[0]["t"], recs[1]["t"])
+
+
+def test_cut_follows_same_count_ommatidia(lib, small):
+    """Replacing an eye's ommatidia with the same count of records whose
+    positions lie much farther from the pose position (0.3 m instead of
+    1 mm, beyond the cut's radius) keeps the near-field cut exact: the
+    guaranteed radius is recomputed from the new records."""
+    rng = np.random.default_rng(5)
+    poses = np.stack([scenes.pose_rows(np.array([rng.uniform(-6, 6), rng.uniform(0.2, 1.5), rng.uniform(-6, 6)]),
+                                       rng.uniform(0, 6.28)) for _ in range(8)])
+    outs = []
+    for f in (0.0, 1.0 / 64):
+        assert lib.crSetCutRadius(f) == 0
+        _load(lib, small["gltf"], 16)
+        omm = eh.getOmmatidia(lib)
+        eh.renderPoses(lib, poses)  # the eye's device state (and its cut bound) from the first records
+        wide = omm.copy()
+        wide[:, 0:3] *= 300.0  # 1 mm -> 0.3 m from the pose position
+        eh.setOmmatidiaFromPacketList(lib, [eh.c_ommatidiumPacket(*[float(x) for x in row]) for row in wide])
+        assert eh.lastError(lib) == ""
+        assert lib.getCurrentEyeOmmatidialCount() == len(omm)
+        outs.append(eh.renderPoses(lib, poses))
+    lib.crSetCutRadius(0.0)
+    assert np.array_equal(outs[0], outs[1])
 
 
 def test_hitbox_batch_matches_point_queries(lib, tmp_path):
