@@ -1995,6 +1995,47 @@ float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* 
       -1.0f);
 }
 
+int crDenoiserAdamStep(float* w, const float* g, float* m, float* v, size_t n, float lr, float c1, float c2,
+                       uint16_t* wbBits) {
+  return guarded(
+      "crDenoiserAdamStep",
+      [&]() -> int {
+        if (n == 0) return 0;
+        if (!w || !g || !m || !v || !wbBits) throw std::runtime_error("null pointer");
+        if (n > 0x7fffffffu) throw std::runtime_error("too many parameters");
+        cudaStream_t s = R().stream();
+        DevBuf<float> dw, dg, dm, dv, sched;
+        DevBuf<uint16_t> wb;
+        DevBuf<int> idx;
+        dw.ensure(n);
+        dg.ensure(n);
+        dm.ensure(n);
+        dv.ensure(n);
+        wb.ensure(n);
+        sched.ensure(3);
+        idx.ensure(1);
+        const float e[3] = {lr, c1, c2};
+        check(cudaMemcpyAsync(dw.ptr, w, n * 4, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(dg.ptr, g, n * 4, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(dm.ptr, m, n * 4, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(dv.ptr, v, n * 4, cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(sched.ptr, e, sizeof(e), cudaMemcpyHostToDevice, s), "cudaMemcpy");
+        check(cudaMemsetAsync(idx.ptr, 0, sizeof(int), s), "cudaMemset");
+        // The training loop's call: step size and bias corrections read from
+        // the device schedule at the device step index.
+        check(adamStep(dw.ptr, dg.ptr, dm.ptr, dv.ptr, static_cast<int>(n), 0.f, 0.9f, 0.999f, 1e-8f, 1, wb.ptr, s,
+                       nullptr, nullptr, sched.ptr, idx.ptr),
+              "adam");
+        check(cudaMemcpyAsync(w, dw.ptr, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(m, dm.ptr, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(v, dv.ptr, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
+        check(cudaMemcpyAsync(wbBits, wb.ptr, n * 2, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
+        check(cudaStreamSynchronize(s), "adam");
+        return 0;
+      },
+      -1);
+}
+
 int crDenoiserSave(const char* path) {
   return guarded(
       "crDenoiserSave",

@@ -259,6 +259,40 @@ __device__ __forceinline__ void putTransposed(int i, float wi, __nv_bfloat16* __
   }
 }
 
+// Explicitly rounded single-precision operations (no FTZ, no contraction),
+// so the --use_fast_math build of this file leaves Adam's arithmetic exact
+// IEEE and a CPU restatement can repeat it bit for bit.
+__device__ __forceinline__ float radd(float a, float b) {
+  float r;
+  asm("add.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float rsub(float a, float b) {
+  float r;
+  asm("sub.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float rmul(float a, float b) {
+  float r;
+  asm("mul.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float rdiv(float a, float b) {
+  float r;
+  asm("div.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_rn(float a) {
+  float r;
+  asm("sqrt.rn.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
+// Adam (Kingma & Ba 2015) with the bias corrections folded in as
+// c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t):
+//   m = b1 m + (1 - b1) g;  v = b2 v + (1 - b2) g g;
+//   w = w - lr (m c1) / (sqrt(v c2) + eps)
+// one correctly rounded float operation at a time, in this order.
 __global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                            float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2,
                            __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbT, WeightBlocks blocks,
@@ -272,11 +306,11 @@ __global__ void adamKernel(float* __restrict__ w, const float* __restrict__ g, f
     c2 = e[2];
   }
   const float gi = g[i];
-  const float mi = b1 * m[i] + (1.f - b1) * gi;
-  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  const float mi = radd(rmul(b1, m[i]), rmul(rsub(1.f, b1), gi));
+  const float vi = radd(rmul(b2, v[i]), rmul(rmul(rsub(1.f, b2), gi), gi));
   m[i] = mi;
   v[i] = vi;
-  const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  const float wi = rsub(w[i], rdiv(rmul(lr, rmul(mi, c1)), radd(rsqrt_rn(rmul(vi, c2)), eps)));
   w[i] = wi;
   if (wb) wb[i] = __float2bfloat16(wi);
   if (wbT) putTransposed(i, wi, wbT, blocks);

@@ -83,6 +83,11 @@ __device__ __forceinline__ float xdiv(float a, float b) {
   asm("div.rn.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
   return r;
 }
+__device__ __forceinline__ float xsqrt(float a) {
+  float r;
+  asm("sqrt.rn.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
 __device__ __forceinline__ float xneg(float a) { return __int_as_float(__float_as_int(a) ^ 0x80000000); }
 
 __device__ __forceinline__ float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
@@ -1730,7 +1735,9 @@ __global__ void adaptiveCombineKernel(AdaptiveBucket B, float* __restrict__ sums
 
 // Minimum-sample labels: for entries still unlabelled, the sample standard
 // deviation (n - 1) across the k renders of this sample count, per channel;
-// when every channel is below thr the entry's label becomes `spp`.
+// when every channel is below thr the entry's label becomes `spp`.  The
+// arithmetic is explicitly rounded (sums in render order, one division, one
+// square root) so that a CPU restatement gives the same labels bit for bit.
 __global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows, uint32_t spp, float thr,
                             uint16_t* __restrict__ label) {
   const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1738,14 +1745,14 @@ __global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows
   float worst = 0.f;
   for (int ch = 0; ch < 3; ++ch) {
     float m = 0.f;
-    for (int j = 0; j < k; ++j) m += outs[(static_cast<size_t>(j) * rows + e) * 3 + ch];
-    m /= static_cast<float>(k);
+    for (int j = 0; j < k; ++j) m = xadd(m, outs[(static_cast<size_t>(j) * rows + e) * 3 + ch]);
+    m = xdiv(m, static_cast<float>(k));
     float v = 0.f;
     for (int j = 0; j < k; ++j) {
-      const float d = outs[(static_cast<size_t>(j) * rows + e) * 3 + ch] - m;
-      v += d * d;
+      const float d = xsub(outs[(static_cast<size_t>(j) * rows + e) * 3 + ch], m);
+      v = xadd(v, xmul(d, d));
     }
-    worst = fmaxf(worst, sqrtf(v / static_cast<float>(k - 1)));
+    worst = fmaxf(worst, xsqrt(xdiv(v, static_cast<float>(k - 1))));
   }
   if (worst < thr) label[e] = static_cast<uint16_t>(spp);
 }
@@ -1906,11 +1913,6 @@ namespace {
 // contraction, so the --use_fast_math build of this file does not change it).
 // With a (y, z) grid only the triangles of the point's cell are tested; the
 // grid lists every triangle the full loop could count there.
-__device__ __forceinline__ float xsqrt(float a) {
-  float r;
-  asm("sqrt.rn.f32 %0, %1;" : "=f"(r) : "f"(a));
-  return r;
-}
 __device__ __forceinline__ float fdot(float ax, float ay, float az, float bx, float by, float bz) {
   return xadd(xadd(xmul(ax, bx), xmul(ay, by)), xmul(az, bz));
 }

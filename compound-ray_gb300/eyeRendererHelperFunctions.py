@@ -171,6 +171,8 @@ def configureExtras(eyeRenderer):
     L.crDenoiserRenderPoses.restype = c_int
     L.crDenoiserGradient.argtypes = [ndpointer(np.uint16, flags="C_CONTIGUOUS"), f32, f32, c_int, f32, f32]
     L.crDenoiserGradient.restype = c_float
+    L.crDenoiserAdamStep.argtypes = [f32, f32, f32, f32, c_size_t, c_float, c_float, c_float,
+                                     ndpointer(np.uint16, flags="C_CONTIGUOUS")]
     L.crDenoiserSave.argtypes = [c_char_p]
     L.crDenoiserSave.restype = c_int
     L.crDenoiserLoad.argtypes = [c_char_p]

@@ -303,6 +303,13 @@ int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long 
  * gradients and the current parameters (crDenoiserParamCount floats each). */
 float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* target, int rows, float* grads,
                          float* params);
+/* No counterpart in the reference.  Test access: one Adam step of the
+ * training loop's kernel (b1 = 0.9, b2 = 0.999, eps = 1e-8; the step size lr
+ * and bias corrections c1 = 1/(1-b1^t), c2 = 1/(1-b2^t) read from a device
+ * schedule entry, as in training) on n host parameters: updates w, m, v in
+ * place and writes the bf16 bit patterns of the new weights.  0 on success. */
+int crDenoiserAdamStep(float* w, const float* g, float* m, float* v, size_t n, float lr, float c1, float c2,
+                       uint16_t* wbBits);
 /* Checkpoint of the parameters and Adam moments (binary, with a header). */
 int crDenoiserSave(const char* path);
 int crDenoiserLoad(const char* path);

@@ -88,3 +88,20 @@ def predict(params, X, base):
     H2 = bf16(np.maximum(H1 @ W2b + b2, 0).astype(np.float32)).astype(np.float64)
     H3 = bf16(np.maximum(H2 @ W3b + b3, 0).astype(np.float32)).astype(np.float64)
     return base + (H3 @ W4b + b4)[:, :3]
+
+
+def adam_step(w, g, m, v, lr, c1, c2, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam step (Kingma & Ba 2015) in float32, one correctly rounded
+    operation at a time in the order of the GPU's adamKernel
+    (compound-ray_gb300/csrc/mlp.cu): m = b1 m + (1 - b1) g,
+    v = b2 v + ((1 - b2) g) g, w = w - (lr (m c1)) / (sqrt(v c2) + eps), with
+    c1 = 1 / (1 - b1^t) and c2 = 1 / (1 - b2^t) given.  Returns (w, m, v,
+    bf16 bit patterns of w)."""
+    f = np.float32
+    w, g, m, v = (np.asarray(a, np.float32) for a in (w, g, m, v))
+    b1, b2, eps, lr, c1, c2 = f(b1), f(b2), f(eps), f(lr), f(c1), f(c2)
+    with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+        m = (b1 * m) + ((f(1) - b1) * g)
+        v = (b2 * v) + (((f(1) - b2) * g) * g)
+        w = w - ((lr * (m * c1)) / (np.sqrt(v * c2) + eps))
+    return w.astype(np.float32), m.astype(np.float32), v.astype(np.float32), bf16_bits(w)

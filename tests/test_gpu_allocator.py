@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 import torch
 
+import allocator_ref
 import eyeRendererHelperFunctions as eh
 import gltf_ref
 import oracle
@@ -179,3 +180,29 @@ def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
     assert rs[1] < rs[0]
     assert lib.crSetAllocatorHalvings(6.5) == -1
     assert "[0, 6]" in eh.lastError(lib)
+
+
+def test_labels_match_numpy_restatement(lib, tmp_path):
+    """The GPU minimum-sample search gives, entry by entry, the labels that
+    oracle/allocator_ref.py computes from the same eight renders per sample
+    count (each render recorded separately through crAdaptiveRecord with the
+    search's seeds 0x5eed0000 + k)."""
+    info = _terrain(lib, tmp_path)
+    n = lib.getCurrentEyeOmmatidialCount()
+    rng = np.random.default_rng(13)
+    poses = scenes.random_poses(info["height_fn"], 1, rng, 20.0)
+    lib.crDenoiserRelease()
+    assert lib.crAllocatorInit(3) == 0
+    thr, seeds = 1.0 / 512.0, 8
+    got = np.zeros((1, n), np.uint16)
+    assert lib.crAllocatorAddTrainingPoses(poses, 1, 8, thr, seeds, got.ctypes.data) == 0, eh.lastError(lib)
+    renders = {}
+    for c in (4, 8, 16, 32, 64, 128, 256, 512, 1024):
+        rec = np.zeros((n * c,), eh.RAY_RECORD_DTYPE)
+        outs = np.zeros((seeds, n, 3), np.float32)
+        for k in range(seeds):
+            assert lib.crAdaptiveRecord(poses, 1, c, 0x5EED0000 + k, rec.ctypes.data, outs[k]) == 0, eh.lastError(lib)
+        renders[c] = outs
+    want = allocator_ref.min_sample_labels(renders, thr)
+    assert np.array_equal(got[0], want), np.flatnonzero(got[0] != want)[:20]
+    assert len(np.unique(want)) >= 4

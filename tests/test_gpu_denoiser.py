@@ -148,3 +148,27 @@ def test_training_beats_the_plain_low_sample_render(lib, tmp_path):
     (tmp_path / "bad.bin").write_bytes(b"nope")
     assert lib.crDenoiserLoad(str(tmp_path / "bad.bin").encode()) == -1
     assert "checkpoint" in eh.lastError(lib)
+
+
+def test_adam_step_matches_reference_bit_for_bit(lib):
+    """adamKernel, as the training loop calls it (step size and bias
+    corrections from the device schedule), against oracle/mlp_ref.adam_step:
+    the fp32 master weights, both moments and the bf16 copies, bit for bit,
+    over two consecutive steps; gradients span zeros, tiny and large values."""
+    rng = np.random.default_rng(21)
+    n = 50000
+    w = rng.normal(0, 0.1, n).astype(np.float32)
+    m = np.zeros(n, np.float32)
+    v = np.zeros(n, np.float32)
+    gw, gm, gv = w.copy(), m.copy(), v.copy()
+    for t, lr in ((1, 1e-3), (2, 7.5e-4)):
+        g = (rng.normal(0, 1, n) * 10.0 ** rng.uniform(-12, 2, n)).astype(np.float32)
+        g[rng.integers(0, n, 500)] = 0.0
+        c1 = np.float32(1.0) / (np.float32(1.0) - np.float32(0.9) ** np.float32(t))
+        c2 = np.float32(1.0) / (np.float32(1.0) - np.float32(0.999) ** np.float32(t))
+        bits = np.zeros(n, np.uint16)
+        assert lib.crDenoiserAdamStep(gw, g, gm, gv, n, lr, float(c1), float(c2), bits) == 0, eh.lastError(lib)
+        w, m, v, wb = mlp_ref.adam_step(w, g, m, v, lr, c1, c2)
+        for name, a, b in (("w", gw, w), ("m", gm, m), ("v", gv, v)):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (name, t, np.flatnonzero(a != b)[:5])
+        assert np.array_equal(bits, wb), (t, np.flatnonzero(bits != wb)[:5])

@@ -145,3 +145,51 @@ def test_render_reduction_is_sequential_sum(small, small_ref):
     for k in range(spp):
         acc = (acc + rgb[:, k] * scale).astype(np.float32)
     assert np.array_equal(out, acc)
+
+
+def test_adam_restatement_against_float64():
+    """oracle/mlp_ref.adam_step follows Adam: within float32 rounding of a
+    float64 evaluation of the same update."""
+    import mlp_ref
+
+    rng = np.random.default_rng(3)
+    w = rng.normal(0, 0.1, 1000).astype(np.float32)
+    g = rng.normal(0, 1e-3, 1000).astype(np.float32)
+    m = rng.normal(0, 1e-4, 1000).astype(np.float32)
+    v = np.abs(rng.normal(0, 1e-6, 1000)).astype(np.float32)
+    c1, c2 = 1.0 / (1 - 0.9 ** 3), 1.0 / (1 - 0.999 ** 3)
+    w2, m2, v2, bits = mlp_ref.adam_step(w, g, m, v, 1e-3, c1, c2)
+    # float64 with the float32 constants: the differences are roundings only,
+    # each a few ulp of the terms summed
+    b1, b2 = float(np.float32(0.9)), float(np.float32(0.999))
+    a1, a2 = float(np.float32(1) - np.float32(0.9)), float(np.float32(1) - np.float32(0.999))
+    m64 = b1 * m.astype(np.float64) + a1 * g
+    v64 = b2 * v.astype(np.float64) + a2 * g.astype(np.float64) ** 2
+    step = 1e-3 * (m64 * c1) / (np.sqrt(v64 * c2) + 1e-8)
+    w64 = w - step
+    ulp = 2.0 ** -23
+    assert (np.abs(m2 - m64) <= 4 * ulp * (np.abs(b1 * m) + np.abs(a1 * g))).all()
+    assert (np.abs(v2 - v64) <= 4 * ulp * (np.abs(b2 * v) + a2 * g.astype(np.float64) ** 2)).all()
+    assert (np.abs(w2 - w64) <= 4 * ulp * np.abs(w) + 1e-3 * np.abs(step)).all()
+    assert np.array_equal(bits, mlp_ref.bf16_bits(w2))
+
+
+def test_label_restatement_rules():
+    """oracle/allocator_ref: the first count whose per-channel deviation
+    across the renders is below the threshold in every channel; entries never
+    below it keep 0; a planted spread in one channel alone delays the label."""
+    import allocator_ref
+
+    rng = np.random.default_rng(4)
+    rows, k, thr = 6, 8, 1.0 / 512
+    renders = {}
+    for i, c in enumerate((4, 8, 16, 32, 64, 128, 256, 512, 1024)):
+        spread = np.array([1e-4, 0.05 / np.sqrt(c), 0.2 / np.sqrt(c), 0.5, 1e-4, 1e-4], np.float32)
+        r = (0.5 + rng.standard_normal((k, rows, 3)) * spread[None, :, None]).astype(np.float32)
+        r[:, 4, 1] = 0.5 + rng.standard_normal(k) * (0.04 / np.sqrt(c))  # one channel only
+        renders[c] = r
+    lab = allocator_ref.min_sample_labels(renders, thr)
+    assert lab[0] == 4 and lab[5] == 4
+    assert lab[3] == 0
+    assert 4 < lab[1] < lab[2] or lab[2] == 0
+    assert lab[4] > 4
