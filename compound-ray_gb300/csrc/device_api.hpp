@@ -332,6 +332,11 @@ struct InsideQuery {
   // floor((y - y0) * inv) clamped to [0, G).  G == 0: test every triangle.
   const uint32_t* cellStart = nullptr;
   const uint32_t* cellItems = nullptr;
+  // Triangles whose cast normal is not finite (zero area): their test does
+  // not depend on the point, so with a grid they are tested for every point
+  // (they are in no cell).
+  const uint32_t* everywhere = nullptr;
+  uint32_t nEverywhere = 0;
   double y0 = 0.0, z0 = 0.0, cellInv = 0.0;
   int G = 0;
 };

@@ -1031,6 +1031,7 @@ bool isInsideHitGeometry(float x, float y, float z, char* name) {
 // count for it.  About two triangles per cell, at most 256 x 256 cells.
 struct HitGrid {
   std::vector<uint32_t> start, items;
+  std::vector<uint32_t> everywhere;  // triangles tested for every point (non-finite cast normal)
   double y0 = 0.0, z0 = 0.0, inv = 0.0;
   int G = 0;
 };
@@ -1060,14 +1061,25 @@ HitGrid buildHitGrid(const HitboxMesh& m) {
     return c < 0.0 ? 0 : (c >= double(g.G) ? g.G - 1 : static_cast<int>(c));
   };
   std::vector<int> box(4 * nt);
+  std::vector<uint8_t> special(nt, 0);
+  for (size_t t = 0; t < nt; ++t)
+    if (hitboxTriangleCountsEverywhere(m, t)) {
+      special[t] = 1;
+      g.everywhere.push_back(static_cast<uint32_t>(t));
+    }
   g.start.assign(static_cast<size_t>(g.G) * g.G + 1, 0);
   for (size_t t = 0; t < nt; ++t) {
+    int* bx = &box[4 * t];
+    if (special[t]) {  // in no cell: listed apart
+      bx[0] = bx[2] = 0;
+      bx[1] = bx[3] = -1;
+      continue;
+    }
     const f3 &a = m.tris[3 * t], &b = m.tris[3 * t + 1], &c = m.tris[3 * t + 2];
     const double y0 = std::min({double(a.y), double(b.y), double(c.y)}) - eps;
     const double y1 = std::max({double(a.y), double(b.y), double(c.y)}) + eps;
     const double z0 = std::min({double(a.z), double(b.z), double(c.z)}) - eps;
     const double z1 = std::max({double(a.z), double(b.z), double(c.z)}) + eps;
-    int* bx = &box[4 * t];
     bx[0] = cellOf(y0, g.y0);
     bx[1] = cellOf(y1, g.y0);
     bx[2] = cellOf(z0, g.z0);
@@ -1123,7 +1135,7 @@ int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, un
         if (nt) check(cudaMemcpyAsync(tri.ptr, hm->tris.data(), nt * 3 * sizeof(float3), cudaMemcpyHostToDevice, st),
                       "cudaMemcpy");
         const HitGrid grid = buildHitGrid(*hm);
-        DevBuf<uint32_t> cellStart, cellItems;
+        DevBuf<uint32_t> cellStart, cellItems, everywhere;
         if (grid.G > 0) {
           cellStart.ensure(grid.start.size());
           cellItems.ensure(std::max<size_t>(1, grid.items.size()));
@@ -1134,6 +1146,14 @@ int crInsideHitGeometryBatch(const float* points, size_t n, const char* name, un
                   "cudaMemcpy");
           q.cellStart = cellStart.ptr;
           q.cellItems = cellItems.ptr;
+          if (!grid.everywhere.empty()) {
+            everywhere.ensure(grid.everywhere.size());
+            check(cudaMemcpyAsync(everywhere.ptr, grid.everywhere.data(), grid.everywhere.size() * 4,
+                                  cudaMemcpyHostToDevice, st),
+                  "cudaMemcpy");
+            q.everywhere = everywhere.ptr;
+            q.nEverywhere = static_cast<uint32_t>(grid.everywhere.size());
+          }
           q.y0 = grid.y0;
           q.z0 = grid.z0;
           q.cellInv = grid.inv;

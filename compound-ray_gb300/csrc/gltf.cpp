@@ -770,6 +770,16 @@ f3 normalize(f3 v) {
 }
 }  // namespace
 
+bool hitboxTriangleCountsEverywhere(const HitboxMesh& m, size_t t) {
+  // The cast's unit normal of triangle t, as pointInsideObject forms it: a
+  // zero-area triangle gives 0 * inf = NaN components (an overflowing one
+  // infinities), its plane and edge comparisons are all false, and it counts
+  // as a crossing for every point, as in the reference.
+  const f3 p0 = m.tris[3 * t], p1 = m.tris[3 * t + 1], p2 = m.tris[3 * t + 2];
+  const f3 n = normalize(cross(sub(p1, p0), sub(p2, p0)));
+  return !(std::isfinite(n.x) && std::isfinite(n.y) && std::isfinite(n.z));
+}
+
 bool pointInsideObject(const HitboxMesh& m, f3 obj, const uint32_t* items, size_t nItems) {
   // The reference's parity cast (sutil/hitscanprocessing.cpp:20-83), in float
   // in its operation order: a ray from x = object box min.x - 1 along +x to

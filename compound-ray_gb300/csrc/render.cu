@@ -1954,9 +1954,12 @@ __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, In
   fnormalize(dx, dy, dz);
   unsigned crossings = 0;
   // The ray runs along x at the point's (y, z): only triangles listed in the
-  // grid cell of (y, z) can be crossed.
+  // grid cell of (y, z), and those whose test does not depend on the point,
+  // can be crossed.  A point at the ray start has a NaN direction, for which
+  // every triangle's comparisons fail and every triangle counts: test them all.
+  const bool grid = q.G > 0 && isfinite(dx) && isfinite(dy) && isfinite(dz);
   uint32_t first = 0, end = nTris;
-  if (q.G > 0) {
+  if (grid) {
     auto cellOf = [&](double v, double v0) {
       const double c = floor(__dmul_rn(__dsub_rn(v, v0), q.cellInv));
       return c < 0.0 ? 0 : (c >= static_cast<double>(q.G) ? q.G - 1 : static_cast<int>(c));
@@ -1965,8 +1968,9 @@ __global__ void insideKernel(const float3* __restrict__ tris, uint32_t nTris, In
     first = q.cellStart[c];
     end = q.cellStart[c + 1];
   }
-  for (uint32_t j = first; j < end; ++j) {
-    const uint32_t t = q.G > 0 ? q.cellItems[j] : j;
+  const uint32_t nSpecial = grid ? q.nEverywhere : 0u;
+  for (uint32_t j = first; j < end + nSpecial; ++j) {
+    const uint32_t t = !grid ? j : (j < end ? q.cellItems[j] : q.everywhere[j - end]);
     const float3 p0 = tris[3 * t], p1 = tris[3 * t + 1], p2 = tris[3 * t + 2];
     float nx, ny, nz;
     fcross(xsub(p1.x, p0.x), xsub(p1.y, p0.y), xsub(p1.z, p0.z), xsub(p2.x, p0.x), xsub(p2.y, p0.y), xsub(p2.z, p0.z),

@@ -136,6 +136,11 @@ bool pointInsideHitbox(const HitboxMesh& m, f3 worldPoint);
 // float parity cast over the listed triangles (items, or all when null).
 bool hitboxObjectPoint(const HitboxMesh& m, f3 worldPoint, f3& objectPoint);
 bool pointInsideObject(const HitboxMesh& m, f3 objectPoint, const uint32_t* items, size_t nItems);
+// Whether triangle t of a hitbox has a non-finite unit normal in that cast
+// (zero area, or an overflowing cross product): such a triangle's test does
+// not depend on the point's position, so a spatial grid must test it for
+// every point.
+bool hitboxTriangleCountsEverywhere(const HitboxMesh& m, size_t t);
 
 // Rotates `point` by `angle` about `axis` (normalised first), the host pose
 // arithmetic of libEyeRenderer3/cameras/DataRecordCamera.h:83-87.
