@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--profile", action="store_true", help="small case for ncu: render --poses poses twice")
     ap.add_argument("--variant", type=int, default=2, help="render-kernel variant for --profile")
     ap.add_argument("--cut", type=float, default=1.0 / 64, help="near-field cut radius (fraction of the scene extent) for --profile")
+    ap.add_argument("--block", type=int, default=0, help="render block size for --profile (0 automatic)")
+    ap.add_argument("--spw", type=int, default=32, help="samples per warp segment for --profile")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder: 0 host SAH, 1 GPU linear BVH")
     ap.add_argument("--profile-learned", action="store_true", help="profiling case: learned render of held-out poses")
     ap.add_argument("--profile-adaptive", action="store_true", help="profiling case: adaptive learned render")
@@ -95,7 +97,7 @@ def source_sha16(path=RENDER_SRC):
         return hashlib.sha256(f.read()).hexdigest()[:16]
 
 
-def launch_counters(variant, cut_fraction, path=COUNTERS_MD):
+def launch_counters(variant, cut_fraction, layout, path=COUNTERS_MD):
     """ncu counters of one full 256-pose launch of this workload, read from
     the committed profile summary's JSON block: entries keyed by render
     variant and near-field cut fraction, each with the warp instructions
@@ -112,11 +114,12 @@ def launch_counters(variant, cut_fraction, path=COUNTERS_MD):
         return None, "no counters (%s)" % type(e).__name__
     sha = source_sha16()
     for e in entries:
-        if e["variant"] == variant and abs(e["cut_fraction"] - cut_fraction) < 1e-9:
+        if e["variant"] == variant and abs(e["cut_fraction"] - cut_fraction) < 1e-9 and \
+                [e["block_threads"], e["samples_per_warp"]] == list(layout):
             if e["render_cu_sha16"] != sha:
                 return None, "counters taken with another render.cu (%s, now %s)" % (e["render_cu_sha16"], sha)
             return e, "matched"
-    return None, "no counters for variant %d, cut %g" % (variant, cut_fraction)
+    return None, "no counters for variant %d, cut %g, layout %s" % (variant, cut_fraction, list(layout))
 
 
 def l2_copy_gbs(dev, mb=32, reps=20):
@@ -413,6 +416,12 @@ def run_ours(args):
     if lib.crAutotune(d_poses.data_ptr(), min(64, P), ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
     cut_fraction = float(lib.crGetCutRadius())  # the autotuner's radius for this workload
+    bt, spw = ctypes.c_int(0), ctypes.c_int(0)
+    lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw))
+    layout = (bt.value, spw.value)
+    tune_all = np.zeros(18, np.float32)
+    lib.crGetAutotuneTimes(tune_all, 18)
+    bvh_width = int(lib.crGetBvhWidth())
 
     # Traversal statistics for the roofline's per-ray bytes (not timed).
     nodes = ctypes_double()
@@ -491,7 +500,8 @@ def run_ours(args):
     hbm_peak, src = peaks()
     l2_peak = l2_copy_gbs(dev)
     l2_achieved = per_ray * rays_launch / launch_s / 1e9
-    counters, why = launch_counters(best.value, cut_fraction) if launch_n == POSES_PER_LAUNCH else (None, "partial launch")
+    counters, why = launch_counters(best.value, cut_fraction, layout) if launch_n == POSES_PER_LAUNCH \
+        else (None, "partial launch")
     issue_peak = 4.0 * SM_COUNT * sm_max_mhz() * 1e6 / 1e12  # T warp instructions/s
     if counters:
         instr_per_ray = counters["warp_instructions"] / counters["rays"]
@@ -508,8 +518,14 @@ def run_ours(args):
         "eye_frames_per_s": value / (N * spp),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": int(poses12.nbytes),
                 "d2h_bytes_per_step": int(P * N * 3 * 4), "api": "crRenderPoses (host pinned poses in, colours out)"},
-        "autotune": {"variant": best.value, "ms_64_poses": [round(float(x), 3) for x in tune_ms],
-                     "near_field_cut_fraction": cut_fraction},
+        "autotune": {"variant": best.value, "block_threads": layout[0], "samples_per_warp": layout[1],
+                     "near_field_cut_fraction": cut_fraction,
+                     "ms_64_poses": {"variants": [round(float(x), 3) for x in tune_all[0:3]],
+                                     "block_128_256_512": [round(float(x), 3) for x in tune_all[3:6]],
+                                     "samples_per_warp_8_16_32": [round(float(x), 3) for x in tune_all[6:9]],
+                                     "cut_0_256_128_64_32_16": [round(float(x), 3) for x in tune_all[9:15]],
+                                     "bvh_width_2_4_8": [round(float(x), 3) for x in tune_all[15:18]]},
+                     "bvh_width": bvh_width},
         # per 256-pose launch: the poses' near-field cuts (when a radius is
         # set) and the render kernel
         "gpu_launches": args.steps * len(chunks) * (RENDER_KERNELS_PER_LAUNCH + (1 if cut_fraction > 0 else 0)),
@@ -680,11 +696,15 @@ def run_batch(lib, eh, args, stream):
     big = int(np.argmax([n * s for n, s in zip(info["n"], info["spp"])]))
     lib.gotoCamera(int(cams[big]))
     prev_cut, prev_variant = float(lib.crGetCutRadius()), int(lib.crGetRenderVariant())
+    _bt, _spw = ctypes.c_int(0), ctypes.c_int(0)
+    lib.crGetRenderLayout(ctypes.byref(_bt), ctypes.byref(_spw))
+    prev_layout, prev_width = (_bt.value, _spw.value), int(lib.crGetBvhWidth())
     tune_ms = np.zeros(lib.crGetRenderVariantCount(), np.float32)
     best = ctypes.c_int(0)
     if lib.crAutotune(d_poses[big * P].data_ptr(), P, ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
     cut = float(lib.crGetCutRadius())
+    tuned = autotune_record(lib)
 
     def timed_batch(cut_fraction):
         lib.crSetCutRadius(cut_fraction)
@@ -715,12 +735,13 @@ def run_batch(lib, eh, args, stream):
     ms, lat = timed_batch(cut)
     lib.crSetCutRadius(prev_cut)  # the later sections keep the main workload's settings
     lib.crSetRenderVariant(prev_variant)
+    lib.crSetRenderLayout(*prev_layout)
+    lib.crSetBvhWidth(prev_width)
     rays = int(sum(n * s for n, s in zip(info["n"], info["spp"])) * P)
     return {"eyes": n_eyes, "poses_per_eye": P, "rays_per_launch": rays, "launch_ms": ms,
             "rays_per_s": rays / (ms / 1000.0),
             "eye_latency_ms_p50": float(np.percentile(lat, 50)), "eye_latency_ms_p99": float(np.percentile(lat, 99)),
-            "autotune": {"variant": int(best.value), "near_field_cut_fraction": cut,
-                         "launch_ms_without_cut": ms_nocut},
+            "autotune": dict(tuned, launch_ms_without_cut=ms_nocut),
             "graph": "near-field cuts + one persistent work-queue kernel (+ chunk sums) replayed from a CUDA graph"}
 
 
@@ -740,15 +761,18 @@ def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_pose
     import scenes
 
     rng = np.random.default_rng(scenes.SEED + 11)
+    val_poses = 200
     if scene == "terrain":
         info = workload(1024)
         train = scenes.random_poses(info["height_fn"], train_poses, rng, 60.0)
         held = scenes.random_poses(info["height_fn"], held_poses, rng, 60.0)
+        val = scenes.random_poses(info["height_fn"], val_poses, rng, 60.0)
         label = "terrain (%d tris), %%d-ommatidium droplet eye" % info["triangles"]
     else:
         info = scenes.small_scene(os.path.join(tempfile.gettempdir(), "cr_bench_small_%d" % scenes.SEED))
         train = scenes.open_poses(info["boxes"], train_poses, rng)
         held = scenes.open_poses(info["boxes"], held_poses, rng)
+        val = scenes.open_poses(info["boxes"], val_poses, rng)
         label = "ground + 64 boxes (770 tris, simple_sky), %d-ommatidium Fibonacci-sphere eye, acceptance 3 deg"
     lib.crSetStream(stream.cuda_stream)
     lib.loadGlTFscene(info["gltf"].encode())
@@ -761,15 +785,62 @@ def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_pose
     if lib.crDenoiserInit(1) != 0 or lib.crDenoiserAddTrainingPoses(train, len(train), 8, 1024) != 0:
         raise RuntimeError(eh.lastError(lib))
     t_data = time.perf_counter() - t0
-    loss = np.zeros(steps, np.float32)
-    t0 = time.perf_counter()
-    if lib.crDenoiserTrain(steps, batch, 1e-3, 3, loss.ctypes.data) != 0:
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    # Model selection on validation poses (neither trained on nor evaluated):
+    # the number of training steps from one initialisation, then the strength
+    # alpha of the correction (its output layer scaled; 0 is the 8-sample
+    # mean), both by the worst channel's RMSE against the poses' 1024-sample
+    # render.  Training on a small set for too long over-fits; the strength
+    # keeps a network that does not generalise from making the render worse.
+    def to16(p12):
+        q = np.zeros((len(p12), 16), np.float32)
+        for k in range(4):
+            q[:, 4 * k:4 * k + 3] = p12[:, 3 * k:3 * k + 3]
+        return torch.from_numpy(q).to(dev)
+
+    d_val = to16(val)
+    d_vout = torch.empty((val_poses, N, 3), dtype=torch.float32, device=dev)
+    lib.setCurrentEyeSamplesPerOmmatidium(1024)
+    if lib.crRenderPosesDevice(d_val.data_ptr(), val_poses, d_vout.data_ptr()) != 0:
         raise RuntimeError(eh.lastError(lib))
-    t_train = time.perf_counter() - t0
+    val_ref = d_vout.cpu().numpy()
+    lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])
+
+    def val_rmse():
+        if lib.crDenoiserRenderPosesDevice(d_val.data_ptr(), val_poses, 8, d_vout.data_ptr()) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        return max(rmse_per_channel(d_vout.cpu().numpy(), val_ref))
+
+    tmpd = tempfile.mkdtemp()
+    ck = lambda name: os.path.join(tmpd, name).encode()
+    if lib.crDenoiserSave(ck("init.bin")) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    by_steps, t_train = {}, 0.0
+    for st in sorted({250, 500, 1000, 2000, 4000, steps}):
+        if lib.crDenoiserLoad(ck("init.bin")) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        loss = np.zeros(st, np.float32)
+        t0 = time.perf_counter()
+        if lib.crDenoiserTrain(st, batch, 1e-3, 3, loss.ctypes.data) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        t_train += time.perf_counter() - t0
+        by_steps[st] = (val_rmse(), float(loss[-min(100, st):].mean()))
+        if lib.crDenoiserSave(ck("steps%d.bin" % st)) != 0:
+            raise RuntimeError(eh.lastError(lib))
+    best_steps = min(by_steps, key=lambda k: by_steps[k][0])
+    by_alpha = {}
+    for a in (1.0, 0.75, 0.5, 0.25, 0.0):
+        if lib.crDenoiserLoad(ck("steps%d.bin" % best_steps)) != 0 or lib.crDenoiserScaleOutput(a) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        by_alpha[a] = val_rmse()
+    best_alpha = min(by_alpha, key=by_alpha.get)
+    if lib.crDenoiserLoad(ck("steps%d.bin" % best_steps)) != 0 or lib.crDenoiserScaleOutput(best_alpha) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    loss = np.array([by_steps[best_steps][1]], np.float32)
     p16 = np.zeros((held_poses, 16), np.float32)
     for k in range(4):
         p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
-    dev = torch.device("cuda", torch.cuda.current_device())
     d_poses = torch.from_numpy(p16).to(dev)
     d_out = torch.empty((held_poses, N, 3), dtype=torch.float32, device=dev)
 
@@ -820,7 +891,10 @@ def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_pose
     fps_learned = held_poses / (ms_learned / 1000.0)
     return {"scene": label % N,
             "train_poses": train_poses, "train_ommatidium_frames": train_poses * N,
-            "held_out_poses": held_poses, "steps": steps, "batch": batch, "final_loss": float(loss[-100:].mean()),
+            "held_out_poses": held_poses, "validation_poses": val_poses, "batch": batch,
+            "steps": best_steps, "final_loss": float(loss[-1]),
+            "validation_rmse_by_steps": {str(k): round(v[0], 7) for k, v in by_steps.items()},
+            "alpha": best_alpha, "validation_rmse_by_alpha": {str(k): round(v, 7) for k, v in by_alpha.items()},
             "data_s": t_data, "train_s": t_train, "rmse_learned_8spp": r_learned, "rmse_plain_8spp": sweep[8][0],
             "rmse_per_channel_learned_8spp": rmse_per_channel(learned_img, ref),
             "rmse_note": "RMSE against the plain 1024-sample render, worst of the R, G, B channels",
@@ -944,6 +1018,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     if lib.crAutotune(d_poses.data_ptr(), 4, ctypes.byref(best), tune_ms) != 0:
         raise RuntimeError(eh.lastError(lib))
     cut = float(lib.crGetCutRadius())
+    tuned = autotune_record(lib)
     # Error budget: the largest number of halvings of the predicted counts
     # (0, 0.5, .., 4) whose adaptive render of validation poses (neither
     # trained on nor evaluated) stays within 90% of 1/255 RMSE against their
@@ -971,6 +1046,23 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
             break
         halvings = float(h)
     if lib.crSetAllocatorHalvings(halvings) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    # Ray-refill schedule of the adaptive kernel (results do not depend on
+    # it): timed on the validation poses, fastest kept.  refill at 32 idle
+    # lanes = whole rounds of 32 rays, no refill.
+    sched_ms = {}
+
+    def val_render():
+        if lib.crAdaptiveRenderPosesDevice(d_vposes.data_ptr(), val_poses, 8, d_vout.data_ptr(), None, None) != 0:
+            raise RuntimeError(eh.lastError(lib))
+
+    for idle in (8, 16, 24, 32):
+        for steps in (8, 16, 32):
+            if lib.crSetAdaptiveSchedule(idle, steps) != 0:
+                raise RuntimeError(eh.lastError(lib))
+            sched_ms["%d/%d" % (idle, steps)] = timed(val_render)
+    best_sched = min(sched_ms, key=sched_ms.get)
+    if lib.crSetAdaptiveSchedule(*[int(x) for x in best_sched.split("/")]) != 0:
         raise RuntimeError(eh.lastError(lib))
     del d_vref, d_vout
     if profile:
@@ -1015,11 +1107,12 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     ms_plain_e2e = timed(plain_e2e)
     lib.crSetBvhBuilder(0)
     lib.crSetAllocatorHalvings(0)
+    lib.crSetBvhWidth(2)  # later sections start from the two-wide BVH
     rays_plain = float(held_poses) * N * 1024
     lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
     return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
-            "autotune": {"variant": best.value, "near_field_cut_fraction": cut},
+            "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms),
             "label_histogram": lab_hist, "halvings": halvings, "validation_poses": val_poses,
             "validation_rmse_by_halvings": val_rmse, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
             "train_s": t_train, "rmse_vs_plain_1024": rmse, "rmse_per_channel": rmse_ch,
@@ -1047,6 +1140,22 @@ def rmse_per_channel(a, ref):
 
 
 TIMING_REPS = 3  # every learned-form and plain timing: best of this many, after one untimed run
+
+
+def autotune_record(lib):
+    """The autotuner's picks and timings (ms) for the current eye: variant,
+    block size, samples per warp, near-field cut, BVH width."""
+    import ctypes
+
+    t = np.zeros(18, np.float32)
+    lib.crGetAutotuneTimes(t, 18)
+    bt, spw = ctypes.c_int(0), ctypes.c_int(0)
+    lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw))
+    r = lambda a: [round(float(x), 3) for x in a]
+    return {"variant": int(lib.crGetRenderVariant()), "block_threads": bt.value, "samples_per_warp": spw.value,
+            "near_field_cut_fraction": float(lib.crGetCutRadius()), "bvh_width": int(lib.crGetBvhWidth()),
+            "ms": {"variants": r(t[0:3]), "block_128_256_512": r(t[3:6]), "samples_per_warp_8_16_32": r(t[6:9]),
+                   "cut_0_256_128_64_32_16": r(t[9:15]), "bvh_width_2_4_8": r(t[15:18])}}
 
 
 def ctypes_double():
@@ -1146,13 +1255,16 @@ def run_profile(args):
     lib.loadGlTFscene(info["gltf"].encode())
     eh.gotoFirstCompoundEye(lib)
     lib.setCurrentEyeSamplesPerOmmatidium(info["spp"])
-    if lib.crSetRenderVariant(args.variant) != 0 or lib.crSetCutRadius(args.cut) != 0:
+    if lib.crSetRenderVariant(args.variant) != 0 or lib.crSetCutRadius(args.cut) != 0 or \
+            lib.crSetRenderLayout(args.block, args.spw) != 0:
         raise RuntimeError(eh.lastError(lib))
     P = min(args.poses, POSES_PER_LAUNCH)
     poses = info["poses"][:P]
     for _ in range(2):
         out = eh.renderPoses(lib, poses)
-    print(json.dumps({"profile_case": "first %d poses of the terrain trajectory" % P, "checksum": float(out.sum())}))
+    print(json.dumps({"profile_case": "first %d poses of the terrain trajectory" % P, "checksum": float(out.sum()),
+                      "variant": args.variant, "cut": args.cut, "block": args.block, "spw": args.spw,
+                      "render_cu_sha16": source_sha16()}))
 
 
 def main():

@@ -21,7 +21,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["render.cu", "lbvh.cu", "mlp.cu", "mlp_tc.cu"]
-CPP_SOURCES = ["gltf.cpp", "png.cpp", "bvh.cpp", "denoiser.cpp", "eye_renderer.cpp"]
+CPP_SOURCES = ["gltf.cpp", "png.cpp", "bvh.cpp", "wbvh.cpp", "denoiser.cpp", "eye_renderer.cpp"]
 
 
 def _run(cmd):

@@ -346,6 +346,19 @@ float Denoiser::gradient(const void* X, const float* base, const float* target, 
   return l;
 }
 
+void Denoiser::scaleOutput(float alpha, cudaStream_t s) {
+  if (!ready()) throw std::runtime_error("denoiser not initialised");
+  const size_t n = kParams - offW4;  // W4 and b4
+  std::vector<float> h(n);
+  ck(cudaMemcpyAsync(h.data(), params_ + offW4, n * 4, cudaMemcpyDeviceToHost, s), "scale");
+  ck(cudaStreamSynchronize(s), "scale");
+  for (float& v : h) v *= alpha;
+  ck(cudaMemcpyAsync(params_ + offW4, h.data(), n * 4, cudaMemcpyHostToDevice, s), "scale");
+  ck(toBf16(params_, wbf_, kParams, s), "bf16 copy");
+  ck(transposeWeightsBf16(params_, kParams, wbfT_, weightBlocks(), s), "bf16 transposes");
+  ck(cudaStreamSynchronize(s), "scale");
+}
+
 // Checkpoint: magic, version, parameter count, Adam step, then the fp32
 // parameters and the two Adam moment vectors.
 void Denoiser::save(const std::string& path, cudaStream_t s) {

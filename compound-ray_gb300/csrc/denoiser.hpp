@@ -65,6 +65,11 @@ class Denoiser {
   float gradient(const void* X, const float* base, const float* target, int rows, float* gradsHost, float* paramsHost,
                  cudaStream_t s, bool tc = false);
 
+  // Scales the output layer (W4, b4) by alpha: the network's correction
+  // becomes alpha times what it was (the layer is linear); alpha 0 leaves the
+  // 8-sample mean.  Refreshes the bf16 copies.
+  void scaleOutput(float alpha, cudaStream_t s);
+
   void save(const std::string& path, cudaStream_t s);
   void load(const std::string& path, cudaStream_t s);
 

@@ -16,6 +16,12 @@ struct DevScene {
   const float4* nodes = nullptr;
   const float4* tris = nullptr;
   const float4* shade = nullptr;
+  // width 2: closest hits are searched in the two-wide BVH (nodes); 4 or 8:
+  // in the wide BVH of that width with quantised child boxes (wnodes,
+  // wbvh.hpp layout), over the same triangles.  The closest hit, and so every
+  // result, is the same in both.
+  const float4* wnodes = nullptr;
+  int width = 2;
   uint32_t triCount = 0;
   int miss = 0;         // 0 = default_background, 1 = simple_sky
   float extent = 0.f;   // largest |coordinate| of any triangle vertex
@@ -70,6 +76,8 @@ struct DevEye {
   float cutRadius = 0.f;
   float maxRel = 0.f;
 };
+// Traversal stack entries of the wide BVH (a node pushes up to W - 1).
+constexpr int kWideStackEntries = 128;
 constexpr int kCutEntries = 8;
 constexpr int kCutStride = 1 + 2 * kCutEntries;
 
@@ -103,20 +111,45 @@ constexpr uint32_t kRngPlanes = 8;
 struct WarpPlan {
   uint32_t segWidth;     // lanes per ommatidium segment (power of two <= 32)
   uint32_t ommPerWarp;   // 32 / segWidth
-  uint32_t chunks;       // warp segments per ommatidium (spp > 32)
+  uint32_t chunks;       // warp segments per ommatidium (spp > segWidth)
   uint64_t tasks;        // warp tasks per pose batch
   uint32_t poseSplits = 1;     // pose ranges the batch is cut into (pre-drawn launches)
   uint32_t posesPerSplit = 0;  // poses per range (0: all)
+  uint32_t blockWarps = 4;     // warps per block of the launch
+  // inBlock: every block holds all `chunks` warps of groupsPerBlock ommatidium
+  // groups and sums the chunk partials in shared memory (no scratch, no
+  // second launch); tasks are then padded to whole blocks.
+  uint32_t inBlock = 0;
+  uint32_t groupsPerBlock = 1;
 };
+// The default plan: 32-sample segments (whole ommatidia when spp < 32).
 WarpPlan planWarps(uint32_t N, uint32_t spp);
+// Layout of the plain render kernel, process-wide (the autotuner sets it):
+// block size in threads (0 = the smallest of 128, 256, 512 that holds all
+// chunk warps of an ommatidium, else 128) and samples per warp segment
+// (0 = 32, or 8 / 16: segments of 8 or 16 samples, several ommatidia per
+// warp; a smaller segment changes the order in which samples are summed,
+// so results change within float rounding).  Results never depend on the
+// block size.
+void setRenderLayout(uint32_t blockThreads, uint32_t samplesPerWarp);
+void renderLayout(uint32_t* blockThreads, uint32_t* samplesPerWarp);
+// Plan of one eye in a batched launch under that layout: its segment width,
+// chunk partials in scratch (P x N x chunks x 3 floats when chunks > 1).
+WarpPlan planBatch(uint32_t N, uint32_t spp);
+// Block size of the batched launch (the layout's, 128 by default).
+uint32_t batchBlockThreads();
 
 // Bytes of DevEye::draws worth providing for a P-pose launch of an
 // N-ommatidium, spp-sample eye: non-zero only when the eye alone has too few
 // samples to fill the GPU, so that its poses are better spread over warps.
 size_t renderDrawBytes(uint32_t N, uint32_t spp, uint32_t P);
 
-// Floats of scratch needed by launchRender for P poses (0 when spp <= 32).
-size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P);
+// Floats of scratch needed by launchRender for P poses of the scene (0 when
+// spp <= 32 or when the chunk partials are summed inside the blocks), for a
+// recording (rec) or counting (stats) launch or neither; forceScratch: the
+// scratch plan (chunk partials in global memory, summed by a second kernel).
+size_t renderScratchFloats(const DevScene& scene, uint32_t N, uint32_t spp, uint32_t P, bool rec = false,
+                           bool stats = false, bool forceScratch = false);
 
 cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t stream);
 
@@ -127,7 +160,7 @@ cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t str
 // generator states advance by one frame per pose and are written back.
 cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* out,
                          float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
-                         unsigned long long* stats = nullptr);
+                         unsigned long long* stats = nullptr, bool forceScratch = false);
 
 // Per-ommatidium sample statistics of a feature render (spp <= 32), each the
 // mean over the samples: colour (3), squared colour (3), hit flag, hit
@@ -299,16 +332,28 @@ struct AdaptiveBucket {
   uint32_t spp = 0;
   float* partials = nullptr;  // adaptivePartialFloats(count, spp) floats when spp > 32
   uint64_t taskBase = 0;      // first warp task of the bucket
+  uint64_t tasks = 0;         // warp tasks of the bucket
+  uint64_t poolBase = 0;      // first warp pool of the bucket (a pool: up to 8 rounds of 32 samples)
 };
 struct AdaptiveLaunch {
   AdaptiveBucket b[kAdaptiveBuckets];
   uint32_t nBuckets = 0;
   uint64_t totalTasks = 0;
+  uint64_t totalPools = 0;
+  // Ray refill: a warp hands its idle lanes new samples once at least
+  // refillIdle of its 32 lanes are idle, checking every `steps` BVH steps.
+  uint32_t refillIdle = 16;
+  int steps = 16;
 };
 // Table of the non-empty buckets among nBuckets (entries, counts, spp and
 // partial buffers per bucket) with their warp-task offsets.
 AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* counts, const uint32_t* spp,
                             float* const* partials, uint32_t nBuckets);
+// The process-wide ray-refill schedule of the adaptive kernel (planAdaptive
+// copies it into every launch): refill at >= refillIdle idle lanes (1..32),
+// check every `steps` BVH steps (1..4096).  Results do not depend on it.
+void setAdaptiveSchedule(uint32_t refillIdle, int steps);
+void adaptiveSchedule(uint32_t* refillIdle, int* steps);
 size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
 // One launch over every bucket: sums[3e..3e+2] = mean sample colour of entry
 // e, samples drawn from the Philox4x32-10 stream (seed, e * 1024 + s).  rec:

@@ -25,6 +25,7 @@
 
 #include "../../include/libEyeRenderer.h"
 #include "bvh.hpp"
+#include "wbvh.hpp"
 #include "device_api.hpp"
 #include "denoiser.hpp"
 #include "scene.hpp"
@@ -166,6 +167,7 @@ void buildSphereGrids(EyeDev& e, const std::vector<Ommatidium>& omm, cudaStream_
 }
 
 constexpr uint32_t kMaxPosesPerLaunch = 256;
+constexpr size_t kTuneSlots = 18;
 
 // Order in which warp segments take an eye's ommatidia: by the 30-bit Morton
 // code of the unit axis direction mapped into the cube [0, 1)^3 (ties by
@@ -224,6 +226,11 @@ struct Renderer {
   int builder = 0;  // 0 = host binned SAH, 1 = GPU linear BVH (crSetBvhBuilder)
   BvhBuildStats bvhStats;
   DevBuf<float4> nodes, tris, shade;
+  int bvhWidth = 2;   // crSetBvhWidth: 2 (the BVH2), 4 or 8 (wide BVH with quantised boxes)
+  int wideBuilt = 0;  // width of the wide BVH in wnodes (0: none)
+  uint32_t nodeSlots = 0;  // BVH2 nodes in the uploaded node array
+  DevBuf<float4> wnodes;
+  WideBvhStats wideStats;
   DevBuf<uint32_t> texels;
   DevBuf<int4> texTable;
   DevBuf<float4> light;  // lighting-on data, uploaded when lighting is first used
@@ -239,6 +246,9 @@ struct Renderer {
   DevBuf<float2> draws;  // pre-drawn random numbers of small-eye launches
   DevBuf<float4> cuts;   // per-pose near-field cuts
   float cutFactor = 0.f; // cut radius as a fraction of the scene extent (0: off)
+  // Timings of the last crAutotune (ms): variants 0-2, block 128/256/512,
+  // samples per warp 8/16/32, cut radius 0, 1/256 .. 1/16 of the extent.
+  std::vector<float> tuneTimes;
   bool projectionGrid = true;  // spherical projections search candidate grids (false: every candidate)
   DevBuf<float> batchOut;
   DevBuf<uint32_t> err;
@@ -262,6 +272,9 @@ struct Renderer {
     nodes.release();
     tris.release();
     shade.release();
+    wnodes.release();
+    wideBuilt = 0;
+    nodeSlots = 0;
     texels.release();
     texTable.release();
     light.release();
@@ -293,6 +306,7 @@ struct Renderer {
     f.ensure(T);
     temp.ensure(lbvhTempBytes(T));
     nodes.ensure(4 * static_cast<size_t>(T - 1));
+    nodeSlots = T - 1;
     tris.ensure(3 * static_cast<size_t>(T));
     shade.ensure(3 * static_cast<size_t>(T));
     cudaStream_t st = stream();
@@ -323,6 +337,41 @@ struct Renderer {
   }
 
   void ensureUploaded() {
+    ensureBase();
+    ensureWide();
+  }
+
+  // The wide BVH of the selected width (crSetBvhWidth), collapsed on the host
+  // from the two-wide BVH on the device when first needed.
+  void ensureWide() {
+    const uint32_t T = dev.triCount;
+    if (bvhWidth == 2 || T == 0 || nodeSlots == 0) {
+      dev.width = 2;
+      dev.wnodes = nullptr;
+      return;
+    }
+    if (wideBuilt != bvhWidth) {
+      const uint32_t inner = nodeSlots;  // the node array (the GPU builder leaves unused slots in it)
+      std::vector<float> hn(16 * static_cast<size_t>(inner)), ht(12 * static_cast<size_t>(T));
+      cudaStream_t st = stream();
+      check(cudaMemcpyAsync(hn.data(), nodes.ptr, hn.size() * 4, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+      check(cudaMemcpyAsync(ht.data(), tris.ptr, ht.size() * 4, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+      check(cudaStreamSynchronize(st), "BVH readback");
+      std::vector<float> w;
+      collapseWideBvh(hn.data(), inner, ht.data(), T, bvhWidth, w, wideStats);
+      if (static_cast<int>(wideStats.maxDepth + 1) * (bvhWidth - 1) + 1 > kWideStackEntries)
+        throw std::runtime_error("wide BVH deeper than its traversal stack");
+      wnodes.release();
+      wnodes.ensure(w.size() / 4);
+      check(cudaMemcpyAsync(wnodes.ptr, w.data(), w.size() * 4, cudaMemcpyHostToDevice, st), "cudaMemcpy");
+      check(cudaStreamSynchronize(st), "wide BVH upload");
+      wideBuilt = bvhWidth;
+    }
+    dev.width = bvhWidth;
+    dev.wnodes = wnodes.ptr;
+  }
+
+  void ensureBase() {
     if (pendingGpuBuild) {
       buildOnDevice();
       pendingGpuBuild = false;
@@ -333,6 +382,7 @@ struct Renderer {
     if (!pendingBvh) return;
     const HostBvh& b = *pendingBvh;
     const size_t nn = b.nodes.size() / 4, nt = b.tris.size() / 4;
+    nodeSlots = static_cast<uint32_t>(nn / 4);
     nodes.ensure(std::max<size_t>(1, nn));
     tris.ensure(std::max<size_t>(1, nt));
     shade.ensure(std::max<size_t>(1, nt));
@@ -520,7 +570,7 @@ struct Renderer {
     ensureRng(e);
     for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
       const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
-      const size_t need = renderScratchFloats(e.N, e.spp, P);
+      const size_t need = renderScratchFloats(dev, e.N, e.spp, P, rec != nullptr, stats != nullptr);
       if (need) scratch.ensure(need);
       DevEye de = devEye(e);
       withDraws(de, P, !rec && !stats);
@@ -1314,7 +1364,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
         size_t outOff = 0, scratchFloats = 0;
         // The near-field cut radius in force now is recorded into the graph.
         r.ensureUploaded();
-        const bool useCuts = r.cutFactor > 0.f && r.dev.extent > 0.f &&
+        const bool useCuts = r.cutFactor > 0.f && r.dev.extent > 0.f && r.dev.width == 2 &&
                              r.bvhStats.maxDepth + kCutEntries + 2 <= 64;
         if (useCuts) {
           b.cuts.ensure(nCams * posesPerCam * kCutStride);
@@ -1333,7 +1383,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
           be.eye = r.devEye(e);
           be.poses = reinterpret_cast<const float4*>(d_poses) + 4 * posesPerCam * i;
           be.out = d_out + outOff;
-          be.plan = planWarps(e.N, e.spp);
+          be.plan = planBatch(e.N, e.spp);
           be.P = static_cast<uint32_t>(posesPerCam);
           be.scratch = nullptr;
           if (useCuts) {
@@ -1347,7 +1397,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
           outOff += 3 * posesPerCam * e.N;
           b.totalTasks += e.N ? be.plan.tasks * 1ull : 0ull;
           if (be.plan.chunks > 1 && e.N) {
-            scratchFloats += renderScratchFloats(e.N, e.spp, static_cast<uint32_t>(posesPerCam));
+            scratchFloats += posesPerCam * e.N * be.plan.chunks * 3;
             b.totalCells += static_cast<unsigned long long>(posesPerCam) * e.N;
           }
         }
@@ -1356,7 +1406,7 @@ int crBatchCreate(const int* cams, size_t nCams, size_t posesPerCam, const float
         for (size_t i = 0; i < nCams; ++i)
           if (table[i].plan.chunks > 1 && table[i].eye.N) {
             table[i].scratch = b.scratch.ptr + so;
-            so += renderScratchFloats(table[i].eye.N, table[i].eye.spp, static_cast<uint32_t>(posesPerCam));
+            so += posesPerCam * table[i].eye.N * table[i].plan.chunks * 3;
           }
         b.table.ensure(nCams);
         b.taskBase.ensure(nCams);
@@ -1487,7 +1537,7 @@ int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out)
         const Camera& c = r.scene.cameras[r.current];
         const uint32_t N = static_cast<uint32_t>(c.omm.size());
         const uint32_t spp = static_cast<uint32_t>(std::max(1, c.spp));
-        const size_t perPose = renderScratchFloats(N, spp, 1);
+        const size_t perPose = renderScratchFloats(r.dev, N, spp, 1, false, false, true);  // chunk partials in scratch
         const size_t cap = noAllocScratchFloats();
         if (perPose > cap)
           throw std::runtime_error("an eye of " + std::to_string(N) + " ommatidia x " + std::to_string(spp) +
@@ -1507,7 +1557,7 @@ int crRenderPosesDeviceNoAlloc(const float* d_poses, size_t count, float* d_out)
         for (size_t first = 0; first < count; first += batch) {
           const uint32_t P = static_cast<uint32_t>(std::min(batch, count - first));
           check(launchRender(r.dev, r.devEye(e), poses + 4 * first, P, d_out + 3 * first * N, perPose ? scratch : nullptr,
-                             r.err.ptr, nullptr, r.stream()),
+                             r.err.ptr, nullptr, r.stream(), nullptr, true),
                 "render launch");
         }
         return 0;
@@ -1539,6 +1589,8 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
         const int prev = renderVariant();
         int best = 0;
         float bestMs = INFINITY;
+        float variantMs[3] = {0.f, 0.f, 0.f};
+        setRenderLayout(0, 0);  // variants timed with the automatic layout
         for (int v = 0; v < renderVariantCount(); ++v) {
           setRenderVariant(v);
           float ms = INFINITY;
@@ -1552,19 +1604,15 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
                   "cudaMemcpy");
           }
           if (msPerVariant) msPerVariant[v] = ms;
+          if (v < 3) variantMs[v] = ms;
           if (ms < bestMs) {
             bestMs = ms;
             best = v;
           }
         }
-        // Near-field cut radius (fraction of the scene extent), with the best variant.
-        setRenderVariant(best);
-        const float factors[] = {0.f, 1.f / 256, 1.f / 128, 1.f / 64, 1.f / 32, 1.f / 16};
-        float bestCut = 0.f, bestCutMs = INFINITY;
-        for (float f : factors) {
-          r.cutFactor = f;
+        auto trial = [&]() {
           float ms = INFINITY;
-          for (int rep = 0; rep < 2; ++rep) {
+          for (int rep = 0; rep < 2; ++rep) {  // first pass warms caches and code
             check(cudaEventRecord(a, st), "cudaEventRecord");
             r.renderDevicePoses(e, reinterpret_cast<const float4*>(d_poses), count, out.ptr, nullptr);
             check(cudaEventRecord(b, st), "cudaEventRecord");
@@ -1573,12 +1621,67 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
             check(cudaMemcpyAsync(e.rng.ptr, saved.ptr, words * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
                   "cudaMemcpy");
           }
+          return ms;
+        };
+        setRenderVariant(best);
+        r.tuneTimes.assign(kTuneSlots, 0.f);
+        for (int v = 0; v < 3; ++v) r.tuneTimes[v] = variantMs[v];
+        // Block size (results identical), then samples per warp segment.
+        const uint32_t blocks[] = {128, 256, 512};
+        uint32_t bestBlock = 128, bestSeg = 0;
+        float bestLayoutMs = INFINITY;
+        for (int k = 0; k < 3; ++k) {
+          setRenderLayout(blocks[k], 0);
+          const float ms = trial();
+          r.tuneTimes[3 + k] = ms;
+          if (ms < bestLayoutMs) {
+            bestLayoutMs = ms;
+            bestBlock = blocks[k];
+          }
+        }
+        const uint32_t segs[] = {8, 16};  // 32 (the default) was timed above
+        r.tuneTimes[8] = bestLayoutMs;
+        for (int k = 0; k < 2; ++k) {
+          setRenderLayout(bestBlock, segs[k]);
+          const float ms = trial();
+          r.tuneTimes[6 + k] = ms;
+          if (ms < bestLayoutMs) {
+            bestLayoutMs = ms;
+            bestSeg = segs[k];
+          }
+        }
+        setRenderLayout(bestBlock, bestSeg);
+        // Near-field cut radius (fraction of the scene extent), with the best variant and layout.
+        const float factors[] = {0.f, 1.f / 256, 1.f / 128, 1.f / 64, 1.f / 32, 1.f / 16};
+        float bestCut = 0.f, bestCutMs = INFINITY;
+        for (int k = 0; k < 6; ++k) {
+          r.cutFactor = factors[k];
+          const float ms = trial();
+          r.tuneTimes[9 + k] = ms;
           if (ms < bestCutMs) {
             bestCutMs = ms;
-            bestCut = f;
+            bestCut = factors[k];
           }
         }
         r.cutFactor = bestCut;
+        // BVH width: the two-wide BVH with its best cut against the wide ones.
+        const int prevWidth = r.bvhWidth;
+        int bestWidth = 2;
+        float bestWidthMs = INFINITY;
+        for (int k = 0; k < 3; ++k) {
+          const int W = k == 0 ? 2 : (k == 1 ? 4 : 8);
+          r.bvhWidth = W;
+          r.ensureUploaded();
+          const float ms = trial();
+          r.tuneTimes[15 + k] = ms;
+          if (ms < bestWidthMs) {
+            bestWidthMs = ms;
+            bestWidth = W;
+          }
+        }
+        r.bvhWidth = bestWidth;
+        r.ensureUploaded();
+        if (bestWidth != prevWidth) ++r.generation;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         r.checkErrWord();
@@ -1586,6 +1689,48 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
         if (bestVariant) *bestVariant = best;
         saved.release();
         out.release();
+        return 0;
+      },
+      -1);
+}
+
+int crGetAutotuneTimes(float* ms, size_t n) {
+  return guarded(
+      "crGetAutotuneTimes",
+      [&]() -> int {
+        if (!ms) throw std::runtime_error("null pointer");
+        const std::vector<float>& t = R().tuneTimes;
+        if (t.empty()) throw std::runtime_error("crAutotune has not run");
+        for (size_t k = 0; k < n; ++k) ms[k] = k < t.size() ? t[k] : 0.f;
+        return 0;
+      },
+      -1);
+}
+
+int crSetRenderLayout(int blockThreads, int samplesPerWarp) {
+  return guarded(
+      "crSetRenderLayout",
+      [&]() -> int {
+        if (blockThreads != 0 && blockThreads != 128 && blockThreads != 256 && blockThreads != 512)
+          throw std::runtime_error("blockThreads must be 0 (automatic), 128, 256 or 512");
+        if (samplesPerWarp != 0 && samplesPerWarp != 8 && samplesPerWarp != 16 && samplesPerWarp != 32)
+          throw std::runtime_error("samplesPerWarp must be 0 (32), 8, 16 or 32");
+        setRenderLayout(static_cast<uint32_t>(blockThreads), samplesPerWarp == 32 ? 0u : static_cast<uint32_t>(samplesPerWarp));
+        ++R().generation;  // recorded batches follow the layout they were made with
+        return 0;
+      },
+      -1);
+}
+
+int crGetRenderLayout(int* blockThreads, int* samplesPerWarp) {
+  return guarded(
+      "crGetRenderLayout",
+      [&]() -> int {
+        if (!blockThreads || !samplesPerWarp) throw std::runtime_error("null pointer");
+        uint32_t bt = 0, sw = 0;
+        renderLayout(&bt, &sw);
+        *blockThreads = static_cast<int>(bt);
+        *samplesPerWarp = sw ? static_cast<int>(sw) : 32;
         return 0;
       },
       -1);
@@ -1861,7 +2006,7 @@ int crDenoiserAddTrainingPoses(const float* poses12, size_t count, int featureSp
         d.out.ensure(std::max<size_t>(1, count * e.N * 3));
         for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
           const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
-          const size_t need = renderScratchFloats(e.N, te.spp, P);
+          const size_t need = renderScratchFloats(r.dev, e.N, te.spp, P);
           if (need) d.scratch.ensure(need);
           check(launchRender(r.dev, te, d.poses.ptr + 4 * first, P, d.out.ptr + 3 * first * e.N,
                              need ? d.scratch.ptr : nullptr, r.errWord(), nullptr, r.stream()),
@@ -2051,6 +2196,19 @@ int crDenoiserAdamStep(float* w, const float* g, float* m, float* v, size_t n, f
         check(cudaMemcpyAsync(v, dv.ptr, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
         check(cudaMemcpyAsync(wbBits, wb.ptr, n * 2, cudaMemcpyDeviceToHost, s), "cudaMemcpy");
         check(cudaStreamSynchronize(s), "adam");
+        return 0;
+      },
+      -1);
+}
+
+int crDenoiserScaleOutput(float alpha) {
+  return guarded(
+      "crDenoiserScaleOutput",
+      [&]() -> int {
+        if (!(alpha >= 0.f && alpha <= 1.f)) throw std::runtime_error("alpha must be in [0, 1]");
+        DenoiseState& d = DS();
+        if (!d.net.ready()) throw std::runtime_error("call crDenoiserInit first");
+        d.net.scaleOutput(alpha, R().stream());
         return 0;
       },
       -1);
@@ -2312,6 +2470,31 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
       -1);
 }
 
+int crSetAdaptiveSchedule(int refillIdle, int steps) {
+  return guarded(
+      "crSetAdaptiveSchedule",
+      [&]() -> int {
+        if (refillIdle < 1 || refillIdle > 32) throw std::runtime_error("refillIdle must be in [1, 32]");
+        if (steps < 1 || steps > 4096) throw std::runtime_error("steps must be in [1, 4096]");
+        setAdaptiveSchedule(static_cast<uint32_t>(refillIdle), steps);
+        return 0;
+      },
+      -1);
+}
+
+int crGetAdaptiveSchedule(int* refillIdle, int* steps) {
+  return guarded(
+      "crGetAdaptiveSchedule",
+      [&]() -> int {
+        if (!refillIdle || !steps) throw std::runtime_error("null pointer");
+        uint32_t r = 0;
+        adaptiveSchedule(&r, steps);
+        *refillIdle = static_cast<int>(r);
+        return 0;
+      },
+      -1);
+}
+
 int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long long seed, void* records,
                      float* sums) {
   return guarded(
@@ -2368,6 +2551,61 @@ int crSetBvhBuilder(int kind) {
 }
 
 int crGetBvhBuilder(void) { return R().builder; }
+
+int crSetBvhWidth(int width) {
+  return guarded(
+      "crSetBvhWidth",
+      [&]() -> int {
+        if (width != 2 && width != 4 && width != 8) throw std::runtime_error("BVH width must be 2, 4 or 8");
+        Renderer& r = R();
+        if (r.bvhWidth != width) ++r.generation;  // recorded batches search the tree they were made with
+        r.bvhWidth = width;
+        return 0;
+      },
+      -1);
+}
+
+int crGetBvhWidth(void) { return R().bvhWidth; }
+
+int crGetWideBvhHost(int width, float* nodesOut, size_t capFloats, uint32_t* nodeCount, float* trisOut) {
+  return guarded(
+      "crGetWideBvhHost",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.loaded || !r.pendingBvh) throw std::runtime_error("needs a scene loaded with the host builder, not yet uploaded");
+        const HostBvh& b = *r.pendingBvh;
+        std::vector<float> w;
+        WideBvhStats st;
+        collapseWideBvh(b.nodes.data(), static_cast<uint32_t>(b.nodes.size() / 16), b.tris.data(),
+                        static_cast<uint32_t>(b.tris.size() / 12), width, w, st);
+        if (nodeCount) *nodeCount = st.nodes;
+        if (nodesOut) {
+          if (capFloats < w.size()) throw std::runtime_error("output too small");
+          std::memcpy(nodesOut, w.data(), w.size() * 4);
+        }
+        if (trisOut)
+          for (size_t t = 0; t < b.tris.size() / 12; ++t)
+            for (int v = 0; v < 3; ++v)
+              for (int a = 0; a < 3; ++a) trisOut[9 * t + 3 * v + a] = b.tris[12 * t + 4 * v + a];
+        return 0;
+      },
+      -1);
+}
+
+int crGetWideBvhStats(uint32_t* nodes, uint32_t* depth, double* meanChildren) {
+  return guarded(
+      "crGetWideBvhStats",
+      [&]() -> int {
+        Renderer& r = R();
+        if (!r.loaded) throw std::runtime_error("no scene loaded");
+        r.ensureUploaded();
+        if (nodes) *nodes = r.dev.width == 2 ? 0u : r.wideStats.nodes;
+        if (depth) *depth = r.dev.width == 2 ? 0u : r.wideStats.maxDepth;
+        if (meanChildren) *meanChildren = r.dev.width == 2 ? 0.0 : r.wideStats.meanChildren;
+        return 0;
+      },
+      -1);
+}
 
 int crSetStream(void* stream) {
   R().userStream = static_cast<cudaStream_t>(stream);

@@ -23,6 +23,7 @@
 #include <curand_kernel.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "device_api.hpp"
 
@@ -313,6 +314,186 @@ __device__ __forceinline__ void traverseFrom(const DevScene& sc, const Ray& r, f
   }
 }
 
+// ---------------------------------------------------------------------------
+// Wide BVH traversal (4 or 8 children per node, 8-bit quantised child boxes;
+// layout in wbvh.hpp).  Per node and axis the ray's entry and exit distances
+// to child k's planes p + q * s are fma(q, s * idir, p * idir - o * idir),
+// the byte q turned into a float exactly through the mantissa (0x4B000000 |
+// q is the float 2^23 + q); the slack of the BVH2 slab test (see setupRay)
+// is folded into the per-node offsets and covers the same rounding, since
+// every plane lies within the scene's extent.  Hit children are ordered
+// near to far by a sorting network; the nearest is entered, the rest pushed
+// far first.
+// ---------------------------------------------------------------------------
+constexpr int kWideStackSize = kWideStackEntries;
+
+__device__ __forceinline__ float byteAsFloat(uint32_t w, int k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, static_cast<uint32_t>(k) | 0x7650u)) - 8388608.0f;
+}
+
+// Compare-exchange of (key, ref) pairs: the smaller key first.
+__device__ __forceinline__ void cex(float& ka, int& ra, float& kb, int& rb) {
+  const bool sw = kb < ka;
+  const float k = sw ? kb : ka;
+  kb = sw ? ka : kb;
+  ka = k;
+  const int r = sw ? rb : ra;
+  rb = sw ? ra : rb;
+  ra = r;
+}
+
+template <int W>
+__device__ __forceinline__ void sortChildren(float* key, int* ref) {
+  if (W == 4) {
+    cex(key[0], ref[0], key[1], ref[1]);
+    cex(key[2], ref[2], key[3], ref[3]);
+    cex(key[0], ref[0], key[2], ref[2]);
+    cex(key[1], ref[1], key[3], ref[3]);
+    cex(key[1], ref[1], key[2], ref[2]);
+  } else {
+    // 19 comparators, depth 6 (checked exhaustively on 0/1 inputs)
+    cex(key[0], ref[0], key[2], ref[2]);
+    cex(key[1], ref[1], key[3], ref[3]);
+    cex(key[4], ref[4], key[6], ref[6]);
+    cex(key[5], ref[5], key[7], ref[7]);
+    cex(key[0], ref[0], key[4], ref[4]);
+    cex(key[1], ref[1], key[5], ref[5]);
+    cex(key[2], ref[2], key[6], ref[6]);
+    cex(key[3], ref[3], key[7], ref[7]);
+    cex(key[0], ref[0], key[1], ref[1]);
+    cex(key[2], ref[2], key[3], ref[3]);
+    cex(key[4], ref[4], key[5], ref[5]);
+    cex(key[6], ref[6], key[7], ref[7]);
+    cex(key[2], ref[2], key[4], ref[4]);
+    cex(key[3], ref[3], key[5], ref[5]);
+    cex(key[1], ref[1], key[4], ref[4]);
+    cex(key[3], ref[3], key[6], ref[6]);
+    cex(key[1], ref[1], key[2], ref[2]);
+    cex(key[3], ref[3], key[4], ref[4]);
+    cex(key[5], ref[5], key[6], ref[6]);
+  }
+}
+
+// Traversal of the W-wide BVH from `node` with `sp` deferred entries, for at
+// most `budget` node visits or leaves; returns true when the search is over
+// (h holds the closest hit), false when the budget ran out (node and sp hold
+// the position to go on from).
+template <int W>
+__device__ __forceinline__ bool traverseWide(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack, int& sp,
+                                             int& node, uint32_t* errFlag, uint32_t& nodeVisits, uint32_t& triTests,
+                                             bool count, int budget) {
+  constexpr int F = W == 8 ? 6 : 4;  // float4 per node
+  const bool negX = r.idx < 0.f, negY = r.idy < 0.f, negZ = r.idz < 0.f;
+  for (int it = 0; it < budget; ++it) {
+    if (node >= 0) {
+      if (count) ++nodeVisits;
+      const float4* n = sc.wnodes + static_cast<size_t>(F) * node;
+      const float4 n0 = __ldg(n);
+      const uint32_t meta = __float_as_uint(n0.w);
+      const int cnt = static_cast<int>(meta >> 24);
+      const float sx = __uint_as_float((meta & 0xFFu) << 23) * r.idx;
+      const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * r.idy;
+      const float sz = __uint_as_float(((meta >> 16) & 0xFFu) << 23) * r.idz;
+      const float bx = fmaf(n0.x, r.idx, r.nox), by = fmaf(n0.y, r.idy, r.noy), bz = fmaf(n0.z, r.idz, r.noz);
+      const float nbx = bx - r.slx, fbx = bx + r.slx;
+      const float nby = by - r.sly, fby = by + r.sly;
+      const float nbz = bz - r.slz, fbz = bz + r.slz;
+      uint32_t lo[3][W / 4], hi[3][W / 4];
+      int ref[W];
+      if (W == 4) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4*>(n + 1));
+        const uint4 b = __ldg(reinterpret_cast<const uint4*>(n + 2));
+        const int4 c = __ldg(reinterpret_cast<const int4*>(n + 3));
+        lo[0][0] = a.x;
+        lo[1][0] = a.y;
+        lo[2][0] = a.z;
+        hi[0][0] = a.w;
+        hi[1][0] = b.x;
+        hi[2][0] = b.y;
+        ref[0] = c.x;
+        ref[1] = c.y;
+        ref[2] = c.z;
+        ref[3] = c.w;
+      } else {
+        const uint4 a = __ldg(reinterpret_cast<const uint4*>(n + 1));
+        const uint4 b = __ldg(reinterpret_cast<const uint4*>(n + 2));
+        const uint4 c = __ldg(reinterpret_cast<const uint4*>(n + 3));
+        const int4 d = __ldg(reinterpret_cast<const int4*>(n + 4));
+        const int4 e = __ldg(reinterpret_cast<const int4*>(n + 5));
+        lo[0][0] = a.x;
+        lo[0][W / 8] = a.y;
+        lo[1][0] = a.z;
+        lo[1][W / 8] = a.w;
+        lo[2][0] = b.x;
+        lo[2][W / 8] = b.y;
+        hi[0][0] = b.z;
+        hi[0][W / 8] = b.w;
+        hi[1][0] = c.x;
+        hi[1][W / 8] = c.y;
+        hi[2][0] = c.z;
+        hi[2][W / 8] = c.w;
+        ref[0] = d.x;
+        ref[1] = d.y;
+        ref[2] = d.z;
+        ref[3] = d.w;
+        ref[W / 2] = e.x;
+        ref[W / 2 + 1] = e.y;
+        ref[W / 2 + 2] = e.z;
+        ref[W / 2 + 3] = e.w;
+      }
+      // near planes: the lower ones along positive direction components
+      uint32_t wn[3][W / 4], wf[3][W / 4];
+#pragma unroll
+      for (int j = 0; j < W / 4; ++j) {
+        wn[0][j] = negX ? hi[0][j] : lo[0][j];
+        wf[0][j] = negX ? lo[0][j] : hi[0][j];
+        wn[1][j] = negY ? hi[1][j] : lo[1][j];
+        wf[1][j] = negY ? lo[1][j] : hi[1][j];
+        wn[2][j] = negZ ? hi[2][j] : lo[2][j];
+        wf[2][j] = negZ ? lo[2][j] : hi[2][j];
+      }
+      float key[W];
+      int nHit = 0;
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        const int j = k >> 2, b = k & 3;
+        const float tnx = fmaf(byteAsFloat(wn[0][j], b), sx, nbx), tfx = fmaf(byteAsFloat(wf[0][j], b), sx, fbx);
+        const float tny = fmaf(byteAsFloat(wn[1][j], b), sy, nby), tfy = fmaf(byteAsFloat(wf[1][j], b), sy, fby);
+        const float tnz = fmaf(byteAsFloat(wn[2][j], b), sz, nbz), tfz = fmaf(byteAsFloat(wf[2][j], b), sz, fbz);
+        const float tn = max3(tnx, tny, fmaxf(tnz, tmin));
+        const float tf = min3(tfx, tfy, fminf(tfz, h.t));
+        const bool hit = k < cnt && tn <= tf;
+        key[k] = hit ? tn : INFINITY;
+        nHit += hit ? 1 : 0;
+      }
+      if (nHit > 0) {
+        sortChildren<W>(key, ref);
+        if (sp + nHit - 1 > kWideStackSize) {
+          atomicOr(errFlag, kErrStackOverflow);
+          return true;
+        }
+#pragma unroll
+        for (int k = W - 1; k >= 1; --k)
+          if (k < nHit) stack[sp++] = ref[k];
+        node = ref[0];
+        continue;
+      }
+    } else {
+      const uint32_t code = ~static_cast<uint32_t>(node);
+      const uint32_t first = code >> 3;
+      const uint32_t tcount = (code & 7u) + 1u;
+      if (count) triTests += tcount;
+      for (uint32_t k = 0; k < tcount; ++k) {
+        const float4* t = sc.tris + 3 * (first + k);
+        testTriangle(r, __ldg(t), __ldg(t + 1), __ldg(t + 2), first + k, tmin, h);
+      }
+    }
+    if (sp == 0) return true;
+    node = stack[--sp];
+  }
+  return false;
+}
+
 // Closest hit over the BVH2; returns the hit in `h` (h.id == ~0u on a miss).
 // cut: null, or the pose's near-field cut (cutKernel): the subtrees whose
 // boxes meet a ball around the eye are searched first, and a hit found there
@@ -365,6 +546,72 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
   float guard;
   if (!beginTrace(sc, r, tmin, tmax, h, stack, sp, node, restart, guard, cut)) return;
   traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests, restart, guard, dlen);
+}
+
+// traverseFrom in bursts: at most `budget` loop iterations (node visits or
+// leaves) from the saved position (node, sp, restart; the stack holds the
+// deferred entries), which is updated in place.  Returns true when the search
+// is over (h holds the closest hit), false when the budget ran out first.
+// Lets a warp stop every few steps to hand finished lanes new rays.
+__device__ __forceinline__ bool traverseBurst(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack,
+                                              int& sp, int& node, bool& restart, float guard, float dlen,
+                                              uint32_t* errFlag, int budget) {
+  for (int it = 0; it < budget; ++it) {
+    if (node >= 0) {
+      const float4* n = sc.nodes + 4 * node;
+      const float4 n0 = __ldg(n + 0);
+      const float4 n1 = __ldg(n + 1);
+      const float4 n2 = __ldg(n + 2);
+      const int4 n3 = __ldg(reinterpret_cast<const int4*>(n + 3));
+      float tn0, tf0, tn1, tf1;
+      childSpan(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, h.t, tn0, tf0);
+      childSpan(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, h.t, tn1, tf1);
+      const bool hit0 = tn0 <= tf0;
+      const bool hit1 = tn1 <= tf1;
+      if (hit0 && hit1) {
+        int first = n3.x, second = n3.y;
+        if (tn1 < tn0) {
+          first = n3.y;
+          second = n3.x;
+        }
+        if (sp >= kStackSize) {
+          atomicOr(errFlag, kErrStackOverflow);
+          return true;
+        }
+        stack[sp++] = second;
+        node = first;
+        continue;
+      }
+      if (hit0) {
+        node = n3.x;
+        continue;
+      }
+      if (hit1) {
+        node = n3.y;
+        continue;
+      }
+    } else {
+      const uint32_t code = ~static_cast<uint32_t>(node);
+      const uint32_t first = code >> 3;
+      const uint32_t count = (code & 7u) + 1u;
+      for (uint32_t k = 0; k < count; ++k) {
+        const float4* t = sc.tris + 3 * (first + k);
+        testTriangle(r, __ldg(t), __ldg(t + 1), __ldg(t + 2), first + k, tmin, h);
+      }
+    }
+    if (sp == 0) {
+      if (restart) {
+        restart = false;
+        if (!(h.id != 0xffffffffu && h.t * dlen <= guard)) {
+          node = 0;
+          continue;
+        }
+      }
+      return true;
+    }
+    node = stack[--sp];
+  }
+  return false;
 }
 
 // Near-field cut of one pose: at most kCutEntries BVH subtrees (box + ref)
@@ -756,11 +1003,16 @@ __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 // autotuner's occupancy knob).
 // One warp task: up to 32 samples of one ommatidium (or whole ommatidia when
 // spp < 32) for all P poses.  Called by whole warps.
-template <int kMode>
+// part: null, or (plan.inBlock) the block's shared-memory chunk partials,
+// [group in block][ommatidium in warp][pose][chunk][3] floats.
+// kWidth: 2 searches the BVH2 (with the near-field cut when eye.cuts is
+// set), 4 or 8 the wide BVH of that width (no cut).
+template <int kMode, int kWidth = 2>
 __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye, const float4* __restrict__ poses,
                                            uint32_t P, const WarpPlan& plan, uint64_t task, float* __restrict__ out,
                                            float* __restrict__ scratch, uint32_t* errFlag,
-                                           RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests) {
+                                           RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests,
+                                           float* __restrict__ part = nullptr) {
   constexpr bool kRecord = (kMode & 3) == 1;
   constexpr bool kCount = (kMode & 3) == 2;
   constexpr bool kFeat = (kMode & 3) == 3;
@@ -778,10 +1030,26 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   const uint32_t chunk = static_cast<uint32_t>(task % plan.chunks);
   const uint32_t slot = group * plan.ommPerWarp + lane / plan.segWidth;
   const uint32_t o = (eye.order && slot < eye.N) ? __ldg(eye.order + slot) : slot;
-  const uint32_t s = chunk * 32u + lane % plan.segWidth;
+  const uint32_t s = chunk * plan.segWidth + lane % plan.segWidth;
   const bool valid = slot < eye.N && s < eye.spp;
   const size_t plane = static_cast<size_t>(eye.N) * eye.spp;
   const size_t sidx = static_cast<size_t>(o) * eye.spp + s;
+  // Where a segment leader writes pose p's sum (or chunk partial): dst0 + p *
+  // dstStride, one of the output, the scratch partials or the block's shared
+  // partials (render and record modes).
+  float* dst0;
+  size_t dstStride;
+  if (plan.chunks == 1) {
+    dst0 = out + static_cast<size_t>(o) * 3;
+    dstStride = static_cast<size_t>(eye.N) * 3;
+  } else if (part) {
+    const uint32_t gs = (group % plan.groupsPerBlock) * plan.ommPerWarp + lane / plan.segWidth;
+    dst0 = part + ((static_cast<size_t>(gs) * P - p0) * plan.chunks + chunk) * 3;
+    dstStride = static_cast<size_t>(plan.chunks) * 3;
+  } else {
+    dst0 = scratch + (static_cast<size_t>(o) * plan.chunks + chunk) * 3;
+    dstStride = static_cast<size_t>(eye.N) * plan.chunks * 3;
+  }
 
   curandState st;
   v3 axis = mk(0.f, 1.f, 0.f), relPos = mk(0.f, 0.f, 0.f), perp = mk(0.f, 0.f, 1.f);
@@ -828,11 +1096,22 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
       const Ray ray = setupRay(org, dir, sc.extent);
       Hit h;
-      if (eye.cuts)
+      if (kWidth != 2) {
+        h.t = 1e16f;
+        h.id = 0xffffffffu;
+        h.pos = 0;
+        if (sc.triCount > 0) {
+          int wstack[kWideStackSize];
+          int wsp = 0, wnode = 0;
+          traverseWide<kWidth == 8 ? 8 : 4>(sc, ray, fpo, h, wstack, wsp, wnode, errFlag, nodeVisits, triTests, kCount,
+                                             0x7fffffff);
+        }
+      } else if (eye.cuts) {
         traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests,
                              eye.cuts + static_cast<size_t>(p) * kCutStride, sqrtf(dot(dir, dir)));
-      else
+      } else {
         traceClosest<kCount>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+      }
       v3 c;
       float b1 = 0.f, b2 = 0.f;
       if (h.id != 0xffffffffu) {
@@ -914,8 +1193,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       continue;
     }
     if ((lane % plan.segWidth) == 0u && o < eye.N) {
-      float* dst = plan.chunks == 1 ? out + (static_cast<size_t>(p) * eye.N + o) * 3
-                                    : scratch + ((static_cast<size_t>(p) * eye.N + o) * plan.chunks + chunk) * 3;
+      float* dst = dst0 + p * dstStride;
       dst[0] = col.x;
       dst[1] = col.y;
       dst[2] = col.z;
@@ -924,17 +1202,47 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   if (valid && !eye.draws) storeState(eye.rng, plane, sidx, st);
 }
 
-template <int kMode, int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses,
-                                                    uint32_t P, WarpPlan plan, float* __restrict__ out,
-                                                    float* __restrict__ scratch, uint32_t* errFlag,
-                                                    RayRecord* __restrict__ rec, unsigned long long* stats) {
+// kRegs: registers per thread the kernel is compiled for (the autotuner's
+// occupancy knob: 96, 80 or 64 allow 640, 768 or 1024 resident threads per
+// SM), independent of the block size, which the plan sets (128-512 threads).
+// With plan.inBlock every block holds all chunk warps of plan.groupsPerBlock
+// ommatidium groups (tasks padded to whole blocks): each warp leaves its
+// per-pose chunk partial in shared memory, and after one barrier the block
+// sums every (ommatidium, pose) over its chunks in chunk order.
+template <int kMode, int kRegs, int kWidth = 2, bool kInBlock = false>
+__global__ void __maxnreg__(kRegs) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses, uint32_t P,
+                                                WarpPlan plan, float* __restrict__ out, float* __restrict__ scratch,
+                                                uint32_t* errFlag, RayRecord* __restrict__ rec,
+                                                unsigned long long* stats) {
+  extern __shared__ float chunkPart[];
   constexpr bool kCount = kMode == 2;
   uint32_t nodeVisits = 0, triTests = 0;
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t task = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  if (task >= plan.tasks) return;  // whole warps exit together
-  renderTask<kMode>(sc, eye, poses, P, plan, task, out, scratch, errFlag, rec, nodeVisits, triTests);
+  if (task >= plan.tasks) return;  // whole warps exit together (never with inBlock: whole blocks)
+  renderTask<kMode, kWidth>(sc, eye, poses, P, plan, task, out, scratch, errFlag, rec, nodeVisits, triTests,
+                            kInBlock ? chunkPart : nullptr);
+  if (kInBlock) {
+    __syncthreads();
+    const uint32_t perBlock = plan.groupsPerBlock * plan.ommPerWarp;  // ommatidium slots of the block
+    for (uint32_t item = threadIdx.x; item < perBlock * P; item += blockDim.x) {
+      const uint32_t gs = item / P, p = item - gs * P;
+      const uint64_t slot = static_cast<uint64_t>(blockIdx.x) * perBlock + gs;
+      if (slot >= eye.N) continue;
+      const uint32_t o = eye.order ? __ldg(eye.order + slot) : static_cast<uint32_t>(slot);
+      const float* src = chunkPart + (static_cast<size_t>(gs) * P + p) * plan.chunks * 3;
+      float x = 0.f, y = 0.f, z = 0.f;
+      for (uint32_t c = 0; c < plan.chunks; ++c) {
+        x += src[3 * c];
+        y += src[3 * c + 1];
+        z += src[3 * c + 2];
+      }
+      float* dst = out + (static_cast<size_t>(p) * eye.N + o) * 3;
+      dst[0] = x;
+      dst[1] = y;
+      dst[2] = z;
+    }
+  }
   if (kCount) {
     unsigned long long nv = nodeVisits, tt = triTests;
     for (int m = 16; m >= 1; m >>= 1) {
@@ -1186,8 +1494,8 @@ __device__ __forceinline__ uint32_t lastAtMost(const T* base, uint32_t n, uint64
 // belongs to the last eye whose taskBase <= t; the eyes' tasks are laid out
 // one eye after another.  ctrl[0] = task counter, ctrl[1] = earliest start
 // (ns), ctrl[2 + e] = completion time of eye e's last task (ns).
-template <int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) batchKernel(DevScene sc, const BatchEye* __restrict__ eyes,
+template <int kRegs, int kWidth = 2>
+__global__ void __maxnreg__(kRegs) batchKernel(DevScene sc, const BatchEye* __restrict__ eyes,
                                                                const unsigned long long* __restrict__ taskBase,
                                                                uint32_t nEyes, unsigned long long totalTasks,
                                                                unsigned long long* ctrl, uint32_t* errFlag) {
@@ -1203,7 +1511,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) batchKernel(DevScene sc, cons
     first = false;
     const uint32_t e = lastAtMost(taskBase, nEyes, task);
     const BatchEye be = eyes[e];
-    renderTask<0>(sc, be.eye, be.poses, be.P, be.plan, task - taskBase[e], be.out, be.scratch, errFlag, nullptr, nv,
+    renderTask<0, kWidth>(sc, be.eye, be.poses, be.P, be.plan, task - taskBase[e], be.out, be.scratch, errFlag, nullptr, nv,
                   tt);
     if (lane == 0) atomicMax(&ctrl[2 + e], globalTimerNs());
   }
@@ -1331,8 +1639,60 @@ WarpPlan planWarps(uint32_t N, uint32_t spp) {
   return p;
 }
 
+static uint32_t g_blockThreads = 0, g_samplesPerWarp = 0;
+
+void setRenderLayout(uint32_t blockThreads, uint32_t samplesPerWarp) {
+  g_blockThreads = (blockThreads == 128 || blockThreads == 256 || blockThreads == 512) ? blockThreads : 0;
+  g_samplesPerWarp = (samplesPerWarp == 8 || samplesPerWarp == 16) ? samplesPerWarp : 0;
+}
+void renderLayout(uint32_t* blockThreads, uint32_t* samplesPerWarp) {
+  *blockThreads = g_blockThreads;
+  *samplesPerWarp = g_samplesPerWarp;
+}
+
 namespace {
 constexpr uint64_t kFillWarps = 16384;  // warps that keep every SM busy (152 SMs x 8 blocks x 4 warps, x3)
+constexpr size_t kChunkSmemMax = 96 * 1024;  // shared memory for in-block chunk sums, per block
+
+// The plain render's plan under the process-wide layout: the segment width,
+// then the block size, and whether the chunk partials of P poses are summed
+// in shared memory (possible when a block holds whole ommatidium groups and
+// their partials fit kChunkSmemMax).
+WarpPlan planRender(uint32_t N, uint32_t spp, uint32_t P, bool forceScratch, bool inBlockAllowed = true) {
+  WarpPlan p = planWarps(N, spp);
+  if (g_samplesPerWarp && g_samplesPerWarp < p.segWidth) {
+    p.segWidth = g_samplesPerWarp;
+    p.ommPerWarp = 32 / p.segWidth;
+    p.chunks = (spp + p.segWidth - 1) / p.segWidth;
+    p.tasks = (static_cast<uint64_t>(N) + p.ommPerWarp - 1) / p.ommPerWarp * p.chunks;
+  }
+  uint32_t bw = g_blockThreads / 32;
+  if (bw == 0) {
+    bw = 4;
+    if (p.chunks > 1 && !forceScratch && inBlockAllowed)
+      for (uint32_t c : {4u, 8u, 16u})
+        if (p.chunks <= c && c % p.chunks == 0) {
+          bw = c;
+          break;
+        }
+  }
+  p.blockWarps = bw;
+  // A small eye's launch may spread its poses over more warps (pre-drawn
+  // random numbers, splitPoses): that plan keeps the chunk partials in scratch.
+  const bool maySplit = P >= 2 && p.tasks < kFillWarps / 2;
+  if (p.chunks > 1 && !forceScratch && inBlockAllowed && !maySplit && bw % p.chunks == 0) {
+    const uint32_t G = bw / p.chunks;
+    const size_t bytes = static_cast<size_t>(G) * p.ommPerWarp * P * p.chunks * 3 * sizeof(float);
+    if (bytes <= kChunkSmemMax) {
+      p.inBlock = 1;
+      p.groupsPerBlock = G;
+      const uint64_t groups = p.tasks / p.chunks;
+      p.tasks = (groups + G - 1) / G * G * p.chunks;
+    }
+  }
+  return p;
+}
+
 
 // Cuts the poses of a pre-drawn launch into ranges so that about kFillWarps
 // warp tasks exist.
@@ -1354,9 +1714,24 @@ size_t renderDrawBytes(uint32_t N, uint32_t spp, uint32_t P) {
   return static_cast<size_t>(P) * N * spp * sizeof(float2);
 }
 
-size_t renderScratchFloats(uint32_t N, uint32_t spp, uint32_t P) {
-  const WarpPlan p = planWarps(N, spp);
-  if (p.chunks == 1) return 0;
+WarpPlan planBatch(uint32_t N, uint32_t spp) {
+  WarpPlan p = planRender(N, spp, 1, true);
+  p.blockWarps = batchBlockThreads() / 32;
+  return p;
+}
+
+uint32_t batchBlockThreads() { return g_blockThreads ? g_blockThreads : 128u; }
+
+// In-block chunk sums are built for the plain and recording renders on the
+// two-wide BVH only.
+static bool inBlockAllowed(const DevScene& scene, bool rec, bool stats) {
+  return !stats && !scene.lighting && (scene.width == 2 || rec);
+}
+
+size_t renderScratchFloats(const DevScene& scene, uint32_t N, uint32_t spp, uint32_t P, bool rec, bool stats,
+                           bool forceScratch) {
+  const WarpPlan p = planRender(N, spp, P, forceScratch, inBlockAllowed(scene, rec, stats));
+  if (p.chunks == 1 || p.inBlock) return 0;
   return static_cast<size_t>(P) * N * p.chunks * 3;
 }
 
@@ -1376,55 +1751,108 @@ cudaError_t launchRngInit(const DevEye& eye, uint32_t* errFlag, cudaStream_t str
   return cudaGetLastError();
 }
 
+namespace {
+// One launch of renderKernel<kMode, kRegs> with the plan's block size and,
+// for in-block chunk sums, the shared memory of the partials.
+// Launch of the kernel instance with (kInBlock) or without in-block chunk sums.
+template <int kMode, int kRegs, int kWidth, bool kInBlock>
+cudaError_t runRenderKernel(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P,
+                            const WarpPlan& plan, float* out, float* scratch, uint32_t* errFlag, RayRecord* rec,
+                            unsigned long long* stats, cudaStream_t stream) {
+  const unsigned block = 32u * plan.blockWarps;
+  const uint64_t blocks = (plan.tasks + plan.blockWarps - 1) / plan.blockWarps;
+  if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
+  size_t smem = 0;
+  if (kInBlock) {
+    smem = static_cast<size_t>(plan.groupsPerBlock) * plan.ommPerWarp * P * plan.chunks * 3 * sizeof(float);
+    if (smem > 48 * 1024) {
+      const cudaError_t e = cudaFuncSetAttribute(renderKernel<kMode, kRegs, kWidth, kInBlock>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(kChunkSmemMax));
+      if (e != cudaSuccess) return e;
+    }
+  }
+  renderKernel<kMode, kRegs, kWidth, kInBlock><<<static_cast<unsigned>(blocks), block, smem, stream>>>(
+      scene, eye, poses, P, plan, out, scratch, errFlag, rec, stats);
+  return cudaGetLastError();
+}
+
+// In-block chunk sums exist for the plain and recording renders on the
+// two-wide BVH (planRender offers them only there, see inBlockAllowed).
+template <int kMode, int kRegs, int kWidth = 2>
+cudaError_t runRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P,
+                      const WarpPlan& plan, float* out, float* scratch, uint32_t* errFlag, RayRecord* rec,
+                      unsigned long long* stats, cudaStream_t stream) {
+  constexpr bool kHasInBlock = (kMode == 0 || kMode == 1) && kWidth == 2;
+  if (plan.inBlock) {
+    if (!kHasInBlock) return cudaErrorInvalidValue;
+    return runRenderKernel<kMode, kRegs, kWidth, kHasInBlock>(scene, eye, poses, P, plan, out, scratch, errFlag,
+                                                              rec, stats, stream);
+  }
+  return runRenderKernel<kMode, kRegs, kWidth, false>(scene, eye, poses, P, plan, out, scratch, errFlag, rec,
+                                                      stats, stream);
+}
+
+// The plain render (mode 0) or the counting render (mode 2) of the scene's
+// BVH width.
+template <int kMode, int kRegs>
+cudaError_t runRenderWidth(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P,
+                           const WarpPlan& plan, float* out, float* scratch, uint32_t* errFlag,
+                           unsigned long long* stats, cudaStream_t stream) {
+  switch (scene.width) {
+    case 4:
+      return runRender<kMode, kRegs, 4>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats, stream);
+    case 8:
+      return runRender<kMode, kRegs, 8>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats, stream);
+    default:
+      return runRender<kMode, kRegs, 2>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats, stream);
+  }
+}
+}  // namespace
+
 cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* out,
                          float* scratch, uint32_t* errFlag, RayRecord* rec, cudaStream_t stream,
-                         unsigned long long* stats) {
+                         unsigned long long* stats, bool forceScratch) {
   if (P == 0 || eye.N == 0) return cudaSuccess;
-  WarpPlan plan = planWarps(eye.N, eye.spp);
-  if (plan.chunks > 1 && scratch == nullptr) return cudaErrorInvalidValue;
+  WarpPlan plan = planRender(eye.N, eye.spp, P, forceScratch, inBlockAllowed(scene, rec != nullptr, stats != nullptr));
+  if (plan.chunks > 1 && !plan.inBlock && scratch == nullptr) return cudaErrorInvalidValue;
   if (eye.draws) {
+    if (plan.inBlock) return cudaErrorInvalidValue;  // planRender keeps splittable launches out of shared memory
     const size_t total = static_cast<size_t>(eye.N) * eye.spp;
     drawsKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(eye, P);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     plan = splitPoses(plan, P);
   }
-  if (eye.cuts) {
+  if (eye.cuts && (scene.width == 2 || rec || scene.lighting)) {  // the wide BVH searches without a cut
     if (!(eye.cutRadius > 0.f)) return cudaErrorInvalidValue;
     cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, eye.cutRadius, eye.maxRel, eye.cuts);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const uint64_t threads = plan.tasks * 32;
-  const unsigned block = 128;
-  const uint64_t blocks = (threads + block - 1) / block;
-  if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
-  const unsigned g = static_cast<unsigned>(blocks);
+  cudaError_t e;
   if (scene.lighting && !stats) {
     if (!scene.light) return cudaErrorInvalidValue;
-    if (rec)
-      renderKernel<5, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
-    else
-      renderKernel<4, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+    e = rec ? runRender<5, 96>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr, stream)
+            : runRender<4, 96>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr, stream);
   } else if (rec) {
-    renderKernel<1, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr);
+    e = runRender<1, 96>(scene, eye, poses, P, plan, out, scratch, errFlag, rec, nullptr, stream);
   } else if (stats) {
-    renderKernel<2, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stats);
+    e = runRenderWidth<2, 96>(scene, eye, poses, P, plan, out, scratch, errFlag, stats, stream);
   } else {
     switch (g_renderVariant) {
       case 1:
-        renderKernel<0, 6><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        e = runRenderWidth<0, 80>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stream);
         break;
       case 2:
-        renderKernel<0, 8><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        e = runRenderWidth<0, 64>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stream);
         break;
       default:
-        renderKernel<0, 5><<<g, block, 0, stream>>>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, nullptr);
+        e = runRenderWidth<0, 96>(scene, eye, poses, P, plan, out, scratch, errFlag, nullptr, stream);
         break;
     }
   }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || plan.chunks == 1) return e;
+  if (e != cudaSuccess || plan.chunks == 1 || plan.inBlock) return e;
   const size_t count = static_cast<size_t>(P) * eye.N;
   combineChunksKernel<<<static_cast<unsigned>((count + 255) / 256), 256, 0, stream>>>(scratch, plan.chunks, count, out);
   return cudaGetLastError();
@@ -1448,28 +1876,21 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const unsigned g = static_cast<unsigned>((plan.tasks * 32 + 127) / 128);
   switch (g_renderVariant) {
-    case 1:
-      renderKernel<3, 6><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
-      break;
-    case 2:
-      renderKernel<3, 8><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
-      break;
-    default:
-      renderKernel<3, 5><<<g, 128, 0, stream>>>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr);
-      break;
+    case 1: return runRender<3, 80>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr, stream);
+    case 2: return runRender<3, 64>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr, stream);
+    default: return runRender<3, 96>(scene, eye, poses, P, plan, stats, nullptr, errFlag, nullptr, nullptr, stream);
   }
-  return cudaGetLastError();
 }
 
 int batchBlocksPerSM(int variant) {
   int blocks = 0;
   cudaError_t e;
+  const int bt = static_cast<int>(batchBlockThreads());
   switch (variant) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<6>, 128, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<8>, 128, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<5>, 128, 0); break;
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<80>, bt, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<64>, bt, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batchKernel<96>, bt, 0); break;
   }
   return e == cudaSuccess ? blocks : 0;
 }
@@ -1485,16 +1906,19 @@ cudaError_t launchBatch(const DevScene& scene, const BatchEye* eyes, const unsig
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
+  const unsigned bt = batchBlockThreads();
+  auto run = [&](auto regsTag) {
+    constexpr int R = decltype(regsTag)::value;
+    switch (scene.width) {
+      case 4: batchKernel<R, 4><<<gridBlocks, bt, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag); break;
+      case 8: batchKernel<R, 8><<<gridBlocks, bt, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag); break;
+      default: batchKernel<R, 2><<<gridBlocks, bt, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag); break;
+    }
+  };
   switch (variant) {
-    case 1:
-      batchKernel<6><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
-      break;
-    case 2:
-      batchKernel<8><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
-      break;
-    default:
-      batchKernel<5><<<gridBlocks, 128, 0, stream>>>(scene, eyes, taskBase, nEyes, totalTasks, ctrl, errFlag);
-      break;
+    case 1: run(std::integral_constant<int, 80>{}); break;
+    case 2: run(std::integral_constant<int, 64>{}); break;
+    default: run(std::integral_constant<int, 96>{}); break;
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || totalCells == 0) return e;
@@ -1557,66 +1981,116 @@ __device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
 }
 
 // One warp task of a bucket: up to 32 samples of one entry, or several whole
-// entries when the bucket's count is below 32 (the render kernel's plan).
-// With more than 32 samples per task (a whole warp on one entry, spl rounds
-// of 32), the task's samples are first sorted by coneKey, so that each round
-// traces 32 rays in neighbouring directions, whose traversals are alike.
-// Every sample is still traced once with its own random numbers; only the
-// order of the per-lane sums changes.  The sort pays on scenes whose
-// traversals are long and vary from ray to ray; on small scenes (fewer than
-// kAdaptiveSortMinTris triangles) it costs more than it saves, and the
-// samples are traced in index order.
+// entries when the bucket's count is below 32 (the render kernel's plan);
+// with more than 32 samples per entry a task is spl rounds of 32 samples of
+// one entry (chunks of 32 * spl samples when the count is larger still).
+//
+// A warp takes a pool of consecutive tasks of one bucket, up to kPoolRounds
+// rounds of 32 sample slots, and works through it with ray refill (warp-level
+// ray compaction):
+//   1. the random numbers of every slot of the pool are drawn first, all 32
+//      lanes busy (Philox4x32-10 stream (seed, e * 1024 + s): one normal,
+//      then one uniform; O(1) set-up per sample).  With more than 32 samples
+//      per task, on scenes whose traversals are long and vary from ray to ray
+//      (at least kAdaptiveSortMinTris triangles), each task's samples are
+//      sorted by where they leave the cone (coneKey, bitonic sort in shared
+//      memory), so that neighbouring slots trace neighbouring directions;
+//   2. each lane traces one slot at a time.  The warp traverses in bursts of
+//      `steps` BVH steps; between bursts, lanes whose ray has finished shade
+//      it and store its colour in shared memory, and once at least
+//      `refillIdle` lanes are idle they all take the next slots of the pool.
+//      So lanes do not wait for the longest ray of a round of 32, and a new
+//      ray's set-up runs on many lanes at once;
+//   3. each task is summed in a fixed order that does not depend on the
+//      scheduling: lane L adds the colours of slot L of the task's rounds in
+//      round order (fma with 1/spp), then the segmented butterfly over the
+//      lanes of an entry.  Results are deterministic.
+// Every sample is traced once with its own random numbers.
 constexpr uint32_t kAdaptiveSortMinTris = 16384;
+constexpr uint32_t kPoolRounds = 8;
+constexpr uint32_t kPoolSlots = 32 * kPoolRounds;
+constexpr uint32_t kAdaptiveWarps = 4;  // warps per 128-thread block
 
-// Random numbers: Philox4x32-10 stream (seed, e * 1024 + s), one normal then
-// one uniform per sample (O(1) set-up per entry, unlike XORWOW's skip-ahead).
+__device__ __forceinline__ uint32_t lanesBelow(uint32_t lane) { return (1u << lane) - 1u; }
+
+template <int kWidth>
 __global__ void __launch_bounds__(128, 5)
     adaptiveKernel(DevScene sc, const float4* __restrict__ omm, uint32_t N, const float4* __restrict__ poses,
                    AdaptiveLaunch L, unsigned long long seed, float* __restrict__ sums, uint32_t* errFlag,
                    RayRecord* __restrict__ rec, const float4* __restrict__ cuts) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // totalTasks < 2^31 (checked at launch)
-  if (task >= L.totalTasks) return;
+  __shared__ uint32_t sortKey[kAdaptiveWarps][kPoolSlots], sortIdx[kAdaptiveWarps][kPoolSlots];
+  __shared__ float2 slotDraw[kAdaptiveWarps][kPoolSlots];  // by sample position k within its task segment
+  __shared__ float slotCol[kAdaptiveWarps][3][kPoolSlots];  // unscaled colour of every slot
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  const uint32_t pool = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // totalPools < 2^26 (checked at launch)
+  if (pool >= L.totalPools) return;  // whole warps
   uint32_t bi = 0;
-  while (bi + 1 < L.nBuckets && task >= L.b[bi + 1].taskBase) ++bi;
+  while (bi + 1 < L.nBuckets && pool >= L.b[bi + 1].poolBase) ++bi;
   const AdaptiveBucket B = L.b[bi];
   const uint32_t spp = B.spp;
   const uint32_t segWidth = spp < 32u ? spp : 32u;
   const uint32_t perWarp = 32u / segWidth;
-  const uint32_t spl = adaptiveSamplesPerLane(spp);
+  const uint32_t spl = adaptiveSamplesPerLane(spp);  // rounds per task
   const uint32_t chunks = adaptiveChunks(spp);
-  const uint32_t t = task - static_cast<uint32_t>(B.taskBase);
-  const uint32_t group = t / chunks;
-  const uint32_t chunk = t - group * chunks;
-  const uint32_t i = group * perWarp + lane / segWidth;  // entry index within the bucket
-  const bool valid = i < B.count;
-  v3 col = mk(0.f, 0.f, 0.f);
-  uint32_t nodeVisits = 0, triTests = 0;
-  __shared__ uint32_t sortKey[4][256], sortIdx[4][256];  // per warp of the block (128 threads)
-  __shared__ float2 sortDraw[4][256];  // the task's random numbers, by sample, drawn once for key and trace
-  uint32_t* key = sortKey[threadIdx.x >> 5];
-  uint32_t* idx = sortIdx[threadIdx.x >> 5];
-  float2* draw = sortDraw[threadIdx.x >> 5];
+  const uint32_t tpp = kPoolRounds / spl;  // tasks per pool
+  const uint64_t task0 = static_cast<uint64_t>(pool - B.poolBase) * tpp;
+  const uint64_t left = B.tasks - task0;
+  const uint32_t nTasks = left < tpp ? static_cast<uint32_t>(left) : tpp;
+  const uint32_t nSlots = nTasks * spl * 32u;
   const bool sorted = spl > 1 && sc.triCount >= kAdaptiveSortMinTris;
-  if (valid && sorted) {  // the warp is one entry (segWidth 32): `valid` is warp-uniform
-    const uint32_t e = B.entries[i];
-    const uint32_t n = 32u * spl;  // 64, 128 or 256
-    for (uint32_t k = lane; k < n; k += 32u) {
+  uint32_t* key = sortKey[w];
+  uint32_t* idx = sortIdx[w];
+  float2* draw = slotDraw[w];
+  float* colR = slotCol[w][0];
+  float* colG = slotCol[w][1];
+  float* colB = slotCol[w][2];
+  const float invSpp = 1.0f / static_cast<float>(spp);
+
+  // Slot j of the pool: round r = j / 32 of task q = r / spl, lane position
+  // j % 32.  Entry (index within the bucket) and sample of a slot:
+  auto slotEntry = [&](uint32_t j) -> uint32_t {
+    const uint64_t t = task0 + (j >> 5) / spl;
+    const uint64_t group = t / chunks;
+    return static_cast<uint32_t>(group * perWarp + (j & 31u) / segWidth);
+  };
+  // Sample position k within the task's segment (slot j's draws are draw[seg + k]).
+  auto slotK = [&](uint32_t j) -> uint32_t {
+    const uint32_t q = (j >> 5) / spl, seg = q * spl * 32u, pos = j - seg;
+    return spl > 1 ? (sorted ? idx[seg + pos] : pos) : (j & 31u) % segWidth;
+  };
+  auto slotSample = [&](uint32_t j, uint32_t k) -> uint32_t {
+    const uint64_t t = task0 + (j >> 5) / spl;
+    const uint32_t chunk = static_cast<uint32_t>(t % chunks);
+    return chunk * 32u * spl + k;
+  };
+
+  // 1. Random numbers (and sort keys) of every slot.
+  for (uint32_t j = lane; j < nSlots; j += 32u) {
+    const uint32_t i = slotEntry(j);
+    const uint32_t q = (j >> 5) / spl, seg = q * spl * 32u;
+    const uint32_t k = spl > 1 ? j - seg : (j & 31u) % segWidth;
+    float2 d = make_float2(0.f, 0.f);
+    if (i < B.count) {
       curandStatePhilox4_32_10_t st;
-      curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + chunk * n + k, 0ull, &st);
-      const float nd = curand_normal(&st);
-      const float ud = curand_uniform(&st);
-      key[k] = coneKey(nd, ud);
-      idx[k] = k;
-      draw[k] = make_float2(nd, ud);
+      curand_init(seed, static_cast<unsigned long long>(B.entries[i]) * 1024ull + slotSample(j, k), 0ull, &st);
+      d.x = curand_normal(&st);
+      d.y = curand_uniform(&st);
     }
-    __syncwarp();
-    // bitonic sort of (key, idx) pairs, ascending
+    draw[spl > 1 ? seg + k : j] = d;
+    if (sorted) {
+      key[j] = coneKey(d.x, d.y);
+      idx[j] = k;
+    }
+  }
+  __syncwarp();
+  if (sorted) {  // bitonic sort of each task's (key, position) pairs, ascending
+    const uint32_t n = 32u * spl;
     for (uint32_t size = 2; size <= n; size <<= 1)
       for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-        for (uint32_t m = lane; m < n / 2; m += 32u) {
-          const uint32_t lo = 2u * stride * (m / stride) + (m % stride), hi = lo + stride;
-          const bool up = (lo & size) == 0u;
+        for (uint32_t m = lane; m < nSlots / 2; m += 32u) {
+          const uint32_t seg = (m / (n / 2)) * n, mm = m % (n / 2);
+          const uint32_t lo = seg + 2u * stride * (mm / stride) + (mm % stride), hi = lo + stride;
+          const bool up = ((lo - seg) & size) == 0u;
           const uint32_t ka = key[lo], kb = key[hi];
           if ((ka > kb) == up) {
             key[lo] = kb;
@@ -1629,47 +2103,24 @@ __global__ void __launch_bounds__(128, 5)
         __syncwarp();
       }
   }
-  if (valid) {
-    const uint32_t e = B.entries[i];
-    const uint32_t p = e / N, o = e - p * N;
-    const float4 a = __ldg(omm + 2 * o), b = __ldg(omm + 2 * o + 1);
-    const v3 axis = mk(a.w, b.x, b.y);
-    const float fpo = b.w;
-    const float sd = b.z / FWHM_SD_RATIO;
-    v3 perp = cross(mk(0.0f, 1.0f, 0.0f), axis);
-    perp = (perp.x + perp.y + perp.z == 0.0f) ? mk(0.0f, 0.0f, 1.0f) : normalize(perp);
-    const v3 relPos = mk(a.x, a.y, a.z) - normalize(axis) * fpo;
-    const float4* pp = poses + 4 * p;
-    const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
-    const v3 org = mk(P0.x, P0.y, P0.z) + mk(X.x, X.y, X.z) * relPos.x + mk(Y.x, Y.y, Y.z) * relPos.y +
-                   mk(Z.x, Z.y, Z.z) * relPos.z;
-    const float invSpp = 1.0f / static_cast<float>(spp);
-    for (uint32_t j = 0; j < spl; ++j) {
-      uint32_t s;
-      float nd, ud;
-      if (sorted) {
-        const uint32_t k = idx[j * 32u + lane];
-        s = chunk * 32u * spl + k;
-        const float2 d = draw[k];
-        nd = d.x;
-        ud = d.y;
-      } else {
-        s = chunk * 32u * spl + j * segWidth + lane % segWidth;
-        curandStatePhilox4_32_10_t st;
-        curand_init(seed, static_cast<unsigned long long>(e) * 1024ull + s, 0ull, &st);
-        nd = curand_normal(&st);
-        ud = curand_uniform(&st);
-      }
-      const v3 splayed = rotatePoint(axis, nd * sd, perp);
-      const v3 rel = rotatePoint(splayed, ud * CR_PI_F, axis);
-      const v3 dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
-      const Ray ray = setupRay(org, dir, sc.extent);
-      Hit h;
-      if (cuts)
-        traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests, cuts + static_cast<size_t>(p) * kCutStride,
-                            sqrtf(dot(dir, dir)));
-      else
-        traceClosest<false>(sc, ray, fpo, 1e16f, h, errFlag, nodeVisits, triTests);
+
+  // 2. Trace with refill.
+  int stack[kWidth == 2 ? kStackSize : kWideStackSize];
+  int sp = 0, node = 0;
+  bool restart = false, live = false;
+  float guard = 0.f, dlen = 0.f, fpo = 0.f;
+  int slot = -1;  // the slot this lane traces, -1 when idle
+  v3 dir = mk(0.f, 0.f, 0.f), org = mk(0.f, 0.f, 0.f);
+  float nd = 0.f, ud = 0.f;
+  Hit h;
+  h.t = 0.f;
+  h.id = 0xffffffffu;
+  h.pos = 0;
+  Ray ray = setupRay(mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 1.f), sc.extent);
+  uint32_t next = 0;  // next slot of the pool to hand out (warp-uniform)
+  for (;;) {
+    // Shade the rays that finished in the last burst.
+    if (slot >= 0 && !live) {
       v3 c;
       float b1 = 0.f, b2 = 0.f;
       if (h.id != 0xffffffffu) {
@@ -1679,8 +2130,12 @@ __global__ void __launch_bounds__(128, 5)
       } else {
         c = shadeMiss(sc.miss, dir);
       }
+      const uint32_t j = static_cast<uint32_t>(slot);
+      colR[j] = c.x;
+      colG[j] = c.y;
+      colB[j] = c.z;
       if (rec) {
-        RayRecord& R = rec[static_cast<size_t>(i) * spp + s];
+        RayRecord& R = rec[static_cast<size_t>(slotEntry(j)) * spp + slotSample(j, slotK(j))];
         R.normalDraw = nd;
         R.uniformDraw = ud;
         R.ox = org.x;
@@ -1698,20 +2153,98 @@ __global__ void __launch_bounds__(128, 5)
         R.b = c.z;
         R.pad = 0.f;
       }
-      col = col + c * invSpp;
+      slot = -1;
+    }
+    // Refill once enough lanes are idle (or all are).
+    const uint32_t idle = __ballot_sync(0xffffffffu, slot < 0);
+    const uint32_t nIdle = __popc(idle);
+    if (next < nSlots && (nIdle >= L.refillIdle || nIdle == 32u)) {
+      if (slot < 0) {
+        const uint32_t j = next + __popc(idle & lanesBelow(lane));
+        if (j < nSlots) {
+          const uint32_t i = slotEntry(j);
+          if (i < B.count) {
+            slot = static_cast<int>(j);
+            const uint32_t e = B.entries[i];
+            const uint32_t p = e / N, o = e - p * N;
+            const uint32_t q = (j >> 5) / spl;
+            const float2 d = draw[spl > 1 ? q * spl * 32u + slotK(j) : j];
+            nd = d.x;
+            ud = d.y;
+            const float4 a = __ldg(omm + 2 * o), b = __ldg(omm + 2 * o + 1);
+            const v3 axis = mk(a.w, b.x, b.y);
+            fpo = b.w;
+            const float sd = b.z / FWHM_SD_RATIO;
+            v3 perp = cross(mk(0.0f, 1.0f, 0.0f), axis);
+            perp = (perp.x + perp.y + perp.z == 0.0f) ? mk(0.0f, 0.0f, 1.0f) : normalize(perp);
+            const v3 relPos = mk(a.x, a.y, a.z) - normalize(axis) * fpo;
+            const float4* pp = poses + 4 * p;
+            const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
+            org = mk(P0.x, P0.y, P0.z) + mk(X.x, X.y, X.z) * relPos.x + mk(Y.x, Y.y, Y.z) * relPos.y +
+                  mk(Z.x, Z.y, Z.z) * relPos.z;
+            const v3 splayed = rotatePoint(axis, nd * sd, perp);
+            const v3 rel = rotatePoint(splayed, ud * CR_PI_F, axis);
+            dir = mk(X.x, X.y, X.z) * rel.x + mk(Y.x, Y.y, Y.z) * rel.y + mk(Z.x, Z.y, Z.z) * rel.z;
+            ray = setupRay(org, dir, sc.extent);
+            dlen = sqrtf(dot(dir, dir));
+            if (kWidth == 2) {
+              live = beginTrace(sc, ray, fpo, 1e16f, h, stack, sp, node, restart, guard,
+                                cuts ? cuts + static_cast<size_t>(p) * kCutStride : nullptr);
+            } else {
+              h.t = 1e16f;
+              h.id = 0xffffffffu;
+              h.pos = 0;
+              sp = 0;
+              node = 0;
+              live = sc.triCount > 0;
+            }
+          } else {  // past the bucket's last entry: contributes nothing
+            colR[j] = colG[j] = colB[j] = 0.f;
+          }
+        }
+      }
+      next = min(nSlots, next + nIdle);
+    }
+    if (__ballot_sync(0xffffffffu, slot >= 0) == 0u) {
+      if (next >= nSlots) break;
+      continue;  // every refilled slot was past the bucket's end: refill again
+    }
+    if (slot >= 0 && live) {
+      if (kWidth == 2) {
+        live = !traverseBurst(sc, ray, fpo, h, stack, sp, node, restart, guard, dlen, errFlag, L.steps);
+      } else {
+        uint32_t nv = 0, tt = 0;
+        live = !traverseWide<kWidth == 8 ? 8 : 4>(sc, ray, fpo, h, stack, sp, node, errFlag, nv, tt, false, L.steps);
+      }
     }
   }
-  for (uint32_t m = segWidth >> 1; m >= 1u; m >>= 1) {
-    col.x += __shfl_xor_sync(0xffffffffu, col.x, static_cast<int>(m));
-    col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
-    col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
-  }
-  if ((lane % segWidth) == 0u && valid) {
-    float* dst = chunks == 1 ? sums + 3 * static_cast<size_t>(B.entries[i])
-                             : B.partials + (static_cast<size_t>(i) * chunks + chunk) * 3;
-    dst[0] = col.x;
-    dst[1] = col.y;
-    dst[2] = col.z;
+  __syncwarp();
+
+  // 3. Fixed-order sums of every task of the pool.
+  for (uint32_t q = 0; q < nTasks; ++q) {
+    v3 col = mk(0.f, 0.f, 0.f);
+    for (uint32_t r = 0; r < spl; ++r) {
+      const uint32_t j = (q * spl + r) * 32u + lane;
+      col.x = fmaf(colR[j], invSpp, col.x);
+      col.y = fmaf(colG[j], invSpp, col.y);
+      col.z = fmaf(colB[j], invSpp, col.z);
+    }
+    for (uint32_t m = segWidth >> 1; m >= 1u; m >>= 1) {
+      col.x += __shfl_xor_sync(0xffffffffu, col.x, static_cast<int>(m));
+      col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
+      col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
+    }
+    const uint32_t j0 = q * spl * 32u + lane;
+    const uint32_t i = slotEntry(j0);
+    if ((lane % segWidth) == 0u && i < B.count) {
+      const uint64_t t = task0 + q;
+      const uint32_t chunk = static_cast<uint32_t>(t % chunks);
+      float* dst = chunks == 1 ? sums + 3 * static_cast<size_t>(B.entries[i])
+                               : B.partials + (static_cast<size_t>(i) * chunks + chunk) * 3;
+      dst[0] = col.x;
+      dst[1] = col.y;
+      dst[2] = col.z;
+    }
   }
 }
 
@@ -1878,10 +2411,22 @@ __global__ void adaptiveFinishKernel(const uint8_t* __restrict__ level, uint64_t
 
 }  // namespace
 
+static uint32_t g_refillIdle = 16;
+static int g_refillSteps = 16;
+
+void setAdaptiveSchedule(uint32_t refillIdle, int steps) {
+  g_refillIdle = refillIdle < 1 ? 1u : (refillIdle > 32 ? 32u : refillIdle);
+  g_refillSteps = steps < 1 ? 1 : (steps > 4096 ? 4096 : steps);
+}
+void adaptiveSchedule(uint32_t* refillIdle, int* steps) {
+  *refillIdle = g_refillIdle;
+  *steps = g_refillSteps;
+}
+
 AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* counts, const uint32_t* spp,
                             float* const* partials, uint32_t nBuckets) {
   AdaptiveLaunch L{};
-  uint64_t tasks = 0;
+  uint64_t tasks = 0, pools = 0;
   for (uint32_t k = 0; k < nBuckets && L.nBuckets < kAdaptiveBuckets; ++k) {
     if (counts[k] == 0) continue;
     AdaptiveBucket& B = L.b[L.nBuckets++];
@@ -1890,11 +2435,18 @@ AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* coun
     B.spp = spp[k];
     B.partials = partials[k];
     B.taskBase = tasks;
+    B.poolBase = pools;
     const uint64_t segWidth = spp[k] < 32 ? spp[k] : 32;
     const uint64_t perWarp = 32 / segWidth, chunks = adaptiveChunks(spp[k]);
-    tasks += (counts[k] + perWarp - 1) / perWarp * chunks;
+    B.tasks = (counts[k] + perWarp - 1) / perWarp * chunks;
+    const uint64_t tpp = kPoolRounds / adaptiveSamplesPerLane(spp[k]);
+    tasks += B.tasks;
+    pools += (B.tasks + tpp - 1) / tpp;
   }
   L.totalTasks = tasks;
+  L.totalPools = pools;
+  L.refillIdle = g_refillIdle;
+  L.steps = g_refillSteps;
   return L;
 }
 
@@ -2010,17 +2562,30 @@ cudaError_t launchCuts(const DevScene& scene, const float4* poses, uint32_t P, f
 cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,
                            RayRecord* rec, cudaStream_t stream, const float4* cuts) {
-  if (L.totalTasks == 0) return cudaSuccess;
+  if (L.totalPools == 0) return cudaSuccess;
   if (rec && L.nBuckets != 1) return cudaErrorInvalidValue;
   for (uint32_t k = 0; k < L.nBuckets; ++k) {
     const uint32_t c = L.b[k].spp;
     if (c == 0 || c > 1024 || (c & (c - 1)) || L.b[k].count > 0xffffffffull || (adaptiveChunks(c) > 1 && !L.b[k].partials))
       return cudaErrorInvalidValue;
   }
-  if (L.totalTasks >= (1ull << 27)) return cudaErrorInvalidConfiguration;  // 32-bit thread ids
-  const uint64_t blocks = (L.totalTasks * 32 + 127) / 128;
-  adaptiveKernel<<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
-                                                                      rec, cuts);
+  if (L.totalPools >= (1ull << 26)) return cudaErrorInvalidConfiguration;  // 32-bit thread ids
+  if (L.refillIdle < 1 || L.refillIdle > 32 || L.steps < 1) return cudaErrorInvalidValue;
+  const uint64_t blocks = (L.totalPools * 32 + 127) / 128;
+  switch (scene.width) {
+    case 4:
+      adaptiveKernel<4><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
+                                                                           rec, nullptr);
+      break;
+    case 8:
+      adaptiveKernel<8><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
+                                                                           rec, nullptr);
+      break;
+    default:
+      adaptiveKernel<2><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
+                                                                           rec, cuts);
+      break;
+  }
   cudaError_t e = cudaGetLastError();
   for (uint32_t k = 0; k < L.nBuckets && e == cudaSuccess; ++k) {
     if (adaptiveChunks(L.b[k].spp) == 1) continue;

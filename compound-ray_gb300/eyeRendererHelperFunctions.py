@@ -171,6 +171,17 @@ def configureExtras(eyeRenderer):
     L.crDenoiserRenderPoses.restype = c_int
     L.crDenoiserGradient.argtypes = [ndpointer(np.uint16, flags="C_CONTIGUOUS"), f32, f32, c_int, f32, f32]
     L.crDenoiserGradient.restype = c_float
+    L.crDenoiserScaleOutput.argtypes = [c_float]
+    L.crSetBvhWidth.argtypes = [c_int]
+    L.crGetWideBvhHost.argtypes = [c_int, ctypes.c_void_p, c_size_t, ctypes.POINTER(ctypes.c_uint32),
+                                   ctypes.c_void_p]
+    L.crGetWideBvhStats.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                    ctypes.POINTER(c_double)]
+    L.crSetRenderLayout.argtypes = [c_int, c_int]
+    L.crGetRenderLayout.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.crGetAutotuneTimes.argtypes = [f32, c_size_t]
+    L.crSetAdaptiveSchedule.argtypes = [c_int, c_int]
+    L.crGetAdaptiveSchedule.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.crDenoiserAdamStep.argtypes = [f32, f32, f32, f32, c_size_t, c_float, c_float, c_float,
                                      ndpointer(np.uint16, flags="C_CONTIGUOUS")]
     L.crDenoiserSave.argtypes = [c_char_p]

@@ -164,6 +164,24 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
  * is not null, crGetRenderVariantCount() timings).  The eye's random streams
  * are restored after every trial, so tuning changes no result.  0 on success. */
 int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant);
+/* No counterpart in the reference.  After the variants, crAutotune times
+ * the block size (128, 256, 512 threads), then the samples per warp segment
+ * (8, 16, 32), then the near-field cut radius, keeping the fastest of each.
+ * Last it times the BVH widths 4 and 8 (crSetBvhWidth) against the two-wide
+ * BVH with its best cut, and keeps the fastest tree.
+ * crGetAutotuneTimes copies its timings (ms): variants 0-2, blocks 128 / 256
+ * / 512, samples per warp 8 / 16 / 32, cut radius 0, 1/256, 1/128, 1/64,
+ * 1/32, 1/16 of the scene extent, BVH width 2 / 4 / 8 (18 values). */
+int crGetAutotuneTimes(float* ms, size_t n);
+/* No counterpart in the reference.  Layout of the render kernel: block size
+ * in threads (0 = the smallest of 128 / 256 / 512 holding all 32-sample
+ * chunk warps of an ommatidium, whose chunk sums then stay in shared memory;
+ * else 128) and samples per warp segment (8, 16 or 32; below 32 a warp
+ * holds several ommatidia, and the samples are summed in another order:
+ * results change within float rounding).  The block size changes no result.
+ * Also used by batches created afterwards.  0 on success. */
+int crSetRenderLayout(int blockThreads, int samplesPerWarp);
+int crGetRenderLayout(int* blockThreads, int* samplesPerWarp);
 /* Near-field cut: the radius, as a fraction of the scene's largest vertex
  * coordinate, of the ball around each pose position whose BVH subtrees every
  * ray searches first (0 = off, the default).  A hit found there within the
@@ -293,6 +311,14 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
  * counterpart in the reference. */
 int crSetAllocatorHalvings(float halvings);
 float crGetAllocatorHalvings(void);
+/* No counterpart in the reference.  Ray-refill schedule of the adaptive
+ * render: each warp works through a pool of up to 256 samples, traversing in
+ * bursts of `steps` BVH steps; between bursts its idle lanes take new samples
+ * once at least refillIdle (1..32) of its 32 lanes are idle (32 = whole
+ * rounds of 32 rays, no refill).  Defaults 16 and 16.  Results do not depend
+ * on it (each entry's samples are summed in a fixed order).  0 on success. */
+int crSetAdaptiveSchedule(int refillIdle, int steps);
+int crGetAdaptiveSchedule(int* refillIdle, int* steps);
 /* Test access: `spp` Philox samples per (pose, ommatidium) of host poses
  * with one seed, recording every ray (records: count x N x spp, as
  * crRenderFrameRecorded) and the per-entry means (sums: count x N x 3). */
@@ -310,9 +336,30 @@ float crDenoiserGradient(const uint16_t* xBf16, const float* base, const float* 
  * place and writes the bf16 bit patterns of the new weights.  0 on success. */
 int crDenoiserAdamStep(float* w, const float* g, float* m, float* v, size_t n, float lr, float c1, float c2,
                        uint16_t* wbBits);
+/* No counterpart in the reference.  Scales the denoiser's correction by
+ * alpha in [0, 1] (its linear output layer is multiplied by alpha; 0 gives
+ * the feature render's 8-sample mean): the strength a caller picks on
+ * validation poses.  0 on success. */
+int crDenoiserScaleOutput(float alpha);
 /* Checkpoint of the parameters and Adam moments (binary, with a header). */
 int crDenoiserSave(const char* path);
 int crDenoiserLoad(const char* path);
+
+/* No counterpart in the reference (whose trees live inside OptiX).  Width
+ * of the BVH the closest-hit searches use: 2 (the two-wide BVH, default; the
+ * only one with the near-field cut), 4 or 8 (a wide BVH with 8-bit quantised
+ * child boxes, collapsed from the two-wide one at the first render that
+ * needs it).  Results are identical for every width.  0 on success. */
+int crSetBvhWidth(int width);
+int crGetBvhWidth(void);
+/* No counterpart in the reference.  Test access: the wide BVH of `width`
+ * (4 or 8) collapsed on the host from a scene loaded with the host builder
+ * and not yet rendered (wbvh.hpp layout, 16 or 24 floats per node), and
+ * (trisOut, may be null) the triangles in leaf order, 9 floats each; nodesOut
+ * may be null to get the count only. */
+int crGetWideBvhHost(int width, float* nodesOut, size_t capFloats, uint32_t* nodeCount, float* trisOut);
+/* Wide BVH in use: nodes, depth and mean children per node (0 for width 2). */
+int crGetWideBvhStats(uint32_t* nodes, uint32_t* depth, double* meanChildren);
 
 /* BVH builder for scenes loaded afterwards: 0 = host binned SAH (default),
  * 1 = GPU linear BVH (Morton codes, radix sort, Karras hierarchy) built at

@@ -105,3 +105,53 @@ def adam_step(w, g, m, v, lr, c1, c2, b1=0.9, b2=0.999, eps=1e-8):
         v = (b2 * v) + (((f(1) - b2) * g) * g)
         w = w - ((lr * (m * c1)) / (np.sqrt(v * c2) + eps))
     return w.astype(np.float32), m.astype(np.float32), v.astype(np.float32), bf16_bits(w)
+
+
+def forward_parts(params, X):
+    """The forward pass with the GPU path's rounding points: the bf16 hidden
+    activations H1..H3 (float64 values) and the output layer's inputs and
+    weights, for error bounds of the GPU's fp32 sums."""
+    W1, b1, W2, b2, W3, b3, W4, b4 = unpack(params)
+    W1b, W2b, W3b, W4b = (bf16(w).astype(np.float64) for w in (W1, W2, W3, W4))
+    X = bf16(X).astype(np.float64)
+    H1 = bf16(np.maximum(X @ W1b + b1, 0).astype(np.float32)).astype(np.float64)
+    H2 = bf16(np.maximum(H1 @ W2b + b2, 0).astype(np.float32)).astype(np.float64)
+    H3 = bf16(np.maximum(H2 @ W3b + b3, 0).astype(np.float32)).astype(np.float64)
+    return X, (H1, H2, H3), (W1b, W2b, W3b, W4b)
+
+
+def gradient_magnitudes(params, X, base, target):
+    """Per parameter, the sum of the absolute values of the terms its gradient
+    adds up (weights: sum over rows of |input| * |upstream gradient|; biases:
+    sum of |upstream gradient|): the scale against which bf16 rounding steps
+    and fp32 summation order are measured.  The upstream gradients pass each
+    ReLU where the reference's mask is open, and also where the
+    pre-activation lies within a few bf16 steps (2^-6 relative to the sum of
+    its absolute terms) of zero, where the GPU's mask may differ."""
+    W1, b1, W2, b2, W3, b3, W4, b4 = unpack(params)
+    Xb, (H1, H2, H3), (W1b, W2b, W3b, W4b) = forward_parts(params, X)
+    rows = len(Xb)
+    pred = base + (H3 @ W4b + b4)[:, :3]
+    dY = np.zeros((rows, OUT))
+    dY[:, :3] = 2.0 * (pred - target) / (3.0 * rows)
+
+    def gate(Hin, Wb, b):
+        z = Hin @ Wb + b
+        scale = np.abs(Hin) @ np.abs(Wb) + np.abs(b)
+        return (z > 0) | (np.abs(z) <= 2.0 ** -6 * scale)
+
+    m1, m2, m3 = gate(Xb, W1b, b1), gate(H1, W2b, b2), gate(H2, W3b, b3)
+    g = np.zeros(N_PARAMS)
+    aY = np.abs(dY)
+    g[OFF_W4:OFF_B4] = (np.abs(H3).T @ aY).ravel()
+    g[OFF_B4:N_PARAMS] = aY.sum(0)
+    a3 = (aY @ np.abs(W4b).T) * m3
+    g[OFF_W3:OFF_B3] = (np.abs(H2).T @ a3).ravel()
+    g[OFF_B3:OFF_W4] = a3.sum(0)
+    a2 = (a3 @ np.abs(W3b).T) * m2
+    g[OFF_W2:OFF_B2] = (np.abs(H1).T @ a2).ravel()
+    g[OFF_B2:OFF_W3] = a2.sum(0)
+    a1 = (a2 @ np.abs(W2b).T) * m1
+    g[OFF_W1:OFF_B1] = (np.abs(Xb).T @ a1).ravel()
+    g[OFF_B1:OFF_W2] = a1.sum(0)
+    return g

@@ -187,7 +187,13 @@ def test_labels_match_numpy_restatement(lib, tmp_path):
     oracle/allocator_ref.py computes from the same eight renders per sample
     count (each render recorded separately through crAdaptiveRecord with the
     search's seeds 0x5eed0000 + k)."""
-    info = _terrain(lib, tmp_path)
+    # a panoramic eye: the horizon and the plants give entries of every count
+    info = scenes.terrain_scene(str(tmp_path), cells=128, extent=60.0, cones=300, n_omm=1500, poses=2,
+                                eye_kind="panoramic", aa_deg=(0.5, 5.0))
+    eh.lastError(lib)
+    lib.loadGlTFscene(info["gltf"].encode())
+    assert eh.lastError(lib) == ""
+    eh.gotoFirstCompoundEye(lib)
     n = lib.getCurrentEyeOmmatidialCount()
     rng = np.random.default_rng(13)
     poses = scenes.random_poses(info["height_fn"], 1, rng, 20.0)

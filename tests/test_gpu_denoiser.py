@@ -38,12 +38,24 @@ def _gradients_case(lib, rows):
     assert loss >= 0, eh.lastError(lib)
     ref_loss, ref_g = mlp_ref.forward_backward(params, X, base, target)
     assert abs(loss - ref_loss) <= 1e-4 * ref_loss + 1e-7
+    # Per element: the GPU sums in fp32 in its own order, and a bf16 rounding
+    # (hidden activations, back-propagated gradients) may land one step
+    # (2^-8 relative) apart, so each gradient may differ from the reference
+    # by a few bf16 steps of the sum of the absolute values of its terms:
+    # 2^-6 of it, elementwise.
+    mag = mlp_ref.gradient_magnitudes(params, X, base, target)
+    err = np.abs(grads.astype(np.float64) - ref_g)
+    tol = 2.0 ** -6 * mag + 1e-9
     for lo, hi, name in [(mlp_ref.OFF_W1, mlp_ref.OFF_B1, "W1"), (mlp_ref.OFF_B1, mlp_ref.OFF_W2, "b1"),
-                         (mlp_ref.OFF_W2, mlp_ref.OFF_B2, "W2"), (mlp_ref.OFF_W3, mlp_ref.OFF_B3, "W3"),
+                         (mlp_ref.OFF_W2, mlp_ref.OFF_B2, "W2"), (mlp_ref.OFF_B2, mlp_ref.OFF_W3, "b2"),
+                         (mlp_ref.OFF_W3, mlp_ref.OFF_B3, "W3"), (mlp_ref.OFF_B3, mlp_ref.OFF_W4, "b3"),
                          (mlp_ref.OFF_W4, mlp_ref.OFF_B4, "W4"), (mlp_ref.OFF_B4, mlp_ref.N_PARAMS, "b4")]:
-        a, b = grads[lo:hi].astype(np.float64), ref_g[lo:hi]
-        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
-        assert rel < 2e-2, "%s gradient relative error %.3g" % (name, rel)
+        bad = err[lo:hi] > tol[lo:hi]
+        assert not bad.any(), "%s: %d elements out of bound, worst %.3g of its bound" % (
+            name, bad.sum(), (err[lo:hi] / tol[lo:hi]).max())
+        # and in aggregate the gradients agree far more closely
+        rel = np.linalg.norm(grads[lo:hi] - ref_g[lo:hi]) / max(np.linalg.norm(ref_g[lo:hi]), 1e-30)
+        assert rel < 1e-2, "%s gradient relative error %.3g" % (name, rel)
 
 
 def test_fused_inference_matches_layer_path(lib, tmp_path):
@@ -86,19 +98,23 @@ def test_fused_inference_matches_layer_path(lib, tmp_path):
         assert lib.crDenoiserRenderPoses(poses, 3, 8, tc) == 0, eh.lastError(lib)
     finally:
         lib.crSetDenoiserKernel(1)
-    corr = np.abs(layered - base).max() + 1e-6
-    terr = np.abs(tc.reshape(-1, 3) - layered)
-    assert terr.max() <= 0.05 * corr and terr.mean() <= 0.005 * corr, (terr.max(), terr.mean(), corr)
     params = np.zeros(mlp_ref.N_PARAMS, np.float32)
     grads = np.zeros(mlp_ref.N_PARAMS, np.float32)
     assert lib.crDenoiserGradient(X[:64].copy(), base[:64].copy(), base[:64].copy(), 64, grads, params) >= 0
-    want = mlp_ref.predict(params, mlp_ref.from_bits(X), base)
-    # fp32 sums on the GPU against float64 here: bf16 roundings of hidden
-    # activations may land one step apart, so compare against the size of
-    # the correction itself.
-    scale = np.abs(want - base).max() + 1e-6
-    err = np.abs(layered - want)
-    assert err.max() <= 0.05 * scale and err.mean() <= 0.005 * scale, (err.max(), err.mean(), scale)
+    # Bounds in bf16 steps of each output's own pre-activation: a hidden bf16
+    # activation that rounds one step (2^-8 relative) apart moves the output
+    # by at most that step times its weight, so per row and channel the
+    # difference is bounded by 8 bf16 steps of sum_j |H3[j] W4[j, c]| (and the
+    # fp32 summation order by far less).
+    Xf = mlp_ref.from_bits(X)
+    _, (H1, H2, H3), (W1b, W2b, W3b, W4b) = mlp_ref.forward_parts(params, Xf)
+    mag = (np.abs(H3) @ np.abs(W4b))[:, :3]
+    tol = 2.0 ** -5 * mag + 1e-7
+    terr = np.abs(tc.reshape(-1, 3) - layered)
+    assert (terr <= tol).all(), ((terr > tol).sum(), (terr / tol).max())
+    want = mlp_ref.predict(params, Xf, base)
+    err = np.abs(layered - want)  # fp32 sums on the GPU against float64 here
+    assert (err <= tol).all(), ((err > tol).sum(), (err / tol).max())
 
 
 def test_training_beats_the_plain_low_sample_render(lib, tmp_path):

@@ -191,10 +191,49 @@ def test_autotune_changes_no_result(lib, small):
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
     # tuning did not advance the streams: a fresh eye renders the same frames
+    # (with the layout and variant of outs[0]: a smaller warp segment sums
+    # the samples in another order)
+    bt, spw = ctypes.c_int(0), ctypes.c_int(0)
+    assert lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw)) == 0
     lib.setCurrentEyeSamplesPerOmmatidium(64)
     assert lib.crAutotune(d.data_ptr(), 4, ctypes.byref(best), ms) == 0
+    times = np.zeros(18, np.float32)
+    assert lib.crGetAutotuneTimes(times, 18) == 0 and (times > 0).all()
+    assert lib.crSetRenderLayout(bt.value, spw.value) == 0 and lib.crSetRenderVariant(0) == 0
     assert np.array_equal(eh.renderPoses(lib, poses), outs[0])
     lib.crSetRenderVariant(best.value)
+    lib.crSetRenderLayout(0, 32)
+    lib.crSetBvhWidth(2)
+
+
+@pytest.mark.parametrize("spp", [48, 100, 256])
+def test_render_layouts(lib, small, spp):
+    """Block sizes 128 / 256 / 512 render the same bits, whether the chunk
+    partials of an ommatidium are summed in shared memory (blocks holding all
+    its chunk warps) or in scratch by a second kernel; warp segments of 8 or
+    16 samples give the same frames within float rounding (another summing
+    order of the same samples: same streams, same rays)."""
+    _load(lib, small["gltf"], spp)
+    poses = np.stack([scenes.pose_rows(np.array([0.2 * k, 0.6, -0.1 * k]), 0.5 * k) for k in range(3)])
+    outs = {}
+    try:
+        for block in (128, 256, 512):
+            for spw in (8, 16, 32):
+                assert lib.crSetRenderLayout(block, spw) == 0, eh.lastError(lib)
+                lib.setCurrentEyeSamplesPerOmmatidium(spp + 1)
+                lib.setCurrentEyeSamplesPerOmmatidium(spp)  # the same streams for every layout
+                # one pose per call: a small eye's multi-pose launches spread
+                # their poses over warps and keep the partials in scratch
+                outs[block, spw] = np.concatenate([eh.renderPoses(lib, poses[k:k + 1]) for k in range(len(poses))])
+                assert eh.lastError(lib) == ""
+    finally:
+        lib.crSetRenderLayout(0, 32)
+    for spw in (8, 16, 32):
+        for block in (256, 512):
+            assert np.array_equal(outs[block, spw], outs[128, spw]), (block, spw)
+    ref = outs[128, 32]
+    for spw in (8, 16):
+        np.testing.assert_allclose(outs[128, spw], ref, rtol=1e-5, atol=1e-7)
 
 
 @pytest.mark.parametrize("size", ["small", "terrain"])
