@@ -1036,16 +1036,41 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     d_vout = torch.empty_like(d_vref)
     if lib.crRenderPosesDevice(d_vposes.data_ptr(), val_poses, d_vref.data_ptr()) != 0:
         raise RuntimeError(eh.lastError(lib))
-    val_rmse, halvings = {}, 0.0
-    for h in np.arange(0.0, 4.01, 0.5):
-        if lib.crSetAllocatorHalvings(float(h)) != 0 or \
-                lib.crAdaptiveRenderPosesDevice(d_vposes.data_ptr(), val_poses, 8, d_vout.data_ptr(), None, None) != 0:
+    # Allocation rule: counts 2^(exponent * log2(predicted) - halvings).  For
+    # each exponent (1: proportional to the predicted count; 1/2: to the
+    # entry's standard deviation, Neyman allocation) the largest halvings
+    # whose validation RMSE (worst channel) stays within 90% of 1/255; then
+    # the exponent whose validation render is fastest.
+    val_rmse, rule_ms = {}, {}
+    vrays = ctypes.c_double(0.0)
+
+    def val_adaptive():
+        if lib.crAdaptiveRenderPosesDevice(d_vposes.data_ptr(), val_poses, 8, d_vout.data_ptr(), None,
+                                           ctypes.byref(vrays)) != 0:
             raise RuntimeError(eh.lastError(lib))
-        val_rmse[str(float(h))] = float(torch.sqrt(((d_vout - d_vref) ** 2).reshape(-1, 3).mean(dim=0)).max())
-        if val_rmse[str(float(h))] > 0.9 / 255.0:
-            break
-        halvings = float(h)
-    if lib.crSetAllocatorHalvings(halvings) != 0:
+
+    best_rule = None
+    for ex in (1.0, 0.75, 0.5):
+        if lib.crSetAllocatorExponent(ex) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        good = None
+        for h in np.arange(0.0, 6.01, 0.5):
+            if lib.crSetAllocatorHalvings(float(h)) != 0:
+                raise RuntimeError(eh.lastError(lib))
+            val_adaptive()
+            r = float(torch.sqrt(((d_vout - d_vref) ** 2).reshape(-1, 3).mean(dim=0)).max())
+            val_rmse["%g/%g" % (ex, h)] = (r, vrays.value)
+            if r > 0.9 / 255.0:
+                break
+            good = float(h)
+        if good is None:
+            continue
+        lib.crSetAllocatorHalvings(good)
+        rule_ms["%g/%g" % (ex, good)] = timed(val_adaptive)
+        if best_rule is None or rule_ms["%g/%g" % (ex, good)] < rule_ms["%g/%g" % best_rule]:
+            best_rule = (ex, good)
+    exponent, halvings = best_rule if best_rule else (1.0, 0.0)
+    if lib.crSetAllocatorExponent(exponent) != 0 or lib.crSetAllocatorHalvings(halvings) != 0:
         raise RuntimeError(eh.lastError(lib))
     # Ray-refill schedule of the adaptive kernel (results do not depend on
     # it): timed on the validation poses, fastest kept.  refill at 32 idle
@@ -1107,14 +1132,16 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     ms_plain_e2e = timed(plain_e2e)
     lib.crSetBvhBuilder(0)
     lib.crSetAllocatorHalvings(0)
+    lib.crSetAllocatorExponent(1.0)
     lib.crSetBvhWidth(2)  # later sections start from the two-wide BVH
     rays_plain = float(held_poses) * N * 1024
     lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
     return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
             "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms),
-            "label_histogram": lab_hist, "halvings": halvings, "validation_poses": val_poses,
-            "validation_rmse_by_halvings": val_rmse, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
+            "label_histogram": lab_hist, "exponent": exponent, "halvings": halvings, "validation_poses": val_poses,
+            "validation_rmse_and_rays_by_exponent_and_halvings": val_rmse,
+            "validation_ms_by_rule": rule_ms, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
             "train_s": t_train, "rmse_vs_plain_1024": rmse, "rmse_per_channel": rmse_ch,
             "rmse_note": "RMSE against the plain 1024-sample render, worst of the R, G, B channels; the "
                          "validation budget is picked on the worst channel too",

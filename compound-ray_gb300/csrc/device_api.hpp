@@ -396,9 +396,10 @@ cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, 
                          cudaStream_t stream);
 // Per-entry bucket level from the allocator's prediction (rows x 3) and the
 // bucket sizes (counts: kAdaptiveBuckets words, zeroed by the caller);
-// halvings: the predicted counts are divided by 2^halvings first.
+// the count rendered is 2^(exponent * log2(predicted count) - halvings).
 cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
-                           unsigned long long* counts, cudaStream_t stream, float halvings = 0.f);
+                           unsigned long long* counts, cudaStream_t stream, float halvings = 0.f,
+                           float exponent = 1.f);
 // Entry lists of rows = P x N entries, pose by pose and within a pose in the
 // eye's `order` (null: index order): bucket k's entries go to
 // entries[bucketBase[k]...] (bucketBase: device, kAdaptiveBuckets words);

@@ -1871,6 +1871,7 @@ struct DenoiseState {
   std::vector<uint16_t> lastLabels;
   double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
   float allocHalvings = 0.f;  // predicted counts are divided by 2^allocHalvings (crSetAllocatorHalvings)
+  float allocExponent = 1.f;  // counts follow the predicted count to this power (crSetAllocatorExponent)
 };
 
 DenoiseState& DS() {
@@ -2355,6 +2356,17 @@ int crSetAllocatorHalvings(float halvings) {
 
 float crGetAllocatorHalvings(void) { return DS().allocHalvings; }
 
+int crSetAllocatorExponent(float exponent) {
+  if (!(exponent >= 0.25f) || exponent > 1.f) {
+    setError("crSetAllocatorExponent: the value must lie in [0.25, 1]");
+    return -1;
+  }
+  DS().allocExponent = exponent;
+  return 0;
+}
+
+float crGetAllocatorExponent(void) { return DS().allocExponent; }
+
 int crAllocatorLoad(const char* path) {
   return guarded(
       "crAllocatorLoad",
@@ -2414,7 +2426,8 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           d.level.ensure(rows);
           d.counts.ensure(kAdaptiveBuckets);
           check(cudaMemsetAsync(d.counts.ptr, 0, kAdaptiveBuckets * 8, st), "cudaMemset");
-          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st, d.allocHalvings), "allocation");
+          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st, d.allocHalvings, d.allocExponent),
+                "allocation");
           unsigned long long cnt[kAdaptiveBuckets];
           check(cudaMemcpyAsync(cnt, d.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st), "cudaMemcpy");
           check(cudaStreamSynchronize(st), "allocation");

@@ -2294,16 +2294,21 @@ __global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows
 // outputs; the predicted count is 2^(10 l)): level = bucket index 0..8 of
 // 4 << index samples, 0x80 | 8 for a fallback entry (more than 1024 needed),
 // or kNoRender (at most featureSpp samples needed: the feature render suffices).
-// halvings: the predicted count (capped at 2048) is divided by 2^halvings
-// first, halvings >= 0 and possibly fractional (the per-entry error budget
-// traded for rays; a halving of 1 or more leaves no fallback).
+// The count rendered is 2^(exponent * log2(predicted) - halvings), the
+// predicted count capped at 2048: exponent 1 divides every predicted count by
+// 2^halvings (halvings >= 0, possibly fractional: the per-entry error budget
+// traded for rays; a halving of 1 or more leaves no fallback); exponent 1/2
+// renders counts proportional to the square root of the predicted count,
+// i.e. to the entry's standard deviation, which for a fixed number of rays
+// minimises the summed squared error of all entries (Neyman allocation).
 __global__ void allocateKernel(const float* __restrict__ pred, uint64_t rows, uint32_t featureSpp,
-                               uint8_t* __restrict__ level, unsigned long long* __restrict__ counts, float halvings) {
+                               uint8_t* __restrict__ level, unsigned long long* __restrict__ counts, float halvings,
+                               float exponent) {
   const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= rows) return;
   const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
   const float l10 = l * 10.0f;
-  float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) - halvings - 1e-3f) : 2.0f;  // NaN: the least count
+  float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) * exponent - halvings - 1e-3f) : 2.0f;  // NaN: the least count
   if (!(kf >= 2.0f)) kf = 2.0f;
   if (kf > 11.0f) kf = 11.0f;
   const int k = static_cast<int>(kf);
@@ -2603,10 +2608,10 @@ cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, 
 }
 
 cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
-                           unsigned long long* counts, cudaStream_t stream, float halvings) {
+                           unsigned long long* counts, cudaStream_t stream, float halvings, float exponent) {
   if (rows == 0) return cudaSuccess;
   allocateKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(pred, rows, featureSpp, level,
-                                                                                  counts, halvings);
+                                                                                  counts, halvings, exponent);
   return cudaGetLastError();
 }
 

@@ -159,6 +159,9 @@ def configureExtras(eyeRenderer):
     L.crSetAllocatorHalvings.argtypes = [c_float]
     L.crSetAllocatorHalvings.restype = c_int
     L.crGetAllocatorHalvings.restype = c_float
+    L.crSetAllocatorExponent.argtypes = [c_float]
+    L.crSetAllocatorExponent.restype = c_int
+    L.crGetAllocatorExponent.restype = c_float
     L.crAdaptiveRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p, c_void_p, c_void_p]
     L.crAdaptiveRenderPosesDevice.restype = c_int
     L.crAdaptiveRecord.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int, c_ulonglong,

@@ -311,6 +311,16 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
  * counterpart in the reference. */
 int crSetAllocatorHalvings(float halvings);
 float crGetAllocatorHalvings(void);
+/* No counterpart in the reference.  Shape of the allocation: the count
+ * rendered for an entry is 2^(exponent * log2(predicted count) - halvings),
+ * exponent in [0.25, 1] (default 1: proportional to the predicted count).
+ * The predicted count is the one that brings the entry's standard deviation
+ * to 1/512, so it grows with the entry's variance; exponent 1/2 makes the
+ * rendered count proportional to the standard deviation instead, which for
+ * a given number of rays minimises the aggregate squared error (Neyman
+ * allocation).  0 on success. */
+int crSetAllocatorExponent(float exponent);
+float crGetAllocatorExponent(void);
 /* No counterpart in the reference.  Ray-refill schedule of the adaptive
  * render: each warp works through a pool of up to 256 samples, traversing in
  * bursts of `steps` BVH steps; between bursts its idle lanes take new samples

@@ -181,6 +181,27 @@ def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
     assert lib.crSetAllocatorHalvings(6.5) == -1
     assert "[0, 6]" in eh.lastError(lib)
 
+    # the allocation exponent: at 1/2 every entry's count exponent is half of
+    # its exponent-1 value, rounded up (within the rounding of the prediction)
+    try:
+        lib.loadGlTFscene(info["gltf"].encode())
+        eh.gotoFirstCompoundEye(lib)
+        assert lib.crSetAllocatorExponent(0.5) == 0 and lib.crGetAllocatorExponent() == 0.5
+        l3 = torch.zeros_like(lev)
+        assert lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), 4, 8, torch.zeros_like(out).data_ptr(),
+                                               l3.data_ptr(), None) == 0, eh.lastError(lib)
+        torch.cuda.synchronize()
+    finally:
+        lib.crSetAllocatorExponent(1.0)
+    lv3 = l3.cpu().numpy().astype(np.int64)
+    k3 = np.where(lv3 == 0xFF, 3, np.where(lv3 == 0x88, 11, (lv3 & 0x7F) + 2))
+    lo = np.maximum(k0 // 2, 2)        # ceil((k0 - 1) / 2)
+    hi = np.maximum((k0 + 1) // 2, 2)  # ceil(k0 / 2)
+    feature_only = lv3 == 0xFF         # count <= 8 = the feature render's: exponent <= 3
+    ok = np.where(feature_only, lo <= 3, (k3 >= lo) & (k3 <= hi))
+    assert ok.all(), (k0[~ok][:10], lv3[~ok][:10])
+    assert lib.crSetAllocatorExponent(0.1) == -1
+
 
 def test_labels_match_numpy_restatement(lib, tmp_path):
     """The GPU minimum-sample search gives, entry by entry, the labels that

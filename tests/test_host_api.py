@@ -218,6 +218,10 @@ def test_setter_ranges(lib):
     assert "[0, 6]" in eh.lastError(lib)
     assert lib.crSetAllocatorHalvings(2.5) == 0 and lib.crGetAllocatorHalvings() == 2.5
     assert lib.crSetAllocatorHalvings(0) == 0 and lib.crGetAllocatorHalvings() == 0.0
+    assert lib.crSetAllocatorExponent(0.2) == -1 and "[0.25, 1]" in eh.lastError(lib)
+    assert lib.crSetAllocatorExponent(1.5) == -1
+    assert lib.crSetAllocatorExponent(0.5) == 0 and lib.crGetAllocatorExponent() == 0.5
+    assert lib.crSetAllocatorExponent(1.0) == 0
     assert lib.crSetCutRadius(1.5) == -1
     assert "[0, 1]" in eh.lastError(lib)
     assert lib.crSetRenderVariant(lib.crGetRenderVariantCount()) == -1
