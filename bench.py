@@ -437,6 +437,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         clocks.start()
+        torch.cuda.nvtx.range_push("timed_steps")  # the launch list captures this range: ncu --nvtx-include timed_steps/
         for _ in range(args.steps):
             flush.fill_(1.0)
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chunks]
@@ -446,6 +447,7 @@ def run_ours(args):
             launch_ms.extend(zip([n for _, n in chunks], ms))
             step_ms.append(sum(ms))
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         clocks.stop()
     if lib.crSynchronize() != 0:
         raise RuntimeError(eh.lastError(lib))
@@ -1054,7 +1056,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
         if lib.crSetAllocatorExponent(ex) != 0:
             raise RuntimeError(eh.lastError(lib))
         good = None
-        for h in np.arange(0.0, 6.01, 0.5):
+        for h in np.arange(-2.0, 6.01, 0.5):
             if lib.crSetAllocatorHalvings(float(h)) != 0:
                 raise RuntimeError(eh.lastError(lib))
             val_adaptive()

@@ -2346,8 +2346,8 @@ int crAllocatorSave(const char* path) {
 }
 
 int crSetAllocatorHalvings(float halvings) {
-  if (!(halvings >= 0.f) || halvings > 6.f) {
-    setError("crSetAllocatorHalvings: the value must lie in [0, 6]");
+  if (!(halvings >= -4.f) || halvings > 6.f) {
+    setError("crSetAllocatorHalvings: the value must lie in [-4, 6]");
     return -1;
   }
   DS().allocHalvings = halvings;

@@ -303,8 +303,9 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
                                 double* raysTraced);
 /* Error budget of the adaptive render: every predicted count (capped at
  * 2048) is divided by 2^halvings before it is rounded up to a bucket
- * (0 <= halvings <= 6, fractions allowed; 0, the default, renders each entry
- * to the 1/512 standard deviation of its label).  Each halving raises an
+ * (-4 <= halvings <= 6, fractions allowed; 0, the default, renders each entry
+ * to the 1/512 standard deviation of its label; negative values render more
+ * samples than predicted, up to 1024).  Each halving raises an
  * extra-sampled entry's expected error by about sqrt(2); from 1 on no entry
  * falls back to the plain 1024-sample render.  Callers pick the largest
  * value that keeps their aggregate error target on validation poses.  No

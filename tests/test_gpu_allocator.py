@@ -179,7 +179,7 @@ def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
     assert np.array_equal(lv[1], np.where(k1 <= 3, 0xFF, k1 - 2))
     assert rs[1] < rs[0]
     assert lib.crSetAllocatorHalvings(6.5) == -1
-    assert "[0, 6]" in eh.lastError(lib)
+    assert "[-4, 6]" in eh.lastError(lib)
 
     # the allocation exponent: at 1/2 every entry's count exponent is half of
     # its exponent-1 value, rounded up (within the rounding of the prediction)

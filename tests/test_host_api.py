@@ -212,10 +212,11 @@ def test_error_contract(lib, tmp_path):
 def test_setter_ranges(lib):
     """Host-side argument checks of the tuning setters (no GPU work)."""
     eh.lastError(lib)
-    assert lib.crSetAllocatorHalvings(-0.5) == -1
-    assert "[0, 6]" in eh.lastError(lib)
+    assert lib.crSetAllocatorHalvings(-4.5) == -1
+    assert "[-4, 6]" in eh.lastError(lib)
     assert lib.crSetAllocatorHalvings(float("nan")) == -1
-    assert "[0, 6]" in eh.lastError(lib)
+    assert "[-4, 6]" in eh.lastError(lib)
+    assert lib.crSetAllocatorHalvings(-1.5) == 0 and lib.crGetAllocatorHalvings() == -1.5
     assert lib.crSetAllocatorHalvings(2.5) == 0 and lib.crGetAllocatorHalvings() == 2.5
     assert lib.crSetAllocatorHalvings(0) == 0 and lib.crGetAllocatorHalvings() == 0.0
     assert lib.crSetAllocatorExponent(0.2) == -1 and "[0.25, 1]" in eh.lastError(lib)
