@@ -1091,6 +1091,16 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     best_sched = min(sched_ms, key=sched_ms.get)
     if lib.crSetAdaptiveSchedule(*[int(x) for x in best_sched.split("/")]) != 0:
         raise RuntimeError(eh.lastError(lib))
+    # Occupancy of the adaptive kernel (resident blocks per SM, i.e. its
+    # register budget), with that schedule.
+    occ_ms = {}
+    for blocks in (5, 6, 8):
+        if lib.crSetAdaptiveOccupancy(blocks) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        occ_ms[str(blocks)] = timed(val_render)
+    best_occ = int(min(occ_ms, key=occ_ms.get))
+    if lib.crSetAdaptiveOccupancy(best_occ) != 0:
+        raise RuntimeError(eh.lastError(lib))
     del d_vref, d_vout
     if profile:
         adaptive()
@@ -1135,12 +1145,14 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     lib.crSetBvhBuilder(0)
     lib.crSetAllocatorHalvings(0)
     lib.crSetAllocatorExponent(1.0)
+    lib.crSetAdaptiveOccupancy(5)
     lib.crSetBvhWidth(2)  # later sections start from the two-wide BVH
     rays_plain = float(held_poses) * N * 1024
     lab_hist = {str(int(v)): int((labels == v).sum()) for v in np.unique(labels)}
     return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
-            "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms),
+            "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms,
+                             adaptive_blocks_per_sm=best_occ, adaptive_ms_by_blocks_per_sm=occ_ms),
             "label_histogram": lab_hist, "exponent": exponent, "halvings": halvings, "validation_poses": val_poses,
             "validation_rmse_and_rays_by_exponent_and_halvings": val_rmse,
             "validation_ms_by_rule": rule_ms, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,

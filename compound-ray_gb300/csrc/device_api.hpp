@@ -344,6 +344,9 @@ struct AdaptiveLaunch {
   // refillIdle of its 32 lanes are idle, checking every `steps` BVH steps.
   uint32_t refillIdle = 16;
   int steps = 16;
+  // Resident 128-thread blocks per SM the kernel's register budget is sized
+  // for on the two-wide BVH: 5 (96 registers), 6 (80) or 8 (64).
+  int blocksPerSM = 5;
 };
 // Table of the non-empty buckets among nBuckets (entries, counts, spp and
 // partial buffers per bucket) with their warp-task offsets.
@@ -354,6 +357,10 @@ AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* coun
 // check every `steps` BVH steps (1..4096).  Results do not depend on it.
 void setAdaptiveSchedule(uint32_t refillIdle, int steps);
 void adaptiveSchedule(uint32_t* refillIdle, int* steps);
+// The process-wide occupancy of the adaptive kernel (5, 6 or 8 blocks per
+// SM; other values mean 5).  Results do not depend on it.
+void setAdaptiveBlocksPerSM(int blocks);
+int adaptiveBlocksPerSM();
 size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
 // One launch over every bucket: sums[3e..3e+2] = mean sample colour of entry
 // e, samples drawn from the Philox4x32-10 stream (seed, e * 1024 + s).  rec:

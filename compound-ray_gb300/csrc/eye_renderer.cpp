@@ -2508,6 +2508,20 @@ int crGetAdaptiveSchedule(int* refillIdle, int* steps) {
       -1);
 }
 
+int crSetAdaptiveOccupancy(int blocksPerSM) {
+  return guarded(
+      "crSetAdaptiveOccupancy",
+      [&]() -> int {
+        if (blocksPerSM != 5 && blocksPerSM != 6 && blocksPerSM != 8)
+          throw std::runtime_error("blocksPerSM must be 5, 6 or 8");
+        setAdaptiveBlocksPerSM(blocksPerSM);
+        return 0;
+      },
+      -1);
+}
+
+int crGetAdaptiveOccupancy(void) { return adaptiveBlocksPerSM(); }
+
 int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long long seed, void* records,
                      float* sums) {
   return guarded(

@@ -2013,8 +2013,8 @@ constexpr uint32_t kAdaptiveWarps = 4;  // warps per 128-thread block
 
 __device__ __forceinline__ uint32_t lanesBelow(uint32_t lane) { return (1u << lane) - 1u; }
 
-template <int kWidth>
-__global__ void __launch_bounds__(128, 5)
+template <int kWidth, int kMinBlocks = 5>
+__global__ void __launch_bounds__(128, kMinBlocks)
     adaptiveKernel(DevScene sc, const float4* __restrict__ omm, uint32_t N, const float4* __restrict__ poses,
                    AdaptiveLaunch L, unsigned long long seed, float* __restrict__ sums, uint32_t* errFlag,
                    RayRecord* __restrict__ rec, const float4* __restrict__ cuts) {
@@ -2418,6 +2418,7 @@ __global__ void adaptiveFinishKernel(const uint8_t* __restrict__ level, uint64_t
 
 static uint32_t g_refillIdle = 16;
 static int g_refillSteps = 16;
+static int g_adaptiveBlocks = 5;
 
 void setAdaptiveSchedule(uint32_t refillIdle, int steps) {
   g_refillIdle = refillIdle < 1 ? 1u : (refillIdle > 32 ? 32u : refillIdle);
@@ -2427,6 +2428,8 @@ void adaptiveSchedule(uint32_t* refillIdle, int* steps) {
   *refillIdle = g_refillIdle;
   *steps = g_refillSteps;
 }
+void setAdaptiveBlocksPerSM(int blocks) { g_adaptiveBlocks = (blocks == 6 || blocks == 8) ? blocks : 5; }
+int adaptiveBlocksPerSM() { return g_adaptiveBlocks; }
 
 AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* counts, const uint32_t* spp,
                             float* const* partials, uint32_t nBuckets) {
@@ -2452,6 +2455,7 @@ AdaptiveLaunch planAdaptive(const uint32_t* const* entries, const uint64_t* coun
   L.totalPools = pools;
   L.refillIdle = g_refillIdle;
   L.steps = g_refillSteps;
+  L.blocksPerSM = g_adaptiveBlocks;
   return L;
 }
 
@@ -2586,9 +2590,16 @@ cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N,
       adaptiveKernel<8><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
                                                                            rec, nullptr);
       break;
-    default:
-      adaptiveKernel<2><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums, errFlag,
-                                                                           rec, cuts);
+    default:  // the two-wide BVH: the register budget follows L.blocksPerSM (6: 80, 8: 64, else 96 registers)
+      if (L.blocksPerSM == 8)
+        adaptiveKernel<2, 8><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums,
+                                                                                errFlag, rec, cuts);
+      else if (L.blocksPerSM == 6)
+        adaptiveKernel<2, 6><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums,
+                                                                                errFlag, rec, cuts);
+      else
+        adaptiveKernel<2, 5><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, omm, N, poses, L, seed, sums,
+                                                                                errFlag, rec, cuts);
       break;
   }
   cudaError_t e = cudaGetLastError();

@@ -184,6 +184,7 @@ def configureExtras(eyeRenderer):
     L.crGetRenderLayout.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.crGetAutotuneTimes.argtypes = [f32, c_size_t]
     L.crSetAdaptiveSchedule.argtypes = [c_int, c_int]
+    L.crSetAdaptiveOccupancy.argtypes = [c_int]
     L.crGetAdaptiveSchedule.argtypes = [ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.crDenoiserAdamStep.argtypes = [f32, f32, f32, f32, c_size_t, c_float, c_float, c_float,
                                      ndpointer(np.uint16, flags="C_CONTIGUOUS")]

@@ -330,6 +330,12 @@ float crGetAllocatorExponent(void);
  * on it (each entry's samples are summed in a fixed order).  0 on success. */
 int crSetAdaptiveSchedule(int refillIdle, int steps);
 int crGetAdaptiveSchedule(int* refillIdle, int* steps);
+/* No counterpart in the reference.  Occupancy of the adaptive render's kernel
+ * on the two-wide BVH: resident 128-thread blocks per SM its register budget
+ * is sized for, 5 (96 registers, the default), 6 (80) or 8 (64).  Results do
+ * not depend on it.  0 on success. */
+int crSetAdaptiveOccupancy(int blocksPerSM);
+int crGetAdaptiveOccupancy(void);
 /* Test access: `spp` Philox samples per (pose, ommatidium) of host poses
  * with one seed, recording every ray (records: count x N x spp, as
  * crRenderFrameRecorded) and the per-entry means (sums: count x N x 3). */

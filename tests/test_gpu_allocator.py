@@ -60,6 +60,17 @@ def test_adaptive_kernel_matches_oracle(lib, small, small_ref):
         lib.crSetCutRadius(0.0)
     assert np.array_equal(rec2["hitId"], rec.reshape(-1)["hitId"])
     assert np.array_equal(sums2, sums)
+    # neither do the kernel's occupancy (register budget) and refill schedule
+    try:
+        for blocks, sched in ((6, (16, 8)), (8, (32, 32))):
+            assert lib.crSetAdaptiveOccupancy(blocks) == 0 and lib.crSetAdaptiveSchedule(*sched) == 0
+            sums3 = np.zeros_like(sums)
+            assert lib.crAdaptiveRecord(poses, 2, spp, 7, rec2.ctypes.data, sums3) == 0, eh.lastError(lib)
+            assert np.array_equal(sums3, sums), blocks
+    finally:
+        lib.crSetAdaptiveOccupancy(5)
+        lib.crSetAdaptiveSchedule(16, 16)
+    assert lib.crSetAdaptiveOccupancy(7) == -1
     # normal / uniform draws look like N(0,1) / U(0,1]
     nd, ud = rec["normalDraw"].ravel(), rec["uniformDraw"].ravel()
     assert abs(nd.mean()) < 0.02 and abs(nd.std() - 1) < 0.02
