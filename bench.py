@@ -65,9 +65,20 @@ def parse_args():
     return ap.parse_args()
 
 
-# Kernels per 256-pose render launch besides the cut kernel: the render
-# kernel (its chunk partials are summed inside the launch).
-RENDER_KERNELS_PER_LAUNCH = 1
+def render_kernels_per_launch(spp, layout, cut_fraction):
+    """The library's kernels in one render launch under the autotuned layout
+    (the rule of render.cu planRender): the near-field cut when a radius is
+    set, the render kernel, and the chunk sums when an ommatidium's samples
+    span several warp segments and a block cannot hold all of them."""
+    block, spw = layout
+    spw = 32 if spw in (0, 32) else spw
+    chunks = -(-spp // spw)
+    bw = block // 32
+    if bw == 0:
+        bw = next((c for c in (4, 8, 16) if chunks <= c and c % chunks == 0), 4)
+    in_block = chunks > 1 and bw % chunks == 0
+    return 1 + (1 if cut_fraction > 0 else 0) + (1 if chunks > 1 and not in_block else 0)
+
 
 
 def bench_config(info, P):
@@ -529,8 +540,9 @@ def run_ours(args):
                                      "bvh_width_2_4_8": [round(float(x), 3) for x in tune_all[15:18]]},
                      "bvh_width": bvh_width},
         # per 256-pose launch: the poses' near-field cuts (when a radius is
-        # set) and the render kernel
-        "gpu_launches": args.steps * len(chunks) * (RENDER_KERNELS_PER_LAUNCH + (1 if cut_fraction > 0 else 0)),
+        # set), the render kernel and, when the layout keeps chunk partials in
+        # scratch, their sums
+        "gpu_launches": args.steps * len(chunks) * render_kernels_per_launch(spp, layout, cut_fraction),
         "roofline": {"bound": "issue", "achieved": issue_achieved, "peak": issue_peak,
                      "unit": "T warp instructions/s", "frac": (issue_achieved / issue_peak) if counters else None,
                      "traffic": traffic,
