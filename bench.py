@@ -1064,7 +1064,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
             raise RuntimeError(eh.lastError(lib))
 
     best_rule = None
-    for ex in (1.0, 0.75, 0.5):
+    for ex in (1.0, 0.75, 0.625, 0.5):
         if lib.crSetAllocatorExponent(ex) != 0:
             raise RuntimeError(eh.lastError(lib))
         good = None

@@ -2018,9 +2018,12 @@ __global__ void __launch_bounds__(128, kMinBlocks)
     adaptiveKernel(DevScene sc, const float4* __restrict__ omm, uint32_t N, const float4* __restrict__ poses,
                    AdaptiveLaunch L, unsigned long long seed, float* __restrict__ sums, uint32_t* errFlag,
                    RayRecord* __restrict__ rec, const float4* __restrict__ cuts) {
-  __shared__ uint32_t sortKey[kAdaptiveWarps][kPoolSlots], sortIdx[kAdaptiveWarps][kPoolSlots];
+  __shared__ uint32_t sortIdx[kAdaptiveWarps][kPoolSlots];
   __shared__ float2 slotDraw[kAdaptiveWarps][kPoolSlots];  // by sample position k within its task segment
-  __shared__ float slotCol[kAdaptiveWarps][3][kPoolSlots];  // unscaled colour of every slot
+  // Unscaled colour of every slot; its red plane holds the sort keys first
+  // (the keys are dead once sorted, before any colour is written), so that
+  // the block needs 24 KB and 8 blocks fit on an SM.
+  __shared__ float slotCol[kAdaptiveWarps][3][kPoolSlots];
   const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
   const uint32_t pool = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // totalPools < 2^26 (checked at launch)
   if (pool >= L.totalPools) return;  // whole warps
@@ -2038,7 +2041,7 @@ __global__ void __launch_bounds__(128, kMinBlocks)
   const uint32_t nTasks = left < tpp ? static_cast<uint32_t>(left) : tpp;
   const uint32_t nSlots = nTasks * spl * 32u;
   const bool sorted = spl > 1 && sc.triCount >= kAdaptiveSortMinTris;
-  uint32_t* key = sortKey[w];
+  uint32_t* key = reinterpret_cast<uint32_t*>(slotCol[w][0]);
   uint32_t* idx = sortIdx[w];
   float2* draw = slotDraw[w];
   float* colR = slotCol[w][0];
