@@ -198,21 +198,26 @@ def test_denoiser_gains_on_the_small_scene(lib, small, tmp_path):
         d = (a.astype(np.float64) - b).reshape(-1, 3)
         return float(np.sqrt((d * d).mean(axis=0)).max())
 
+    def fetch(t):
+        # The library renders on its own stream: wait for it before reading.
+        assert lib.crSynchronize() == 0, eh.lastError(lib)
+        return t.cpu().numpy()
+
     d_val, d_held = dev(val), dev(held)
     out_val = torch.empty((200, N, 3), dtype=torch.float32, device="cuda")
     out_held = torch.empty((1000, N, 3), dtype=torch.float32, device="cuda")
     lib.setCurrentEyeSamplesPerOmmatidium(1024)
     assert lib.crRenderPosesDevice(d_val.data_ptr(), 200, out_val.data_ptr()) == 0
-    val_ref = out_val.cpu().numpy()
+    val_ref = fetch(out_val)
     assert lib.crRenderPosesDevice(d_held.data_ptr(), 1000, out_held.data_ptr()) == 0
-    held_ref = out_held.cpu().numpy()
+    held_ref = fetch(out_held)
     lib.setCurrentEyeSamplesPerOmmatidium(8)
     assert lib.crRenderPosesDevice(d_held.data_ptr(), 1000, out_held.data_ptr()) == 0
-    plain8 = out_held.cpu().numpy()
+    plain8 = fetch(out_held)
 
     def val_rmse():
         assert lib.crDenoiserRenderPosesDevice(d_val.data_ptr(), 200, 8, out_val.data_ptr()) == 0, eh.lastError(lib)
-        return worst(out_val.cpu().numpy(), val_ref)
+        return worst(fetch(out_val), val_ref)
 
     ck = lambda name: str(tmp_path / name).encode()
     assert lib.crDenoiserSave(ck("init.bin")) == 0
@@ -230,7 +235,7 @@ def test_denoiser_gains_on_the_small_scene(lib, small, tmp_path):
     alpha = min(by_alpha, key=by_alpha.get)
     assert lib.crDenoiserLoad(ck("s%d.bin" % best)) == 0 and lib.crDenoiserScaleOutput(alpha) == 0
     assert lib.crDenoiserRenderPosesDevice(d_held.data_ptr(), 1000, 8, out_held.data_ptr()) == 0
-    learned = out_held.cpu().numpy()
+    learned = fetch(out_held)
     r_learned, r_plain = worst(learned, held_ref), worst(plain8, held_ref)
     print("steps", by_steps, "alpha", by_alpha, "held-out", r_learned, r_plain)
     assert r_learned < r_plain, (r_learned, r_plain, by_steps, by_alpha)
