@@ -500,10 +500,11 @@ def run_ours(args):
     # Roofline of the render kernel.  Its limit is instruction issue: warp
     # instructions per ray (ncu, committed summary, this variant and cut) x
     # live rays/s against 4 schedulers x 1 instruction per cycle on every SM
-    # at the maximum clock.  The per-ray demand bytes (node, triangle and
-    # shading fetches, state, output) are served by L1/L2 -- the scene fits
-    # the 129 MB L2 -- so their rate is reported against an L2-resident copy
-    # measured here, not against HBM.
+    # at the maximum clock.  The secondary entry is the kernel's L2 traffic
+    # (lts__t_bytes of the same capture) at this run's rate against an
+    # L2-resident copy measured here -- the scene fits the 129 MB L2.  The
+    # per-ray demand bytes (node, triangle and shading fetches) are reported
+    # beside it; L1 serves most of them.
     full = [ms for n, ms in launch_ms if n == POSES_PER_LAUNCH] or [ms for _, ms in launch_ms]
     launch_n = POSES_PER_LAUNCH if len(full) and P >= POSES_PER_LAUNCH else P
     rays_launch = launch_n * N * spp
@@ -512,7 +513,6 @@ def run_ours(args):
     launch_s = statistics.mean(full) / 1000.0
     hbm_peak, src = peaks()
     l2_peak = l2_copy_gbs(dev)
-    l2_achieved = per_ray * rays_launch / launch_s / 1e9
     counters, why = launch_counters(best.value, cut_fraction, layout) if launch_n == POSES_PER_LAUNCH \
         else (None, "partial launch")
     issue_peak = 4.0 * SM_COUNT * sm_max_mhz() * 1e6 / 1e12  # T warp instructions/s
@@ -520,8 +520,11 @@ def run_ours(args):
         instr_per_ray = counters["warp_instructions"] / counters["rays"]
         issue_achieved = instr_per_ray * rays_launch / launch_s / 1e12
         traffic = counters["dram_bytes"]
+        # L2 traffic (lts__t_bytes of the same capture) at this run's rate
+        l2_per_ray = counters["l2_bytes"] / counters["rays"]
+        l2_achieved = l2_per_ray * rays_launch / launch_s / 1e9
     else:
-        instr_per_ray = issue_achieved = traffic = None
+        instr_per_ray = issue_achieved = traffic = l2_per_ray = l2_achieved = None
     clk = clocks.summary()
     line = {
         "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -551,10 +554,16 @@ def run_ours(args):
                      "counters_file": os.path.relpath(COUNTERS_MD, ROOT),
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of the render kernel on one "
                                      "256-pose launch (ncu, same file)",
-                     "l2": {"achieved": l2_achieved, "peak": l2_peak, "unit": "GB/s", "frac": l2_achieved / l2_peak,
-                            "bytes_per_ray": per_ray,
+                     "l2": {"achieved": l2_achieved, "peak": l2_peak, "unit": "GB/s",
+                            "frac": (l2_achieved / l2_peak) if counters else None,
+                            "bytes_per_ray": l2_per_ray,
+                            "bytes_source": "lts__t_bytes.sum of the render kernel on one 256-pose launch (ncu, "
+                                            "counters file)",
                             "peak_source": "32 MB L2-resident device copy, read + write bytes, best of 20, "
                                            "measured in this run"},
+                     "demand_bytes_per_ray": per_ray,
+                     "demand_note": "node, triangle and shading bytes the traversal requests per ray; L1 serves "
+                                    "most of them, so they are not an L2 or DRAM figure",
                      "hbm_peak_gbs": hbm_peak, "hbm_peak_source": src,
                      "node_visits_per_ray": nodes.value, "tri_tests_per_ray": tris.value,
                      "hit_fraction": hit_frac, "launch_ms": statistics.mean(full), "rays_per_launch": rays_launch,

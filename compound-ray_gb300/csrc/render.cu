@@ -2035,6 +2035,9 @@ __global__ void __launch_bounds__(128, kMinBlocks)
   const uint32_t perWarp = 32u / segWidth;
   const uint32_t spl = adaptiveSamplesPerLane(spp);  // rounds per task
   const uint32_t chunks = adaptiveChunks(spp);
+  // segWidth, spl and chunks are powers of two (spp is): their logarithms
+  // turn the slot arithmetic below into shifts and masks.
+  const uint32_t lsw = __ffs(segWidth) - 1, lspl = __ffs(spl) - 1, lch = __ffs(chunks) - 1;
   const uint32_t tpp = kPoolRounds / spl;  // tasks per pool
   const uint64_t task0 = static_cast<uint64_t>(pool - B.poolBase) * tpp;
   const uint64_t left = B.tasks - task0;
@@ -2052,26 +2055,26 @@ __global__ void __launch_bounds__(128, kMinBlocks)
   // Slot j of the pool: round r = j / 32 of task q = r / spl, lane position
   // j % 32.  Entry (index within the bucket) and sample of a slot:
   auto slotEntry = [&](uint32_t j) -> uint32_t {
-    const uint64_t t = task0 + (j >> 5) / spl;
-    const uint64_t group = t / chunks;
-    return static_cast<uint32_t>(group * perWarp + (j & 31u) / segWidth);
+    const uint64_t t = task0 + ((j >> 5) >> lspl);
+    const uint64_t group = t >> lch;
+    return static_cast<uint32_t>(group * perWarp + ((j & 31u) >> lsw));
   };
   // Sample position k within the task's segment (slot j's draws are draw[seg + k]).
   auto slotK = [&](uint32_t j) -> uint32_t {
-    const uint32_t q = (j >> 5) / spl, seg = q * spl * 32u, pos = j - seg;
-    return spl > 1 ? (sorted ? idx[seg + pos] : pos) : (j & 31u) % segWidth;
+    const uint32_t seg = j & ~((32u << lspl) - 1u), pos = j - seg;
+    return spl > 1 ? (sorted ? idx[seg + pos] : pos) : (j & (segWidth - 1u));
   };
   auto slotSample = [&](uint32_t j, uint32_t k) -> uint32_t {
-    const uint64_t t = task0 + (j >> 5) / spl;
-    const uint32_t chunk = static_cast<uint32_t>(t % chunks);
-    return chunk * 32u * spl + k;
+    const uint64_t t = task0 + ((j >> 5) >> lspl);
+    const uint32_t chunk = static_cast<uint32_t>(t) & (chunks - 1u);
+    return (chunk << (5 + lspl)) + k;
   };
 
   // 1. Random numbers (and sort keys) of every slot.
   for (uint32_t j = lane; j < nSlots; j += 32u) {
     const uint32_t i = slotEntry(j);
-    const uint32_t q = (j >> 5) / spl, seg = q * spl * 32u;
-    const uint32_t k = spl > 1 ? j - seg : (j & 31u) % segWidth;
+    const uint32_t seg = j & ~((32u << lspl) - 1u);
+    const uint32_t k = spl > 1 ? j - seg : (j & (segWidth - 1u));
     float2 d = make_float2(0.f, 0.f);
     if (i < B.count) {
       curandStatePhilox4_32_10_t st;
@@ -2087,12 +2090,12 @@ __global__ void __launch_bounds__(128, kMinBlocks)
   }
   __syncwarp();
   if (sorted) {  // bitonic sort of each task's (key, position) pairs, ascending
-    const uint32_t n = 32u * spl;
+    const uint32_t n = 32u * spl, lhalf = 4 + lspl;  // n / 2 = 2^lhalf compare-exchanges per task
     for (uint32_t size = 2; size <= n; size <<= 1)
-      for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t ls = __ffs(size) - 2, stride = size >> 1; stride > 0; stride >>= 1, --ls) {
         for (uint32_t m = lane; m < nSlots / 2; m += 32u) {
-          const uint32_t seg = (m / (n / 2)) * n, mm = m % (n / 2);
-          const uint32_t lo = seg + 2u * stride * (mm / stride) + (mm % stride), hi = lo + stride;
+          const uint32_t seg = (m >> lhalf) << (lhalf + 1), mm = m & ((1u << lhalf) - 1u);
+          const uint32_t lo = seg + (((mm >> ls) << ls) << 1) + (mm & (stride - 1u)), hi = lo + stride;
           const bool up = ((lo - seg) & size) == 0u;
           const uint32_t ka = key[lo], kb = key[hi];
           if ((ka > kb) == up) {
@@ -2170,8 +2173,7 @@ __global__ void __launch_bounds__(128, kMinBlocks)
             slot = static_cast<int>(j);
             const uint32_t e = B.entries[i];
             const uint32_t p = e / N, o = e - p * N;
-            const uint32_t q = (j >> 5) / spl;
-            const float2 d = draw[spl > 1 ? q * spl * 32u + slotK(j) : j];
+            const float2 d = draw[spl > 1 ? (j & ~((32u << lspl) - 1u)) + slotK(j) : j];
             nd = d.x;
             ud = d.y;
             const float4 a = __ldg(omm + 2 * o), b = __ldg(omm + 2 * o + 1);
@@ -2237,11 +2239,11 @@ __global__ void __launch_bounds__(128, kMinBlocks)
       col.y += __shfl_xor_sync(0xffffffffu, col.y, static_cast<int>(m));
       col.z += __shfl_xor_sync(0xffffffffu, col.z, static_cast<int>(m));
     }
-    const uint32_t j0 = q * spl * 32u + lane;
+    const uint32_t j0 = (q << (5 + lspl)) + lane;
     const uint32_t i = slotEntry(j0);
-    if ((lane % segWidth) == 0u && i < B.count) {
+    if ((lane & (segWidth - 1u)) == 0u && i < B.count) {
       const uint64_t t = task0 + q;
-      const uint32_t chunk = static_cast<uint32_t>(t % chunks);
+      const uint32_t chunk = static_cast<uint32_t>(t) & (chunks - 1u);
       float* dst = chunks == 1 ? sums + 3 * static_cast<size_t>(B.entries[i])
                                : B.partials + (static_cast<size_t>(i) * chunks + chunk) * 3;
       dst[0] = col.x;
@@ -2308,23 +2310,29 @@ __global__ void allocateKernel(const float* __restrict__ pred, uint64_t rows, ui
                                uint8_t* __restrict__ level, unsigned long long* __restrict__ counts, float halvings,
                                float exponent) {
   const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= rows) return;
-  const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
-  const float l10 = l * 10.0f;
-  float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) * exponent - halvings - 1e-3f) : 2.0f;  // NaN: the least count
-  if (!(kf >= 2.0f)) kf = 2.0f;
-  if (kf > 11.0f) kf = 11.0f;
-  const int k = static_cast<int>(kf);
-  uint8_t lv;
-  if ((1u << k) <= featureSpp) {
-    lv = kNoRender;
-  } else if (k == 11) {
-    lv = 0x80 | 8;
-  } else {
-    lv = static_cast<uint8_t>(k - 2);
+  int bucket = -1;  // counted bucket of this row (-1: none)
+  if (e < rows) {
+    const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
+    const float l10 = l * 10.0f;
+    float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) * exponent - halvings - 1e-3f) : 2.0f;  // NaN: the least count
+    if (!(kf >= 2.0f)) kf = 2.0f;
+    if (kf > 11.0f) kf = 11.0f;
+    const int k = static_cast<int>(kf);
+    uint8_t lv;
+    if ((1u << k) <= featureSpp) {
+      lv = kNoRender;
+    } else if (k == 11) {
+      lv = 0x80 | 8;
+    } else {
+      lv = static_cast<uint8_t>(k - 2);
+    }
+    level[e] = lv;
+    if (lv != kNoRender) bucket = lv & 0x7f;
   }
-  level[e] = lv;
-  if (lv != kNoRender) atomicAdd(counts + (lv & 0x7f), 1ull);
+  // One atomic per bucket and warp (blockDim is a multiple of 32).
+  const unsigned peers = __match_any_sync(0xffffffffu, bucket);
+  if (bucket >= 0 && (threadIdx.x & 31u) == static_cast<unsigned>(__ffs(peers) - 1))
+    atomicAdd(counts + bucket, static_cast<unsigned long long>(__popc(peers)));
 }
 
 // Ordered bucket lists in three steps, so that every bucket lists its
@@ -2357,17 +2365,24 @@ __global__ void __launch_bounds__(kScatterTile) bucketCountKernel(const uint8_t*
     tileCounts[static_cast<size_t>(blockIdx.x) * kAdaptiveBuckets + threadIdx.x] = cnt[threadIdx.x];
 }
 
-// One thread per bucket: tileCounts[t][k] becomes the first slot of tile t's
-// bucket-k entries (bucket k starting at bucketBase[k]).
+// One warp per bucket: tileCounts[t][k] becomes the first slot of tile t's
+// bucket-k entries (bucket k starting at bucketBase[k]); the warp scans 32
+// tiles per step with shuffles.
 __global__ void bucketScanKernel(unsigned long long* __restrict__ tileCounts, uint64_t tiles,
                                  const unsigned long long* __restrict__ bucketBase) {
-  const int k = threadIdx.x;
-  if (k >= static_cast<int>(kAdaptiveBuckets)) return;
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (k >= static_cast<int>(kAdaptiveBuckets)) return;  // whole warps
   unsigned long long run = bucketBase[k];
-  for (uint64_t t = 0; t < tiles; ++t) {
-    const unsigned long long c = tileCounts[t * kAdaptiveBuckets + k];
-    tileCounts[t * kAdaptiveBuckets + k] = run;
-    run += c;
+  for (uint64_t t0 = 0; t0 < tiles; t0 += 32) {
+    const uint64_t t = t0 + lane;
+    const unsigned long long c = t < tiles ? tileCounts[t * kAdaptiveBuckets + k] : 0ull;
+    unsigned long long inc = c;  // inclusive prefix over the warp's 32 tiles
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long o = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += o;
+    }
+    if (t < tiles) tileCounts[t * kAdaptiveBuckets + k] = run + inc - c;
+    run += __shfl_sync(0xffffffffu, inc, 31);
   }
 }
 
@@ -2641,7 +2656,7 @@ cudaError_t launchScatterBuckets(const uint8_t* level, uint64_t rows, uint32_t N
   const uint64_t tiles = (rows + kScatterTile - 1) / kScatterTile;
   if (tiles > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
   bucketCountKernel<<<static_cast<unsigned>(tiles), kScatterTile, 0, stream>>>(level, rows, N, order, scratch);
-  bucketScanKernel<<<1, 32, 0, stream>>>(scratch, tiles, bucketBase);
+  bucketScanKernel<<<1, 32 * kAdaptiveBuckets, 0, stream>>>(scratch, tiles, bucketBase);
   bucketPlaceKernel<<<static_cast<unsigned>(tiles), kScatterTile, 0, stream>>>(level, rows, N, order, scratch,
                                                                                 entries);
   return cudaGetLastError();
