@@ -1059,11 +1059,16 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     d_vout = torch.empty_like(d_vref)
     if lib.crRenderPosesDevice(d_vposes.data_ptr(), val_poses, d_vref.data_ptr()) != 0:
         raise RuntimeError(eh.lastError(lib))
-    # Allocation rule: counts 2^(exponent * log2(predicted) - halvings).  For
-    # each exponent (1: proportional to the predicted count; 1/2: to the
-    # entry's standard deviation, Neyman allocation) the largest halvings
-    # whose validation RMSE (worst channel) stays within 90% of 1/255; then
-    # the exponent whose validation render is fastest.
+    # Allocation rule: counts 2^(exponent * log2(predicted) - halvings -
+    # cost_exponent * log2(cost / 16)), cost the entry's traversal steps per
+    # ray in the feature render.  exponent 1: proportional to the predicted
+    # count; 1/2: to the entry's standard deviation (Neyman allocation);
+    # cost_exponent 1/2 with it: to sigma / sqrt(cost), the least error for
+    # a fixed render time.  Also whether the denoiser serves the entries the
+    # feature render covers (without it they keep the 8-sample mean and its
+    # inference is skipped).  For each (denoiser, cost exponent, exponent)
+    # the largest halvings whose validation RMSE (worst channel) stays
+    # within 90% of 1/255; then the rule whose validation render is fastest.
     val_rmse, rule_ms = {}, {}
     vrays = ctypes.c_double(0.0)
 
@@ -1072,28 +1077,48 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
                                            ctypes.byref(vrays)) != 0:
             raise RuntimeError(eh.lastError(lib))
 
-    best_rule = None
-    for ex in (1.0, 0.75, 0.625, 0.5):
-        if lib.crSetAllocatorExponent(ex) != 0:
-            raise RuntimeError(eh.lastError(lib))
-        good = None
-        for h in np.arange(-2.0, 6.01, 0.5):
-            if lib.crSetAllocatorHalvings(float(h)) != 0:
+    den_path = os.path.join(tempfile.gettempdir(), "cr_bench_denoiser_%s_%d.bin" % (scene, os.getpid()))
+    if lib.crDenoiserSave(den_path.encode()) != 0:
+        raise RuntimeError(eh.lastError(lib))
+
+    def use_denoiser(on):
+        if on:
+            if lib.crDenoiserInit(4) != 0 or lib.crDenoiserLoad(den_path.encode()) != 0:
                 raise RuntimeError(eh.lastError(lib))
-            val_adaptive()
-            r = float(torch.sqrt(((d_vout - d_vref) ** 2).reshape(-1, 3).mean(dim=0)).max())
-            val_rmse["%g/%g" % (ex, h)] = (r, vrays.value)
-            if r > 0.9 / 255.0:
-                break
-            good = float(h)
-        if good is None:
-            continue
-        lib.crSetAllocatorHalvings(good)
-        rule_ms["%g/%g" % (ex, good)] = timed(val_adaptive)
-        if best_rule is None or rule_ms["%g/%g" % (ex, good)] < rule_ms["%g/%g" % best_rule]:
-            best_rule = (ex, good)
-    exponent, halvings = best_rule if best_rule else (1.0, 0.0)
-    if lib.crSetAllocatorExponent(exponent) != 0 or lib.crSetAllocatorHalvings(halvings) != 0:
+        else:
+            lib.crDenoiserRelease()
+
+    best_rule = None
+    for den in (1, 0):
+        use_denoiser(den)
+        for ce in (0.0, 0.25, 0.5):
+            if lib.crSetAllocatorCostExponent(ce) != 0:
+                raise RuntimeError(eh.lastError(lib))
+            for ex in (1.0, 0.75, 0.625, 0.5):
+                if lib.crSetAllocatorExponent(ex) != 0:
+                    raise RuntimeError(eh.lastError(lib))
+                good = None
+                for h in np.arange(-3.0, 6.01, 0.5):
+                    if lib.crSetAllocatorHalvings(float(h)) != 0:
+                        raise RuntimeError(eh.lastError(lib))
+                    val_adaptive()
+                    r = float(torch.sqrt(((d_vout - d_vref) ** 2).reshape(-1, 3).mean(dim=0)).max())
+                    val_rmse["%d/%g/%g/%g" % (den, ce, ex, h)] = (r, vrays.value)
+                    if r > 0.9 / 255.0:
+                        break
+                    good = float(h)
+                if good is None:
+                    continue
+                lib.crSetAllocatorHalvings(good)
+                key = (den, ce, ex, good)
+                rule_ms["%d/%g/%g/%g" % key] = timed(val_adaptive)
+                if best_rule is None or rule_ms["%d/%g/%g/%g" % key] < rule_ms["%d/%g/%g/%g" % best_rule]:
+                    best_rule = key
+    use_denoiser_on, cost_exponent, exponent, halvings = best_rule if best_rule else (1, 0.0, 1.0, 0.0)
+    use_denoiser(use_denoiser_on)
+    os.remove(den_path)
+    if lib.crSetAllocatorExponent(exponent) != 0 or lib.crSetAllocatorHalvings(halvings) != 0 or \
+            lib.crSetAllocatorCostExponent(cost_exponent) != 0:
         raise RuntimeError(eh.lastError(lib))
     # Ray-refill schedule of the adaptive kernel (results do not depend on
     # it): timed on the validation poses, fastest kept.  refill at 32 idle
@@ -1166,6 +1191,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     lib.crSetBvhBuilder(0)
     lib.crSetAllocatorHalvings(0)
     lib.crSetAllocatorExponent(1.0)
+    lib.crSetAllocatorCostExponent(0.0)
     lib.crSetAdaptiveOccupancy(5)
     lib.crSetBvhWidth(2)  # later sections start from the two-wide BVH
     rays_plain = float(held_poses) * N * 1024
@@ -1174,8 +1200,9 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
             "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms,
                              adaptive_blocks_per_sm=best_occ, adaptive_ms_by_blocks_per_sm=occ_ms),
-            "label_histogram": lab_hist, "exponent": exponent, "halvings": halvings, "validation_poses": val_poses,
-            "validation_rmse_and_rays_by_exponent_and_halvings": val_rmse,
+            "label_histogram": lab_hist, "exponent": exponent, "halvings": halvings,
+            "cost_exponent": cost_exponent, "denoiser_used": bool(use_denoiser_on), "validation_poses": val_poses,
+            "validation_rmse_and_rays_by_denoiser_cost_exponent_exponent_halvings": val_rmse,
             "validation_ms_by_rule": rule_ms, "scene_gen_s": t_scene, "load_s": t_load, "data_s": t_data,
             "train_s": t_train, "rmse_vs_plain_1024": rmse, "rmse_per_channel": rmse_ch,
             "rmse_note": "RMSE against the plain 1024-sample render, worst of the R, G, B channels; the "

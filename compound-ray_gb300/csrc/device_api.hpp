@@ -165,10 +165,13 @@ cudaError_t launchRender(const DevScene& scene, const DevEye& eye, const float4*
 // Per-ommatidium sample statistics of a feature render (spp <= 32), each the
 // mean over the samples: colour (3), squared colour (3), hit flag, hit
 // distance (0 on a miss), hit-triangle normal facing the ray in the eye's
-// frame (3, 0 on a miss).  stats: P x N x kFeatureStats floats.
+// frame (3, 0 on a miss), and the traversal cost (BVH node visits plus
+// triangle tests; the allocator's cost term).  stats: P x N x kFeatureStats
+// floats.
 // cutsReady: eye.cuts already holds these poses' near-field cuts (else they
 // are built first when eye.cuts is set).
-constexpr int kFeatureStats = 11;
+constexpr int kFeatureStats = 12;
+constexpr int kCostStat = 11;  // index of the traversal cost in a stats row
 cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float4* poses, uint32_t P, float* stats,
                            uint32_t* errFlag, cudaStream_t stream, bool cutsReady = false);
 
@@ -403,10 +406,14 @@ cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, 
                          cudaStream_t stream);
 // Per-entry bucket level from the allocator's prediction (rows x 3) and the
 // bucket sizes (counts: kAdaptiveBuckets words, zeroed by the caller);
-// the count rendered is 2^(exponent * log2(predicted count) - halvings).
+// the count rendered is 2^(exponent * log2(predicted count) - halvings -
+// costExponent * log2(cost / kCostRef)), cost the entry's traversal cost
+// from the feature statistics (stats: rows x kFeatureStats; unused when
+// costExponent is 0).
+constexpr float kCostRef = 16.0f;
 cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
                            unsigned long long* counts, cudaStream_t stream, float halvings = 0.f,
-                           float exponent = 1.f);
+                           float exponent = 1.f, const float* stats = nullptr, float costExponent = 0.f);
 // Entry lists of rows = P x N entries, pose by pose and within a pose in the
 // eye's `order` (null: index order): bucket k's entries go to
 // entries[bucketBase[k]...] (bucketBase: device, kAdaptiveBuckets words);

@@ -1870,8 +1870,10 @@ struct DenoiseState {
   DevBuf<unsigned long long> counts, tileScratch;
   std::vector<uint16_t> lastLabels;
   double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
+  uint64_t lastPassRows = 0;  // rows of the last adaptive pass (its pred, stats and level stay in place)
   float allocHalvings = 0.f;  // predicted counts are divided by 2^allocHalvings (crSetAllocatorHalvings)
   float allocExponent = 1.f;  // counts follow the predicted count to this power (crSetAllocatorExponent)
+  float allocCostExponent = 0.f;  // counts scale as traversal cost^-this (crSetAllocatorCostExponent)
 };
 
 DenoiseState& DS() {
@@ -2367,6 +2369,17 @@ int crSetAllocatorExponent(float exponent) {
 
 float crGetAllocatorExponent(void) { return DS().allocExponent; }
 
+int crSetAllocatorCostExponent(float costExponent) {
+  if (!(costExponent >= 0.f) || costExponent > 1.f) {
+    setError("crSetAllocatorCostExponent: the value must lie in [0, 1]");
+    return -1;
+  }
+  DS().allocCostExponent = costExponent;
+  return 0;
+}
+
+float crGetAllocatorCostExponent(void) { return DS().allocCostExponent; }
+
 int crAllocatorLoad(const char* path) {
   return guarded(
       "crAllocatorLoad",
@@ -2426,7 +2439,8 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
           d.level.ensure(rows);
           d.counts.ensure(kAdaptiveBuckets);
           check(cudaMemsetAsync(d.counts.ptr, 0, kAdaptiveBuckets * 8, st), "cudaMemset");
-          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st, d.allocHalvings, d.allocExponent),
+          check(launchAllocate(d.pred.ptr, rows, fs, d.level.ptr, d.counts.ptr, st, d.allocHalvings, d.allocExponent,
+                               d.stats.ptr, d.allocCostExponent),
                 "allocation");
           unsigned long long cnt[kAdaptiveBuckets];
           check(cudaMemcpyAsync(cnt, d.counts.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, st), "cudaMemcpy");
@@ -2475,9 +2489,33 @@ int crAdaptiveRenderPosesDevice(const float* d_poses, size_t count, int featureS
             check(cudaMemcpyAsync(d_level + first * e.N, d.level.ptr, rows, cudaMemcpyDeviceToDevice, st),
                   "cudaMemcpy");
           d.adaptiveFrame += P;
+          d.lastPassRows = rows;
         }
         d.lastRays = rays;
         if (raysTraced) *raysTraced = rays;
+        return 0;
+      },
+      -1);
+}
+
+int crAdaptiveLastPass(float* prediction, float* cost, uint8_t* level, size_t rows) {
+  return guarded(
+      "crAdaptiveLastPass",
+      [&]() -> int {
+        DenoiseState& d = DS();
+        if (d.lastPassRows == 0) throw std::runtime_error("no adaptive render yet");
+        if (rows != d.lastPassRows)
+          throw std::runtime_error("rows must equal the last pass's rows (" + std::to_string(d.lastPassRows) + ")");
+        cudaStream_t st = R().stream();
+        if (prediction)
+          check(cudaMemcpyAsync(prediction, d.pred.ptr, rows * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                "cudaMemcpy");
+        if (cost)
+          check(cudaMemcpy2DAsync(cost, sizeof(float), d.stats.ptr + kCostStat, kFeatureStats * sizeof(float),
+                                  sizeof(float), rows, cudaMemcpyDeviceToHost, st),
+                "cudaMemcpy2D");
+        if (level) check(cudaMemcpyAsync(level, d.level.ptr, rows, cudaMemcpyDeviceToHost, st), "cudaMemcpy");
+        check(cudaStreamSynchronize(st), "adaptive pass copy");
         return 0;
       },
       -1);

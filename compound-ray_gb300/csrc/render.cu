@@ -1014,8 +1014,8 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
                                            RayRecord* __restrict__ rec, uint32_t& nodeVisits, uint32_t& triTests,
                                            float* __restrict__ part = nullptr) {
   constexpr bool kRecord = (kMode & 3) == 1;
-  constexpr bool kCount = (kMode & 3) == 2;
   constexpr bool kFeat = (kMode & 3) == 3;
+  constexpr bool kCount = (kMode & 3) == 2 || kFeat;  // feature mode: the per-entry traversal cost
   constexpr bool kLit = (kMode & 4) != 0;  // lighting-on shading (modes 4 render, 5 record)
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t p0 = 0, p1 = P;
@@ -1074,7 +1074,8 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
     v3 col = mk(0.f, 0.f, 0.f);
     // Feature mode: per-sample squared colour, hit flag, hit distance and the
     // hit triangle's normal in the eye's frame (facing the ray), all / spp.
-    float f2x = 0.f, f2y = 0.f, f2z = 0.f, fHit = 0.f, fT = 0.f, fnx = 0.f, fny = 0.f, fnz = 0.f;
+    float f2x = 0.f, f2y = 0.f, f2z = 0.f, fHit = 0.f, fT = 0.f, fnx = 0.f, fny = 0.f, fnz = 0.f, fCost = 0.f;
+    const uint32_t steps0 = nodeVisits + triTests;
     if (valid) {
       const float4* pp = poses + 4 * p;
       const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
@@ -1143,6 +1144,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       }
       col = c * invSpp;
       if (kFeat) {
+        fCost = static_cast<float>(nodeVisits + triTests - steps0) * invSpp;
         f2x = c.x * c.x * invSpp;
         f2y = c.y * c.y * invSpp;
         f2z = c.z * c.z * invSpp;
@@ -1173,6 +1175,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
         fnx += __shfl_xor_sync(0xffffffffu, fnx, static_cast<int>(m));
         fny += __shfl_xor_sync(0xffffffffu, fny, static_cast<int>(m));
         fnz += __shfl_xor_sync(0xffffffffu, fnz, static_cast<int>(m));
+        fCost += __shfl_xor_sync(0xffffffffu, fCost, static_cast<int>(m));
       }
     }
     if (kFeat) {
@@ -1189,6 +1192,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
         dst[8] = fnx;
         dst[9] = fny;
         dst[10] = fnz;
+        dst[kCostStat] = fCost;
       }
       continue;
     }
@@ -2306,15 +2310,25 @@ __global__ void labelKernel(const float* __restrict__ outs, int k, uint64_t rows
 // renders counts proportional to the square root of the predicted count,
 // i.e. to the entry's standard deviation, which for a fixed number of rays
 // minimises the summed squared error of all entries (Neyman allocation).
+// costExponent > 0 further divides the count by (cost / kCostRef)^costExponent,
+// cost the entry's mean BVH node visits plus triangle tests per ray in the
+// feature render (at least 1), so that for a fixed render time rather than a
+// fixed number of rays the error is smallest at exponent = costExponent = 1/2.
 __global__ void allocateKernel(const float* __restrict__ pred, uint64_t rows, uint32_t featureSpp,
                                uint8_t* __restrict__ level, unsigned long long* __restrict__ counts, float halvings,
-                               float exponent) {
+                               float exponent, const float* __restrict__ stats, float costExponent) {
   const uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   int bucket = -1;  // counted bucket of this row (-1: none)
   if (e < rows) {
     const float l = (pred[3 * e] + pred[3 * e + 1] + pred[3 * e + 2]) * (1.0f / 3.0f);
     const float l10 = l * 10.0f;
-    float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) * exponent - halvings - 1e-3f) : 2.0f;  // NaN: the least count
+    // Cost term: entries whose rays cost more get fewer of them (for a fixed
+    // render time the summed squared error is smallest with counts in
+    // proportion to sigma / sqrt(cost): exponent 1/2, costExponent 1/2).
+    const float shift =
+        costExponent != 0.0f ? costExponent * log2f(fmaxf(stats[e * kFeatureStats + kCostStat], 1.0f) / kCostRef)
+                             : 0.0f;
+    float kf = l10 == l10 ? ceilf(fminf(l10, 11.0f) * exponent - halvings - shift - 1e-3f) : 2.0f;  // NaN: least
     if (!(kf >= 2.0f)) kf = 2.0f;
     if (kf > 11.0f) kf = 11.0f;
     const int k = static_cast<int>(kf);
@@ -2637,10 +2651,12 @@ cudaError_t launchLabels(const float* outs, int k, uint64_t rows, uint32_t spp, 
 }
 
 cudaError_t launchAllocate(const float* pred, uint64_t rows, uint32_t featureSpp, uint8_t* level,
-                           unsigned long long* counts, cudaStream_t stream, float halvings, float exponent) {
+                           unsigned long long* counts, cudaStream_t stream, float halvings, float exponent,
+                           const float* stats, float costExponent) {
   if (rows == 0) return cudaSuccess;
-  allocateKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(pred, rows, featureSpp, level,
-                                                                                  counts, halvings, exponent);
+  if (costExponent != 0.0f && !stats) return cudaErrorInvalidValue;
+  allocateKernel<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, stream>>>(
+      pred, rows, featureSpp, level, counts, halvings, exponent, stats, costExponent);
   return cudaGetLastError();
 }
 

@@ -162,6 +162,11 @@ def configureExtras(eyeRenderer):
     L.crSetAllocatorExponent.argtypes = [c_float]
     L.crSetAllocatorExponent.restype = c_int
     L.crGetAllocatorExponent.restype = c_float
+    L.crSetAllocatorCostExponent.argtypes = [c_float]
+    L.crSetAllocatorCostExponent.restype = c_int
+    L.crGetAllocatorCostExponent.restype = c_float
+    L.crAdaptiveLastPass.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t]
+    L.crAdaptiveLastPass.restype = c_int
     L.crAdaptiveRenderPosesDevice.argtypes = [c_void_p, c_size_t, c_int, c_void_p, c_void_p, c_void_p]
     L.crAdaptiveRenderPosesDevice.restype = c_int
     L.crAdaptiveRecord.argtypes = [ndpointer(np.float32, flags="C_CONTIGUOUS"), c_size_t, c_int, c_ulonglong,

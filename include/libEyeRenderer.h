@@ -322,6 +322,24 @@ float crGetAllocatorHalvings(void);
  * allocation).  0 on success. */
 int crSetAllocatorExponent(float exponent);
 float crGetAllocatorExponent(void);
+/* No counterpart in the reference.  Cost term of the allocation: the count
+ * is further divided by (cost / 16)^costExponent, cost the entry's mean BVH
+ * node visits plus triangle tests per ray in the feature render (at least
+ * 1).  costExponent in [0, 1], default 0 (no cost term).  For a fixed
+ * render time, rather than a fixed number of rays, the aggregate squared
+ * error is smallest with counts in proportion to sigma / sqrt(cost):
+ * exponent 1/2 and costExponent 1/2.  0 on success. */
+int crSetAllocatorCostExponent(float costExponent);
+float crGetAllocatorCostExponent(void);
+/* No counterpart in the reference.  Copies what the last pass of the last
+ * crAdaptiveRenderPosesDevice call decided (a call covers its poses in
+ * passes of at least 256 poses and up to 2^21 entries): per entry (pose-
+ * major, rows = poses of the pass x ommatidia) the allocator's three outputs
+ * (prediction: rows x 3 floats; the predicted count is 2^(10 x their mean)),
+ * the feature render's traversal cost (cost: rows floats) and the level
+ * (level: rows bytes, as crAdaptiveRenderPosesDevice writes it).  Any
+ * pointer may be null.  rows must equal the pass's rows.  0 on success. */
+int crAdaptiveLastPass(float* prediction, float* cost, uint8_t* level, size_t rows);
 /* No counterpart in the reference.  Ray-refill schedule of the adaptive
  * render: each warp works through a pool of up to 256 samples, traversing in
  * bursts of `steps` BVH steps; between bursts its idle lanes take new samples

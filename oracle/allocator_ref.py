@@ -50,3 +50,34 @@ def min_sample_labels(renders, thr):
     for c in counts:
         label_pass(renders[c], c, thr, label)
     return label
+
+
+NO_RENDER = 0xFF  # level of an entry whose feature render suffices (kNoRender)
+COST_REF = 16.0
+
+
+def allocate_levels(pred, cost, feature_spp, halvings, exponent, cost_exponent):
+    """Bucket level of every entry as the GPU allocateKernel
+    (compound-ray_gb300/csrc/render.cu) decides it: the predicted count is
+    2^(10 l), l the mean of the allocator's three outputs (pred: rows x 3);
+    the count rendered is 2^k with k = ceil(exponent * min(10 l, 11) -
+    halvings - cost_exponent * log2(max(cost, 1) / 16) - 1e-3) clamped to
+    [2, 11]; 2^k <= feature_spp -> NO_RENDER, k = 11 -> 0x80 | 8 (fallback
+    to a 1024-sample render alone), else k - 2.
+    Returns (levels uint8, near) where `near` marks entries whose ceil
+    argument lies within 1e-4 of an integer: the GPU's log2 is the fast
+    hardware approximation, so the level there may differ by one."""
+    f = np.float32
+    pred = np.asarray(pred, np.float32).reshape(-1, 3)
+    cost = np.asarray(cost, np.float32).reshape(-1)
+    l = (pred[:, 0] + pred[:, 1] + pred[:, 2]) * f(1.0 / 3.0)
+    l10 = l * f(10.0)
+    shift = (f(cost_exponent) * np.log2(np.maximum(cost, f(1.0)) / f(COST_REF)).astype(np.float32)
+             if cost_exponent != 0 else np.zeros_like(l10))
+    arg = np.minimum(l10, f(11.0)) * f(exponent) - f(halvings) - shift - f(1e-3)
+    near = np.abs(arg - np.round(arg)) < 1e-4
+    kf = np.ceil(arg)
+    kf = np.where(np.isnan(l10), f(2.0), kf)
+    kf = np.clip(np.where(kf >= 2.0, kf, 2.0), 2.0, 11.0).astype(np.int64)
+    lv = np.where((1 << kf) <= feature_spp, NO_RENDER, np.where(kf == 11, 0x80 | 8, kf - 2)).astype(np.uint8)
+    return lv, near

@@ -213,6 +213,36 @@ def test_allocator_labels_training_and_adaptive_render(lib, tmp_path):
     assert ok.all(), (k0[~ok][:10], lv3[~ok][:10])
     assert lib.crSetAllocatorExponent(0.1) == -1
 
+    # Entry by entry against the numpy restatement of the allocation, from
+    # the last pass's predictions and traversal costs, with every term on.
+    rows = 4 * n
+    for ex, h, ce in ((1.0, 0.0, 0.0), (0.75, -0.5, 0.5), (0.5, 1.5, 1.0)):
+        try:
+            assert lib.crSetAllocatorExponent(ex) == 0 and lib.crSetAllocatorHalvings(h) == 0
+            assert lib.crSetAllocatorCostExponent(ce) == 0
+            l4 = torch.zeros_like(lev)
+            assert lib.crAdaptiveRenderPosesDevice(d_poses.data_ptr(), 4, 8, torch.zeros_like(out).data_ptr(),
+                                                   l4.data_ptr(), None) == 0, eh.lastError(lib)
+            torch.cuda.synchronize()
+        finally:
+            lib.crSetAllocatorExponent(1.0)
+            lib.crSetAllocatorHalvings(0.0)
+            lib.crSetAllocatorCostExponent(0.0)
+        pred = np.zeros((rows, 3), np.float32)
+        cost = np.zeros(rows, np.float32)
+        lvl = np.zeros(rows, np.uint8)
+        assert lib.crAdaptiveLastPass(pred.ctypes.data, cost.ctypes.data, lvl.ctypes.data, rows) == 0, \
+            eh.lastError(lib)
+        assert np.array_equal(lvl, l4.cpu().numpy().reshape(-1))
+        # traversal cost: mean node visits + triangle tests per ray, every
+        # entry of this terrain eye traverses something
+        assert np.isfinite(cost).all() and (cost >= 0).all() and cost.mean() > 1.0
+        want, near = allocator_ref.allocate_levels(pred, cost, 8, h, ex, ce)
+        assert near.mean() < 0.01
+        assert np.array_equal(lvl[~near], want[~near]), (ex, h, ce, lvl[~near][:8], want[~near][:8])
+    assert lib.crAdaptiveLastPass(None, None, None, rows + 1) == -1
+    assert "rows must equal" in eh.lastError(lib)
+
 
 def test_labels_match_numpy_restatement(lib, tmp_path):
     """The GPU minimum-sample search gives, entry by entry, the labels that

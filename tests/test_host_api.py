@@ -223,6 +223,10 @@ def test_setter_ranges(lib):
     assert lib.crSetAllocatorExponent(1.5) == -1
     assert lib.crSetAllocatorExponent(0.5) == 0 and lib.crGetAllocatorExponent() == 0.5
     assert lib.crSetAllocatorExponent(1.0) == 0
+    assert lib.crSetAllocatorCostExponent(-0.1) == -1 and "[0, 1]" in eh.lastError(lib)
+    assert lib.crSetAllocatorCostExponent(float("nan")) == -1
+    assert lib.crSetAllocatorCostExponent(0.5) == 0 and lib.crGetAllocatorCostExponent() == 0.5
+    assert lib.crSetAllocatorCostExponent(0.0) == 0
     assert lib.crSetCutRadius(1.5) == -1
     assert "[0, 1]" in eh.lastError(lib)
     assert lib.crSetRenderVariant(lib.crGetRenderVariantCount()) == -1

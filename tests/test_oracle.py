@@ -193,3 +193,28 @@ def test_label_restatement_rules():
     assert lab[3] == 0
     assert 4 < lab[1] < lab[2] or lab[2] == 0
     assert lab[4] > 4
+
+
+def test_allocation_restatement_rules():
+    """oracle/allocator_ref.allocate_levels: counts 2^ceil(exponent * log2
+    predicted - halvings - cost term), clamped to [4, 2048]; at most the
+    feature render's count -> no render; 2048 -> the 1024 fallback; a NaN
+    prediction gets the least count; the cost term halves the count of an
+    entry 4x costlier at cost exponent 1/2."""
+    import allocator_ref
+
+    NR = allocator_ref.NO_RENDER
+    # predicted counts 2^(10 l): l = 0.3 -> 8, 0.5 -> 32, 0.8 -> 256, 1.2 -> capped at 2048
+    pred = np.repeat(np.array([[0.3], [0.5], [0.8], [1.2], [np.nan]], np.float32), 3, axis=1)
+    cost = np.full(5, 16.0, np.float32)
+    lv, near = allocator_ref.allocate_levels(pred, cost, 8, 0.0, 1.0, 0.0)
+    assert not near[:4].any()
+    assert lv.tolist() == [NR, 3, 6, 0x88, NR]  # 8 <= feature spp; 32 = 4 << 3; 256 = 4 << 6; fallback; NaN
+    lv, _ = allocator_ref.allocate_levels(pred, cost, 8, 1.0, 1.0, 0.0)
+    assert lv.tolist() == [NR, 2, 5, 8, NR]  # one halving: every count halves, the fallback joins 1024
+    lv, _ = allocator_ref.allocate_levels(pred, cost, 8, 0.0, 0.5, 0.0)
+    assert lv.tolist() == [NR, NR, 2, 4, NR]  # square root: 2^ceil(1.5), 2^ceil(2.5) = 8, 2^4, 2^ceil(5.5)
+    lv, _ = allocator_ref.allocate_levels(pred, np.full(5, 64.0, np.float32), 8, 0.0, 1.0, 0.5)
+    assert lv.tolist() == [NR, 2, 5, 8, NR]  # cost 4 x 16 at cost exponent 1/2: one halving
+    lv, _ = allocator_ref.allocate_levels(pred, np.full(5, 0.25, np.float32), 8, 0.0, 1.0, 0.5)
+    assert lv.tolist() == [3, 5, 8, 0x88, NR]  # cost below 1 counts as 1 = 16 / 2^4: 2^(4 x 1/2) times more
