@@ -1130,7 +1130,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
             raise RuntimeError(eh.lastError(lib))
 
     for idle in (8, 16, 24, 32):
-        for steps in (8, 16, 32):
+        for steps in (8, 16, 32, 128):
             if lib.crSetAdaptiveSchedule(idle, steps) != 0:
                 raise RuntimeError(eh.lastError(lib))
             sched_ms["%d/%d" % (idle, steps)] = timed(val_render)

@@ -75,6 +75,14 @@ struct DevEye {
   float4* cuts = nullptr;
   float cutRadius = 0.f;
   float maxRel = 0.f;
+  // philox: the random numbers come from counter-based Philox4x32-10
+  //       streams (philoxSeed, ((frame0 + p) * N + o) * spp + s) for pose p
+  //       of the launch, ommatidium o and sample s: no generator states and
+  //       no pre-drawn numbers, so a launch may spread its poses over any
+  //       number of warps (feature renders).
+  bool philox = false;
+  unsigned long long philoxSeed = 0;
+  unsigned long long frame0 = 0;
 };
 // Traversal stack entries of the wide BVH (a node pushes up to W - 1).
 constexpr int kWideStackEntries = 128;

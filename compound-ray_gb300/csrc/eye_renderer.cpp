@@ -1852,9 +1852,9 @@ struct DenoiseState {
   size_t cam = static_cast<size_t>(-1);
   uint64_t generation = ~0ull;
   DevBuf<int> nb;
-  DevBuf<uint32_t> featRng, targetRng;
-  uint32_t featSpp = 0, targetSpp = 0;
-  bool featReady = false, targetReady = false;
+  DevBuf<uint32_t> targetRng;  // XORWOW streams of the 1024-sample training targets
+  uint32_t targetSpp = 0;
+  bool targetReady = false;
   DevBuf<float> stats, base, out, scratch;
   DevBuf<float4> derived, axes;  // inputs of the tcgen05 inference (deriveFeatureStats)
   DevBuf<uint16_t> X;
@@ -1870,6 +1870,7 @@ struct DenoiseState {
   DevBuf<unsigned long long> counts, tileScratch;
   std::vector<uint16_t> lastLabels;
   double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
+  uint64_t featFrame = 0;  // feature-render frames of the current eye so far (the Philox stream position)
   uint64_t lastPassRows = 0;  // rows of the last adaptive pass (its pred, stats and level stay in place)
   float allocHalvings = 0.f;  // predicted counts are divided by 2^allocHalvings (crSetAllocatorHalvings)
   float allocExponent = 1.f;  // counts follow the predicted count to this power (crSetAllocatorExponent)
@@ -1892,9 +1893,10 @@ EyeDev& denoiseEye(Renderer& r, DenoiseState& d) {
     d.nb.release();
     d.nb.ensure(std::max<size_t>(1, static_cast<size_t>(kNeighbours) * e.N));
     check(nearestOmmatidia(e.omm.ptr, e.N, d.nb.ptr, r.stream()), "neighbour search");
-    d.featReady = d.targetReady = false;
-    d.featSpp = d.targetSpp = 0;
+    d.targetReady = false;
+    d.targetSpp = 0;
     d.adaptiveFrame = 0;
+    d.featFrame = 0;
   }
   return e;
 }
@@ -1921,30 +1923,28 @@ DevEye streamsFor(Renderer& r, EyeDev& e, DevBuf<uint32_t>& rng, uint32_t& haveS
 // Feature render of `count` poses into d.stats; with `rows`, also the
 // feature rows and residual bases (d.X, d.base) the training set and the
 // layer-by-layer path use.
+constexpr unsigned long long kFeatureSeed = 0xfea70000ull;  // Philox key of the feature renders
+
 void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dposes, size_t count, uint32_t featSpp,
                      bool rows = true) {
   if (featSpp < 1 || featSpp > 32) throw std::runtime_error("feature renders use 1 to 32 samples per ommatidium");
-  const DevEye fe = streamsFor(r, e, d.featRng, d.featSpp, d.featReady, featSpp);
+  if (count > 0xffffffffull) throw std::runtime_error("too many poses in one feature render");
+  // Counter-based Philox streams: frame (featFrame + p) of the eye, so all
+  // poses render in one launch spread over any number of warps; reloading
+  // the scene or switching eyes restarts the frame count.
+  DevEye fe;
+  fe.omm = e.omm.ptr;
+  fe.order = e.order.ptr;
+  fe.N = e.N;
+  fe.spp = featSpp;
+  fe.philox = true;
+  fe.philoxSeed = kFeatureSeed;
+  fe.frame0 = d.featFrame;
+  d.featFrame += count;
   d.stats.ensure(std::max<size_t>(1, count * e.N * kFeatureStats));
-  // The near-field cuts of all poses in one launch (one thread per pose).
-  DevEye all = fe;
-  r.withCuts(all, static_cast<uint32_t>(count), e.maxRel);
-  if (all.cuts)
-    check(launchCuts(r.dev, dposes, static_cast<uint32_t>(count), all.cutRadius, all.maxRel, all.cuts, r.stream()),
-          "cuts");
-  for (size_t first = 0; first < count; first += kMaxPosesPerLaunch) {
-    const uint32_t P = static_cast<uint32_t>(std::min<size_t>(kMaxPosesPerLaunch, count - first));
-    DevEye de = fe;
-    r.withDraws(de, P, true);
-    if (all.cuts) {
-      de.cuts = all.cuts + first * kCutStride;
-      de.cutRadius = all.cutRadius;
-      de.maxRel = all.maxRel;
-    }
-    check(launchFeatures(r.dev, de, dposes + 4 * first, P, d.stats.ptr + first * e.N * kFeatureStats, r.errWord(),
-                         r.stream(), true),
-          "feature render");
-  }
+  r.withCuts(fe, static_cast<uint32_t>(count), e.maxRel);
+  check(launchFeatures(r.dev, fe, dposes, static_cast<uint32_t>(count), d.stats.ptr, r.errWord(), r.stream(), false),
+        "feature render");
   if (!rows) return;
   d.X.ensure(std::max<size_t>(1, count * e.N * kFeatureWidth));
   d.base.ensure(std::max<size_t>(1, count * e.N * 3));

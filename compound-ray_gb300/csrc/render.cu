@@ -1055,7 +1055,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   v3 axis = mk(0.f, 1.f, 0.f), relPos = mk(0.f, 0.f, 0.f), perp = mk(0.f, 0.f, 1.f);
   float sd = 0.f, fpo = 0.f;
   if (valid) {
-    if (!eye.draws) loadState(eye.rng, plane, sidx, st);
+    if (!kFeat && !eye.draws) loadState(eye.rng, plane, sidx, st);
     const float4 a = __ldg(eye.omm + 2 * o);
     const float4 b = __ldg(eye.omm + 2 * o + 1);
     axis = mk(a.w, b.x, b.y);
@@ -1080,7 +1080,12 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       const float4* pp = poses + 4 * p;
       const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
       float nd, ud;
-      if (eye.draws) {
+      if (kFeat) {  // feature renders draw from counter-based streams (launchFeatures requires eye.philox)
+        curandStatePhilox4_32_10_t ps;
+        curand_init(eye.philoxSeed, ((eye.frame0 + p) * eye.N + o) * eye.spp + s, 0ull, &ps);
+        nd = curand_normal(&ps);
+        ud = curand_uniform(&ps);
+      } else if (eye.draws) {
         const float2 dr = eye.draws[(static_cast<size_t>(p) * eye.N + o) * eye.spp + s];
         nd = dr.x;
         ud = dr.y;
@@ -1203,7 +1208,7 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       dst[2] = col.z;
     }
   }
-  if (valid && !eye.draws) storeState(eye.rng, plane, sidx, st);
+  if (!kFeat && valid && !eye.draws) storeState(eye.rng, plane, sidx, st);
 }
 
 // kRegs: registers per thread the kernel is compiled for (the autotuner's
@@ -1700,9 +1705,9 @@ WarpPlan planRender(uint32_t N, uint32_t spp, uint32_t P, bool forceScratch, boo
 
 // Cuts the poses of a pre-drawn launch into ranges so that about kFillWarps
 // warp tasks exist.
-WarpPlan splitPoses(WarpPlan plan, uint32_t P) {
-  if (P < 2 || plan.tasks >= kFillWarps / 2) return plan;
-  uint64_t S = (kFillWarps + plan.tasks - 1) / plan.tasks;
+WarpPlan splitPoses(WarpPlan plan, uint32_t P, uint64_t fill = kFillWarps) {
+  if (P < 2 || plan.tasks >= fill / 2) return plan;
+  uint64_t S = (fill + plan.tasks - 1) / plan.tasks;
   if (S > P) S = P;
   const uint32_t pps = static_cast<uint32_t>((P + S - 1) / S);
   plan.posesPerSplit = pps;
@@ -1867,13 +1872,10 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
   if (P == 0 || eye.N == 0) return cudaSuccess;
   WarpPlan plan = planWarps(eye.N, eye.spp);
   if (plan.chunks != 1) return cudaErrorInvalidValue;  // feature renders use at most 32 samples
-  if (eye.draws) {
-    const size_t total = static_cast<size_t>(eye.N) * eye.spp;
-    drawsKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(eye, P);
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    plan = splitPoses(plan, P);
-  }
+  if (!eye.philox) return cudaErrorInvalidValue;  // feature renders draw from Philox streams
+  // Counter-based draws: spread the poses over enough warps for about a
+  // dozen waves, so that the last one costs little.
+  plan = splitPoses(plan, P, 4 * kFillWarps);
   if (eye.cuts && !cutsReady) {
     if (!(eye.cutRadius > 0.f)) return cudaErrorInvalidValue;
     cutKernel<<<(P + 63) / 64, 64, 0, stream>>>(scene, poses, P, eye.cutRadius, eye.maxRel, eye.cuts);
