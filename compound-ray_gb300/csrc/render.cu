@@ -548,16 +548,28 @@ __device__ __forceinline__ void traceClosest(const DevScene& sc, const Ray& r, f
   traverseFrom<kCount>(sc, r, tmin, h, stack, sp, node, errFlag, nodeVisits, triTests, restart, guard, dlen);
 }
 
-// traverseFrom in bursts: at most `budget` loop iterations (node visits or
-// leaves) from the saved position (node, sp, restart; the stack holds the
-// deferred entries), which is updated in place.  Returns true when the search
-// is over (h holds the closest hit), false when the budget ran out first.
-// Lets a warp stop every few steps to hand finished lanes new rays.
+// traverseFrom in bursts: at most `budget` steps (node visits or leaves)
+// from the saved position (node, sp, restart; the stack holds the deferred
+// entries), which is updated in place.  Returns true when the search is over
+// (h holds the closest hit), false when the budget ran out first.  Lets a
+// warp stop every few steps to hand finished lanes new rays.  Each lane
+// visits the nodes and leaves in traverseFrom's order, but the loop is
+// "while-while" (Aila and Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): a lane descends inner nodes until it holds
+// a leaf, and the warp tests leaves together, so lanes at inner nodes and
+// lanes at leaves do not alternate step by step.  On the adaptive kernel's
+// rays this is about 5% faster than the single-loop form; on the plain
+// kernel's coherent rays it was not (its traverseFrom keeps one loop).
 __device__ __forceinline__ bool traverseBurst(const DevScene& sc, const Ray& r, float tmin, Hit& h, int* stack,
                                               int& sp, int& node, bool& restart, float guard, float dlen,
                                               uint32_t* errFlag, int budget) {
-  for (int it = 0; it < budget; ++it) {
-    if (node >= 0) {
+  int it = 0;
+  for (;;) {
+    // Inner nodes until this lane reaches a leaf, the end of the search or
+    // the budget.
+    while (node >= 0) {
+      if (it >= budget) return false;
+      ++it;
       const float4* n = sc.nodes + 4 * node;
       const float4 n0 = __ldg(n + 0);
       const float4 n1 = __ldg(n + 1);
@@ -590,7 +602,21 @@ __device__ __forceinline__ bool traverseBurst(const DevScene& sc, const Ray& r, 
         node = n3.y;
         continue;
       }
-    } else {
+      if (sp == 0) {
+        if (restart) {
+          restart = false;
+          if (!(h.id != 0xffffffffu && h.t * dlen <= guard)) {
+            node = 0;
+            continue;
+          }
+        }
+        return true;
+      }
+      node = stack[--sp];
+    }
+    if (it >= budget) return false;
+    ++it;
+    {
       const uint32_t code = ~static_cast<uint32_t>(node);
       const uint32_t first = code >> 3;
       const uint32_t count = (code & 7u) + 1u;
@@ -611,7 +637,6 @@ __device__ __forceinline__ bool traverseBurst(const DevScene& sc, const Ray& r, 
     }
     node = stack[--sp];
   }
-  return false;
 }
 
 // Near-field cut of one pose: at most kCutEntries BVH subtrees (box + ref)
