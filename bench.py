@@ -1147,6 +1147,16 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     best_occ = int(min(occ_ms, key=occ_ms.get))
     if lib.crSetAdaptiveOccupancy(best_occ) != 0:
         raise RuntimeError(eh.lastError(lib))
+    # Near-field cut of the adaptive render (results do not depend on it):
+    # the plain render's tuned radius or none, whichever renders the
+    # validation poses faster.  Each render below runs with its own radius.
+    cut_ms = {}
+    for c in sorted({cut, 0.0}):
+        if lib.crSetCutRadius(c) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        cut_ms["%g" % c] = timed(val_render)
+    adaptive_cut = float(min(cut_ms, key=cut_ms.get))
+    lib.crSetCutRadius(adaptive_cut)
     del d_vref, d_vout
     if profile:
         adaptive()
@@ -1156,7 +1166,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         print(json.dumps({"profile_case": "adaptive learned render of %d held-out poses, twice" % held_poses,
-                          "rays": rays.value, "variant": best.value, "cut": cut}))
+                          "rays": rays.value, "variant": best.value, "cut": adaptive_cut}))
         return None
     ms_adaptive = timed(adaptive)
     img = d_out.cpu().numpy()
@@ -1166,6 +1176,7 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
         if lib.crRenderPosesDevice(d_poses.data_ptr(), held_poses, d_out.data_ptr()) != 0:
             raise RuntimeError(eh.lastError(lib))
 
+    lib.crSetCutRadius(cut)
     ms_plain = timed(plain)
     ref = d_out.cpu().numpy()
     rmse_ch = rmse_per_channel(img, ref)
@@ -1186,7 +1197,9 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
         plain()
         h_out.copy_(d_out, non_blocking=True)
 
+    lib.crSetCutRadius(adaptive_cut)
     ms_adaptive_e2e = timed(adaptive_e2e)
+    lib.crSetCutRadius(cut)
     ms_plain_e2e = timed(plain_e2e)
     lib.crSetBvhBuilder(0)
     lib.crSetAllocatorHalvings(0)
@@ -1199,7 +1212,8 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     return {"scene": label % N,
             "train_poses": train_poses, "held_out_poses": held_poses, "threshold": threshold, "seeds": seeds,
             "autotune": dict(tuned, refill_schedule=best_sched, refill_ms_by_idle_lanes_and_steps=sched_ms,
-                             adaptive_blocks_per_sm=best_occ, adaptive_ms_by_blocks_per_sm=occ_ms),
+                             adaptive_blocks_per_sm=best_occ, adaptive_ms_by_blocks_per_sm=occ_ms,
+                             adaptive_cut_fraction=adaptive_cut, adaptive_ms_by_cut_fraction=cut_ms),
             "label_histogram": lab_hist, "exponent": exponent, "halvings": halvings,
             "cost_exponent": cost_exponent, "denoiser_used": bool(use_denoiser_on), "validation_poses": val_poses,
             "validation_rmse_and_rays_by_denoiser_cost_exponent_exponent_halvings": val_rmse,
