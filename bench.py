@@ -1077,6 +1077,20 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
                                            ctypes.byref(vrays)) != 0:
             raise RuntimeError(eh.lastError(lib))
 
+    # Near-field cut of the adaptive render first: the plain render's tuned
+    # radius or none, whichever renders the validation poses faster (default
+    # rule).  The cut changes no ray's hit, but the feature render's
+    # traversal costs depend on it, and with a cost term so does the
+    # allocation: the rule below is chosen under the cut the held-out
+    # render uses.  Each render below runs with its own radius.
+    cut_ms = {}
+    for c in sorted({cut, 0.0}):
+        if lib.crSetCutRadius(c) != 0:
+            raise RuntimeError(eh.lastError(lib))
+        cut_ms["%g" % c] = timed(val_adaptive)
+    adaptive_cut = float(min(cut_ms, key=cut_ms.get))
+    lib.crSetCutRadius(adaptive_cut)
+
     den_path = os.path.join(tempfile.gettempdir(), "cr_bench_denoiser_%s_%d.bin" % (scene, os.getpid()))
     if lib.crDenoiserSave(den_path.encode()) != 0:
         raise RuntimeError(eh.lastError(lib))
@@ -1147,16 +1161,6 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     best_occ = int(min(occ_ms, key=occ_ms.get))
     if lib.crSetAdaptiveOccupancy(best_occ) != 0:
         raise RuntimeError(eh.lastError(lib))
-    # Near-field cut of the adaptive render (results do not depend on it):
-    # the plain render's tuned radius or none, whichever renders the
-    # validation poses faster.  Each render below runs with its own radius.
-    cut_ms = {}
-    for c in sorted({cut, 0.0}):
-        if lib.crSetCutRadius(c) != 0:
-            raise RuntimeError(eh.lastError(lib))
-        cut_ms["%g" % c] = timed(val_render)
-    adaptive_cut = float(min(cut_ms, key=cut_ms.get))
-    lib.crSetCutRadius(adaptive_cut)
     del d_vref, d_vout
     if profile:
         adaptive()

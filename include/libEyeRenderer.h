@@ -328,7 +328,10 @@ float crGetAllocatorExponent(void);
  * 1).  costExponent in [0, 1], default 0 (no cost term).  For a fixed
  * render time, rather than a fixed number of rays, the aggregate squared
  * error is smallest with counts in proportion to sigma / sqrt(cost):
- * exponent 1/2 and costExponent 1/2.  0 on success. */
+ * exponent 1/2 and costExponent 1/2.  With a cost term the allocation
+ * depends on how the rays traverse: the near-field cut radius, the BVH
+ * builder and its width change the costs, and so which entries get how many
+ * samples (no ray's hit changes).  0 on success. */
 int crSetAllocatorCostExponent(float costExponent);
 float crGetAllocatorCostExponent(void);
 /* No counterpart in the reference.  Copies what the last pass of the last
