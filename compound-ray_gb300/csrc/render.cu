@@ -2020,8 +2020,9 @@ __device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
 // rounds of 32 sample slots, and works through it with ray refill (warp-level
 // ray compaction):
 //   1. the random numbers of every slot of the pool are drawn first, all 32
-//      lanes busy (Philox4x32-10 stream (seed, e * 1024 + s): one normal,
-//      then one uniform; O(1) set-up per sample).  With more than 32 samples
+//      lanes busy (netDraw: sample s of entry e is point s of a digitally
+//      shifted Sobol' net, so an entry's samples are stratified over its
+//      cone; O(1) set-up per sample).  With more than 32 samples
 //      per task, on scenes whose traversals are long and vary from ray to ray
 //      (at least kAdaptiveSortMinTris triangles), each task's samples are
 //      sorted by where they leave the cone (coneKey, bitonic sort in shared
@@ -2038,6 +2039,40 @@ __device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
 //      lanes of an entry.  Results are deterministic.
 // Every sample is traced once with its own random numbers.
 constexpr uint32_t kAdaptiveSortMinTris = 16384;
+
+// SplitMix64's output function (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014): a bijective 64-bit mix.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Draws of sample k of an entry in the adaptive render: point k of the
+// two-dimensional Sobol' sequence (dimension 1 the van der Corput sequence in
+// base 2, i.e. k bit-reversed; dimension 2 the generator matrix whose
+// columns start at 2^31 and follow v <- v ^ (v >> 1)) with a random digital
+// shift per entry (both coordinates XORed with mix64 of the seed and the
+// entry).  The first 2^m points of this (0, 2)-sequence form a (0, m, 2)-net,
+// and a digital shift keeps that, so an entry's 2^m samples are stratified
+// in every elementary interval of area 2^-m and each is still uniform, so
+// the estimate stays unbiased.  Coordinate 1 -> the normal draw through the
+// inverse normal distribution at the midpoint of its 2^-23 cell (23 bits,
+// so that the midpoint is exact in float: with 24 the top cell's midpoint
+// rounds to 1 and its draw to infinity), coordinate 2 -> the uniform draw in
+// (0, 1].
+__device__ __forceinline__ float2 netDraw(unsigned long long seed, uint32_t entry, uint32_t k) {
+  const unsigned long long h = mix64(seed + (static_cast<unsigned long long>(entry) + 1ull) * 0x9E3779B97F4A7C15ull);
+  uint32_t x2 = 0u;
+  for (uint32_t v = 0x80000000u, b = k; b != 0u; b >>= 1, v ^= v >> 1)
+    if (b & 1u) x2 ^= v;
+  const uint32_t x1 = __brev(k) ^ static_cast<uint32_t>(h);
+  x2 ^= static_cast<uint32_t>(h >> 32);
+  float2 d;
+  d.x = normcdfinvf((static_cast<float>(x1 >> 9) + 0.5f) * (1.0f / 8388608.0f));
+  d.y = 1.0f - static_cast<float>(x2 >> 8) * (1.0f / 16777216.0f);
+  return d;
+}
 constexpr uint32_t kPoolRounds = 8;
 constexpr uint32_t kPoolSlots = 32 * kPoolRounds;
 constexpr uint32_t kAdaptiveWarps = 4;  // warps per 128-thread block
@@ -2107,12 +2142,7 @@ __global__ void __launch_bounds__(128, kMinBlocks)
     const uint32_t seg = j & ~((32u << lspl) - 1u);
     const uint32_t k = spl > 1 ? j - seg : (j & (segWidth - 1u));
     float2 d = make_float2(0.f, 0.f);
-    if (i < B.count) {
-      curandStatePhilox4_32_10_t st;
-      curand_init(seed, static_cast<unsigned long long>(B.entries[i]) * 1024ull + slotSample(j, k), 0ull, &st);
-      d.x = curand_normal(&st);
-      d.y = curand_uniform(&st);
-    }
+    if (i < B.count) d = netDraw(seed, B.entries[i], slotSample(j, k));
     draw[spl > 1 ? seg + k : j] = d;
     if (sorted) {
       key[j] = coneKey(d.x, d.y);

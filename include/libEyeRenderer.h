@@ -294,8 +294,9 @@ int crAllocatorLoad(const char* path);
  * estimate (the feature mean when no denoiser is trained); where featureSpp <
  * c <= 1024 an extra c-sample render combined with the feature samples by
  * sample count; where c > 1024 (the predicted variance at 1024 samples is
- * above the threshold) a plain 1024-sample render alone.  Extra samples come
- * from Philox4x32-10 streams (seed, entry * 1024 + sample).  d_level: null,
+ * above the threshold) a plain 1024-sample render alone.  An entry's extra
+ * samples are the points of a randomly shifted two-dimensional Sobol' net
+ * (stratified over its cone; unbiased).  d_level: null,
  * or count x N bytes receiving each entry's bucket (index k = 4 << k samples,
  * 0x88 = 1024-sample fallback, 0xFF = feature render only).  raysTraced:
  * null, or receives the rays of the call.  0 on success. */
@@ -357,8 +358,8 @@ int crGetAdaptiveSchedule(int* refillIdle, int* steps);
  * not depend on it.  0 on success. */
 int crSetAdaptiveOccupancy(int blocksPerSM);
 int crGetAdaptiveOccupancy(void);
-/* Test access: `spp` Philox samples per (pose, ommatidium) of host poses
- * with one seed, recording every ray (records: count x N x spp, as
+/* Test access: `spp` samples per (pose, ommatidium) of host poses, the
+ * adaptive render's stratified net draws with one seed, recording every ray (records: count x N x spp, as
  * crRenderFrameRecorded) and the per-entry means (sums: count x N x 3). */
 int crAdaptiveRecord(const float* poses12, size_t count, int spp, unsigned long long seed, void* records,
                      float* sums);

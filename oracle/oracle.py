@@ -239,3 +239,50 @@ def ref_points_in_mesh(tris, xform, pts):
     if L.ref_points_in_mesh(_f32(tris).reshape(-1), len(tris), _f32(xform).reshape(-1), pts, len(pts), out) != 0:
         raise RuntimeError("empty hitbox mesh")
     return out
+
+
+_MASK64 = (1 << 64) - 1
+
+
+def _mix64(z):
+    """SplitMix64's output function on Python ints (mod 2^64)."""
+    z &= _MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+    return z ^ (z >> 31)
+
+
+def net_draws(seed, entries, samples):
+    """Draws (normal, uniform) of the adaptive render's sample `samples[i]`
+    of entry `entries[i]`, restating netDraw (compound-ray_gb300/csrc/
+    render.cu): point k of the two-dimensional Sobol' sequence (k
+    bit-reversed; and the generator matrix with columns 2^31, v ^ (v >> 1),
+    ...) XORed with a per-entry shift from SplitMix64's mix of seed +
+    (entry + 1) * 0x9E3779B97F4A7C15; the first coordinate's top 23 bits
+    through the inverse normal distribution at the middle of their cell
+    (float64 here), the second's as 1 - x / 2^24.  The uniform draw is exact;
+    the normal draw is the float64 value of what the GPU computes with
+    normcdfinvf."""
+    from statistics import NormalDist
+
+    inv = NormalDist().inv_cdf
+    entries = np.asarray(entries, np.int64).reshape(-1)
+    samples = np.asarray(samples, np.int64).reshape(-1)
+    nd = np.empty(len(entries), np.float64)
+    ud = np.empty(len(entries), np.float32)
+    shifts = {}
+    for i, (e, k) in enumerate(zip(entries.tolist(), samples.tolist())):
+        h = shifts.get(e)
+        if h is None:
+            h = shifts[e] = _mix64(seed + (e + 1) * 0x9E3779B97F4A7C15)
+        x2, v, b = 0, 0x80000000, k
+        while b:
+            if b & 1:
+                x2 ^= v
+            b >>= 1
+            v ^= v >> 1
+        x1 = int("{:032b}".format(k)[::-1], 2) ^ (h & 0xFFFFFFFF)
+        x2 ^= h >> 32
+        nd[i] = inv(((x1 >> 9) + 0.5) / 8388608.0)
+        ud[i] = np.float32(1.0) - np.float32((x2 >> 8) * (1.0 / 16777216.0))
+    return nd, ud

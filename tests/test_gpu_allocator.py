@@ -1,5 +1,5 @@
-"""The learned sample allocator and the adaptive render: the Philox-sampled
-adaptive kernel against the oracle ray by ray; its estimates against the
+"""The learned sample allocator and the adaptive render: the adaptive kernel
+(stratified Sobol'-net samples) against the oracle ray by ray; its estimates against the
 plain render; minimum-sample labels; a trained allocator's adaptive render
 against the 1024-sample plain render (error and rays); determinism and the
 checkpoint round trip."""
@@ -39,6 +39,17 @@ def test_adaptive_kernel_matches_oracle(lib, small, small_ref):
     sums = np.zeros((2, N, 3), np.float32)
     assert lib.crAdaptiveRecord(poses, 2, spp, 7, rec.ctypes.data, sums) == 0, eh.lastError(lib)
     rec = rec.reshape(2, N * spp)
+    # The draws: sample s of entry e is point s of the entry's digitally
+    # shifted Sobol' net (seed 7), as oracle.net_draws restates it.
+    nd, ud = oracle.net_draws(7, np.repeat(np.arange(2 * N), spp), np.tile(np.arange(spp), 2 * N))
+    assert np.array_equal(rec["uniformDraw"].reshape(-1), ud)
+    got = rec["normalDraw"].reshape(-1).astype(np.float64)
+    # normcdfinvf under fast maths: close to float64 in the body of the
+    # distribution, a few 1e-3 off far in the tails (its logarithm is the
+    # fast approximation)
+    body = np.abs(nd) < 3.0
+    assert (np.abs(got - nd)[body] <= 4e-6 * np.maximum(1.0, np.abs(nd[body]))).all(), np.abs(got - nd)[body].max()
+    assert np.abs(got - nd).max() <= 5e-3
     for p in range(2):
         r = rec[p]
         draws = np.stack([r["normalDraw"], r["uniformDraw"]], axis=1)
@@ -71,10 +82,15 @@ def test_adaptive_kernel_matches_oracle(lib, small, small_ref):
         lib.crSetAdaptiveOccupancy(5)
         lib.crSetAdaptiveSchedule(16, 16)
     assert lib.crSetAdaptiveOccupancy(7) == -1
-    # normal / uniform draws look like N(0,1) / U(0,1]
+    # normal / uniform draws look like N(0,1) / U(0,1], and each entry's 64
+    # samples are stratified: one per 1/64 of the normal draw's distribution
     nd, ud = rec["normalDraw"].ravel(), rec["uniformDraw"].ravel()
     assert abs(nd.mean()) < 0.02 and abs(nd.std() - 1) < 0.02
     assert ud.min() > 0 and ud.max() <= 1 and abs(ud.mean() - 0.5) < 0.01
+    from statistics import NormalDist
+    cdf = np.vectorize(NormalDist().cdf)
+    cells = np.floor(cdf(nd[:4 * spp].astype(np.float64)) * spp).astype(np.int64).reshape(4, spp)
+    assert all(len(set(c.tolist())) == spp for c in cells)
 
 
 def test_adaptive_estimate_matches_plain_render(lib, tmp_path):

@@ -218,3 +218,25 @@ def test_allocation_restatement_rules():
     assert lv.tolist() == [NR, 2, 5, 8, NR]  # cost 4 x 16 at cost exponent 1/2: one halving
     lv, _ = allocator_ref.allocate_levels(pred, np.full(5, 0.25, np.float32), 8, 0.0, 1.0, 0.5)
     assert lv.tolist() == [3, 5, 8, 0x88, NR]  # cost below 1 counts as 1 = 16 / 2^4: 2^(4 x 1/2) times more
+
+
+def test_net_draws_are_stratified_nets():
+    """oracle.net_draws (the adaptive render's draws): the first 2^m samples
+    of an entry form a (0, m, 2)-net after the digital shift -- exactly one
+    point in each elementary interval of area 2^-m (checked for the
+    2^a x 2^(m-a) grids) -- and different entries get different shifts."""
+    from statistics import NormalDist
+
+    cdf = NormalDist().cdf
+    m = 6
+    n = 1 << m
+    nd, ud = oracle.net_draws(0xada90000, np.repeat([0, 1, 12345], n), np.tile(np.arange(n), 3))
+    for e in range(3):
+        u1 = np.array([cdf(x) for x in nd[e * n:(e + 1) * n]])
+        u2 = 1.0 - ud[e * n:(e + 1) * n].astype(np.float64)
+        for a in range(m + 1):
+            cells = np.floor(u1 * (1 << a)).astype(np.int64) * (1 << (m - a)) + \
+                np.floor(u2 * (1 << (m - a))).astype(np.int64)
+            assert len(set(cells.tolist())) == n, (e, a)
+    assert not np.array_equal(nd[:n], nd[n:2 * n])
+    assert ud.min() > 0 and ud.max() <= 1
