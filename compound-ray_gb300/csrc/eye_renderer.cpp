@@ -1941,6 +1941,7 @@ void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dpos
   fe.philoxSeed = kFeatureSeed;
   fe.frame0 = d.featFrame;
   d.featFrame += count;
+  d.lastPassRows = 0;  // the statistics of the last adaptive pass are overwritten
   d.stats.ensure(std::max<size_t>(1, count * e.N * kFeatureStats));
   r.withCuts(fe, static_cast<uint32_t>(count), e.maxRel);
   check(launchFeatures(r.dev, fe, dposes, static_cast<uint32_t>(count), d.stats.ptr, r.errWord(), r.stream(), false),
@@ -2503,7 +2504,8 @@ int crAdaptiveLastPass(float* prediction, float* cost, uint8_t* level, size_t ro
       "crAdaptiveLastPass",
       [&]() -> int {
         DenoiseState& d = DS();
-        if (d.lastPassRows == 0) throw std::runtime_error("no adaptive render yet");
+        if (d.lastPassRows == 0)
+          throw std::runtime_error("no adaptive pass to read (none yet, or a later feature render replaced it)");
         if (rows != d.lastPassRows)
           throw std::runtime_error("rows must equal the last pass's rows (" + std::to_string(d.lastPassRows) + ")");
         cudaStream_t st = R().stream();

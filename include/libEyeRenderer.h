@@ -342,7 +342,9 @@ float crGetAllocatorCostExponent(void);
  * (prediction: rows x 3 floats; the predicted count is 2^(10 x their mean)),
  * the feature render's traversal cost (cost: rows floats) and the level
  * (level: rows bytes, as crAdaptiveRenderPosesDevice writes it).  Any
- * pointer may be null.  rows must equal the pass's rows.  0 on success. */
+ * pointer may be null.  rows must equal the pass's rows.  Any later call
+ * that renders features (training, the denoised render) replaces the pass;
+ * the call then fails.  0 on success. */
 int crAdaptiveLastPass(float* prediction, float* cost, uint8_t* level, size_t rows);
 /* No counterpart in the reference.  Ray-refill schedule of the adaptive
  * render: each warp works through a pool of up to 256 samples, traversing in

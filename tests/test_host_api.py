@@ -227,6 +227,7 @@ def test_setter_ranges(lib):
     assert lib.crSetAllocatorCostExponent(float("nan")) == -1
     assert lib.crSetAllocatorCostExponent(0.5) == 0 and lib.crGetAllocatorCostExponent() == 0.5
     assert lib.crSetAllocatorCostExponent(0.0) == 0
+    assert lib.crAdaptiveLastPass(None, None, None, 1) == -1 and "no adaptive pass" in eh.lastError(lib)
     assert lib.crSetCutRadius(1.5) == -1
     assert "[0, 1]" in eh.lastError(lib)
     assert lib.crSetRenderVariant(lib.crGetRenderVariantCount()) == -1
