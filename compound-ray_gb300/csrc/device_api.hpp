@@ -75,13 +75,14 @@ struct DevEye {
   float4* cuts = nullptr;
   float cutRadius = 0.f;
   float maxRel = 0.f;
-  // philox: the random numbers come from counter-based Philox4x32-10
-  //       streams (philoxSeed, ((frame0 + p) * N + o) * spp + s) for pose p
-  //       of the launch, ommatidium o and sample s: no generator states and
-  //       no pre-drawn numbers, so a launch may spread its poses over any
-  //       number of warps (feature renders).
-  bool philox = false;
-  unsigned long long philoxSeed = 0;
+  // netDraws: sample s of ommatidium o at pose p of the launch takes point s
+  //       of a digitally shifted two-dimensional Sobol' net, the shift drawn
+  //       from (drawSeed, (frame0 + p) * N + o) (render.cu, netDraw): no
+  //       generator states and no pre-drawn numbers, so a launch may spread
+  //       its poses over any number of warps, and each ommatidium's samples
+  //       are stratified over its cone (feature renders).
+  bool netDraws = false;
+  unsigned long long drawSeed = 0;
   unsigned long long frame0 = 0;
 };
 // Traversal stack entries of the wide BVH (a node pushes up to W - 1).
@@ -374,7 +375,8 @@ void setAdaptiveBlocksPerSM(int blocks);
 int adaptiveBlocksPerSM();
 size_t adaptivePartialFloats(uint64_t count, uint32_t spp);
 // One launch over every bucket: sums[3e..3e+2] = mean sample colour of entry
-// e, samples drawn from the Philox4x32-10 stream (seed, e * 1024 + s).  rec:
+// e, its samples the points of a digitally shifted Sobol' net keyed by
+// (seed, e) (render.cu, netDraw).  rec:
 // null, or count x spp records of a single-bucket launch (tests).
 cudaError_t launchAdaptive(const DevScene& scene, const float4* omm, uint32_t N, const float4* poses,
                            const AdaptiveLaunch& L, unsigned long long seed, float* sums, uint32_t* errFlag,

@@ -1862,7 +1862,7 @@ struct DenoiseState {
   // Sample-count allocator: a second network of the same shape, trained on
   // minimum-sample labels; and the adaptive render's buffers.
   Denoiser alloc;
-  uint64_t adaptiveFrame = 0;  // frames rendered adaptively since the eye was bound (Philox seed offset)
+  uint64_t adaptiveFrame = 0;  // frames rendered adaptively since the eye was bound (draw seed offset)
   DevBuf<float> pred, learned, sums, partials, labelOuts;
   DevBuf<uint32_t> entries;
   DevBuf<uint8_t> level;
@@ -1870,7 +1870,7 @@ struct DenoiseState {
   DevBuf<unsigned long long> counts, tileScratch;
   std::vector<uint16_t> lastLabels;
   double lastRays = 0;  // rays traced by the last adaptive render (feature + adaptive)
-  uint64_t featFrame = 0;  // feature-render frames of the current eye so far (the Philox stream position)
+  uint64_t featFrame = 0;  // feature-render frames of the current eye so far (keys its draws)
   uint64_t lastPassRows = 0;  // rows of the last adaptive pass (its pred, stats and level stay in place)
   float allocHalvings = 0.f;  // predicted counts are divided by 2^allocHalvings (crSetAllocatorHalvings)
   float allocExponent = 1.f;  // counts follow the predicted count to this power (crSetAllocatorExponent)
@@ -1923,22 +1923,22 @@ DevEye streamsFor(Renderer& r, EyeDev& e, DevBuf<uint32_t>& rng, uint32_t& haveS
 // Feature render of `count` poses into d.stats; with `rows`, also the
 // feature rows and residual bases (d.X, d.base) the training set and the
 // layer-by-layer path use.
-constexpr unsigned long long kFeatureSeed = 0xfea70000ull;  // Philox key of the feature renders
+constexpr unsigned long long kFeatureSeed = 0xfea70000ull;  // draw seed of the feature renders
 
 void denoiseFeatures(Renderer& r, DenoiseState& d, EyeDev& e, const float4* dposes, size_t count, uint32_t featSpp,
                      bool rows = true) {
   if (featSpp < 1 || featSpp > 32) throw std::runtime_error("feature renders use 1 to 32 samples per ommatidium");
   if (count > 0xffffffffull) throw std::runtime_error("too many poses in one feature render");
-  // Counter-based Philox streams: frame (featFrame + p) of the eye, so all
-  // poses render in one launch spread over any number of warps; reloading
-  // the scene or switching eyes restarts the frame count.
+  // Stratified draws keyed by frame (featFrame + p) of the eye and the
+  // ommatidium, so all poses render in one launch spread over any number of
+  // warps; reloading the scene or switching eyes restarts the frame count.
   DevEye fe;
   fe.omm = e.omm.ptr;
   fe.order = e.order.ptr;
   fe.N = e.N;
   fe.spp = featSpp;
-  fe.philox = true;
-  fe.philoxSeed = kFeatureSeed;
+  fe.netDraws = true;
+  fe.drawSeed = kFeatureSeed;
   fe.frame0 = d.featFrame;
   d.featFrame += count;
   d.lastPassRows = 0;  // the statistics of the last adaptive pass are overwritten

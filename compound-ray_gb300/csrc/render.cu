@@ -1020,6 +1020,41 @@ __global__ void drawsKernel(DevEye eye, uint32_t P) {
   storeState(eye.rng, total, idx, st);
 }
 
+// SplitMix64's output function (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014): a bijective 64-bit mix.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Draws of sample k of an entry (the adaptive render's (pose, ommatidium)
+// entries; a feature render's (frame, ommatidium)): point k of the
+// two-dimensional Sobol' sequence (dimension 1 the van der Corput sequence in
+// base 2, i.e. k bit-reversed; dimension 2 the generator matrix whose
+// columns start at 2^31 and follow v <- v ^ (v >> 1)) with a random digital
+// shift per entry (both coordinates XORed with mix64 of the seed and the
+// entry).  The first 2^m points of this (0, 2)-sequence form a (0, m, 2)-net,
+// and a digital shift keeps that, so an entry's 2^m samples are stratified
+// in every elementary interval of area 2^-m and each is still uniform, so
+// the estimate stays unbiased.  Coordinate 1 -> the normal draw through the
+// inverse normal distribution at the midpoint of its 2^-23 cell (23 bits,
+// so that the midpoint is exact in float: with 24 the top cell's midpoint
+// rounds to 1 and its draw to infinity), coordinate 2 -> the uniform draw in
+// (0, 1].
+__device__ __forceinline__ float2 netDraw(unsigned long long seed, unsigned long long entry, uint32_t k) {
+  const unsigned long long h = mix64(seed + (entry + 1ull) * 0x9E3779B97F4A7C15ull);
+  uint32_t x2 = 0u;
+  for (uint32_t v = 0x80000000u, b = k; b != 0u; b >>= 1, v ^= v >> 1)
+    if (b & 1u) x2 ^= v;
+  const uint32_t x1 = __brev(k) ^ static_cast<uint32_t>(h);
+  x2 ^= static_cast<uint32_t>(h >> 32);
+  float2 d;
+  d.x = normcdfinvf((static_cast<float>(x1 >> 9) + 0.5f) * (1.0f / 8388608.0f));
+  d.y = 1.0f - static_cast<float>(x2 >> 8) * (1.0f / 16777216.0f);
+  return d;
+}
+
 __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 
 // kMode: 0 = render, 1 = render and record every ray, 2 = render and count
@@ -1105,11 +1140,10 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       const float4* pp = poses + 4 * p;
       const float4 P0 = __ldg(pp), X = __ldg(pp + 1), Y = __ldg(pp + 2), Z = __ldg(pp + 3);
       float nd, ud;
-      if (kFeat) {  // feature renders draw from counter-based streams (launchFeatures requires eye.philox)
-        curandStatePhilox4_32_10_t ps;
-        curand_init(eye.philoxSeed, ((eye.frame0 + p) * eye.N + o) * eye.spp + s, 0ull, &ps);
-        nd = curand_normal(&ps);
-        ud = curand_uniform(&ps);
+      if (kFeat) {  // feature renders: each ommatidium's samples a net (launchFeatures requires eye.netDraws)
+        const float2 dr = netDraw(eye.drawSeed, (eye.frame0 + p) * eye.N + o, s);
+        nd = dr.x;
+        ud = dr.y;
       } else if (eye.draws) {
         const float2 dr = eye.draws[(static_cast<size_t>(p) * eye.N + o) * eye.spp + s];
         nd = dr.x;
@@ -1897,7 +1931,7 @@ cudaError_t launchFeatures(const DevScene& scene, const DevEye& eye, const float
   if (P == 0 || eye.N == 0) return cudaSuccess;
   WarpPlan plan = planWarps(eye.N, eye.spp);
   if (plan.chunks != 1) return cudaErrorInvalidValue;  // feature renders use at most 32 samples
-  if (!eye.philox) return cudaErrorInvalidValue;  // feature renders draw from Philox streams
+  if (!eye.netDraws) return cudaErrorInvalidValue;  // feature renders draw from shifted nets
   // Counter-based draws: spread the poses over enough warps for about a
   // dozen waves, so that the last one costs little.
   plan = splitPoses(plan, P, 4 * kFillWarps);
@@ -2040,39 +2074,6 @@ __device__ __forceinline__ uint32_t coneKey(float nd, float ud) {
 // Every sample is traced once with its own random numbers.
 constexpr uint32_t kAdaptiveSortMinTris = 16384;
 
-// SplitMix64's output function (Steele, Lea and Flood, "Fast splittable
-// pseudorandom number generators", OOPSLA 2014): a bijective 64-bit mix.
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-// Draws of sample k of an entry in the adaptive render: point k of the
-// two-dimensional Sobol' sequence (dimension 1 the van der Corput sequence in
-// base 2, i.e. k bit-reversed; dimension 2 the generator matrix whose
-// columns start at 2^31 and follow v <- v ^ (v >> 1)) with a random digital
-// shift per entry (both coordinates XORed with mix64 of the seed and the
-// entry).  The first 2^m points of this (0, 2)-sequence form a (0, m, 2)-net,
-// and a digital shift keeps that, so an entry's 2^m samples are stratified
-// in every elementary interval of area 2^-m and each is still uniform, so
-// the estimate stays unbiased.  Coordinate 1 -> the normal draw through the
-// inverse normal distribution at the midpoint of its 2^-23 cell (23 bits,
-// so that the midpoint is exact in float: with 24 the top cell's midpoint
-// rounds to 1 and its draw to infinity), coordinate 2 -> the uniform draw in
-// (0, 1].
-__device__ __forceinline__ float2 netDraw(unsigned long long seed, uint32_t entry, uint32_t k) {
-  const unsigned long long h = mix64(seed + (static_cast<unsigned long long>(entry) + 1ull) * 0x9E3779B97F4A7C15ull);
-  uint32_t x2 = 0u;
-  for (uint32_t v = 0x80000000u, b = k; b != 0u; b >>= 1, v ^= v >> 1)
-    if (b & 1u) x2 ^= v;
-  const uint32_t x1 = __brev(k) ^ static_cast<uint32_t>(h);
-  x2 ^= static_cast<uint32_t>(h >> 32);
-  float2 d;
-  d.x = normcdfinvf((static_cast<float>(x1 >> 9) + 0.5f) * (1.0f / 8388608.0f));
-  d.y = 1.0f - static_cast<float>(x2 >> 8) * (1.0f / 16777216.0f);
-  return d;
-}
 constexpr uint32_t kPoolRounds = 8;
 constexpr uint32_t kPoolSlots = 32 * kPoolRounds;
 constexpr uint32_t kAdaptiveWarps = 4;  // warps per 128-thread block
