@@ -887,6 +887,15 @@ def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_pose
 
     ms_learned = timed(learned)
     learned_img = d_out.cpu().numpy()
+    # The same render without the network's correction (alpha 0): the
+    # stratified 8-sample feature mean alone, to separate what the network
+    # adds from what the stratified samples give.
+    if lib.crDenoiserScaleOutput(0.0) != 0:
+        raise RuntimeError(eh.lastError(lib))
+    learned()
+    mean_img = d_out.cpu().numpy()
+    if lib.crDenoiserLoad(ck("steps%d.bin" % best_steps)) != 0 or lib.crDenoiserScaleOutput(best_alpha) != 0:
+        raise RuntimeError(eh.lastError(lib))
 
     def plain(spp):
         lib.setCurrentEyeSamplesPerOmmatidium(spp)
@@ -919,6 +928,9 @@ def run_learned(lib, eh, args, stream, scene="small", train_poses=200, held_pose
             "validation_rmse_by_steps": {str(k): round(v[0], 7) for k, v in by_steps.items()},
             "alpha": best_alpha, "validation_rmse_by_alpha": {str(k): round(v, 7) for k, v in by_alpha.items()},
             "data_s": t_data, "train_s": t_train, "rmse_learned_8spp": r_learned, "rmse_plain_8spp": sweep[8][0],
+            "rmse_feature_mean_8spp": rmse(mean_img),
+            "feature_mean_note": "the learned form's own 8-sample mean (stratified net samples) without the "
+                                 "network's correction",
             "rmse_per_channel_learned_8spp": rmse_per_channel(learned_img, ref),
             "rmse_note": "RMSE against the plain 1024-sample render, worst of the R, G, B channels",
             "timing": "CUDA events, best of %d after one untimed run, for every render" % TIMING_REPS,
