@@ -1057,6 +1057,39 @@ __device__ __forceinline__ float2 netDraw(unsigned long long seed, unsigned long
 
 __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 
+// In-block chunk sums keep the partials of kInBlockPoses poses at a time in
+// shared memory: [ommatidium slot of the block][pose of the group][chunk][3].
+constexpr uint32_t kInBlockPoses = 16;
+
+// Sums the block's chunk partials of poses pg0 .. pg0 + count - 1 in chunk
+// order into out (P x N x 3), between two barriers: every warp of the block
+// has written its partials of these poses before, and none overwrites them
+// before the sums are read.  Called by every thread of the block.
+__device__ __forceinline__ void flushChunkSums(const float* __restrict__ part, const WarpPlan& plan,
+                                               const DevEye& eye, float* __restrict__ out, uint32_t pg0,
+                                               uint32_t count) {
+  __syncthreads();
+  const uint32_t perBlock = plan.groupsPerBlock * plan.ommPerWarp;  // ommatidium slots of the block
+  for (uint32_t item = threadIdx.x; item < perBlock * count; item += blockDim.x) {
+    const uint32_t gs = item / count, pp = item - gs * count;
+    const uint64_t slot = static_cast<uint64_t>(blockIdx.x) * perBlock + gs;
+    if (slot >= eye.N) continue;
+    const uint32_t o = eye.order ? __ldg(eye.order + slot) : static_cast<uint32_t>(slot);
+    const float* src = part + (static_cast<size_t>(gs) * kInBlockPoses + pp) * plan.chunks * 3;
+    float x = 0.f, y = 0.f, z = 0.f;
+    for (uint32_t c = 0; c < plan.chunks; ++c) {
+      x += src[3 * c];
+      y += src[3 * c + 1];
+      z += src[3 * c + 2];
+    }
+    float* dst = out + (static_cast<size_t>(pg0 + pp) * eye.N + o) * 3;
+    dst[0] = x;
+    dst[1] = y;
+    dst[2] = z;
+  }
+  __syncthreads();
+}
+
 // kMode: 0 = render, 1 = render and record every ray, 2 = render and count
 // node visits / triangle tests into stats[0..1].  kMinBlocks: resident
 // 128-thread blocks per SM the register allocation is sized for (the
@@ -1064,7 +1097,9 @@ __constant__ float FWHM_SD_RATIO = 2.35482004503094938202313865291f;
 // One warp task: up to 32 samples of one ommatidium (or whole ommatidia when
 // spp < 32) for all P poses.  Called by whole warps.
 // part: null, or (plan.inBlock) the block's shared-memory chunk partials,
-// [group in block][ommatidium in warp][pose][chunk][3] floats.
+// [group in block][ommatidium in warp][pose of the group][chunk][3] floats
+// for kInBlockPoses poses at a time; with it every thread of the block
+// calls this function with the same poses (flushChunkSums has barriers).
 // kWidth: 2 searches the BVH2 (with the near-field cut when eye.cuts is
 // set), 4 or 8 the wide BVH of that width (no cut).
 template <int kMode, int kWidth = 2>
@@ -1102,9 +1137,9 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
   if (plan.chunks == 1) {
     dst0 = out + static_cast<size_t>(o) * 3;
     dstStride = static_cast<size_t>(eye.N) * 3;
-  } else if (part) {
+  } else if (part) {  // pose p's partial at (p - p0) % kInBlockPoses of the group
     const uint32_t gs = (group % plan.groupsPerBlock) * plan.ommPerWarp + lane / plan.segWidth;
-    dst0 = part + ((static_cast<size_t>(gs) * P - p0) * plan.chunks + chunk) * 3;
+    dst0 = part + (static_cast<size_t>(gs) * kInBlockPoses * plan.chunks + chunk) * 3;
     dstStride = static_cast<size_t>(plan.chunks) * 3;
   } else {
     dst0 = scratch + (static_cast<size_t>(o) * plan.chunks + chunk) * 3;
@@ -1261,10 +1296,17 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
       continue;
     }
     if ((lane % plan.segWidth) == 0u && o < eye.N) {
-      float* dst = dst0 + p * dstStride;
+      float* dst = dst0 + (part ? (p - p0) % kInBlockPoses : p) * dstStride;
       dst[0] = col.x;
       dst[1] = col.y;
       dst[2] = col.z;
+    }
+    // In-block sums: after each group of kInBlockPoses poses (and the last),
+    // the block sums the group's partials (every warp of the block runs the
+    // same poses, so all of them reach these barriers).
+    if (part && ((p - p0 + 1) % kInBlockPoses == 0 || p + 1 == p1)) {
+      const uint32_t pg0 = p0 + (p - p0) / kInBlockPoses * kInBlockPoses;
+      flushChunkSums(part, plan, eye, out, pg0, p + 1 - pg0);
     }
   }
   if (!kFeat && valid && !eye.draws) storeState(eye.rng, plane, sidx, st);
@@ -1275,8 +1317,9 @@ __device__ __forceinline__ void renderTask(const DevScene& sc, const DevEye& eye
 // SM), independent of the block size, which the plan sets (128-512 threads).
 // With plan.inBlock every block holds all chunk warps of plan.groupsPerBlock
 // ommatidium groups (tasks padded to whole blocks): each warp leaves its
-// per-pose chunk partial in shared memory, and after one barrier the block
-// sums every (ommatidium, pose) over its chunks in chunk order.
+// per-pose chunk partial in shared memory, and after every kInBlockPoses
+// poses the block sums each (ommatidium, pose) of the group over its chunks
+// in chunk order (flushChunkSums), so the buffer holds 16 poses at a time.
 template <int kMode, int kRegs, int kWidth = 2, bool kInBlock = false>
 __global__ void __maxnreg__(kRegs) renderKernel(DevScene sc, DevEye eye, const float4* __restrict__ poses, uint32_t P,
                                                 WarpPlan plan, float* __restrict__ out, float* __restrict__ scratch,
@@ -1290,27 +1333,6 @@ __global__ void __maxnreg__(kRegs) renderKernel(DevScene sc, DevEye eye, const f
   if (task >= plan.tasks) return;  // whole warps exit together (never with inBlock: whole blocks)
   renderTask<kMode, kWidth>(sc, eye, poses, P, plan, task, out, scratch, errFlag, rec, nodeVisits, triTests,
                             kInBlock ? chunkPart : nullptr);
-  if (kInBlock) {
-    __syncthreads();
-    const uint32_t perBlock = plan.groupsPerBlock * plan.ommPerWarp;  // ommatidium slots of the block
-    for (uint32_t item = threadIdx.x; item < perBlock * P; item += blockDim.x) {
-      const uint32_t gs = item / P, p = item - gs * P;
-      const uint64_t slot = static_cast<uint64_t>(blockIdx.x) * perBlock + gs;
-      if (slot >= eye.N) continue;
-      const uint32_t o = eye.order ? __ldg(eye.order + slot) : static_cast<uint32_t>(slot);
-      const float* src = chunkPart + (static_cast<size_t>(gs) * P + p) * plan.chunks * 3;
-      float x = 0.f, y = 0.f, z = 0.f;
-      for (uint32_t c = 0; c < plan.chunks; ++c) {
-        x += src[3 * c];
-        y += src[3 * c + 1];
-        z += src[3 * c + 2];
-      }
-      float* dst = out + (static_cast<size_t>(p) * eye.N + o) * 3;
-      dst[0] = x;
-      dst[1] = y;
-      dst[2] = z;
-    }
-  }
   if (kCount) {
     unsigned long long nv = nodeVisits, tt = triTests;
     for (int m = 16; m >= 1; m >>= 1) {
@@ -1750,7 +1772,7 @@ WarpPlan planRender(uint32_t N, uint32_t spp, uint32_t P, bool forceScratch, boo
   const bool maySplit = P >= 2 && p.tasks < kFillWarps / 2;
   if (p.chunks > 1 && !forceScratch && inBlockAllowed && !maySplit && bw % p.chunks == 0) {
     const uint32_t G = bw / p.chunks;
-    const size_t bytes = static_cast<size_t>(G) * p.ommPerWarp * P * p.chunks * 3 * sizeof(float);
+    const size_t bytes = static_cast<size_t>(G) * p.ommPerWarp * kInBlockPoses * p.chunks * 3 * sizeof(float);
     if (bytes <= kChunkSmemMax) {
       p.inBlock = 1;
       p.groupsPerBlock = G;
@@ -1832,7 +1854,7 @@ cudaError_t runRenderKernel(const DevScene& scene, const DevEye& eye, const floa
   if (blocks > 0x7fffffffULL) return cudaErrorInvalidConfiguration;
   size_t smem = 0;
   if (kInBlock) {
-    smem = static_cast<size_t>(plan.groupsPerBlock) * plan.ommPerWarp * P * plan.chunks * 3 * sizeof(float);
+    smem = static_cast<size_t>(plan.groupsPerBlock) * plan.ommPerWarp * kInBlockPoses * plan.chunks * 3 * sizeof(float);
     if (smem > 48 * 1024) {
       const cudaError_t e = cudaFuncSetAttribute(renderKernel<kMode, kRegs, kWidth, kInBlock>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -236,6 +236,28 @@ def test_render_layouts(lib, small, spp):
         np.testing.assert_allclose(outs[128, spw], ref, rtol=1e-5, atol=1e-7)
 
 
+def test_in_block_sums_over_pose_groups(lib, small):
+    """A multi-pose launch whose chunk partials are summed in shared memory
+    (512-thread blocks holding the 16 chunk warps of an ommatidium at 512
+    samples) flushes them every 16 poses; 40 poses (groups of 16, 16 and 8)
+    render the same bits as the scratch layout (128-thread blocks)."""
+    _load(lib, small["gltf"], 512)
+    rng = np.random.default_rng(3)
+    poses = scenes.open_poses(small["boxes"], 40, rng)
+    outs = {}
+    try:
+        for block in (128, 512):
+            assert lib.crSetRenderLayout(block, 32) == 0, eh.lastError(lib)
+            lib.setCurrentEyeSamplesPerOmmatidium(511)
+            lib.setCurrentEyeSamplesPerOmmatidium(512)  # the same streams for both layouts
+            outs[block] = eh.renderPoses(lib, poses)
+            assert eh.lastError(lib) == ""
+    finally:
+        lib.crSetRenderLayout(0, 32)
+    assert np.array_equal(outs[512], outs[128])
+    assert np.isfinite(outs[128]).all() and (outs[128] > 0).any()
+
+
 @pytest.mark.parametrize("size", ["small", "terrain"])
 def test_gpu_built_bvh_renders_identical_bits(lib, small, tmp_path, size):
     """The GPU linear BVH and the host SAH BVH give bit-identical renders:
