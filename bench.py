@@ -1350,10 +1350,14 @@ def run_profile_learned(args):
         p16[:, 4 * k:4 * k + 3] = held[:, 3 * k:3 * k + 3]
     d_poses = torch.from_numpy(p16).cuda()
     d_out = torch.empty((P, N, 3), dtype=torch.float32, device="cuda")
-    for _ in range(2):
+    for rep in range(2):
+        if rep == 1:
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("learned_render")  # ncu --nvtx --nvtx-include learned_render/
         if lib.crDenoiserRenderPosesDevice(d_poses.data_ptr(), P, 8, d_out.data_ptr()) != 0:
             raise RuntimeError(eh.lastError(lib))
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     print(json.dumps({"profile_case": "learned render of %d held-out terrain poses, twice" % P,
                       "denoiser_kernel": args.denoiser_kernel, "checksum": float(d_out.sum())}))
 
