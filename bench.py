@@ -1079,8 +1079,9 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
     # a fixed render time.  Also whether the denoiser serves the entries the
     # feature render covers (without it they keep the 8-sample mean and its
     # inference is skipped).  For each (denoiser, cost exponent, exponent)
-    # the largest halvings whose validation RMSE (worst channel) stays
-    # within 90% of 1/255; then the rule whose validation render is fastest.
+    # the largest halvings (to a quarter) whose validation RMSE (worst
+    # channel) stays within 90% of 1/255; then the rule whose validation
+    # render is fastest.
     val_rmse, rule_ms = {}, {}
     vrays = ctypes.c_double(0.0)
 
@@ -1124,17 +1125,24 @@ def run_adaptive(lib, eh, args, stream, scene="large", train_poses=16, held_pose
                 if lib.crSetAllocatorExponent(ex) != 0:
                     raise RuntimeError(eh.lastError(lib))
                 good = None
-                for h in np.arange(-3.0, 6.01, 0.5):
+
+                def passes(h):
                     if lib.crSetAllocatorHalvings(float(h)) != 0:
                         raise RuntimeError(eh.lastError(lib))
                     val_adaptive()
                     r = float(torch.sqrt(((d_vout - d_vref) ** 2).reshape(-1, 3).mean(dim=0)).max())
                     val_rmse["%d/%g/%g/%g" % (den, ce, ex, h)] = (r, vrays.value)
-                    if r > 0.9 / 255.0:
+                    return r <= 0.9 / 255.0
+
+                # steps of 1/2 from -3, then the quarter step above the last pass
+                for h in np.arange(-3.0, 6.01, 0.5):
+                    if not passes(h):
                         break
                     good = float(h)
                 if good is None:
                     continue
+                if good + 0.25 <= 6.0 and passes(good + 0.25):
+                    good += 0.25
                 lib.crSetAllocatorHalvings(good)
                 key = (den, ce, ex, good)
                 rule_ms["%d/%g/%g/%g" % key] = timed(val_adaptive)
