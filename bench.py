@@ -430,8 +430,8 @@ def run_ours(args):
     bt, spw = ctypes.c_int(0), ctypes.c_int(0)
     lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw))
     layout = (bt.value, spw.value)
-    tune_all = np.zeros(18, np.float32)
-    lib.crGetAutotuneTimes(tune_all, 18)
+    tune_all = np.zeros(20, np.float32)
+    lib.crGetAutotuneTimes(tune_all, 20)
     bvh_width = int(lib.crGetBvhWidth())
 
     # Traversal statistics for the roofline's per-ray bytes (not timed).
@@ -540,7 +540,8 @@ def run_ours(args):
                                      "block_128_256_512": [round(float(x), 3) for x in tune_all[3:6]],
                                      "samples_per_warp_8_16_32": [round(float(x), 3) for x in tune_all[6:9]],
                                      "cut_0_256_128_64_32_16": [round(float(x), 3) for x in tune_all[9:15]],
-                                     "bvh_width_2_4_8": [round(float(x), 3) for x in tune_all[15:18]]},
+                                     "bvh_width_2_4_8": [round(float(x), 3) for x in tune_all[15:18]],
+                                     "cut_refined_div_mul_sqrt2": [round(float(x), 3) for x in tune_all[18:20]]},
                      "bvh_width": bvh_width},
         # per 256-pose launch: the poses' near-field cuts (when a radius is
         # set), the render kernel and, when the layout keeps chunk partials in
@@ -1274,15 +1275,16 @@ def autotune_record(lib):
     block size, samples per warp, near-field cut, BVH width."""
     import ctypes
 
-    t = np.zeros(18, np.float32)
-    lib.crGetAutotuneTimes(t, 18)
+    t = np.zeros(20, np.float32)
+    lib.crGetAutotuneTimes(t, 20)
     bt, spw = ctypes.c_int(0), ctypes.c_int(0)
     lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw))
     r = lambda a: [round(float(x), 3) for x in a]
     return {"variant": int(lib.crGetRenderVariant()), "block_threads": bt.value, "samples_per_warp": spw.value,
             "near_field_cut_fraction": float(lib.crGetCutRadius()), "bvh_width": int(lib.crGetBvhWidth()),
             "ms": {"variants": r(t[0:3]), "block_128_256_512": r(t[3:6]), "samples_per_warp_8_16_32": r(t[6:9]),
-                   "cut_0_256_128_64_32_16": r(t[9:15]), "bvh_width_2_4_8": r(t[15:18])}}
+                   "cut_0_256_128_64_32_16": r(t[9:15]), "bvh_width_2_4_8": r(t[15:18]),
+                   "cut_refined_div_mul_sqrt2": r(t[18:20])}}
 
 
 def ctypes_double():

@@ -167,7 +167,7 @@ void buildSphereGrids(EyeDev& e, const std::vector<Ommatidium>& omm, cudaStream_
 }
 
 constexpr uint32_t kMaxPosesPerLaunch = 256;
-constexpr size_t kTuneSlots = 18;
+constexpr size_t kTuneSlots = 20;
 
 // Order in which warp segments take an eye's ommatidia: by the 30-bit Morton
 // code of the unit axis direction mapped into the cube [0, 1)^3 (ties by
@@ -1664,6 +1664,24 @@ int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPe
           }
         }
         r.cutFactor = bestCut;
+        // Refinement: the geometric midpoints on either side of the best
+        // non-zero radius (a factor of sqrt 2 each way).
+        if (bestCut > 0.f) {
+          const float around[] = {bestCut * 0.70710678f, bestCut * 1.41421356f};
+          float refined = bestCut;
+          for (int k = 0; k < 2; ++k) {
+            if (!(around[k] <= 1.f)) continue;
+            r.cutFactor = around[k];
+            const float ms = trial();
+            r.tuneTimes[18 + k] = ms;
+            if (ms < bestCutMs) {
+              bestCutMs = ms;
+              refined = around[k];
+            }
+          }
+          bestCut = refined;
+          r.cutFactor = bestCut;
+        }
         // BVH width: the two-wide BVH with its best cut against the wide ones.
         const int prevWidth = r.bvhWidth;
         int bestWidth = 2;

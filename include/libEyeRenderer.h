@@ -166,12 +166,15 @@ int crMeasureTraversal(const float* d_poses, size_t count, double* nodesPerRay, 
 int crAutotune(const float* d_poses, size_t count, int* bestVariant, float* msPerVariant);
 /* No counterpart in the reference.  After the variants, crAutotune times
  * the block size (128, 256, 512 threads), then the samples per warp segment
- * (8, 16, 32), then the near-field cut radius, keeping the fastest of each.
- * Last it times the BVH widths 4 and 8 (crSetBvhWidth) against the two-wide
- * BVH with its best cut, and keeps the fastest tree.
+ * (8, 16, 32), then the near-field cut radius, keeping the fastest of each;
+ * a non-zero best radius is refined by trying it divided and multiplied by
+ * sqrt(2).  Last it times the BVH widths 4 and 8 (crSetBvhWidth) against the
+ * two-wide BVH with its best cut, and keeps the fastest tree.
  * crGetAutotuneTimes copies its timings (ms): variants 0-2, blocks 128 / 256
  * / 512, samples per warp 8 / 16 / 32, cut radius 0, 1/256, 1/128, 1/64,
- * 1/32, 1/16 of the scene extent, BVH width 2 / 4 / 8 (18 values). */
+ * 1/32, 1/16 of the scene extent, BVH width 2 / 4 / 8, and the refinement's
+ * radius / sqrt 2 and x sqrt 2 (20 values; the last two 0 when the best
+ * radius was 0). */
 int crGetAutotuneTimes(float* ms, size_t n);
 /* No counterpart in the reference.  Layout of the render kernel: block size
  * in threads (0 = the smallest of 128 / 256 / 512 holding all 32-sample

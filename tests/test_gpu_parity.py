@@ -197,8 +197,13 @@ def test_autotune_changes_no_result(lib, small):
     assert lib.crGetRenderLayout(ctypes.byref(bt), ctypes.byref(spw)) == 0
     lib.setCurrentEyeSamplesPerOmmatidium(64)
     assert lib.crAutotune(d.data_ptr(), 4, ctypes.byref(best), ms) == 0
-    times = np.zeros(18, np.float32)
-    assert lib.crGetAutotuneTimes(times, 18) == 0 and (times > 0).all()
+    times = np.zeros(20, np.float32)
+    assert lib.crGetAutotuneTimes(times, 20) == 0 and (times[:18] > 0).all()
+    # the cut refinement ran exactly when the best grid radius was not 0
+    if lib.crGetCutRadius() > 0:
+        assert (times[18:] > 0).all()
+    else:
+        assert (times[18:] == 0).all()
     assert lib.crSetRenderLayout(bt.value, spw.value) == 0 and lib.crSetRenderVariant(0) == 0
     assert np.array_equal(eh.renderPoses(lib, poses), outs[0])
     lib.crSetRenderVariant(best.value)
